@@ -1,0 +1,455 @@
+"""GB300 assembly of the fluid_mc equations of GALES-multi-fluid — Python host side.
+
+This mirrors the reference's assembly-facing interface for the hot path:
+
+  reference (C++, sim/fluid_mc/P0/main.cpp)          here
+  ----------------------------------------------     ---------------------------------------------
+  fluid_properties props  (props.txt mix_of_ch)      Material([custom_chemical(...), ideal_gas(...)])
+  read_setup setup        (setup.txt flags)           Setup(dim, tau=2019, dc_2006=True, ...)
+  fluid_ic_bc / fluid_dofs_ic_bc policies             Setup.dirichlet / Setup.neumann / Setup.mass_flux
+  Mesh<dim>               (mesh file)                 Mesh(coords, conn, node_flag, ...)
+  linear_system lp(model) (linear_system.hpp:40-66)   LinearSystem (pattern from FluidAssembly.pattern())
+  fluid_assembly::execute() -> seconds                FluidAssembly.execute(I, P, dt, lp) -> seconds
+  residual_check::execute (residual_check.hpp:42-80)  ResidualCheck.execute(b, it_count)
+
+All arithmetic runs in the CUDA library libgales_asm.so through the C ABI of
+include/gales_asm.h; nothing here computes the assembly on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import abi
+from .abi import (FORM_FP64, FORM_MIXED, SCATTER_ATOMIC, SCATTER_COLOURED, TAU_2001, TAU_2007,
+                  TAU_2014, TAU_2019, TAU_NONE, VJP_EXACT, VJP_FROZEN)
+
+R_UNIVERSAL = 8.314462  # chemicals.hpp:229
+
+
+class GalesError(RuntimeError):
+    def __init__(self, code: int, msg: str, first_bad: int = -1):
+        super().__init__(f"GALES status {code:#x}: {msg}")
+        self.code = code
+        self.first_bad = first_bad
+
+
+# ---------------------------------------------------------------------------
+# Materials (src/fem/physical_props/fluid/chemicals.hpp, fluid_properties.hpp)
+
+def custom_chemical(rho: float, mu: float, cp: float, kappa: float, alpha: float, beta: float,
+                    chemical_diffusivity: float = 1.e-10) -> abi.ChemicalDesc:
+    """custom_chemical(rho, mu, cp, kappa, alpha, beta) of chemicals.hpp:23-33."""
+    c = abi.ChemicalDesc()
+    c.kind = abi.CH_CUSTOM
+    c.rho, c.mu, c.cp, c.kappa, c.alpha, c.beta = rho, mu, cp, kappa, alpha, beta
+    c.cv = cp
+    c.chemical_diffusivity = chemical_diffusivity
+    return c
+
+
+def ideal_gas(molar_mass: float, gamma: float = 1.4, chemical_diffusivity: float = 1.e-10) -> abi.ChemicalDesc:
+    """ideal_gas(molar_mass, gamma) of chemicals.hpp:237-246 (mu = 1e-5, kappa = mu cp / 0.72)."""
+    c = abi.ChemicalDesc()
+    c.kind = abi.CH_IDEAL_GAS
+    c.R = R_UNIVERSAL / molar_mass
+    c.gamma = gamma
+    c.cv = c.R / (gamma - 1.0)
+    c.cp = gamma * c.cv
+    c.mu = 1.e-5
+    c.kappa = c.mu * c.cp / 0.72
+    c.chemical_diffusivity = chemical_diffusivity
+    return c
+
+
+IDEAL_GAS_MOLAR_MASS = {"H2O": 0.01802, "CO2": 0.04401, "AIR": 0.02897, "HE": 0.004, "ARGON": 0.06}
+
+
+def ideal_gas_named(name: str) -> abi.ChemicalDesc:
+    """ideal_gas(std::string) of chemicals.hpp:201-234."""
+    key = name.upper()
+    gamma = 1.67 if key in ("HE", "ARGON") else 1.4
+    return ideal_gas(IDEAL_GAS_MOLAR_MASS[key], gamma)
+
+
+def ideal_gas_params(molar_mass: float, mu: float, cp: float, kappa: float,
+                     chemical_diffusivity: float = 1.e-10) -> abi.ChemicalDesc:
+    """Ideal gas parameterised by (M, mu, cp): R = R_u/M, cv = cp - R, gamma = cp/cv.
+
+    This is the parameterisation in which the VJP reports d/d(theta) for a gas
+    component; at the reference constructor's values it reproduces ideal_gas().
+    """
+    c = abi.ChemicalDesc()
+    c.kind = abi.CH_IDEAL_GAS
+    c.R = R_UNIVERSAL / molar_mass
+    c.cp = cp
+    c.cv = cp - c.R
+    c.gamma = cp / c.cv
+    c.mu = mu
+    c.kappa = kappa
+    c.chemical_diffusivity = chemical_diffusivity
+    return c
+
+
+class Material:
+    """mix_of_ch mixture of 1..4 chemicals (fluid_properties.hpp:199-227)."""
+
+    def __init__(self, chemicals: Sequence[abi.ChemicalDesc]):
+        if not 1 <= len(chemicals) <= 4:
+            raise ValueError("nb_comp must be 1..4")
+        self.chemicals = list(chemicals)
+        self.desc = abi.MaterialDesc()
+        self.desc.nb_comp = len(chemicals)
+        for i, c in enumerate(chemicals):
+            self.desc.comp[i] = c
+
+    @property
+    def nb_comp(self) -> int:
+        return self.desc.nb_comp
+
+
+# ---------------------------------------------------------------------------
+# Setup flags and boundary-condition policy as data
+
+class Setup:
+    """read_setup flags (setup.txt:24-31) plus the ic_bc policy of one case.
+
+    dirichlet[flag] = list of constrained dof indices for nodes with that flag
+    (fluid_dofs_ic_bc::dof_constraint); neumann/mass flux overrides per side flag
+    (fluid_ic_bc::neumann_*, mass_flux*).
+    """
+
+    def __init__(self, dim: int, tau: int = TAU_2019, dc_2006: bool = True, dc_sharp: float = 2.0,
+                 dc_scale_fact: float = 1.0, steady_state: bool = False,
+                 gravity: Optional[Sequence[float]] = None, p_ref: float = 70.e6, T_ref: float = 1300.0,
+                 v_ref: Sequence[float] = (0.0, 0.0, 0.0)):
+        self.dim = dim
+        d = abi.SetupDesc()
+        d.tau = tau
+        d.dc_2006 = int(dc_2006)
+        d.steady_state = int(steady_state)
+        d.dc_sharp = dc_sharp
+        d.dc_scale_fact = dc_scale_fact
+        g = gravity if gravity is not None else ((0.0, -9.81, 0.0) if dim == 2 else (0.0, 0.0, 0.0))
+        for i in range(3):
+            d.gravity[i] = g[i] if i < len(g) else 0.0
+            d.v_ref[i] = v_ref[i] if i < len(v_ref) else 0.0
+        d.p_ref = p_ref
+        d.T_ref = T_ref
+        self.desc = d
+
+    def dirichlet(self, flag: int, dofs: Sequence[int]) -> "Setup":
+        m = 0
+        for k in dofs:
+            m |= 1 << k
+        self.desc.dirichlet_mask[flag] |= m
+        return self
+
+    def dirichlet_all_flags(self, dofs: Sequence[int]) -> "Setup":
+        for f in range(abi.MAX_FLAGS):
+            self.dirichlet(f, dofs)
+        return self
+
+    def neumann_tau(self, flag: int, k: int, j: int, value: float = 0.0) -> "Setup":
+        lo, hi = min(k, j), max(k, j)
+        bc = self.desc.side_bc[flag]
+        bc.tau_mask |= 1 << (lo * 3 + hi)
+        bc.tau[lo * 3 + hi] = value
+        return self
+
+    def neumann_q(self, flag: int, k: int, value: float = 0.0) -> "Setup":
+        bc = self.desc.side_bc[flag]
+        bc.q_mask |= 1 << k
+        bc.q[k] = value
+        return self
+
+    def neumann_J(self, flag: int, k: int, comp: int, value: float = 0.0) -> "Setup":
+        bc = self.desc.side_bc[flag]
+        bc.J_mask |= 1 << (k * 8 + comp)
+        bc.J[k][comp] = value
+        return self
+
+    def mass_flux(self, flag: int, k: int, value: float) -> "Setup":
+        bc = self.desc.side_bc[flag]
+        bc.mass_flux_mask |= 1 << k
+        bc.mass_flux[k] = value
+        return self
+
+
+def p0_policy(setup: Setup, nb_comp: int, wall_flag: int = 5, dirichlet_T_everywhere: bool = True) -> Setup:
+    """The shipped P0 case's boundary policy (fluid_ic_bc.hpp:84-194):
+    no-slip velocity on nodes with flag 5, T Dirichlet on every node, and on side
+    flag 5 zero heat flux and zero species-0 flux in every direction."""
+    dim = setup.dim
+    setup.dirichlet(wall_flag, list(range(1, 1 + dim)))
+    if dirichlet_T_everywhere:
+        setup.dirichlet_all_flags([dim + 1])
+    for k in range(dim):
+        setup.neumann_q(wall_flag, k, 0.0)
+        if nb_comp > 1:
+            setup.neumann_J(wall_flag, k, 0, 0.0)
+    return setup
+
+
+# ---------------------------------------------------------------------------
+# Mesh
+
+def _ptr(a: Optional[np.ndarray], ctype):
+    if a is None:
+        return C.cast(None, C.POINTER(ctype))
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+@dataclass
+class Mesh:
+    """One-rank mesh: node ids are 0..n_nodes-1 (= node gid).
+
+    Element node order and local side numbering follow element.hpp; bd_sides is
+    an (n, 3) array of (element, local side, side flag > 0).
+    """
+    coords: np.ndarray               # (n_nodes, dim) float64
+    conn: np.ndarray                 # (n_el, nen) int32
+    node_flag: np.ndarray            # (n_nodes,) int32
+    el_on_boundary: np.ndarray       # (n_el,) uint8
+    bd_sides: np.ndarray             # (n_bd, 3) int32
+    name: str = ""
+    _desc: Optional[abi.MeshDesc] = field(default=None, repr=False)
+
+    def __post_init__(self):
+        self.coords = np.ascontiguousarray(self.coords, dtype=np.float64)
+        self.conn = np.ascontiguousarray(self.conn, dtype=np.int32)
+        self.node_flag = np.ascontiguousarray(self.node_flag, dtype=np.int32)
+        self.el_on_boundary = np.ascontiguousarray(self.el_on_boundary, dtype=np.uint8)
+        bd = np.asarray(self.bd_sides, dtype=np.int32).reshape(-1, 3)
+        self._bd_el = np.ascontiguousarray(bd[:, 0])
+        self._bd_loc = np.ascontiguousarray(bd[:, 1])
+        self._bd_flag = np.ascontiguousarray(bd[:, 2])
+        self.bd_sides = bd
+
+    @property
+    def dim(self) -> int:
+        return self.coords.shape[1]
+
+    @property
+    def nen(self) -> int:
+        return self.conn.shape[1]
+
+    @property
+    def n_nodes(self) -> int:
+        return self.coords.shape[0]
+
+    @property
+    def n_elements(self) -> int:
+        return self.conn.shape[0]
+
+    def desc(self) -> abi.MeshDesc:
+        if self._desc is None:
+            d = abi.MeshDesc()
+            d.dim, d.nen = self.dim, self.nen
+            d.n_nodes, d.n_elements = self.n_nodes, self.n_elements
+            d.coords = _ptr(self.coords, C.c_double)
+            d.conn = _ptr(self.conn, C.c_int32)
+            d.node_flag = _ptr(self.node_flag, C.c_int32)
+            d.el_on_boundary = _ptr(self.el_on_boundary, C.c_uint8)
+            d.n_bd_sides = len(self._bd_el)
+            d.bd_side_el = _ptr(self._bd_el, C.c_int32)
+            d.bd_side_local = _ptr(self._bd_loc, C.c_int32)
+            d.bd_side_flag = _ptr(self._bd_flag, C.c_int32)
+            self._desc = d
+        return self._desc
+
+
+def nb_dofs(dim: int, nb_comp: int) -> int:
+    """nb_dofs_f = 2 + dim + nb_comp - 1 (main.cpp:82)."""
+    return 2 + dim + nb_comp - 1
+
+
+# ---------------------------------------------------------------------------
+# Linear system and assembly
+
+def _addr(x) -> int:
+    """Address of a numpy array or a torch tensor (host or device)."""
+    if isinstance(x, np.ndarray):
+        if not x.flags.c_contiguous:
+            raise ValueError("array must be C-contiguous")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return x.data_ptr()
+    raise TypeError(f"unsupported buffer type {type(x)}")
+
+
+class LinearSystem:
+    """linear_system (linear_system.hpp:35-105): CSR matrix A and rhs b.
+
+    row_ptr/col are the one-rank FECrsGraph (sorted global columns per row);
+    vals and rhs are float64 numpy arrays or torch tensors (host or cuda).
+    """
+
+    def __init__(self, row_ptr: np.ndarray, col: np.ndarray, vals=None, rhs=None):
+        self.row_ptr = row_ptr
+        self.col = col
+        n_rows = len(row_ptr) - 1
+        self.vals = vals if vals is not None else np.zeros(int(row_ptr[-1]), dtype=np.float64)
+        self.rhs = rhs if rhs is not None else np.zeros(n_rows, dtype=np.float64)
+
+    @property
+    def n_rows(self) -> int:
+        return len(self.row_ptr) - 1
+
+    def matrix_scipy(self):
+        import scipy.sparse as sp
+        vals = self.vals if isinstance(self.vals, np.ndarray) else self.vals.detach().cpu().numpy()
+        return sp.csr_matrix((vals, self.col, self.row_ptr), shape=(self.n_rows, self.n_rows))
+
+    def clear(self):
+        """linear_system::clear (linear_system.hpp:90-94); execute() does this itself."""
+        self.vals[...] = 0.0 if isinstance(self.vals, np.ndarray) else self.vals.zero_()
+        self.rhs[...] = 0.0 if isinstance(self.rhs, np.ndarray) else self.rhs.zero_()
+
+
+class FluidAssembly:
+    """fluid_assembly<fluid<ic_bc,dim>, scatter<dofs_ic_bc>, dim> on one GPU.
+
+    The constructor also does what linear_system's constructor (graph build) and
+    the fluid integral's constructor (u_ref_inv) do in the reference.
+    """
+
+    def __init__(self, mesh: Mesh, material: Material, setup: Setup, device: int = 0):
+        self.mesh, self.material, self.setup = mesh, material, setup
+        self.dim = mesh.dim
+        self.nb_comp = material.nb_comp
+        self.nd = nb_dofs(self.dim, self.nb_comp)
+        self.n_rows = mesh.n_nodes * self.nd
+        L = abi.lib()
+        h = C.c_void_p()
+        rc = L.gales_asm_create(C.byref(mesh.desc()), C.byref(material.desc), C.byref(setup.desc), device,
+                                C.byref(h))
+        if rc != 0:
+            raise GalesError(rc, "gales_asm_create failed (see stderr)")
+        self._h = h
+        self._L = L
+        self.last_seconds = 0.0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gales_asm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            fb = C.c_int64(-1)
+            self._L.gales_asm_status(self._h, C.byref(fb))
+            raise GalesError(rc, self._L.gales_asm_last_error(self._h).decode(), fb.value)
+
+    # pattern / graph / colouring
+    def pattern(self):
+        n_rows, nnz = C.c_int64(), C.c_int64()
+        rp, cl = C.POINTER(C.c_int64)(), C.POINTER(C.c_int32)()
+        self._check(self._L.gales_asm_pattern(self._h, C.byref(n_rows), C.byref(nnz), C.byref(rp), C.byref(cl)))
+        row_ptr = np.ctypeslib.as_array(rp, shape=(n_rows.value + 1,)).copy()
+        col = np.ctypeslib.as_array(cl, shape=(nnz.value,)).copy() if nnz.value else np.zeros(0, np.int32)
+        return row_ptr, col
+
+    def nnz(self) -> int:
+        n, nn = C.c_int64(), C.c_int64()
+        self._check(self._L.gales_asm_node_graph(self._h, C.byref(n), C.byref(nn), None, None))
+        return nn.value * self.nd * self.nd
+
+    def node_graph(self):
+        n, nn = C.c_int64(), C.c_int64()
+        rp, cl = C.POINTER(C.c_int64)(), C.POINTER(C.c_int32)()
+        self._check(self._L.gales_asm_node_graph(self._h, C.byref(n), C.byref(nn), C.byref(rp), C.byref(cl)))
+        return (np.ctypeslib.as_array(rp, shape=(n.value + 1,)).copy(),
+                np.ctypeslib.as_array(cl, shape=(nn.value,)).copy())
+
+    def colouring(self):
+        nc = C.c_int32()
+        cp = C.POINTER(C.c_int32)()
+        self._check(self._L.gales_asm_colouring(self._h, C.byref(nc), C.byref(cp)))
+        return np.ctypeslib.as_array(cp, shape=(self.mesh.n_elements,)).copy(), nc.value
+
+    def linear_system(self, device=None) -> LinearSystem:
+        row_ptr, col = self.pattern()
+        if device is None:
+            return LinearSystem(row_ptr, col)
+        import torch
+        vals = torch.zeros(int(row_ptr[-1]), dtype=torch.float64, device=device)
+        rhs = torch.zeros(len(row_ptr) - 1, dtype=torch.float64, device=device)
+        return LinearSystem(row_ptr, col, vals, rhs)
+
+    def set_scatter(self, mode: int):
+        self._check(self._L.gales_asm_set_scatter(self._h, mode))
+
+    # the hot path
+    def execute(self, I, P, dt: float, lp: LinearSystem, form: int = FORM_FP64, stream: int = 0) -> float:
+        """fluid_assembly::execute(): fill lp.vals and lp.rhs; returns wall seconds."""
+        t0 = time.perf_counter()
+        self._check(self._L.gales_asm_assemble(self._h, _addr(I), _addr(P), float(dt), form, _addr(lp.vals),
+                                               _addr(lp.rhs), stream or None))
+        self.last_seconds = time.perf_counter() - t0
+        return self.last_seconds
+
+    def residual(self, I, P, dt: float, rhs, form: int = FORM_FP64, stream: int = 0) -> float:
+        t0 = time.perf_counter()
+        self._check(self._L.gales_asm_residual(self._h, _addr(I), _addr(P), float(dt), form, _addr(rhs),
+                                               stream or None))
+        return time.perf_counter() - t0
+
+    def vjp(self, I, P, dt: float, lam, mode: int, g_state, g_params=None, stream: int = 0):
+        self._check(self._L.gales_asm_vjp(self._h, _addr(I), _addr(P), float(dt), _addr(lam), mode,
+                                          _addr(g_state), _addr(g_params) if g_params is not None else None,
+                                          stream or None))
+
+    def element_blocks(self, I, P, dt: float, elements, which: int = 0, form: int = FORM_FP64,
+                       want_matrix: bool = True):
+        """Batched fluid::execute_i (which=0) / execute_b (which=1): local (m, r) per element."""
+        el = np.ascontiguousarray(elements, dtype=np.int32)
+        N = self.mesh.nen * self.nd
+        m = np.zeros((len(el), N, N)) if want_matrix else None
+        r = np.zeros((len(el), N))
+        self._check(self._L.gales_asm_element_blocks(self._h, _addr(I), _addr(P), float(dt), form, which,
+                                                     el.ctypes.data_as(C.POINTER(C.c_int32)), len(el),
+                                                     _addr(m) if want_matrix else None, _addr(r), None))
+        return m, r
+
+    def device_ms(self) -> float:
+        return self._L.gales_asm_last_ms(self._h)
+
+    def launch_count(self) -> int:
+        return self._L.gales_asm_launch_count(self._h)
+
+
+class ResidualCheck:
+    """residual_check (residual_check.hpp:42-80): ||b||_2 against iteration 0."""
+
+    def __init__(self):
+        self.res0 = 0.0
+
+    def execute(self, b, it_count: int):
+        n = float(np.linalg.norm(np.asarray(b if isinstance(b, np.ndarray) else b.detach().cpu().numpy())))
+        if it_count == 0:
+            self.res0 = n
+            return False, n
+        rel = n / self.res0 if self.res0 else math.inf
+        return n <= max(1.e-8 * self.res0, 1.e-5), rel
+
+
+__all__ = [
+    "abi", "GalesError", "custom_chemical", "ideal_gas", "ideal_gas_named", "ideal_gas_params", "Material",
+    "Setup", "p0_policy", "Mesh", "nb_dofs", "LinearSystem", "FluidAssembly", "ResidualCheck",
+    "FORM_FP64", "FORM_MIXED", "TAU_NONE", "TAU_2001", "TAU_2019", "TAU_2007", "TAU_2014",
+    "VJP_EXACT", "VJP_FROZEN", "SCATTER_ATOMIC", "SCATTER_COLOURED",
+]

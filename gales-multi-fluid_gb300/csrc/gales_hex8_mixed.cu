@@ -1,0 +1,13 @@
+// Kernel instances for the hex8 element (dim 3, 8 nodes, 8 interior points,
+// 6 sides with 4 points each; element.hpp gauss_data tables).
+#include "gales_launch.cuh"
+
+namespace gales {
+
+using D_hex8 = ElementDispatch<3, 8, 8, 6, 4>;
+
+LaunchResult interior_hex8_mixed(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
+  return D_hex8::interior<GALES_FORM_MIXED>(k, nc, want_m, n, st);
+}
+
+}  // namespace gales

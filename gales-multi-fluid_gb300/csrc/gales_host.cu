@@ -1,0 +1,861 @@
+// Host side of the C ABI declared in include/gales_asm.h.
+//
+// The handle replaces, for one rank and one GPU, the objects the reference's
+// assembly reads and fills: linear_system's FECrsGraph (linear_system.hpp:40-66),
+// the per-element dof gids of scatter::execute (scatter.hpp:44-57), the Dirichlet
+// policy of fluid_dofs_ic_bc (fluid_dofs_ic_bc.hpp:86-117) and the fluid
+// integral's constructor state (u_ref_inv, fluid_2d.hpp:123-135).  Everything the
+// kernels read lives in device memory owned by the handle; the caller owns the
+// state and output buffers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/gales_asm.h"
+#include "gales_launch.cuh"
+
+using namespace gales;
+
+namespace {
+
+struct ElemInfo {
+  int nq, nsides, nsn, nqs;
+  double gp[8][3];
+  double sgp[6][4][3];
+  double W_in, W_bd;
+};
+
+// Gauss tables of element.hpp:63-176 (2D) and 360-477 (3D), weights of
+// quad.hpp:165-186 and 497-513.
+bool elem_info(int dim, int nen, ElemInfo& o) {
+  memset(&o, 0, sizeof(o));
+  if (dim == 2 && nen == 3) {
+    o.nq = 3; o.nsides = 3; o.nsn = 2; o.nqs = 2;
+    const double g[3][2] = {{1.0 / 6.0, 1.0 / 6.0}, {4.0 / 6.0, 1.0 / 6.0}, {1.0 / 6.0, 4.0 / 6.0}};
+    for (int i = 0; i < 3; ++i) { o.gp[i][0] = g[i][0]; o.gp[i][1] = g[i][1]; }
+    const double gm = 0.5 * (1.0 - 1.0 / sqrt(3.0)), gpl = 0.5 * (1.0 + 1.0 / sqrt(3.0));
+    const double s[3][2][2] = {{{gpl, 1.0 - gpl}, {gm, 1.0 - gm}}, {{0.0, gpl}, {0.0, gm}}, {{gm, 0.0}, {gpl, 0.0}}};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 2; ++j) { o.sgp[i][j][0] = s[i][j][0]; o.sgp[i][j][1] = s[i][j][1]; }
+    o.W_in = 1.0 / 6.0; o.W_bd = 1.0 / 2.0;
+    return true;
+  }
+  if (dim == 2 && nen == 4) {
+    o.nq = 4; o.nsides = 4; o.nsn = 2; o.nqs = 2;
+    const double gm = -1.0 / sqrt(3.0), gpl = 1.0 / sqrt(3.0);
+    const double g[4][2] = {{gm, gm}, {gpl, gm}, {gpl, gpl}, {gm, gpl}};
+    for (int i = 0; i < 4; ++i) { o.gp[i][0] = g[i][0]; o.gp[i][1] = g[i][1]; }
+    const double s[4][2][2] = {{{gm, -1.0}, {gpl, -1.0}}, {{1.0, gm}, {1.0, gpl}},
+                               {{gpl, 1.0}, {gm, 1.0}}, {{-1.0, gpl}, {-1.0, gm}}};
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 2; ++j) { o.sgp[i][j][0] = s[i][j][0]; o.sgp[i][j][1] = s[i][j][1]; }
+    o.W_in = 1.0; o.W_bd = 1.0;
+    return true;
+  }
+  if (dim == 3 && nen == 4) {
+    o.nq = 4; o.nsides = 4; o.nsn = 3; o.nqs = 3;
+    const double a = 0.1381966011250105, b = 0.5854101966249685;
+    const double g[4][3] = {{a, a, a}, {b, a, a}, {a, b, a}, {a, a, b}};
+    for (int i = 0; i < 4; ++i)
+      for (int d = 0; d < 3; ++d) o.gp[i][d] = g[i][d];
+    const double t = 1.0 / 6.0, f = 4.0 / 6.0;
+    const double s[4][3][3] = {{{f, t, t}, {t, f, t}, {t, t, f}},
+                               {{0.0, t, t}, {0.0, t, f}, {0.0, f, t}},
+                               {{t, 0.0, t}, {f, 0.0, t}, {t, 0.0, f}},
+                               {{t, t, 0.0}, {t, f, 0.0}, {f, t, 0.0}}};
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int d = 0; d < 3; ++d) o.sgp[i][j][d] = s[i][j][d];
+    o.W_in = 1.0 / 24.0; o.W_bd = 1.0 / 6.0;
+    return true;
+  }
+  if (dim == 3 && nen == 8) {
+    o.nq = 8; o.nsides = 6; o.nsn = 4; o.nqs = 4;
+    const double m = -1.0 / sqrt(3.0), p = 1.0 / sqrt(3.0);
+    const double g[8][3] = {{m, m, m}, {p, m, m}, {p, p, m}, {m, p, m}, {m, m, p}, {p, m, p}, {p, p, p}, {m, p, p}};
+    for (int i = 0; i < 8; ++i)
+      for (int d = 0; d < 3; ++d) o.gp[i][d] = g[i][d];
+    const double s[6][4][3] = {{{m, m, 1.0}, {p, m, 1.0}, {p, p, 1.0}, {m, p, 1.0}},
+                               {{m, m, -1.0}, {m, p, -1.0}, {p, p, -1.0}, {p, m, -1.0}},
+                               {{-1.0, m, m}, {-1.0, m, p}, {-1.0, p, p}, {-1.0, p, m}},
+                               {{1.0, m, m}, {1.0, p, m}, {1.0, p, p}, {1.0, m, p}},
+                               {{p, 1.0, m}, {m, 1.0, m}, {m, 1.0, p}, {p, 1.0, p}},
+                               {{p, -1.0, m}, {p, -1.0, p}, {m, -1.0, p}, {m, -1.0, m}}};
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 4; ++j)
+        for (int d = 0; d < 3; ++d) o.sgp[i][j][d] = s[i][j][d];
+    o.W_in = 1.0; o.W_bd = 1.0;
+    return true;
+  }
+  return false;
+}
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+int hw_threads() {
+  unsigned n = std::thread::hardware_concurrency();
+  return n == 0 ? 1 : (int)std::min(n, 32u);
+}
+
+template <typename F>
+void parallel_for(int64_t n, F f) {
+  const int nt = (int)std::min<int64_t>(hw_threads(), std::max<int64_t>(1, n / 4096));
+  if (nt <= 1) {
+    f(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int64_t chunk = (n + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    const int64_t lo = t * chunk, hi = std::min(n, lo + chunk);
+    if (lo >= hi) break;
+    th.emplace_back([=] { f(lo, hi); });
+  }
+  for (auto& x : th) x.join();
+}
+
+}  // namespace
+
+struct gales_asm {
+  int device = 0;
+  int dim = 0, nen = 0, nc = 0, nd = 0;
+  int64_t n_nodes = 0, n_el = 0, n_rows = 0, nnz = 0, nnz_nodes = 0;
+  ElemInfo ei;
+  gales_material_desc mat;
+  gales_setup_desc setup;
+  double u_ref_inv[GALES_MAX_ND];
+  // host copies
+  std::vector<int32_t> conn;
+  std::vector<int32_t> node_flag;
+  std::vector<int64_t> node_rp;
+  std::vector<int32_t> node_col;
+  std::vector<int64_t> row_ptr;   // scalar CSR, built on request
+  std::vector<int32_t> col;
+  std::vector<int32_t> colour;
+  int32_t n_colours = 0;
+  std::vector<int32_t> colour_order;  // elements sorted by colour
+  std::vector<int64_t> colour_off;
+  std::vector<int32_t> bd_list;
+  std::vector<int8_t> bd_sides;
+  std::vector<int8_t> el_sides;  // side flags of every element [n_el][nsides]
+  // device
+  DevBuf<double> d_coords;
+  DevBuf<int32_t> d_conn, d_node_flag, d_colour_order, d_bd_list;
+  DevBuf<int64_t> d_node_rp;
+  DevBuf<uint16_t> d_slot;
+  DevBuf<int8_t> d_bd_sides;
+  DevBuf<gales_side_bc> d_side_bc;
+  DevBuf<unsigned int> d_status;
+  DevBuf<unsigned long long> d_first_bad;
+  DevBuf<double> s_I, s_P, s_vals, s_rhs, s_aux;  // staging for host pointers
+  unsigned int* h_status = nullptr;              // pinned
+  unsigned long long* h_first_bad = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int32_t scatter_mode = GALES_SCATTER_ATOMIC;
+  int status = 0;
+  int64_t first_bad = -1;
+  double last_ms = 0.0;
+  int64_t launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(gales_asm* h, int code, const std::string& msg) {
+  if (h) {
+    h->err = msg;
+    h->status = code;
+  }
+  return code;
+}
+
+int cuda_fail(gales_asm* h, cudaError_t e, const char* what) {
+  return fail(h, GALES_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(h, call, what)                          \
+  do {                                             \
+    cudaError_t e__ = (call);                      \
+    if (e__ != cudaSuccess) return cuda_fail(h, e__, what); \
+  } while (0)
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Reference fluid properties at the dc_2006 reference state (fluid_2d.hpp:123-135):
+// props at (p_ref, T_ref, Y = 0.5 for every component), U at v_ref.
+void compute_u_ref_inv(gales_asm* h) {
+  for (int i = 0; i < GALES_MAX_ND; ++i) h->u_ref_inv[i] = 0.0;
+  if (!h->setup.dc_2006) return;
+  const int nc = h->nc, dim = h->dim;
+  const double p = h->setup.p_ref, T = h->setup.T_ref;
+  double rho = 0.0, cv = 0.0;
+  for (int c = 0; c < nc; ++c) {
+    const gales_chemical_desc& q = h->mat.comp[c];
+    double r, v;
+    if (q.kind == GALES_CH_CUSTOM) {
+      r = q.rho;
+      v = (q.beta == 0.0) ? q.cp : q.cp - T * q.alpha * q.alpha / (r * q.beta);
+    } else {
+      r = p / (q.R * T);
+      v = q.cv;
+    }
+    rho += 0.5 / r;
+    cv += 0.5 * v;
+  }
+  rho = 1. / rho;
+  double v2 = 0.0;
+  for (int k = 0; k < dim; ++k) v2 += h->setup.v_ref[k] * h->setup.v_ref[k];
+  const double E = cv * T + 0.5 * (v2);
+  double u[GALES_MAX_ND];
+  u[0] = rho;
+  for (int k = 0; k < dim; ++k) u[1 + k] = rho * h->setup.v_ref[k];
+  u[dim + 1] = rho * E;
+  for (int i = 0; i < nc - 1; ++i) u[dim + 2 + i] = rho * 0.5;
+  for (int i = 0; i < h->nd; ++i) h->u_ref_inv[i] = (u[i] < DBL_EPSILON) ? 0.0 : 1.0 / u[i];
+}
+
+// Node graph of linear_system.hpp:46-63 on one rank: sorted unique neighbours.
+void build_graph(gales_asm* h) {
+  const int nen = h->nen;
+  const int64_t nn = h->n_nodes, ne = h->n_el;
+  std::vector<int64_t> cnt(nn + 1, 0);
+  for (int64_t e = 0; e < ne; ++e)
+    for (int a = 0; a < nen; ++a) cnt[h->conn[e * nen + a] + 1] += 1;
+  for (int64_t i = 0; i < nn; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int64_t> el_of(cnt[nn]);
+  {
+    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t e = 0; e < ne; ++e)
+      for (int a = 0; a < nen; ++a) el_of[fill[h->conn[e * nen + a]]++] = e;
+  }
+  std::vector<int32_t> deg(nn, 0);
+  std::vector<std::vector<int32_t>> rows(nn);
+  parallel_for(nn, [&](int64_t lo, int64_t hi) {
+    std::vector<int32_t> tmp;
+    for (int64_t i = lo; i < hi; ++i) {
+      tmp.clear();
+      for (int64_t t = cnt[i]; t < cnt[i + 1]; ++t) {
+        const int64_t e = el_of[t];
+        for (int b = 0; b < nen; ++b) tmp.push_back(h->conn[e * nen + b]);
+      }
+      std::sort(tmp.begin(), tmp.end());
+      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+      rows[i] = tmp;
+      deg[i] = (int32_t)tmp.size();
+    }
+  });
+  h->node_rp.assign(nn + 1, 0);
+  for (int64_t i = 0; i < nn; ++i) h->node_rp[i + 1] = h->node_rp[i] + deg[i];
+  h->nnz_nodes = h->node_rp[nn];
+  h->node_col.resize(h->nnz_nodes);
+  parallel_for(nn, [&](int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; ++i) {
+      std::copy(rows[i].begin(), rows[i].end(), h->node_col.begin() + h->node_rp[i]);
+      std::vector<int32_t>().swap(rows[i]);
+    }
+  });
+  h->nnz = h->nnz_nodes * (int64_t)h->nd * h->nd;
+}
+
+// Greedy colouring in element order (the oracle states the same rule).
+void build_colouring(gales_asm* h) {
+  const int nen = h->nen;
+  const int64_t nn = h->n_nodes, ne = h->n_el;
+  std::vector<int64_t> cnt(nn + 1, 0);
+  for (int64_t e = 0; e < ne; ++e)
+    for (int a = 0; a < nen; ++a) cnt[h->conn[e * nen + a] + 1] += 1;
+  for (int64_t i = 0; i < nn; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int64_t> el_of(cnt[nn]);
+  {
+    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t e = 0; e < ne; ++e)
+      for (int a = 0; a < nen; ++a) el_of[fill[h->conn[e * nen + a]]++] = e;
+  }
+  h->colour.assign(ne, -1);
+  std::vector<int64_t> mark(64, -1);
+  int32_t ncol = 0;
+  for (int64_t e = 0; e < ne; ++e) {
+    for (int a = 0; a < nen; ++a) {
+      const int32_t n = h->conn[e * nen + a];
+      for (int64_t t = cnt[n]; t < cnt[n + 1]; ++t) {
+        const int32_t c = h->colour[el_of[t]];
+        if (c >= 0) {
+          if ((size_t)c >= mark.size()) mark.resize(2 * c + 1, -1);
+          mark[c] = e;
+        }
+      }
+    }
+    int32_t c = 0;
+    while ((size_t)c < mark.size() && mark[c] == e) ++c;
+    if ((size_t)c >= mark.size()) mark.resize(2 * c + 1, -1);
+    h->colour[e] = c;
+    ncol = std::max(ncol, c + 1);
+  }
+  h->n_colours = ncol;
+  h->colour_off.assign(ncol + 1, 0);
+  for (int64_t e = 0; e < ne; ++e) h->colour_off[h->colour[e] + 1] += 1;
+  for (int c = 0; c < ncol; ++c) h->colour_off[c + 1] += h->colour_off[c];
+  h->colour_order.resize(ne);
+  std::vector<int64_t> fill(h->colour_off.begin(), h->colour_off.end() - 1);
+  for (int64_t e = 0; e < ne; ++e) h->colour_order[fill[h->colour[e]]++] = (int32_t)e;
+}
+
+int validate(gales_asm* h, const gales_mesh_desc* m, const gales_material_desc* mat,
+             const gales_setup_desc* s) {
+  if (!m || !mat || !s) return fail(h, GALES_ERR_BAD_INPUT, "null descriptor");
+  if (!elem_info(m->dim, m->nen, h->ei))
+    return fail(h, GALES_ERR_UNSUPPORTED, "unsupported element (dim, nen)");
+  if (mat->nb_comp < 1 || mat->nb_comp > 4)
+    return fail(h, GALES_ERR_UNSUPPORTED, "nb_comp must be 1..4");
+  if (m->n_nodes <= 0 || m->n_elements < 0 || !m->coords || (!m->conn && m->n_elements > 0))
+    return fail(h, GALES_ERR_BAD_INPUT, "empty or null mesh arrays");
+  if (m->n_nodes >= INT32_MAX) return fail(h, GALES_ERR_BAD_INPUT, "n_nodes exceeds int32 node ids");
+  for (int64_t i = 0; i < m->n_elements * m->nen; ++i)
+    if (m->conn[i] < 0 || m->conn[i] >= m->n_nodes)
+      return fail(h, GALES_ERR_BAD_INPUT, "connectivity entry out of range at " + std::to_string(i));
+  if (m->n_bd_sides > 0 && (!m->bd_side_el || !m->bd_side_local || !m->bd_side_flag))
+    return fail(h, GALES_ERR_BAD_INPUT, "null boundary side arrays");
+  for (int64_t i = 0; i < m->n_bd_sides; ++i) {
+    if (m->bd_side_el[i] < 0 || m->bd_side_el[i] >= m->n_elements)
+      return fail(h, GALES_ERR_BAD_INPUT, "boundary side element out of range");
+    if (m->bd_side_local[i] < 0 || m->bd_side_local[i] >= h->ei.nsides)
+      return fail(h, GALES_ERR_BAD_INPUT, "boundary side local index out of range");
+    if (m->bd_side_flag[i] <= 0 || m->bd_side_flag[i] >= GALES_MAX_FLAGS)
+      return fail(h, GALES_ERR_BAD_INPUT, "boundary side flag must be in 1..31");
+  }
+  for (int c = 0; c < mat->nb_comp; ++c) {
+    const int k = mat->comp[c].kind;
+    if (k != GALES_CH_CUSTOM && k != GALES_CH_IDEAL_GAS)
+      return fail(h, GALES_ERR_UNSUPPORTED, "unknown chemical kind");
+  }
+  const int t = s->tau;
+  if (t != GALES_TAU_NONE && t != 2001 && t != 2019 && t != 2007 && t != 2014)
+    return fail(h, GALES_ERR_BAD_INPUT, "unknown tau variant");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gales_chemical_custom(gales_chemical_desc* c, double rho, double mu, double cp, double kappa,
+                           double alpha, double beta) {
+  memset(c, 0, sizeof(*c));
+  c->kind = GALES_CH_CUSTOM;
+  c->rho = rho; c->mu = mu; c->cp = cp; c->kappa = kappa; c->alpha = alpha; c->beta = beta;
+  c->cv = cp;
+  c->chemical_diffusivity = 1.e-10;
+}
+
+void gales_chemical_ideal_gas(gales_chemical_desc* c, double molar_mass, double gamma) {
+  memset(c, 0, sizeof(*c));
+  c->kind = GALES_CH_IDEAL_GAS;
+  c->R = 8.314462 / molar_mass;
+  c->gamma = gamma;
+  c->cv = c->R / (gamma - 1.0);
+  c->cp = gamma * c->cv;
+  c->mu = 1.e-5;
+  c->kappa = c->mu * c->cp / 0.72;
+  c->chemical_diffusivity = 1.e-10;
+}
+
+void gales_setup_default(gales_setup_desc* s, int32_t dim) {
+  memset(s, 0, sizeof(*s));
+  s->tau = GALES_TAU_NON_DIAG_COMP_2019;
+  s->dc_2006 = 1;
+  s->steady_state = 0;
+  s->dc_sharp = 2.0;
+  s->dc_scale_fact = 1.0;
+  if (dim == 2) s->gravity[1] = -9.81;
+  s->p_ref = 70.e6;
+  s->T_ref = 1300.0;
+}
+
+int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
+                     const gales_setup_desc* s, int device, gales_asm** out) {
+  if (!out) return GALES_ERR_BAD_INPUT;
+  *out = nullptr;
+  gales_asm* h = new gales_asm();
+  int rc = validate(h, m, mat, s);
+  if (rc) {
+    // keep the message reachable through a handle-less error path
+    fprintf(stderr, "gales_asm_create: %s\n", h->err.c_str());
+    delete h;
+    return rc;
+  }
+  h->device = device;
+  h->dim = m->dim; h->nen = m->nen; h->nc = mat->nb_comp;
+  h->nd = 2 + h->dim + h->nc - 1;
+  h->n_nodes = m->n_nodes; h->n_el = m->n_elements;
+  h->n_rows = h->n_nodes * h->nd;
+  h->mat = *mat;
+  h->setup = *s;
+  h->conn.assign(m->conn, m->conn + m->n_elements * m->nen);
+  h->node_flag.assign(h->n_nodes, 0);
+  if (m->node_flag) std::copy(m->node_flag, m->node_flag + h->n_nodes, h->node_flag.begin());
+  compute_u_ref_inv(h);
+  build_graph(h);
+  // per-element slot table: position of node a within node b's graph row
+  std::vector<uint16_t> slot((size_t)h->n_el * h->nen * h->nen);
+  bool slot_ok = true;
+  for (int64_t i = 0; i < h->n_nodes; ++i)
+    if (h->node_rp[i + 1] - h->node_rp[i] > 65535) slot_ok = false;
+  if (!slot_ok) {
+    int code = fail(h, GALES_ERR_UNSUPPORTED, "node degree above 65535");
+    fprintf(stderr, "gales_asm_create: %s\n", h->err.c_str());
+    delete h;
+    return code;
+  }
+  {
+    const int nen = h->nen;
+    parallel_for(h->n_el, [&](int64_t lo, int64_t hi) {
+      for (int64_t e = lo; e < hi; ++e)
+        for (int b = 0; b < nen; ++b) {
+          const int32_t nb = h->conn[e * nen + b];
+          const int32_t* r0 = h->node_col.data() + h->node_rp[nb];
+          const int32_t* r1 = h->node_col.data() + h->node_rp[nb + 1];
+          for (int a = 0; a < nen; ++a) {
+            const int32_t na = h->conn[e * nen + a];
+            slot[((size_t)e * nen + b) * nen + a] = (uint16_t)(std::lower_bound(r0, r1, na) - r0);
+          }
+        }
+    });
+  }
+  build_colouring(h);
+  // boundary elements (fluid_assembly.hpp:57) and their side flags (mesh.hpp:409-446)
+  {
+    std::vector<int32_t> pos(h->n_el, -1);
+    if (m->el_on_boundary)
+      for (int64_t e = 0; e < h->n_el; ++e)
+        if (m->el_on_boundary[e]) {
+          pos[e] = (int32_t)h->bd_list.size();
+          h->bd_list.push_back((int32_t)e);
+        }
+    h->bd_sides.assign(h->bd_list.size() * h->ei.nsides, 0);
+    h->el_sides.assign((size_t)h->n_el * h->ei.nsides, 0);
+    for (int64_t i = 0; i < m->n_bd_sides; ++i)
+      h->el_sides[(size_t)m->bd_side_el[i] * h->ei.nsides + m->bd_side_local[i]] = (int8_t)m->bd_side_flag[i];
+    for (int64_t i = 0; i < m->n_bd_sides; ++i) {
+      const int32_t e = m->bd_side_el[i];
+      if (pos[e] >= 0) h->bd_sides[(size_t)pos[e] * h->ei.nsides + m->bd_side_local[i]] = (int8_t)m->bd_side_flag[i];
+    }
+  }
+  cudaError_t ce = cudaSetDevice(device);
+  auto bail = [&](cudaError_t e, const char* what) {
+    fprintf(stderr, "gales_asm_create: %s: %s\n", what, cudaGetErrorString(e));
+    gales_asm_destroy(h);
+    return GALES_ERR_CUDA;
+  };
+  if (ce != cudaSuccess) return bail(ce, "cudaSetDevice");
+#define UP(buf, src, count, what)                                                              \
+  do {                                                                                         \
+    cudaError_t e_ = buf.alloc(count);                                                         \
+    if (e_ != cudaSuccess) return bail(e_, what);                                              \
+    if ((count) > 0) {                                                                         \
+      e_ = cudaMemcpy(buf.p, src, (count) * sizeof(*buf.p), cudaMemcpyHostToDevice);           \
+      if (e_ != cudaSuccess) return bail(e_, what);                                            \
+    }                                                                                          \
+  } while (0)
+  UP(h->d_coords, m->coords, (size_t)h->n_nodes * h->dim, "coords");
+  UP(h->d_conn, h->conn.data(), h->conn.size(), "conn");
+  UP(h->d_node_flag, h->node_flag.data(), h->node_flag.size(), "node_flag");
+  UP(h->d_node_rp, h->node_rp.data(), h->node_rp.size(), "node_rp");
+  UP(h->d_slot, slot.data(), slot.size(), "slot");
+  UP(h->d_colour_order, h->colour_order.data(), h->colour_order.size(), "colour_order");
+  UP(h->d_bd_list, h->bd_list.data(), h->bd_list.size(), "bd_list");
+  UP(h->d_bd_sides, h->bd_sides.data(), h->bd_sides.size(), "bd_sides");
+  UP(h->d_side_bc, h->setup.side_bc, (size_t)GALES_MAX_FLAGS, "side_bc");
+#undef UP
+  if ((ce = h->d_status.alloc(1)) != cudaSuccess) return bail(ce, "status");
+  if ((ce = h->d_first_bad.alloc(1)) != cudaSuccess) return bail(ce, "first_bad");
+  if ((ce = cudaMallocHost(&h->h_status, sizeof(unsigned int))) != cudaSuccess) return bail(ce, "pinned");
+  if ((ce = cudaMallocHost(&h->h_first_bad, sizeof(unsigned long long))) != cudaSuccess) return bail(ce, "pinned");
+  if ((ce = cudaEventCreate(&h->ev0)) != cudaSuccess) return bail(ce, "event");
+  if ((ce = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(ce, "event");
+  *out = h;
+  return 0;
+}
+
+void gales_asm_destroy(gales_asm* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  h->d_coords.release(); h->d_conn.release(); h->d_node_flag.release();
+  h->d_colour_order.release(); h->d_bd_list.release(); h->d_node_rp.release();
+  h->d_slot.release(); h->d_bd_sides.release(); h->d_side_bc.release();
+  h->d_status.release(); h->d_first_bad.release();
+  h->s_I.release(); h->s_P.release(); h->s_vals.release(); h->s_rhs.release(); h->s_aux.release();
+  if (h->h_status) cudaFreeHost(h->h_status);
+  if (h->h_first_bad) cudaFreeHost(h->h_first_bad);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  delete h;
+}
+
+int gales_asm_pattern(gales_asm* h, int64_t* n_rows, int64_t* nnz, const int64_t** row_ptr,
+                      const int32_t** col) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (h->nnz > INT64_MAX / 2) return fail(h, GALES_ERR_UNSUPPORTED, "nnz overflow");
+  if (h->row_ptr.empty()) {
+    const int nd = h->nd;
+    if ((int64_t)h->n_nodes * nd > INT32_MAX) return fail(h, GALES_ERR_UNSUPPORTED, "column ids exceed int32");
+    h->row_ptr.resize(h->n_rows + 1);
+    h->col.resize(h->nnz);
+    h->row_ptr[0] = 0;
+    for (int64_t i = 0; i < h->n_nodes; ++i) {
+      const int64_t deg = h->node_rp[i + 1] - h->node_rp[i];
+      for (int k = 0; k < nd; ++k) h->row_ptr[i * nd + k + 1] = h->node_rp[i] * nd * nd + (k + 1) * deg * nd;
+    }
+    parallel_for(h->n_nodes, [&](int64_t lo, int64_t hi) {
+      for (int64_t i = lo; i < hi; ++i)
+        for (int k = 0; k < nd; ++k) {
+          int64_t p = h->row_ptr[i * nd + k];
+          for (int64_t t = h->node_rp[i]; t < h->node_rp[i + 1]; ++t)
+            for (int kk = 0; kk < nd; ++kk) h->col[p++] = h->node_col[t] * nd + kk;
+        }
+    });
+  }
+  if (n_rows) *n_rows = h->n_rows;
+  if (nnz) *nnz = h->nnz;
+  if (row_ptr) *row_ptr = h->row_ptr.data();
+  if (col) *col = h->col.data();
+  return 0;
+}
+
+int gales_asm_node_graph(gales_asm* h, int64_t* n_nodes, int64_t* nnz_nodes, const int64_t** node_row_ptr,
+                         const int32_t** node_col) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (n_nodes) *n_nodes = h->n_nodes;
+  if (nnz_nodes) *nnz_nodes = h->nnz_nodes;
+  if (node_row_ptr) *node_row_ptr = h->node_rp.data();
+  if (node_col) *node_col = h->node_col.data();
+  return 0;
+}
+
+int gales_asm_colouring(gales_asm* h, int32_t* n_colours, const int32_t** colour) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (n_colours) *n_colours = h->n_colours;
+  if (colour) *colour = h->colour.data();
+  return 0;
+}
+
+int gales_asm_set_scatter(gales_asm* h, int32_t mode) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (mode != GALES_SCATTER_ATOMIC && mode != GALES_SCATTER_COLOURED)
+    return fail(h, GALES_ERR_BAD_INPUT, "unknown scatter mode");
+  h->scatter_mode = mode;
+  return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+KParams base_params(gales_asm* h, double dt) {
+  KParams k;
+  memset(&k, 0, sizeof(k));
+  for (int c = 0; c < h->nc; ++c) {
+    const gales_chemical_desc& q = h->mat.comp[c];
+    DevChem& d = k.ch[c];
+    d.kind = q.kind;
+    d.rho = q.rho; d.mu = q.mu; d.cp = q.cp; d.cv = q.cv; d.kappa = q.kappa;
+    d.alpha = q.alpha; d.beta = q.beta; d.R = q.R; d.gamma = q.gamma; d.D = q.chemical_diffusivity;
+  }
+  k.dt = dt;
+  k.dc_sharp = h->setup.dc_sharp;
+  k.dc_scale = h->setup.dc_scale_fact;
+  for (int d = 0; d < 3; ++d) k.gravity[d] = h->setup.gravity[d];
+  for (int i = 0; i < GALES_MAX_ND; ++i) k.u_ref_inv[i] = h->u_ref_inv[i];
+  memcpy(k.gp, h->ei.gp, sizeof(k.gp));
+  memcpy(k.sgp, h->ei.sgp, sizeof(k.sgp));
+  k.W_in = h->ei.W_in;
+  k.W_bd = h->ei.W_bd;
+  k.tau = h->setup.tau;
+  k.dc_2006 = h->setup.dc_2006;
+  k.steady = h->setup.steady_state;
+  k.n_sides = h->ei.nsides;
+  k.n_side_nodes = h->ei.nsn;
+  k.n_side_q = h->ei.nqs;
+  for (int i = 0; i < GALES_MAX_FLAGS; ++i) k.dirichlet_mask[i] = h->setup.dirichlet_mask[i];
+  k.coords = h->d_coords.p;
+  k.conn = h->d_conn.p;
+  k.node_flag = h->d_node_flag.p;
+  k.node_rp = h->d_node_rp.p;
+  k.slot = h->d_slot.p;
+  k.n_elements = h->n_el;
+  k.side_bc = h->d_side_bc.p;
+  k.status = h->d_status.p;
+  k.first_bad = h->d_first_bad.p;
+  return k;
+}
+
+LaunchResult dispatch_interior(gales_asm* h, const KParams& k, int form, bool want_m, long long n,
+                               cudaStream_t st) {
+  const bool f64 = form == GALES_FORM_FP64;
+  if (h->dim == 2 && h->nen == 3)
+    return f64 ? interior_tri3_fp64(k, h->nc, want_m, n, st) : interior_tri3_mixed(k, h->nc, want_m, n, st);
+  if (h->dim == 2 && h->nen == 4)
+    return f64 ? interior_quad4_fp64(k, h->nc, want_m, n, st) : interior_quad4_mixed(k, h->nc, want_m, n, st);
+  if (h->dim == 3 && h->nen == 4)
+    return f64 ? interior_tet4_fp64(k, h->nc, want_m, n, st) : interior_tet4_mixed(k, h->nc, want_m, n, st);
+  return f64 ? interior_hex8_fp64(k, h->nc, want_m, n, st) : interior_hex8_mixed(k, h->nc, want_m, n, st);
+}
+
+LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, long long n, cudaStream_t st) {
+  if (h->dim == 2 && h->nen == 3) return boundary_tri3(k, h->nc, n, st);
+  if (h->dim == 2 && h->nen == 4) return boundary_quad4(k, h->nc, n, st);
+  if (h->dim == 3 && h->nen == 4) return boundary_tet4(k, h->nc, n, st);
+  return boundary_hex8(k, h->nc, n, st);
+}
+
+// Device-side body of one assembly on device pointers (no host synchronisation).
+int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, int form, double* dvals,
+                 double* drhs, cudaStream_t st) {
+  KParams k = base_params(h, dt);
+  k.I = dI;
+  k.P = dP;
+  k.vals = dvals;
+  k.rhs = drhs;
+  k.scatter_mode = (h->scatter_mode == GALES_SCATTER_COLOURED) ? 1 : 0;
+  const bool want_m = dvals != nullptr;
+  CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
+  CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  if (dvals) CK(h, cudaMemsetAsync(dvals, 0, (size_t)h->nnz * sizeof(double), st), "memset vals");
+  CK(h, cudaMemsetAsync(drhs, 0, (size_t)h->n_rows * sizeof(double), st), "memset rhs");
+  h->launches += 0;
+  if (h->scatter_mode == GALES_SCATTER_COLOURED) {
+    for (int c = 0; c < h->n_colours; ++c) {
+      KParams kc = k;
+      kc.el_list = h->d_colour_order.p + h->colour_off[c];
+      kc.n_list = h->colour_off[c + 1] - h->colour_off[c];
+      LaunchResult r = dispatch_interior(h, kc, form, want_m, kc.n_list, st);
+      if (r.err != cudaSuccess) return cuda_fail(h, r.err, "interior kernel");
+      h->launches += r.launches;
+    }
+  } else {
+    LaunchResult r = dispatch_interior(h, k, form, want_m, h->n_el, st);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "interior kernel");
+    h->launches += r.launches;
+  }
+  if (!h->bd_list.empty()) {
+    // the boundary pass always uses atomics: boundary elements of one colour may
+    // still be scattered twice, but its own elements may share nodes
+    KParams kb = k;
+    kb.scatter_mode = 0;
+    kb.el_list = h->d_bd_list.p;
+    kb.n_list = (int64_t)h->bd_list.size();
+    kb.bd_sides = h->d_bd_sides.p;
+    LaunchResult r = dispatch_boundary(h, kb, kb.n_list, st);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
+    h->launches += r.launches;
+  }
+  return 0;
+}
+
+int finish(gales_asm* h, cudaStream_t st) {
+  CK(h, cudaMemcpyAsync(h->h_status, h->d_status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, st), "status");
+  CK(h, cudaMemcpyAsync(h->h_first_bad, h->d_first_bad.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st),
+     "first_bad");
+  CK(h, cudaStreamSynchronize(st), "synchronize");
+  h->status = (int)*h->h_status;
+  h->first_bad = (*h->h_first_bad == ULLONG_MAX) ? -1 : (int64_t)*h->h_first_bad;
+  if (h->status) {
+    char buf[160];
+    snprintf(buf, sizeof(buf), "kernel status 0x%x at element %lld", h->status, (long long)h->first_bad);
+    h->err = buf;
+  } else {
+    h->err.clear();
+  }
+  return h->status;
+}
+
+int assemble_impl(gales_asm* h, const double* I, const double* P, double dt, int32_t form, double* vals,
+                  double* rhs, void* stream) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (!I || !P || !rhs) return fail(h, GALES_ERR_BAD_INPUT, "null state or rhs pointer");
+  if (form != GALES_FORM_FP64 && form != GALES_FORM_MIXED) return fail(h, GALES_ERR_BAD_INPUT, "unknown form");
+  if (!(dt > 0.0)) return fail(h, GALES_ERR_BAD_INPUT, "dt must be positive");
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t sb = (size_t)h->n_rows * sizeof(double);
+  const double* dI = I;
+  const double* dP = P;
+  double* dvals = vals;
+  double* drhs = rhs;
+  const bool hI = !is_device_ptr(I), hP = !is_device_ptr(P);
+  const bool hV = vals && !is_device_ptr(vals), hR = !is_device_ptr(rhs);
+  CK(h, cudaEventRecord(h->ev0, st), "event");
+  if (hI) {
+    CK(h, h->s_I.alloc(h->n_rows), "staging I");
+    CK(h, cudaMemcpyAsync(h->s_I.p, I, sb, cudaMemcpyHostToDevice, st), "copy I");
+    dI = h->s_I.p;
+  }
+  if (hP) {
+    CK(h, h->s_P.alloc(h->n_rows), "staging P");
+    CK(h, cudaMemcpyAsync(h->s_P.p, P, sb, cudaMemcpyHostToDevice, st), "copy P");
+    dP = h->s_P.p;
+  }
+  if (hV) {
+    CK(h, h->s_vals.alloc(h->nnz), "staging vals");
+    dvals = h->s_vals.p;
+  }
+  if (hR) {
+    CK(h, h->s_rhs.alloc(h->n_rows), "staging rhs");
+    drhs = h->s_rhs.p;
+  }
+  int rc = run_assembly(h, dI, dP, dt, form, dvals, drhs, st);
+  if (rc) return rc;
+  if (hV) CK(h, cudaMemcpyAsync(vals, dvals, (size_t)h->nnz * sizeof(double), cudaMemcpyDeviceToHost, st), "copy vals");
+  if (hR) CK(h, cudaMemcpyAsync(rhs, drhs, sb, cudaMemcpyDeviceToHost, st), "copy rhs");
+  CK(h, cudaEventRecord(h->ev1, st), "event");
+  rc = finish(h, st);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gales_asm_assemble(gales_asm* h, const double* I, const double* P, double dt, int32_t form, double* vals,
+                       double* rhs, void* stream) {
+  if (h && !vals) return fail(h, GALES_ERR_BAD_INPUT, "null vals pointer (use gales_asm_residual)");
+  return assemble_impl(h, I, P, dt, form, vals, rhs, stream);
+}
+
+int gales_asm_residual(gales_asm* h, const double* I, const double* P, double dt, int32_t form, double* rhs,
+                       void* stream) {
+  return assemble_impl(h, I, P, dt, form, nullptr, rhs, stream);
+}
+
+int gales_asm_element_blocks(gales_asm* h, const double* I, const double* P, double dt, int32_t form,
+                             int32_t which, const int32_t* elements, int64_t n, double* m_out, double* r_out,
+                             void* stream) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (!I || !P || !elements || !r_out || n < 0) return fail(h, GALES_ERR_BAD_INPUT, "null argument");
+  if (which != 0 && which != 1) return fail(h, GALES_ERR_BAD_INPUT, "which must be 0 or 1");
+  if (form != GALES_FORM_FP64 && form != GALES_FORM_MIXED) return fail(h, GALES_ERR_BAD_INPUT, "unknown form");
+  if (n == 0) return 0;
+  for (int64_t i = 0; i < n; ++i)
+    if (elements[i] < 0 || elements[i] >= h->n_el) return fail(h, GALES_ERR_BAD_INPUT, "element out of range");
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = h->nen * h->nd;
+  const size_t sb = (size_t)h->n_rows * sizeof(double);
+  const double* dI = I;
+  const double* dP = P;
+  if (!is_device_ptr(I)) {
+    CK(h, h->s_I.alloc(h->n_rows), "staging I");
+    CK(h, cudaMemcpyAsync(h->s_I.p, I, sb, cudaMemcpyHostToDevice, st), "copy I");
+    dI = h->s_I.p;
+  }
+  if (!is_device_ptr(P)) {
+    CK(h, h->s_P.alloc(h->n_rows), "staging P");
+    CK(h, cudaMemcpyAsync(h->s_P.p, P, sb, cudaMemcpyHostToDevice, st), "copy P");
+    dP = h->s_P.p;
+  }
+  DevBuf<int32_t> d_list;
+  DevBuf<int8_t> d_sides;
+  DevBuf<double> d_m, d_r;
+  CK(h, d_list.alloc(n), "element list");
+  CK(h, cudaMemcpy(d_list.p, elements, n * sizeof(int32_t), cudaMemcpyHostToDevice), "copy list");
+  const bool hm = m_out && !is_device_ptr(m_out), hr = !is_device_ptr(r_out);
+  double* dm = m_out;
+  double* dr = r_out;
+  if (hm) { CK(h, d_m.alloc((size_t)n * N * N), "m staging"); dm = d_m.p; }
+  if (hr) { CK(h, d_r.alloc((size_t)n * N), "r staging"); dr = d_r.p; }
+  KParams k = base_params(h, dt);
+  k.I = dI;
+  k.P = dP;
+  k.el_list = d_list.p;
+  k.n_list = n;
+  k.local_m = dm;
+  k.local_r = dr;
+  k.vals = dm;
+  CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
+  CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  if (dm) CK(h, cudaMemsetAsync(dm, 0, (size_t)n * N * N * sizeof(double), st), "memset m");
+  CK(h, cudaMemsetAsync(dr, 0, (size_t)n * N * sizeof(double), st), "memset r");
+  LaunchResult r;
+  if (which == 0) {
+    r = dispatch_interior(h, k, form, dm != nullptr, n, st);
+  } else {
+    std::vector<int8_t> sides((size_t)n * h->ei.nsides);
+    for (int64_t i = 0; i < n; ++i)
+      for (int s2 = 0; s2 < h->ei.nsides; ++s2)
+        sides[i * h->ei.nsides + s2] = h->el_sides[(size_t)elements[i] * h->ei.nsides + s2];
+    CK(h, d_sides.alloc(sides.size()), "sides");
+    CK(h, cudaMemcpy(d_sides.p, sides.data(), sides.size(), cudaMemcpyHostToDevice), "copy sides");
+    k.bd_sides = d_sides.p;
+    r = dispatch_boundary(h, k, n, st);
+  }
+  if (r.err != cudaSuccess) return cuda_fail(h, r.err, "element kernel");
+  h->launches += r.launches;
+  if (hm) CK(h, cudaMemcpyAsync(m_out, dm, (size_t)n * N * N * sizeof(double), cudaMemcpyDeviceToHost, st), "copy m");
+  if (hr) CK(h, cudaMemcpyAsync(r_out, dr, (size_t)n * N * sizeof(double), cudaMemcpyDeviceToHost, st), "copy r");
+  int rc = finish(h, st);
+  d_list.release(); d_sides.release(); d_m.release(); d_r.release();
+  return rc;
+}
+
+int gales_asm_vjp(gales_asm* h, const double*, const double*, double, const double*, int32_t, double*, double*,
+                  void*) {
+  return fail(h, GALES_ERR_UNSUPPORTED, "vjp not available in this build");
+}
+
+int gales_asm_norm2(gales_asm* h, const double* rhs, double* out, void* stream) {
+  (void)stream;
+  if (!h || !rhs || !out) return GALES_ERR_BAD_INPUT;
+  return fail(h, GALES_ERR_UNSUPPORTED, "norm2 not available in this build");
+}
+
+int gales_asm_status(gales_asm* h, int64_t* first_bad_element) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (first_bad_element) *first_bad_element = h->first_bad;
+  return h->status;
+}
+
+const char* gales_asm_last_error(gales_asm* h) { return h ? h->err.c_str() : "null handle"; }
+
+double gales_asm_last_ms(gales_asm* h) { return h ? h->last_ms : 0.0; }
+
+int64_t gales_asm_launch_count(gales_asm* h) { return h ? h->launches : 0; }
+
+}  // extern "C"

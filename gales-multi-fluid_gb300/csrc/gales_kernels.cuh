@@ -1,0 +1,1123 @@
+// Element assembly kernels for fluid_mc (interior and boundary passes).
+//
+// Interior kernel, one CTA per batch of EB elements (one warp per element):
+//   point phase  - one thread per (element, quadrature point), FP64: geometry
+//                  (quad.hpp:196-231, 523-571), interpolation (quad.hpp:817-885),
+//                  mixture EOS at P and I (fluid_2d.hpp:179-195), flux scalars
+//                  (fluid_2d.hpp:391-603), tau (fluid_2d.hpp:877-1022) and the dc
+//                  viscosity (fluid_2d.hpp:1027-1065).  Results go to shared memory
+//                  in the form's arithmetic type S.
+//   matrix phase - one warp per element, lanes over the (nen*nd)^2 block entries:
+//                  Galerkin, least-squares and dc terms of RM_i (fluid_2d.hpp:251-333)
+//                  accumulated in registers over the quadrature points, then the
+//                  Dirichlet row replacement of scatter::execute (scatter.hpp:62-78)
+//                  and FP64 atomic adds into the CSR values and rhs (scatter.hpp:96-97).
+// Boundary kernel, one warp per boundary element: execute_b/RM_b
+// (fluid_2d.hpp:209-245, 341-364, 610-868) and its own scatter pass
+// (fluid_assembly.hpp:57-63), all in FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gales_physics.cuh"
+
+namespace gales {
+
+struct KParams {
+  // mixture and flags
+  DevChem ch[GALES_MAX_COMP];
+  double dt;
+  double dc_sharp, dc_scale;
+  double gravity[3];
+  double u_ref_inv[GALES_MAX_ND];
+  double gp[8][3];
+  double W_in, W_bd;
+  int32_t tau, dc_2006, steady;
+  int32_t n_sides, n_side_nodes, n_side_q;
+  uint32_t dirichlet_mask[GALES_MAX_FLAGS];
+  double sgp[6][4][3];
+  // mesh
+  const double* coords;
+  const int32_t* conn;
+  const int32_t* node_flag;
+  const int64_t* node_rp;      // node graph row pointers [n_nodes+1]
+  const uint16_t* slot;        // [n_el][nen][nen]: position of node a in node b's graph row
+  int64_t n_elements;
+  const int32_t* el_list;      // optional element list (colour batch / boundary elements)
+  int64_t n_list;
+  const int8_t* bd_sides;      // [n_list][n_sides] side flags of the listed boundary elements
+  const gales_side_bc* side_bc;  // [GALES_MAX_FLAGS]
+  // state and outputs
+  const double* I;
+  const double* P;
+  double* vals;
+  double* rhs;
+  unsigned int* status;
+  unsigned long long* first_bad;
+  int32_t scatter_mode;        // 0 atomics, 1 plain read-modify-write (coloured batches)
+  double* local_m;             // element-level output [n_list][(nen*nd)^2] (no scatter) or null
+  double* local_r;             // element-level output [n_list][nen*nd] (r = -r_) or null
+};
+
+__device__ __forceinline__ void flag_error(const KParams& k, unsigned int bits, long long e) {
+  atomicOr(k.status, bits);
+  atomicMin(k.first_bad, (unsigned long long)e);
+}
+
+template <typename S>
+__device__ __forceinline__ void add_to(double* p, S v, int mode) {
+  if (mode == 0) atomicAdd(p, (double)v);
+  else *p += (double)v;
+}
+
+// ---------------------------------------------------------------------------
+// Geometry at a point (quad.hpp).  dl: local derivatives; returns J.
+template <int DIM, int NEN>
+__device__ __forceinline__ void shape_local(const double* pt, double* sh, double (&dl)[DIM][NEN]) {
+  if constexpr (DIM == 2 && NEN == 3) {
+    const double xi = pt[0], eta = pt[1];
+    sh[0] = 1.0 - xi - eta; sh[1] = xi; sh[2] = eta;
+    dl[0][0] = -1.0; dl[1][0] = -1.0;
+    dl[0][1] = 1.0;  dl[1][1] = 0.0;
+    dl[0][2] = 0.0;  dl[1][2] = 1.0;
+  } else if constexpr (DIM == 2 && NEN == 4) {
+    const double xi = pt[0], eta = pt[1];
+    sh[0] = 0.25 * (1.0 - xi) * (1.0 - eta);
+    sh[1] = 0.25 * (1.0 + xi) * (1.0 - eta);
+    sh[2] = 0.25 * (1.0 + xi) * (1.0 + eta);
+    sh[3] = 0.25 * (1.0 - xi) * (1.0 + eta);
+    dl[0][0] = -0.25 * (1. - eta); dl[1][0] = -0.25 * (1. - xi);
+    dl[0][1] = 0.25 * (1. - eta);  dl[1][1] = -0.25 * (1. + xi);
+    dl[0][2] = 0.25 * (1. + eta);  dl[1][2] = 0.25 * (1. + xi);
+    dl[0][3] = -0.25 * (1. + eta); dl[1][3] = 0.25 * (1. - xi);
+  } else if constexpr (DIM == 3 && NEN == 4) {
+    const double xi = pt[0], eta = pt[1], zeta = pt[2];
+    sh[0] = 1.0 - xi - eta - zeta; sh[1] = xi; sh[2] = eta; sh[3] = zeta;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) dl[k][i] = (i == 0) ? -1.0 : ((i == k + 1) ? 1.0 : 0.0);
+  } else {
+    const double xi = pt[0], eta = pt[1], zeta = pt[2];
+    const double sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+    const double sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+    const double sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const double ax = sx[i] < 0 ? (1.0 - xi) : (1.0 + xi);
+      const double ay = sy[i] < 0 ? (1.0 - eta) : (1.0 + eta);
+      const double az = sz[i] < 0 ? (1.0 - zeta) : (1.0 + zeta);
+      sh[i] = 0.125 * ax * ay * az;
+      dl[0][i] = (sx[i] < 0 ? -0.125 : 0.125) * ay * az;
+      dl[1][i] = (sy[i] < 0 ? -0.125 : 0.125) * ax * az;
+      dl[2][i] = (sz[i] < 0 ? -0.125 : 0.125) * ax * ay;
+    }
+  }
+}
+
+// Mapping derivatives and global shape gradients; optionally metrics G, g and the
+// boundary area vector JN (quad.hpp:196-345, 523-691).
+template <int DIM, int NEN>
+struct Geo {
+  double sh[NEN], ds[DIM][NEN], J, G[DIM][DIM], g[DIM], JN[DIM];
+};
+
+template <int DIM, int NEN>
+__device__ __forceinline__ void geometry(const double (&X)[NEN][DIM], const double* pt, bool interior,
+                                         Geo<DIM, NEN>& o) {
+  double dl[DIM][NEN];
+  shape_local<DIM, NEN>(pt, o.sh, dl);
+  if constexpr (DIM == 2) {
+    double dx_dxi = 0.0, dx_deta = 0.0, dy_dxi = 0.0, dy_deta = 0.0;
+#pragma unroll
+    for (int i = 0; i < NEN; ++i) {
+      dx_dxi += dl[0][i] * X[i][0];
+      dx_deta += dl[1][i] * X[i][0];
+      dy_dxi += dl[0][i] * X[i][1];
+      dy_deta += dl[1][i] * X[i][1];
+    }
+    o.J = dx_dxi * dy_deta - dy_dxi * dx_deta;
+    const double dxi_dx = (1 / o.J) * (dy_deta);
+    const double deta_dx = (1 / o.J) * (-dy_dxi);
+    const double dxi_dy = (1 / o.J) * (-dx_deta);
+    const double deta_dy = (1 / o.J) * (dx_dxi);
+#pragma unroll
+    for (int i = 0; i < NEN; ++i) {
+      o.ds[0][i] = dl[0][i] * dxi_dx + dl[1][i] * deta_dx;
+      o.ds[1][i] = dl[0][i] * dxi_dy + dl[1][i] * deta_dy;
+    }
+    if (interior) {
+      o.g[0] = dxi_dx + deta_dx;
+      o.g[1] = dxi_dy + deta_dy;
+      o.G[0][0] = dxi_dx * dxi_dx + deta_dx * deta_dx;
+      o.G[1][1] = dxi_dy * dxi_dy + deta_dy * deta_dy;
+      o.G[0][1] = dxi_dx * dxi_dy + deta_dx * deta_dy;
+      o.G[1][0] = o.G[0][1];
+    } else {
+      const double xi = pt[0], eta = pt[1];
+      o.JN[0] = 0.0; o.JN[1] = 0.0;
+      if constexpr (NEN == 4) {
+        if (eta == 1.0) { o.JN[0] = -dy_dxi; o.JN[1] = dx_dxi; }
+        else if (eta == -1.0) { o.JN[0] = dy_dxi; o.JN[1] = -dx_dxi; }
+        else if (xi == 1.0) { o.JN[0] = dy_deta; o.JN[1] = -dx_deta; }
+        else if (xi == -1.0) { o.JN[0] = -dy_deta; o.JN[1] = dx_deta; }
+      } else {
+        if (xi == 0.0) { o.JN[0] = -dy_deta; o.JN[1] = dx_deta; }
+        else if (eta == 0.0) { o.JN[0] = dy_dxi; o.JN[1] = -dx_dxi; }
+        else { o.JN[0] = dy_deta - dy_dxi; o.JN[1] = dx_dxi - dx_deta; }
+      }
+    }
+  } else {
+    double a[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // a[i][j] = d x_i / d xi_j
+#pragma unroll
+    for (int n = 0; n < NEN; ++n)
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) a[i][j] += dl[j][n] * X[n][i];
+    const double dx_dxi = a[0][0], dx_deta = a[0][1], dx_dzeta = a[0][2];
+    const double dy_dxi = a[1][0], dy_deta = a[1][1], dy_dzeta = a[1][2];
+    const double dz_dxi = a[2][0], dz_deta = a[2][1], dz_dzeta = a[2][2];
+    o.J = dx_dxi * (dy_deta * dz_dzeta - dz_deta * dy_dzeta) -
+          dy_dxi * (dx_deta * dz_dzeta - dz_deta * dx_dzeta) +
+          dz_dxi * (dx_deta * dy_dzeta - dy_deta * dx_dzeta);
+    const double iJ = 1 / o.J;
+    const double dxi_dx = iJ * (dy_deta * dz_dzeta - dz_deta * dy_dzeta);
+    const double deta_dx = iJ * (-dy_dxi * dz_dzeta + dz_dxi * dy_dzeta);
+    const double dzeta_dx = iJ * (dy_dxi * dz_deta - dz_dxi * dy_deta);
+    const double dxi_dy = iJ * (-dx_deta * dz_dzeta + dz_deta * dx_dzeta);
+    const double deta_dy = iJ * (dx_dxi * dz_dzeta - dz_dxi * dx_dzeta);
+    const double dzeta_dy = iJ * (-dx_dxi * dz_deta + dz_dxi * dx_deta);
+    const double dxi_dz = iJ * (dx_deta * dy_dzeta - dy_deta * dx_dzeta);
+    const double deta_dz = iJ * (-dx_dxi * dy_dzeta + dy_dxi * dx_dzeta);
+    const double dzeta_dz = iJ * (dx_dxi * dy_deta - dy_dxi * dx_deta);
+#pragma unroll
+    for (int i = 0; i < NEN; ++i) {
+      o.ds[0][i] = dl[0][i] * dxi_dx + dl[1][i] * deta_dx + dl[2][i] * dzeta_dx;
+      o.ds[1][i] = dl[0][i] * dxi_dy + dl[1][i] * deta_dy + dl[2][i] * dzeta_dy;
+      o.ds[2][i] = dl[0][i] * dxi_dz + dl[1][i] * deta_dz + dl[2][i] * dzeta_dz;
+    }
+    if (interior) {
+      o.g[0] = dxi_dx + deta_dx + dzeta_dx;
+      o.g[1] = dxi_dy + deta_dy + dzeta_dy;
+      o.g[2] = dxi_dz + deta_dz + dzeta_dz;
+      o.G[0][0] = dxi_dx * dxi_dx + deta_dx * deta_dx + dzeta_dx * dzeta_dx;
+      o.G[1][1] = dxi_dy * dxi_dy + deta_dy * deta_dy + dzeta_dy * dzeta_dy;
+      o.G[2][2] = dxi_dz * dxi_dz + deta_dz * deta_dz + dzeta_dz * dzeta_dz;
+      o.G[0][1] = dxi_dx * dxi_dy + deta_dx * deta_dy + dzeta_dx * dzeta_dy;
+      o.G[1][2] = dxi_dy * dxi_dz + deta_dy * deta_dz + dzeta_dy * dzeta_dz;
+      o.G[0][2] = dxi_dz * dxi_dx + deta_dz * deta_dx + dzeta_dz * dzeta_dx;
+      o.G[1][0] = o.G[0][1];
+      o.G[2][1] = o.G[1][2];
+      o.G[2][0] = o.G[0][2];
+    } else {
+      const double xi = pt[0], eta = pt[1], zeta = pt[2];
+      double* JN = o.JN;
+      JN[0] = JN[1] = JN[2] = 0.0;
+      if constexpr (NEN == 8) {
+        if (zeta == 1.0) {
+          JN[0] = dy_dxi * dz_deta - dz_dxi * dy_deta;
+          JN[1] = dz_dxi * dx_deta - dx_dxi * dz_deta;
+          JN[2] = dx_dxi * dy_deta - dy_dxi * dx_deta;
+        } else if (zeta == -1.0) {
+          JN[0] = -dy_dxi * dz_deta + dz_dxi * dy_deta;
+          JN[1] = -dz_dxi * dx_deta + dx_dxi * dz_deta;
+          JN[2] = -dx_dxi * dy_deta + dy_dxi * dx_deta;
+        } else if (eta == 1.0) {
+          JN[0] = dy_dzeta * dz_dxi - dy_dxi * dz_dzeta;
+          JN[1] = dz_dzeta * dx_dxi - dz_dxi * dx_dzeta;
+          JN[2] = dx_dzeta * dy_dxi - dx_dxi * dy_dzeta;
+        } else if (eta == -1.0) {
+          JN[0] = -dy_dzeta * dz_dxi + dy_dxi * dz_dzeta;
+          JN[1] = -dz_dzeta * dx_dxi + dz_dxi * dx_dzeta;
+          JN[2] = -dx_dzeta * dy_dxi + dx_dxi * dy_dzeta;
+        } else if (xi == 1.0) {
+          JN[0] = dy_deta * dz_dzeta - dy_dzeta * dz_deta;
+          JN[1] = dz_deta * dx_dzeta - dz_dzeta * dx_deta;
+          JN[2] = dx_deta * dy_dzeta - dx_dzeta * dy_deta;
+        } else if (xi == -1.0) {
+          JN[0] = -dy_deta * dz_dzeta + dy_dzeta * dz_deta;
+          JN[1] = -dz_deta * dx_dzeta + dz_dzeta * dx_deta;
+          JN[2] = -dx_deta * dy_dzeta + dx_dzeta * dy_deta;
+        }
+      } else {
+        if (xi == 0.0) {
+          JN[0] = dz_deta * dy_dzeta - dy_deta * dz_dzeta;
+          JN[1] = dx_deta * dz_dzeta - dz_deta * dx_dzeta;
+          JN[2] = dy_deta * dx_dzeta - dx_deta * dy_dzeta;
+        } else if (eta == 0.0) {
+          JN[0] = dz_dzeta * dy_dxi - dy_dzeta * dz_dxi;
+          JN[1] = dz_dxi * dx_dzeta - dx_dxi * dz_dzeta;
+          JN[2] = dy_dzeta * dx_dxi - dx_dzeta * dy_dxi;
+        } else if (zeta == 0.0) {
+          JN[0] = dz_dxi * dy_deta - dy_dxi * dz_deta;
+          JN[1] = dx_dxi * dz_deta - dx_deta * dz_dxi;
+          JN[2] = dy_dxi * dx_deta - dx_dxi * dy_deta;
+        } else {
+          JN[0] = (dz_dzeta - dz_dxi) * (dy_deta - dy_dxi) - (dy_dzeta - dy_dxi) * (dz_deta - dz_dxi);
+          JN[1] = (dx_dzeta - dx_dxi) * (dz_deta - dz_dxi) - (dx_deta - dx_dxi) * (dz_dzeta - dz_dxi);
+          JN[2] = (dx_deta - dx_dxi) * (dy_dzeta - dy_dxi) - (dx_dzeta - dx_dxi) * (dy_deta - dy_dxi);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Per-quadrature-point record written by the point phase.
+template <int DIM, int NEN, int NC, typename S>
+struct QP {
+  using L = Layout<DIM, NC>;
+  static constexpr int ND = L::ND;
+  S sh[NEN], ds[DIM][NEN], JxW;
+  S p, v[DIM], Y[NC], rho, E, drho_dp, drho_dT, de_dp, de_dT, mu, lambda, kappa;
+  S drho_dY[L::NYA], dE_dY[L::NYA], rhoD[L::NYA], rhoDH[L::NYA];
+  S tau[ND][ND];
+  S nu;             // dc_scale_fact * nu_shoc (0 when dc is off or inactive)
+  S rv[ND];         // coefficient of N_b:    (U - U_P)/dt - S
+  S rf[DIM][ND];    // coefficient of dN_b/dx_k:  F_dif,k - F_adv,k + shock dI/dx_k
+  S res[ND];        // least-squares residual Res (fluid_2d.hpp:282)
+};
+
+// Point phase for one (element, quadrature point).  FORM selects the tau inverse:
+// GALES_FORM_FP64 uses the uBLAS-faithful LU; GALES_FORM_MIXED the closed form.
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
+__device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, NC, S>& out) {
+  using L = Layout<DIM, NC>;
+  constexpr int ND = L::ND;
+  int nodes[NEN];
+  double X[NEN][DIM];
+#pragma unroll
+  for (int a = 0; a < NEN; ++a) {
+    nodes[a] = __ldg(k.conn + e * NEN + a);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) X[a][d] = __ldg(k.coords + (long long)nodes[a] * DIM + d);
+  }
+  Geo<DIM, NEN> q;
+  geometry<DIM, NEN>(X, k.gp[iq], true, q);
+  if (!(q.J > 0.0)) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
+  const double JxW = q.J * k.W_in;
+  double Pq[ND], Iq[ND], dI[DIM][ND];
+#pragma unroll
+  for (int j = 0; j < ND; ++j) {
+    Pq[j] = 0.0; Iq[j] = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) dI[d][j] = 0.0;
+  }
+#pragma unroll
+  for (int i = 0; i < NEN; ++i) {
+    const double* pi = k.P + (long long)nodes[i] * ND;
+    const double* ii = k.I + (long long)nodes[i] * ND;
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      const double pv = __ldg(pi + j), iv = __ldg(ii + j);
+      Pq[j] += q.sh[i] * pv;
+      Iq[j] += q.sh[i] * iv;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) dI[d][j] += q.ds[d][i] * iv;
+    }
+  }
+  // previous-level conservative vector U_P (props at P with shear rate 0)
+  double p, v[DIM], T, Y[NC];
+  assign<DIM, NC>(Pq, p, v, T, Y);
+  double rhoP, cvP;
+  mixture_rho_cv<NC>(k.ch, p, T, Y, rhoP, cvP);
+  double UP[ND];
+  conservative<DIM, NC>(rhoP, cvP, v, T, Y, UP);
+  // current iterate
+  assign<DIM, NC>(Iq, p, v, T, Y);
+  Props<NC> pr;
+  mixture<NC>(k.ch, p, T, Y, pr);
+  Coef<DIM, NC> c;
+  make_coef<DIM, NC>(pr, p, v, T, Y, c);
+  double U[ND];
+  conservative<DIM, NC>(pr.rho, pr.cv, v, T, Y, U);
+  const double dt = k.dt;
+  // source S (fluid_2d.hpp:597-599)
+  double Sv[ND];
+#pragma unroll
+  for (int r = 0; r < ND; ++r) Sv[r] = 0.0;
+  {
+    double gv = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      Sv[1 + d] = pr.rho * k.gravity[d];
+      gv += k.gravity[d] * v[d];
+    }
+    Sv[L::iT] = pr.rho * (gv);
+  }
+  // residual pieces
+  double Res[ND], AdI[ND], t[ND];
+  {
+    double dd[ND];
+#pragma unroll
+    for (int j = 0; j < ND; ++j) dd[j] = (Iq[j] - Pq[j]) / dt;
+    dudy_mv<DIM, NC>(c, dd, Res);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      a_mv<DIM, NC>(c, d, dI[d], t);
+#pragma unroll
+      for (int j = 0; j < ND; ++j) {
+        Res[j] = Res[j] + t[j];
+        AdI[j] = (d == 0) ? t[j] : AdI[j] + t[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < ND; ++j) Res[j] = Res[j] - Sv[j];
+  }
+#pragma unroll
+  for (int j = 0; j < ND; ++j) out.rv[j] = S((U[j] - UP[j]) / dt - Sv[j]);
+  // tau
+  double tau[ND][ND];
+#pragma unroll
+  for (int r = 0; r < ND; ++r)
+#pragma unroll
+    for (int cc = 0; cc < ND; ++cc) tau[r][cc] = 0.0;
+  const double v_nrm = sqrt(vsq<DIM>(v));
+  if (v_nrm >= kEps && k.tau != GALES_TAU_NONE) {
+    double dv[DIM][DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) dv[i][j] = dI[j][1 + i];
+    const double h = compute_h<DIM>(q.G, v, dv);
+    double trG = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) trG += q.G[d][d];
+    const double cs = pr.c, rho = pr.rho, mu = pr.mu, cv = pr.cv, kappa = pr.kappa;
+    bool nondiag = false;
+    if (k.tau == GALES_TAU_NON_DIAG_COMP_2001) {
+      double lambda_sqr = 0.0 * (v_nrm * v_nrm + cs * cs) + (0.0) * 0.5 * cs * cs;
+      lambda_sqr += 0.5 * cs * sqrt(cs * cs * 0.0 * 0.0 + 16 * 0.0 * 0.0 * v_nrm * v_nrm);
+      if (!k.steady) lambda_sqr += 4 / (dt * dt);
+      const double lam = 1.0 / sqrt(lambda_sqr) + h / (2 * v_nrm);
+      const double use = k.steady ? lam : fmin(dt * 0.5, lam);
+      tau[0][0] = use;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) tau[1 + d][1 + d] = fmin(use, rho * h * h / (mu * 12));
+      tau[L::iT][L::iT] = fmin(use, rho * h * h * cv / (kappa * 12));
+#pragma unroll
+      for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = fmin(use, h * h / (pr.D_c[i] * 12));
+      nondiag = true;
+    } else if (k.tau == GALES_TAU_NON_DIAG_COMP_2019) {
+      double use;
+      if (k.steady) use = h / (2.0 * (v_nrm + cs)) + h / (2.0 * v_nrm);
+      else use = fmin(dt * 0.5, h / (2.0 * (v_nrm + cs)) + h / (2.0 * v_nrm));
+      tau[0][0] = use;
+      const double tm = fmin(use, h * h * rho / (12.0 * mu));
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) tau[1 + d][1 + d] = tm;
+      tau[L::iT][L::iT] = fmin(use, h * h * rho * cv / (12.0 * kappa));
+#pragma unroll
+      for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = fmin(use, h * h / (12.0 * pr.D_c[i]));
+      nondiag = true;
+    } else if (k.tau == GALES_TAU_DIAG_INCOMP_2007) {
+      double use = 0.0;
+#pragma unroll
+      for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) use += q.G[i][j] * q.G[i][j];
+      double vGv = 0.0;
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) {
+        double s = 0.0;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) s += q.G[i][j] * v[j];
+        vGv += v[i] * s;
+      }
+      const double nu = mu / rho;
+      double tau_m = vGv + 9.0 * use * (nu * nu);
+      if (!k.steady) tau_m += 4.0 / (dt * dt);
+      tau_m = 1.0 / sqrt(tau_m);
+      double gg = 0.0;
+#pragma unroll
+      for (int i = 0; i < DIM; ++i) gg += q.g[i] * q.g[i];
+      const double tau_c = 1.0 / (rho * tau_m * gg);
+      const double de = kappa / (rho * cv);
+      double tau_e = vGv + 9.0 * use * (de * de);
+      if (!k.steady) tau_e += 4.0 / (dt * dt);
+      tau_e = 1.0 / sqrt(tau_e);
+      tau[0][0] = tau_c;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) tau[1 + d][1 + d] = tau_m / rho;
+      tau[L::iT][L::iT] = tau_e / (rho * cv);
+#pragma unroll
+      for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = tau_m;
+    } else if (k.tau == GALES_TAU_DIAG_2014) {
+#pragma unroll
+      for (int i = 0; i < ND; ++i) {
+        const double a0 = dudy_entry<DIM, NC, double>(c, i, i);
+        const double tt = 4.0 / (dt * dt) * (a0 * a0);
+        double ta = 0.0, td = 0.0;
+#pragma unroll
+        for (int kk = 0; kk < DIM; ++kk)
+#pragma unroll
+          for (int ll = 0; ll < DIM; ++ll) {
+            const double ak = a_entry<DIM, NC, double>(c, kk, i, i);
+            const double al = a_entry<DIM, NC, double>(c, ll, i, i);
+            const double kv = k_entry<DIM, NC, double>(c, kk, ll, i, i);
+            ta += q.G[kk][ll] * (ak * al);
+            td += q.G[kk][ll] * q.G[kk][ll] * (kv * kv);
+          }
+        tau[i][i] = 1.0 / (sqrt(tt) + sqrt(ta) + sqrt(td) + 1.e-8);
+      }
+      tau[0][0] = 1.0 / (tau[0][0] + rho * tau[1][1] * (trG));
+    }
+    if (nondiag) {
+      double Xinv[ND][ND];
+      if constexpr (FORM == GALES_FORM_FP64) {
+        double A0[ND][ND];
+#pragma unroll
+        for (int r = 0; r < ND; ++r)
+#pragma unroll
+          for (int cc = 0; cc < ND; ++cc) A0[r][cc] = dudy_entry<DIM, NC, double>(c, r, cc);
+        if (lu_inverse<ND>(A0, Xinv)) flag_error(k, GALES_ERR_SINGULAR, e);
+      } else {
+        dydu_closed<DIM, NC>(c, Xinv);
+      }
+      double td[ND];
+#pragma unroll
+      for (int i = 0; i < ND; ++i) td[i] = tau[i][i];
+#pragma unroll
+      for (int r = 0; r < ND; ++r)
+#pragma unroll
+        for (int cc = 0; cc < ND; ++cc) tau[r][cc] = Xinv[r][cc] * td[cc];
+      if (v_nrm / cs < 0.1) {
+        tau[0][0] = 1.0 / (1.0 / tau[0][0] + 1.0 / (rho * tau[1][1] * (trG)));
+#pragma unroll
+        for (int cc = 1; cc < ND; ++cc) tau[0][cc] = 0.0;
+      }
+    }
+  }
+  // discontinuity capturing (fluid_2d.hpp:1027-1065)
+  double nu = 0.0;
+  double dU[DIM][ND];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) dudy_mv<DIM, NC>(c, dI[d], dU[d]);
+  if (k.dc_2006) {
+    double s = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) s += dU[d][0] * dU[d][0];
+    const double del_rho_nrm = sqrt(s);
+    if (!(del_rho_nrm < kEps)) {
+      double Jv[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) Jv[d] = dU[d][0] / del_rho_nrm;
+      double h = 0.0;
+#pragma unroll
+      for (int i = 0; i < NEN; ++i) {
+        double tt = Jv[0] * q.ds[0][i];
+#pragma unroll
+        for (int d = 1; d < DIM; ++d) tt = tt + Jv[d] * q.ds[d][i];
+        h += fabs(tt);
+      }
+      if (h > kEps) {
+        h = 1.0 / h;
+        double Zn = 0.0, Un = 0.0, use1 = 0.0;
+#pragma unroll
+        for (int j = 0; j < ND; ++j) {
+          const double z = k.u_ref_inv[j] * (AdI[j] - Sv[j]);
+          const double u = k.u_ref_inv[j] * U[j];
+          Zn += z * z;
+          Un += u * u;
+        }
+        Zn = sqrt(Zn);
+        Un = sqrt(Un);
+        const double a = k.dc_sharp;
+        if (a == 1.0 || a == 1.5) {
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            double n2 = 0.0;
+#pragma unroll
+            for (int j = 0; j < ND; ++j) {
+              const double u = k.u_ref_inv[j] * dU[d][j];
+              n2 += u * u;
+            }
+            const double n = sqrt(n2);
+            use1 += n * n;
+          }
+        }
+        if (a == 1.0) nu = Zn * h * (1.0 / sqrt(use1));
+        else if (a == 2.0) nu = Zn * h * h / Un;
+        else if (a == 1.5) nu = Zn * h * ((1.0 / sqrt(use1)) + h / Un) / 2.0;
+        nu = k.dc_scale * nu;
+      }
+    }
+  }
+  // F_dif - F_adv + shock dI (fluid_2d.hpp:253-262, 311-318)
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    double fd[ND];
+#pragma unroll
+    for (int j = 0; j < ND; ++j) fd[j] = 0.0;
+#pragma unroll
+    for (int l = 0; l < DIM; ++l) {
+      k_mv<DIM, NC>(c, d, l, dI[l], t);
+#pragma unroll
+      for (int j = 0; j < ND; ++j) fd[j] = (l == 0) ? t[j] : fd[j] + t[j];
+    }
+    const double vk = v[d];
+    double fa[ND];
+    fa[0] = pr.rho * vk;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) fa[1 + j] = (j == d) ? pr.rho * vk * vk + p : pr.rho * vk * v[j];
+    fa[L::iT] = vk * (pr.rho * c.E + p);
+#pragma unroll
+    for (int i = 0; i < NC - 1; ++i) fa[L::iY + i] = pr.rho * vk * Y[i];
+#pragma unroll
+    for (int j = 0; j < ND; ++j) out.rf[d][j] = S(fd[j] - fa[j] + nu * dU[d][j]);
+  }
+  // write the record
+#pragma unroll
+  for (int i = 0; i < NEN; ++i) {
+    out.sh[i] = S(q.sh[i]);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) out.ds[d][i] = S(q.ds[d][i]);
+  }
+  out.JxW = S(JxW);
+  out.p = S(p);
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) out.v[d] = S(v[d]);
+#pragma unroll
+  for (int i = 0; i < NC; ++i) out.Y[i] = S(Y[i]);
+  out.rho = S(c.rho); out.E = S(c.E);
+  out.drho_dp = S(c.drho_dp); out.drho_dT = S(c.drho_dT);
+  out.de_dp = S(c.de_dp); out.de_dT = S(c.de_dT);
+  out.mu = S(c.mu); out.lambda = S(c.lambda); out.kappa = S(c.kappa);
+#pragma unroll
+  for (int i = 0; i < L::NYA; ++i) {
+    out.drho_dY[i] = S(c.drho_dY[i]); out.dE_dY[i] = S(c.dE_dY[i]);
+    out.rhoD[i] = S(c.rhoD[i]); out.rhoDH[i] = S(c.rhoDH[i]);
+  }
+#pragma unroll
+  for (int r = 0; r < ND; ++r)
+#pragma unroll
+    for (int cc = 0; cc < ND; ++cc) out.tau[r][cc] = S(tau[r][cc]);
+  out.nu = S(nu);
+#pragma unroll
+  for (int j = 0; j < ND; ++j) out.res[j] = S(Res[j]);
+  if (!isfinite(JxW) || !isfinite(pr.rho) || !isfinite(nu)) flag_error(k, GALES_ERR_NONFINITE, e);
+}
+
+// Viscous/diffusive tangent contracted with the two shape gradients:
+// sum_kl dN_b/dx_k K_kl(jb,ja) dN_a/dx_l, in closed form (fluid_2d.hpp:531-571).
+template <int DIM, int NC, typename S, typename C>
+__device__ __forceinline__ S kk_entry(const C& c, const S* gb, const S* ga, int jb, int ja) {
+  using L = Layout<DIM, NC>;
+  if (jb == 0 || ja == 0) return S(0);
+  S gg = gb[0] * ga[0];
+#pragma unroll
+  for (int d = 1; d < DIM; ++d) gg += gb[d] * ga[d];
+  if (jb < L::iT) {
+    if (ja >= L::iT) return S(0);
+    const int j = jb - 1, m = ja - 1;
+    S x = c.mu * gb[m] * ga[j] + c.lambda * gb[j] * ga[m];
+    if (j == m) x += c.mu * gg;
+    return x;
+  }
+  if (jb == L::iT) {
+    if (ja < L::iT) {
+      const int m = ja - 1;
+      S gav = ga[0] * c.v[0], gbv = gb[0] * c.v[0];
+#pragma unroll
+      for (int d = 1; d < DIM; ++d) { gav += ga[d] * c.v[d]; gbv += gb[d] * c.v[d]; }
+      return c.mu * gg * c.v[m] + c.mu * gb[m] * gav + c.lambda * gbv * ga[m];
+    }
+    if (ja == L::iT) return c.kappa * gg;
+    return c.rhoDH[ja - L::iY] * gg;
+  }
+  return (ja == jb) ? c.rhoD[jb - L::iY] * gg : S(0);
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory layout of the interior kernel.
+template <int DIM, int NEN, int NC, int NQ, int EB, typename S>
+struct InteriorSmem {
+  static constexpr int ND = Layout<DIM, NC>::ND;
+  QP<DIM, NEN, NC, S> qp[EB][NQ];
+  struct Warp {
+    S D[ND][ND];           // DUDY
+    S WA[NEN][ND][ND];     // sum_k dN_b/dx_k A_k
+    S FPT[NEN][ND][ND];    // (WA_b - N_b S0) tau
+    S RM[NEN][ND][ND];     // N_a DUDY/dt + WA_a - N_a S0
+    double diag[NEN * ND];
+    int nodes[NEN];
+    int64_t rowbase[NEN];
+    int32_t rowlen[NEN];
+    uint32_t blocked[NEN];
+  } w[EB];
+};
+
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, bool WANT_M>
+__global__ void __launch_bounds__(256) interior_kernel(const KParams k) {
+  using L = Layout<DIM, NC>;
+  constexpr int ND = L::ND;
+  constexpr int EB = 8;
+  constexpr int N = NEN * ND;
+  constexpr int NT = N * N;
+  constexpr int NPL = (NT + 31) / 32;
+  using SM = InteriorSmem<DIM, NEN, NC, NQ, EB, S>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SM& sm = *reinterpret_cast<SM*>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long nlist = k.el_list ? k.n_list : k.n_elements;
+  const long long base = (long long)blockIdx.x * EB;
+
+  // ---- point phase
+  if (tid < EB * NQ) {
+    const int le = tid / NQ, iq = tid % NQ;
+    const long long li = base + le;
+    if (li < nlist) {
+      const long long e = k.el_list ? (long long)k.el_list[li] : li;
+      point_phase<DIM, NEN, NC, NQ, FORM, S>(k, e, iq, sm.qp[le][iq]);
+    }
+  }
+  __syncthreads();
+
+  // ---- matrix phase: warp per element
+  const long long li = base + warp;
+  if (li >= nlist) return;
+  const long long e = k.el_list ? (long long)k.el_list[li] : li;
+  auto& W = sm.w[warp];
+  if (lane < NEN) {
+    const int nd_ = __ldg(k.conn + e * NEN + lane);
+    W.nodes[lane] = nd_;
+    const int64_t r0 = __ldg(k.node_rp + nd_), r1 = __ldg(k.node_rp + nd_ + 1);
+    W.rowbase[lane] = r0 * (int64_t)(ND * ND);
+    W.rowlen[lane] = (int32_t)((r1 - r0) * ND);
+    const int fl = k.node_flag ? __ldg(k.node_flag + nd_) : 0;
+    W.blocked[lane] = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
+  }
+  constexpr int RPL = (N + 31) / 32;
+  S macc[NPL];
+#pragma unroll
+  for (int i = 0; i < NPL; ++i) macc[i] = S(0);
+  S racc[RPL];
+#pragma unroll
+  for (int i = 0; i < RPL; ++i) racc[i] = S(0);
+  const S dt = S(k.dt);
+  for (int iq = 0; iq < NQ; ++iq) {
+    const auto& c = sm.qp[warp][iq];
+    __syncwarp();
+    for (int t = lane; t < ND * ND; t += 32) {
+      const int r = t / ND, col = t % ND;
+      W.D[r][col] = dudy_entry<DIM, NC, S>(c, r, col);
+    }
+    for (int t = lane; t < NEN * ND * ND; t += 32) {
+      const int b = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
+      S x = c.ds[0][b] * a_entry<DIM, NC, S>(c, 0, r, col);
+#pragma unroll
+      for (int d = 1; d < DIM; ++d) x = madd(c.ds[d][b], a_entry<DIM, NC, S>(c, d, r, col), x);
+      W.WA[b][r][col] = x;
+    }
+    __syncwarp();
+    for (int t = lane; t < NEN * ND * ND; t += 32) {
+      const int b = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
+      // S0 has entries only in row rho E: S0(iT, 1+k) = rho g_k
+      S x = S(0);
+#pragma unroll
+      for (int m = 0; m < ND; ++m) {
+        S w = W.WA[b][r][m];
+        if (r == L::iT && m >= 1 && m <= DIM) w = w - c.sh[b] * (c.rho * S(k.gravity[m - 1]));
+        x = madd(w, c.tau[m][col], x);
+      }
+      W.FPT[b][r][col] = x;
+      S s0 = S(0);
+      if (r == L::iT && col >= 1 && col <= DIM) s0 = c.rho * S(k.gravity[col - 1]);
+      W.RM[b][r][col] = W.D[r][col] * c.sh[b] / dt + W.WA[b][r][col] - s0 * c.sh[b];
+    }
+    __syncwarp();
+    if constexpr (WANT_M) {
+#pragma unroll
+      for (int i = 0; i < NPL; ++i) {
+        const int t = lane + 32 * i;
+        if (NT % 32 != 0 && t >= NT) break;
+        const int row = t / N, colx = t % N;
+        const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
+        S lsq = S(0);
+#pragma unroll
+        for (int m = 0; m < ND; ++m) lsq = madd(W.FPT[b][jb][m], W.RM[a][m][ja], lsq);
+        S gb[DIM], ga[DIM];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) { gb[d] = c.ds[d][b]; ga[d] = c.ds[d][a]; }
+        S gg = gb[0] * ga[0];
+#pragma unroll
+        for (int d = 1; d < DIM; ++d) gg += gb[d] * ga[d];
+        const S Dv = W.D[jb][ja];
+        S s0 = S(0);
+        if (jb == L::iT && ja >= 1 && ja <= DIM) s0 = c.rho * S(k.gravity[ja - 1]);
+        S gal = c.sh[b] * Dv * c.sh[a] / dt - c.sh[a] * W.WA[b][jb][ja] - c.sh[b] * s0 * c.sh[a];
+        gal += kk_entry<DIM, NC, S>(c, gb, ga, jb, ja);
+        gal += c.nu * gg * Dv;
+        macc[i] = madd(c.JxW, gal + lsq, macc[i]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+      const int t = lane + 32 * i;
+      if (t < N) {
+        const int b = t / ND, jb = t % ND;
+        S x = c.sh[b] * c.rv[jb];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) x = madd(c.ds[d][b], c.rf[d][jb], x);
+#pragma unroll
+        for (int m = 0; m < ND; ++m) x = madd(W.FPT[b][jb][m], c.res[m], x);
+        racc[i] = madd(c.JxW, x, racc[i]);
+      }
+    }
+  }
+  __syncwarp();
+  if (k.local_r) {  // element-level output of execute_i (fluid_2d.hpp:200-201): m = m_, r = -r_
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+      const int t = lane + 32 * i;
+      if (t < N) k.local_r[li * N + t] = -(double)racc[i];
+    }
+    if (WANT_M && k.local_m) {
+#pragma unroll
+      for (int i = 0; i < NPL; ++i) {
+        const int t = lane + 32 * i;
+        if (NT % 32 != 0 && t >= NT) break;
+        k.local_m[li * NT + t] = (double)macc[i];
+      }
+    }
+    return;
+  }
+  // ---- Dirichlet rows (scatter.hpp:62-78) and scatter (scatter.hpp:96-97)
+  double avg = 0.0;
+  if constexpr (WANT_M) {
+#pragma unroll
+    for (int i = 0; i < NPL; ++i) {
+      const int t = lane + 32 * i;
+      if (NT % 32 != 0 && t >= NT) break;
+      const int row = t / N, colx = t % N;
+      if (row == colx) W.diag[row] = (double)macc[i];
+    }
+    __syncwarp();
+    avg = 1.0;
+    for (int i = 0; i < N; ++i) avg += W.diag[i];
+    avg /= N;
+  }
+  const int mode = k.scatter_mode;
+#pragma unroll
+  for (int i = 0; i < RPL; ++i) {
+    const int t = lane + 32 * i;
+    if (t < N) {
+      const int b = t / ND, jb = t % ND;
+      const bool blk = (W.blocked[b] >> jb) & 1u;
+      const double rv = blk ? avg * 0.0 : -(double)racc[i];
+      add_to(k.rhs + (long long)W.nodes[b] * ND + jb, rv, mode);
+    }
+  }
+  if constexpr (WANT_M) {
+#pragma unroll
+    for (int i = 0; i < NPL; ++i) {
+      const int t = lane + 32 * i;
+      if (NT % 32 != 0 && t >= NT) break;
+      const int row = t / N, colx = t % N;
+      const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
+      double val = (double)macc[i];
+      if ((W.blocked[b] >> jb) & 1u) val = (row == colx) ? avg : 0.0;
+      if (val != 0.0) {
+        const int64_t off = W.rowbase[b] + (int64_t)jb * W.rowlen[b] +
+                            (int64_t)__ldg(k.slot + (e * NEN + b) * NEN + a) * ND + ja;
+        add_to(k.vals + off, val, mode);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Boundary pass (fluid_2d.hpp:209-245, 341-364, 610-868), one warp per listed
+// boundary element, FP64.  Each lane evaluates the point physics redundantly.
+
+// Entry of the boundary-modified K_kl (fluid_2d.hpp:819-867).
+template <int DIM>
+__device__ __forceinline__ int energy_source(int a, int l, int m) {
+  if (l == a && m == a) return a;
+  if (l == a) return m;
+  if (m == a) return l;
+  if (m == l) return a;
+  return -1;
+}
+
+template <int DIM, int NC>
+__device__ __forceinline__ double k_entry_bd(const Coef<DIM, NC>& c, const gales_side_bc& bc, int k,
+                                             int l, int r, int col) {
+  using L = Layout<DIM, NC>;
+  double x = k_entry<DIM, NC, double>(c, k, l, r, col);
+  if (x == 0.0) return x;
+  auto tau_set = [&](int i, int j) {
+    const int lo = i < j ? i : j, hi = i < j ? j : i;
+    return (bc.tau_mask >> (lo * 3 + hi)) & 1u;
+  };
+  if (r >= 1 && r < L::iT && col >= 1 && col < L::iT) {
+    if (tau_set(k, r - 1)) return 0.0;
+  }
+  if (r == L::iT && col >= 1 && col < L::iT) {
+    const int j = energy_source<DIM>(k, l, col - 1);
+    if (j >= 0 && tau_set(k, j)) return 0.0;
+  }
+  if (k == l && r == L::iT && col == L::iT && ((bc.q_mask >> k) & 1u)) return 0.0;
+  if (k == l && col >= L::iY) {
+    const int i = col - L::iY;
+    if (((bc.J_mask >> (k * 8 + i)) & 1u) && (r == col || r == L::iT)) return 0.0;
+  }
+  return x;
+}
+
+template <int DIM, int NC>
+__device__ __forceinline__ double a_entry_bd(const Coef<DIM, NC>& c, const gales_side_bc& bc, int k,
+                                             int r, int col) {
+  using L = Layout<DIM, NC>;
+  if (!((bc.mass_flux_mask >> k) & 1u)) return a_entry<DIM, NC, double>(c, k, r, col);
+  const double mf = bc.mass_flux[k];
+  if (r == 1 + k && col == 0) return 1.0;
+  if (r >= 1 && r < L::iT && col == r) return mf;
+  if (r == L::iT) {
+    if (col == 0) return c.v[k] + mf * c.de_dp;
+    if (col < L::iT) return (col - 1 == k) ? c.p + mf * c.v[k] : mf * c.v[col - 1];
+    if (col == L::iT) return mf * c.de_dT;
+    return mf * c.dE_dY[col - L::iY];
+  }
+  if (r >= L::iY && col == r) return mf;
+  return 0.0;
+}
+
+template <int DIM, int NEN, int NC, int NS, int NSQ>
+__global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
+  using L = Layout<DIM, NC>;
+  constexpr int ND = L::ND;
+  constexpr int N = NEN * ND;
+  constexpr int NT = N * N;
+  constexpr int NPL = (NT + 31) / 32;
+  const int lane = threadIdx.x;
+  const long long li = blockIdx.x;
+  if (li >= k.n_list) return;
+  const long long e = k.el_list[li];
+  __shared__ double diag[N];
+  int nodes[NEN];
+  double X[NEN][DIM], Ie[NEN][ND];
+#pragma unroll
+  for (int a = 0; a < NEN; ++a) {
+    nodes[a] = __ldg(k.conn + e * NEN + a);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) X[a][d] = __ldg(k.coords + (long long)nodes[a] * DIM + d);
+#pragma unroll
+    for (int j = 0; j < ND; ++j) Ie[a][j] = __ldg(k.I + (long long)nodes[a] * ND + j);
+  }
+  constexpr int RPL = (N + 31) / 32;
+  double macc[NPL];
+#pragma unroll
+  for (int i = 0; i < NPL; ++i) macc[i] = 0.0;
+  double racc[RPL];
+#pragma unroll
+  for (int i = 0; i < RPL; ++i) racc[i] = 0.0;
+  for (int s = 0; s < NS; ++s) {
+    const int flag = k.bd_sides[li * NS + s];
+    if (flag <= 0) continue;
+    const gales_side_bc& bc = k.side_bc[flag < GALES_MAX_FLAGS ? flag : 0];
+    for (int iq = 0; iq < NSQ; ++iq) {
+      Geo<DIM, NEN> q;
+      geometry<DIM, NEN>(X, k.sgp[s][iq], false, q);
+      if (!(q.J > 0.0) && lane == 0) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
+      double JNxW[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) JNxW[d] = q.JN[d] * k.W_bd;
+      double Iq[ND], dI[DIM][ND];
+#pragma unroll
+      for (int j = 0; j < ND; ++j) {
+        double a = 0.0;
+#pragma unroll
+        for (int i = 0; i < NEN; ++i) a += q.sh[i] * Ie[i][j];
+        Iq[j] = a;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          double b = 0.0;
+#pragma unroll
+          for (int i = 0; i < NEN; ++i) b += q.ds[d][i] * Ie[i][j];
+          dI[d][j] = b;
+        }
+      }
+      double p, v[DIM], T, Y[NC];
+      assign<DIM, NC>(Iq, p, v, T, Y);
+      Props<NC> pr;
+      mixture<NC>(k.ch, p, T, Y, pr);
+      Coef<DIM, NC> c;
+      make_coef<DIM, NC>(pr, p, v, T, Y, c);
+      // advective flux (fluid_2d.hpp:581-595), mass-flux override (fluid_2d.hpp:674-680, 732-738)
+      double Fa[DIM][ND], Fd[DIM][ND];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        const double vk = v[d];
+        if ((bc.mass_flux_mask >> d) & 1u) {
+          const double mf = bc.mass_flux[d];
+          Fa[d][0] = mf;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) Fa[d][1 + j] = (j == d) ? mf * v[j] + p : mf * v[j];
+          Fa[d][L::iT] = mf * c.E + p * v[d];
+#pragma unroll
+          for (int i = 0; i < NC - 1; ++i) Fa[d][L::iY + i] = mf * Y[i];
+        } else {
+          Fa[d][0] = pr.rho * vk;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) Fa[d][1 + j] = (j == d) ? pr.rho * vk * vk + p : pr.rho * vk * v[j];
+          Fa[d][L::iT] = vk * (pr.rho * c.E + p);
+#pragma unroll
+          for (int i = 0; i < NC - 1; ++i) Fa[d][L::iY + i] = pr.rho * vk * Y[i];
+        }
+      }
+      // diffusive flux from stresses with Neumann overrides (fluid_2d.hpp:761-817)
+      {
+        const double lambda = -2.0 * pr.mu / 3.0;
+        double div = 0.0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) div += dI[d][1 + d];
+        double ts[DIM][DIM], qf[DIM], Jf[DIM][L::NYA];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+          for (int b = 0; b < DIM; ++b) {
+            if (a == b) ts[a][b] = lambda * (div) + 2.0 * pr.mu * dI[a][1 + a];
+            else {
+              const int lo = a < b ? a : b, hi = a < b ? b : a;
+              ts[a][b] = pr.mu * (dI[hi][1 + lo] + dI[lo][1 + hi]);
+            }
+          }
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) qf[d] = -pr.kappa * dI[d][L::iT];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+#pragma unroll
+          for (int i = 0; i < NC - 1; ++i) Jf[d][i] = pr.rho * pr.D_c[i] * dI[d][L::iY + i];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+          for (int b = a; b < DIM; ++b)
+            if ((bc.tau_mask >> (a * 3 + b)) & 1u) { ts[a][b] = bc.tau[a * 3 + b]; ts[b][a] = ts[a][b]; }
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+          if ((bc.q_mask >> d) & 1u) qf[d] = bc.q[d];
+#pragma unroll
+        for (int i = 0; i < NC - 1; ++i)
+#pragma unroll
+          for (int d = 0; d < DIM; ++d)
+            if ((bc.J_mask >> (d * 8 + i)) & 1u) Jf[d][i] = bc.J[d][i];
+        double H[L::NYA];
+#pragma unroll
+        for (int i = 0; i < NC - 1; ++i) H[i] = pr.e_c[i] + p / pr.rho_c[i];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          double HJ = 0.0;
+#pragma unroll
+          for (int i = 0; i < NC - 1; ++i) HJ += H[i] * Jf[d][i];
+          Fd[d][0] = 0.0;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) Fd[d][1 + j] = ts[d][j];
+          double en = ts[d][0] * v[0];
+#pragma unroll
+          for (int j = 1; j < DIM; ++j) en = en + ts[d][j] * v[j];
+          Fd[d][L::iT] = en - qf[d] - HJ;
+#pragma unroll
+          for (int i = 0; i < NC - 1; ++i) Fd[d][L::iY + i] = Jf[d][i];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < RPL; ++i) {
+        const int t = lane + 32 * i;
+        if (t < N) {
+          const int b = t / ND, j = t % ND;
+          double x = 0.0;
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) x += q.sh[b] * Fa[d][j] * JNxW[d];
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) x -= q.sh[b] * Fd[d][j] * JNxW[d];
+          racc[i] += x;
+        }
+      }
+#pragma unroll 1
+      for (int i = 0; i < NPL; ++i) {
+        const int t = lane + 32 * i;
+        if (t >= NT) break;
+        const int row = t / N, colx = t % N;
+        const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
+        double x = 0.0;
+        for (int d = 0; d < DIM; ++d) x += q.sh[b] * a_entry_bd<DIM, NC>(c, bc, d, jb, ja) * JNxW[d] * q.sh[a];
+        for (int d = 0; d < DIM; ++d)
+          for (int l = 0; l < DIM; ++l)
+            x -= q.sh[b] * k_entry_bd<DIM, NC>(c, bc, d, l, jb, ja) * JNxW[d] * q.ds[l][a];
+        macc[i] += x;
+      }
+    }
+  }
+  if (k.local_r) {  // element-level output of execute_b: m = m_, r = -r_
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+      const int t = lane + 32 * i;
+      if (t < N) k.local_r[li * N + t] = -racc[i];
+    }
+    if (k.local_m) {
+#pragma unroll 1
+      for (int i = 0; i < NPL; ++i) {
+        const int t = lane + 32 * i;
+        if (t >= NT) break;
+        k.local_m[li * NT + t] = macc[i];
+      }
+    }
+    return;
+  }
+  // second scatter pass with its own Dirichlet average
+#pragma unroll
+  for (int i = 0; i < NPL; ++i) {
+    const int t = lane + 32 * i;
+    if (t >= NT) break;
+    const int row = t / N, colx = t % N;
+    if (row == colx) diag[row] = macc[i];
+  }
+  __syncwarp();
+  double avg = 1.0;
+  for (int i = 0; i < N; ++i) avg += diag[i];
+  avg /= N;
+  uint32_t blocked[NEN];
+  int64_t rowbase[NEN];
+  int32_t rowlen[NEN];
+#pragma unroll
+  for (int a = 0; a < NEN; ++a) {
+    const int fl = k.node_flag ? __ldg(k.node_flag + nodes[a]) : 0;
+    blocked[a] = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
+    const int64_t r0 = __ldg(k.node_rp + nodes[a]), r1 = __ldg(k.node_rp + nodes[a] + 1);
+    rowbase[a] = r0 * (int64_t)(ND * ND);
+    rowlen[a] = (int32_t)((r1 - r0) * ND);
+  }
+  const int mode = k.scatter_mode;
+#pragma unroll
+  for (int i = 0; i < RPL; ++i) {
+    const int t = lane + 32 * i;
+    if (t < N) {
+      const int b = t / ND, jb = t % ND;
+      const bool blk = (blocked[b] >> jb) & 1u;
+      const double rv = blk ? avg * 0.0 : -racc[i];
+      add_to(k.rhs + (long long)nodes[b] * ND + jb, rv, mode);
+    }
+  }
+  if (k.vals) {
+#pragma unroll 1
+    for (int i = 0; i < NPL; ++i) {
+      const int t = lane + 32 * i;
+      if (t >= NT) break;
+      const int row = t / N, colx = t % N;
+      const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
+      double val = macc[i];
+      if ((blocked[b] >> jb) & 1u) val = (row == colx) ? avg : 0.0;
+      if (val != 0.0) {
+        const int64_t off = rowbase[b] + (int64_t)jb * rowlen[b] +
+                            (int64_t)__ldg(k.slot + (e * NEN + b) * NEN + a) * ND + ja;
+        add_to(k.vals + off, val, mode);
+      }
+    }
+  }
+}
+
+}  // namespace gales

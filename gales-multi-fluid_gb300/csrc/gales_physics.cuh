@@ -1,0 +1,528 @@
+// Point-level physics of the fluid_mc element integral, evaluated in FP64 at one
+// quadrature point: mixture EOS, conservative variables, the frozen-coefficient
+// matrices in structured (formula) form, the stabilisation parameter tau and the
+// discontinuity-capturing viscosity.  Generic in the space dimension DIM and the
+// number of components NC; ND = DIM + 1 + NC dofs per node, ordered
+// (p, v_1..v_DIM, T, Y_1..Y_{NC-1}) with conservative rows (rho, rho v, rho E, rho Y).
+//
+// Reference: sim/fluid_mc/P0/fluid_2d.hpp (2D only; the 3D form here is the
+// dimension-generic extension), src/fem/physical_props/fluid/fluid_properties.hpp,
+// chemicals.hpp, src/fem/mesh/quad.hpp, src/fem/base/algorithm.hpp.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/gales_asm.h"
+
+namespace gales {
+
+constexpr double kEps = 2.220446049250313e-16;  // DBL_EPSILON, fluid_2d.hpp:93
+
+// The library is compiled without floating-point contraction (-fmad=false) so that
+// the point-level physics performs exactly the IEEE operations of the reference, in
+// its order.  This matters beyond rounding: compute_h (quad.hpp:367-375) decides
+// between normalising and not normalising the cross-stream direction from a value
+// that is pure rounding noise whenever the element's velocity field is rank one
+// (e.g. every node but one on a no-slip wall), so only identical arithmetic takes
+// identical branches.  The matrix-phase loops, whose summation order is already
+// restructured, request fused multiply-adds explicitly through madd().
+__device__ __forceinline__ double madd(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float madd(float a, float b, float c) { return fmaf(a, b, c); }
+
+struct DevChem {
+  int32_t kind;
+  int32_t pad;
+  double rho, mu, cp, cv, kappa, alpha, beta, R, gamma, D;
+};
+
+template <int DIM, int NC>
+struct Layout {
+  static constexpr int ND = DIM + 1 + NC;
+  static constexpr int iT = DIM + 1;   // T column == rho E row
+  static constexpr int iY = DIM + 2;   // first Y column == first rho Y row
+  static constexpr int NY = NC - 1;    // number of Y dofs
+  static constexpr int NYA = NC > 1 ? NC - 1 : 1;  // array extent
+};
+
+// Mixture properties (fluid_properties.hpp:199-227; chemicals.hpp:43-47, 258-264).
+template <int NC>
+struct Props {
+  double rho, mu, cp, cv, kappa, c, alpha, beta;
+  double rho_c[NC], e_c[NC], D_c[NC];
+};
+
+template <int NC>
+__device__ __forceinline__ void mixture(const DevChem* ch, double p, double T, const double* Y,
+                                        Props<NC>& o) {
+  double rho = 0.0, mu = 0.0, cp = 0.0, cv = 0.0, kappa = 0.0, c2 = 0.0;
+  double calpha[NC], cbeta[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const DevChem& q = ch[c];
+    double r, v, s, a, b;
+    if (q.kind == GALES_CH_CUSTOM) {
+      r = q.rho; a = q.alpha; b = q.beta;
+      s = (b == 0.0) ? 1.e20 : 1.0 / sqrt(r * b);
+      v = (b == 0.0) ? q.cp : q.cp - T * a * a / (r * b);
+    } else {
+      r = p / (q.R * T);
+      b = 1.0 / p;
+      a = 1.0 / T;
+      s = sqrt(q.gamma * q.R * T);
+      v = q.cv;
+    }
+    calpha[c] = a; cbeta[c] = b;
+    rho += Y[c] / r;
+    mu += Y[c] * q.mu;
+    cp += Y[c] * q.cp;
+    cv += Y[c] * v;
+    kappa += Y[c] * q.kappa;
+    c2 += Y[c] / ((r * r) * (s * s));
+    o.rho_c[c] = r;
+    o.e_c[c] = v * T;
+    o.D_c[c] = q.D;
+  }
+  rho = 1. / rho;
+  double c = sqrt(1.0 / c2);
+  c /= rho;
+  double alpha = 0.0, beta = 0.0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    alpha += Y[c] * calpha[c] * rho / o.rho_c[c];
+    beta += Y[c] * cbeta[c] * rho / o.rho_c[c];
+  }
+  o.rho = rho; o.mu = mu; o.cp = cp; o.cv = cv; o.kappa = kappa; o.c = c;
+  o.alpha = alpha; o.beta = beta;
+}
+
+// Only rho and cv (what U(P) needs); same operations as mixture().
+template <int NC>
+__device__ __forceinline__ void mixture_rho_cv(const DevChem* ch, double p, double T,
+                                               const double* Y, double& rho_out, double& cv_out) {
+  double rho = 0.0, cv = 0.0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const DevChem& q = ch[c];
+    double r, v;
+    if (q.kind == GALES_CH_CUSTOM) {
+      r = q.rho;
+      v = (q.beta == 0.0) ? q.cp : q.cp - T * q.alpha * q.alpha / (r * q.beta);
+    } else {
+      r = p / (q.R * T);
+      v = q.cv;
+    }
+    rho += Y[c] / r;
+    cv += Y[c] * v;
+  }
+  rho_out = 1. / rho;
+  cv_out = cv;
+}
+
+// Scalars from which every frozen-coefficient matrix of the point is built
+// (fluid_2d.hpp:393-404, 531-533).
+template <int DIM, int NC>
+struct Coef {
+  using L = Layout<DIM, NC>;
+  double p, v[DIM], T, Y[NC];
+  double rho, E, drho_dp, drho_dT, de_dp, de_dT, mu, lambda, kappa, c, cv;
+  double drho_dY[L::NYA], dE_dY[L::NYA], rhoD[L::NYA], rhoDH[L::NYA];
+};
+
+// assign(): fluid_2d.hpp:112-121
+template <int DIM, int NC>
+__device__ __forceinline__ void assign(const double* w, double& p, double* v, double& T, double* Y) {
+  using L = Layout<DIM, NC>;
+  p = w[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) v[k] = w[1 + k];
+  T = w[L::iT];
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < NC - 1; ++i) {
+    Y[i] = w[L::iY + i];
+    s += Y[i];
+  }
+  Y[NC - 1] = 1.0 - s;
+}
+
+template <int DIM>
+__device__ __forceinline__ double vsq(const double* v) {
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) s += v[k] * v[k];
+  return s;
+}
+
+// U(): fluid_2d.hpp:372-385
+template <int DIM, int NC>
+__device__ __forceinline__ void conservative(double rho, double cv, const double* v, double T,
+                                             const double* Y, double* u) {
+  using L = Layout<DIM, NC>;
+  const double E = cv * T + 0.5 * (vsq<DIM>(v));
+  u[0] = rho;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) u[1 + k] = rho * v[k];
+  u[L::iT] = rho * E;
+#pragma unroll
+  for (int i = 0; i < NC - 1; ++i) u[L::iY + i] = rho * Y[i];
+}
+
+template <int DIM, int NC>
+__device__ __forceinline__ void make_coef(const Props<NC>& pr, double p, const double* v, double T,
+                                          const double* Y, Coef<DIM, NC>& c) {
+  c.p = p; c.T = T;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) c.v[k] = v[k];
+#pragma unroll
+  for (int i = 0; i < NC; ++i) c.Y[i] = Y[i];
+  const double rho = pr.rho;
+  c.rho = rho;
+  c.cv = pr.cv;
+  c.E = pr.cv * T + 0.5 * (vsq<DIM>(v));
+  c.drho_dp = rho * pr.beta;
+  c.drho_dT = -rho * pr.alpha;
+  c.de_dp = (pr.beta * p - pr.alpha * T) / rho;
+  c.de_dT = pr.cp - p * pr.alpha / rho;
+  c.mu = pr.mu;
+  c.lambda = -2.0 * pr.mu / 3.0;
+  c.kappa = pr.kappa;
+  c.c = pr.c;
+#pragma unroll
+  for (int i = 0; i < NC - 1; ++i) {
+    c.drho_dY[i] = -rho * rho * (1. / pr.rho_c[i] - 1 / pr.rho_c[NC - 1]);
+    c.dE_dY[i] = pr.e_c[i] - pr.e_c[NC - 1];
+    const double H = pr.e_c[i] + p / pr.rho_c[i];
+    c.rhoD[i] = rho * pr.D_c[i];
+    c.rhoDH[i] = rho * pr.D_c[i] * H;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Matrix entries in formula form.  Each returns entry (r, col) of the matrix the
+// reference builds densely (fluid_2d.hpp:407-575); zero where it has no entry.
+// T is the arithmetic type (double for the FP64 form, float for the mixed form).
+
+// DUDY (fluid_2d.hpp:407-441)
+template <int DIM, int NC, typename T, typename C>
+__device__ __forceinline__ T dudy_entry(const C& c, int r, int col) {
+  using L = Layout<DIM, NC>;
+  if (r == 0) {
+    if (col == 0) return c.drho_dp;
+    if (col == L::iT) return c.drho_dT;
+    if (col >= L::iY) return c.drho_dY[col - L::iY];
+    return T(0);
+  }
+  if (r < L::iT) {
+    const int j = r - 1;
+    if (col == 0) return c.drho_dp * c.v[j];
+    if (col == r) return c.rho;
+    if (col == L::iT) return c.drho_dT * c.v[j];
+    if (col >= L::iY) return c.v[j] * c.drho_dY[col - L::iY];
+    return T(0);
+  }
+  if (r == L::iT) {
+    if (col == 0) return c.drho_dp * c.E + c.rho * c.de_dp;
+    if (col < L::iT) return c.rho * c.v[col - 1];
+    if (col == L::iT) return c.drho_dT * c.E + c.rho * c.de_dT;
+    return c.E * c.drho_dY[col - L::iY] + c.rho * c.dE_dY[col - L::iY];
+  }
+  const int i = r - L::iY;
+  if (col == 0) return c.drho_dp * c.Y[i];
+  if (col == L::iT) return c.drho_dT * c.Y[i];
+  if (col >= L::iY) {
+    T x = c.Y[i] * c.drho_dY[col - L::iY];
+    if (col == r) x += c.rho;
+    return x;
+  }
+  return T(0);
+}
+
+// A_k (fluid_2d.hpp:444-524)
+template <int DIM, int NC, typename T, typename C>
+__device__ __forceinline__ T a_entry(const C& c, int k, int r, int col) {
+  using L = Layout<DIM, NC>;
+  const T vk = c.v[k];
+  if (r == 0) {
+    if (col == 0) return c.drho_dp * vk;
+    if (col == 1 + k) return c.rho;
+    if (col == L::iT) return c.drho_dT * vk;
+    if (col >= L::iY) return c.drho_dY[col - L::iY] * vk;
+    return T(0);
+  }
+  if (r < L::iT) {
+    const int j = r - 1;
+    const T vj = c.v[j];
+    if (j == k) {
+      if (col == 0) return c.drho_dp * vk * vk + T(1.0);
+      if (col == 1 + k) return T(2.0) * c.rho * vk;
+      if (col == L::iT) return c.drho_dT * vk * vk;
+      if (col >= L::iY) return c.drho_dY[col - L::iY] * vk * vk;
+      return T(0);
+    }
+    if (col == 0) return c.drho_dp * vj * vk;
+    if (col == 1 + k) return c.rho * vj;
+    if (col == 1 + j) return c.rho * vk;
+    if (col == L::iT) return c.drho_dT * vj * vk;
+    if (col >= L::iY) return c.drho_dY[col - L::iY] * vj * vk;
+    return T(0);
+  }
+  if (r == L::iT) {
+    if (col == 0) return vk + vk * (c.drho_dp * c.E + c.rho * c.de_dp);
+    if (col < L::iT) {
+      const int j = col - 1;
+      if (j == k) return c.p + c.rho * c.E + c.rho * vk * vk;
+      const int lo = j < k ? j : k, hi = j < k ? k : j;
+      return c.rho * c.v[lo] * c.v[hi];
+    }
+    if (col == L::iT) return vk * (c.drho_dT * c.E + c.rho * c.de_dT);
+    return (c.E * c.drho_dY[col - L::iY] + c.rho * c.dE_dY[col - L::iY]) * vk;
+  }
+  const int i = r - L::iY;
+  if (col == 0) return c.drho_dp * c.Y[i] * vk;
+  if (col == 1 + k) return c.rho * c.Y[i];
+  if (col == L::iT) return c.drho_dT * c.Y[i] * vk;
+  if (col >= L::iY) {
+    T x = c.Y[i] * c.drho_dY[col - L::iY] * vk;
+    if (col == r) x += c.rho * vk;
+    return x;
+  }
+  return T(0);
+}
+
+// K_kl (fluid_2d.hpp:531-571)
+template <int DIM, int NC, typename T, typename C>
+__device__ __forceinline__ T k_entry(const C& c, int k, int l, int r, int col) {
+  using L = Layout<DIM, NC>;
+  if (r == 0 || col == 0) return T(0);
+  if (k == l) {
+    if (r < L::iT) {
+      if (col != r) return T(0);
+      return (r - 1 == k) ? c.lambda + T(2) * c.mu : c.mu;
+    }
+    if (r == L::iT) {
+      if (col < L::iT) {
+        const int m = col - 1;
+        return (m == k) ? (c.lambda + T(2) * c.mu) * c.v[k] : c.mu * c.v[m];
+      }
+      if (col == L::iT) return c.kappa;
+      return c.rhoDH[col - L::iY];
+    }
+    return (col == r) ? c.rhoD[r - L::iY] : T(0);
+  }
+  if (r == 1 + k && col == 1 + l) return c.lambda;
+  if (r == 1 + l && col == 1 + k) return c.mu;
+  if (r == L::iT) {
+    if (col == 1 + k) return c.mu * c.v[l];
+    if (col == 1 + l) return c.lambda * c.v[k];
+  }
+  return T(0);
+}
+
+// y = DUDY x, in ascending column order (the order of a dense uBLAS prod()).
+template <int DIM, int NC>
+__device__ __forceinline__ void dudy_mv(const Coef<DIM, NC>& c, const double* x, double* y) {
+  using L = Layout<DIM, NC>;
+#pragma unroll
+  for (int r = 0; r < L::ND; ++r) {
+    double t = 0.0;
+#pragma unroll
+    for (int col = 0; col < L::ND; ++col) {
+      const double a = dudy_entry<DIM, NC, double>(c, r, col);
+      t += a * x[col];
+    }
+    y[r] = t;
+  }
+}
+
+template <int DIM, int NC>
+__device__ __forceinline__ void a_mv(const Coef<DIM, NC>& c, int k, const double* x, double* y) {
+  using L = Layout<DIM, NC>;
+#pragma unroll
+  for (int r = 0; r < L::ND; ++r) {
+    double t = 0.0;
+#pragma unroll
+    for (int col = 0; col < L::ND; ++col) t += a_entry<DIM, NC, double>(c, k, r, col) * x[col];
+    y[r] = t;
+  }
+}
+
+template <int DIM, int NC>
+__device__ __forceinline__ void k_mv(const Coef<DIM, NC>& c, int k, int l, const double* x, double* y) {
+  using L = Layout<DIM, NC>;
+#pragma unroll
+  for (int r = 0; r < L::ND; ++r) {
+    double t = 0.0;
+#pragma unroll
+    for (int col = 0; col < L::ND; ++col) t += k_entry<DIM, NC, double>(c, k, l, r, col) * x[col];
+    y[r] = t;
+  }
+}
+
+// GALES::inverse (algorithm.hpp:399-416): uBLAS lu_factorize (partial pivoting on
+// the first max |.| of the column, reciprocal column scaling) + lu_substitute
+// against the identity.  Returns nonzero if a zero pivot was met.
+template <int N>
+__device__ __forceinline__ int lu_inverse(double (&A)[N][N], double (&X)[N][N]) {
+  int pm[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) pm[i] = i;
+  int singular = 0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    int imax = i;
+    double t = 0.0;
+#pragma unroll
+    for (int r = i; r < N; ++r) {
+      const double u = fabs(A[r][i]);
+      if (u > t) { imax = r; t = u; }
+    }
+    if (t == 0.0) imax = i;
+    if (A[imax][i] != 0.0) {
+      if (imax != i) {
+        pm[i] = imax;
+#pragma unroll
+        for (int r = i + 1; r < N; ++r)
+          if (r == imax)
+#pragma unroll
+            for (int c = 0; c < N; ++c) { const double s = A[i][c]; A[i][c] = A[r][c]; A[r][c] = s; }
+      }
+      const double rcp = 1.0 / A[i][i];
+#pragma unroll
+      for (int r = i + 1; r < N; ++r) A[r][i] *= rcp;
+    } else if (singular == 0) {
+      singular = i + 1;
+    }
+#pragma unroll
+    for (int r = i + 1; r < N; ++r)
+#pragma unroll
+      for (int c = i + 1; c < N; ++c) A[r][c] -= A[r][i] * A[i][c];
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < N; ++j) X[i][j] = (i == j) ? 1.0 : 0.0;
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int r = i + 1; r < N; ++r)
+      if (pm[i] == r)
+#pragma unroll
+        for (int c = 0; c < N; ++c) { const double s = X[i][c]; X[i][c] = X[r][c]; X[r][c] = s; }
+#pragma unroll
+  for (int l = 0; l < N; ++l)
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+      const double t = X[r][l];
+      if (t != 0.0)
+#pragma unroll
+        for (int m = r + 1; m < N; ++m) X[m][l] -= A[m][r] * t;
+    }
+#pragma unroll
+  for (int l = N - 1; l >= 0; --l)
+#pragma unroll
+    for (int r = N - 1; r >= 0; --r) {
+      const double t = X[r][l] /= A[r][r];
+      if (t != 0.0)
+#pragma unroll
+        for (int m = r - 1; m >= 0; --m) X[m][l] -= A[m][r] * t;
+    }
+  return singular;
+}
+
+// DUDY^{-1} in closed form.  DUDY = w r0^T + rho M with w = (1, v, E, Y),
+// r0 = its first row and M sparse, so DUDY x = y reduces to a 2x2 solve for
+// (x_p, x_T).  Used by the mixed form only.
+template <int DIM, int NC>
+__device__ __forceinline__ void dydu_closed(const Coef<DIM, NC>& c, double (&X)[Layout<DIM, NC>::ND][Layout<DIM, NC>::ND]) {
+  using L = Layout<DIM, NC>;
+  constexpr int ND = L::ND;
+  const double irho = 1.0 / c.rho;
+  const double det = c.drho_dp * c.de_dT - c.drho_dT * c.de_dp;
+  const double idet = 1.0 / det;
+#pragma unroll
+  for (int col = 0; col < ND; ++col) {
+    // y = e_col
+    const double s = (col == 0) ? 1.0 : 0.0;
+    double xv[DIM], xy[L::NYA];
+    double R1 = s, R2 = 0.0;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) xv[j] = (((col == 1 + j) ? 1.0 : 0.0) - c.v[j] * s) * irho;
+#pragma unroll
+    for (int i = 0; i < NC - 1; ++i) xy[i] = (((col == L::iY + i) ? 1.0 : 0.0) - c.Y[i] * s) * irho;
+    R2 = (((col == L::iT) ? 1.0 : 0.0) - c.E * s) * irho;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) R2 -= c.v[j] * xv[j];
+#pragma unroll
+    for (int i = 0; i < NC - 1; ++i) {
+      R1 -= c.drho_dY[i] * xy[i];
+      R2 -= c.dE_dY[i] * xy[i];
+    }
+    X[0][col] = (R1 * c.de_dT - c.drho_dT * R2) * idet;
+    X[L::iT][col] = (c.drho_dp * R2 - c.de_dp * R1) * idet;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) X[1 + j][col] = xv[j];
+#pragma unroll
+    for (int i = 0; i < NC - 1; ++i) X[L::iY + i][col] = xy[i];
+  }
+}
+
+// compute_h: quad.hpp:356-383 (2D), 701-739 (3D).  dv[i][j] = d v_i / d x_j.
+template <int DIM>
+__device__ __forceinline__ double compute_h(const double (&G)[DIM][DIM], const double* v,
+                                            const double (&dv)[DIM][DIM]) {
+  double nrm_v = sqrt(vsq<DIM>(v));
+  double s0[DIM], s1[DIM], alpha[DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) s0[i] = v[i] / nrm_v;
+  auto quadform = [&](const double* s) {
+    double Gs[DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      double t = 0.0;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) t += G[i][j] * s[j];
+      Gs[i] = t;
+    }
+    double r = 0.0;
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) r += s[i] * Gs[i];
+    return r;
+  };
+  alpha[0] = quadform(s0);
+  double acc[DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
+    double t = 0.0;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) t += dv[i][j] * v[j];
+    acc[i] = t;
+  }
+  double ip = 0.0;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) ip += acc[i] * s0[i];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) s1[i] = acc[i] - ip * s0[i];
+  const double nrm_s1 = sqrt(vsq<DIM>(s1));
+  if (nrm_s1 > kEps)
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) s1[i] /= nrm_s1;
+  alpha[1] = quadform(s1);
+  if constexpr (DIM == 3) {
+    double s2[3];
+    s2[0] = s0[1] * s1[2] - s0[2] * s1[1];
+    s2[1] = s1[0] * s0[2] - s1[2] * s0[0];
+    s2[2] = s0[0] * s1[1] - s0[1] * s1[0];
+    const double nrm_s2 = sqrt(vsq<3>(s2));
+    if (nrm_s2 > kEps)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) s2[i] /= nrm_s2;
+    alpha[2] = quadform(s2);
+  }
+  double h = 0.0;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+    if (alpha[i] != 0.0) h += 1.0 / alpha[i];
+  return 2 * sqrt(fabs(h));
+}
+
+}  // namespace gales

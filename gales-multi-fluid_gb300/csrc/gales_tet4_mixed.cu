@@ -1,0 +1,13 @@
+// Kernel instances for the tet4 element (dim 3, 4 nodes, 4 interior points,
+// 4 sides with 3 points each; element.hpp gauss_data tables).
+#include "gales_launch.cuh"
+
+namespace gales {
+
+using D_tet4 = ElementDispatch<3, 4, 4, 4, 3>;
+
+LaunchResult interior_tet4_mixed(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
+  return D_tet4::interior<GALES_FORM_MIXED>(k, nc, want_m, n, st);
+}
+
+}  // namespace gales

@@ -1,0 +1,295 @@
+"""Seeded synthetic meshes, materials and nodal states for the fluid_mc workloads.
+
+The reference's case meshes and states are not available, so the workloads are
+built here with the shapes, sizes and value distributions of the benchmark
+configurations:
+
+  channel_tri      2 m x 1 m channel, 64 x 32 quads split into 4096 CCW triangles
+                   (2145 nodes), 2 components, 5 dofs
+  box_tet_delaunay unit box, Delaunay tetrahedra of a jittered lattice
+                   (n = 56 gives about 1.0M tets), 3 components, 7 dofs
+  box_hex          structured hexahedra with seeded node jitter, 4 components, 8 dofs
+  channel_quad     2D quadrilaterals (tests)
+
+State: hydrostatic pressure 1e5..1e8 Pa with 1 % noise, velocity from 8 random
+Fourier modes (0.1 m/s amplitude), T = 1273 +- 50 K, smooth mass fractions, and
+P = I + a small seeded perturbation.  Everything is drawn from
+numpy.random.default_rng(seed).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import Material, Mesh, Setup, custom_chemical, ideal_gas, ideal_gas_named, nb_dofs, p0_policy
+
+# local side tables of element.hpp:100-104, 145-149, 401-408, 455-460
+SIDES = {
+    (2, 3): [[1, 2], [2, 0], [0, 1]],
+    (2, 4): [[0, 1], [1, 2], [2, 3], [3, 0]],
+    (3, 4): [[1, 2, 3], [0, 3, 2], [0, 1, 3], [0, 2, 1]],
+    (3, 8): [[4, 5, 6, 7], [0, 3, 2, 1], [0, 4, 7, 3], [1, 2, 6, 5], [2, 3, 7, 6], [1, 5, 4, 0]],
+}
+
+WALL = 5     # no-slip wall flag of the shipped policy (fluid_ic_bc.hpp:92,100,165)
+OPEN = 2     # boundary without velocity Dirichlet
+
+
+def boundary_sides(conn: np.ndarray, dim: int, coords: np.ndarray, face_flag) -> np.ndarray:
+    """(element, local side, flag) of every side that belongs to one element only.
+
+    face_flag(centroids) -> int flags (> 0) for the boundary faces.
+    """
+    nen = conn.shape[1]
+    table = np.asarray(SIDES[(dim, nen)])
+    ns, nsn = table.shape
+    faces = conn[:, table]                         # (n_el, ns, nsn)
+    key = np.sort(faces.reshape(-1, nsn), axis=1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    single = np.nonzero(cnt[inv.ravel()] == 1)[0]
+    el = (single // ns).astype(np.int32)
+    loc = (single % ns).astype(np.int32)
+    cen = coords[faces.reshape(-1, nsn)[single]].mean(axis=1)
+    flag = np.asarray(face_flag(cen), dtype=np.int32)
+    keep = flag > 0
+    return np.stack([el[keep], loc[keep], flag[keep]], axis=1)
+
+
+def _finish(coords, conn, node_flag, face_flag, name) -> Mesh:
+    dim = coords.shape[1]
+    bd = boundary_sides(conn, dim, coords, face_flag)
+    el_bd = np.zeros(conn.shape[0], dtype=np.uint8)
+    el_bd[bd[:, 0]] = 1
+    return Mesh(coords, conn, node_flag, el_bd, bd, name=name)
+
+
+def _box_flags(x: np.ndarray, lo: np.ndarray, hi: np.ndarray, open_top: bool) -> np.ndarray:
+    """Node flags: WALL on the box faces, OPEN on the top face (last axis, max) if open_top."""
+    tol = 1e-9 * float(np.max(hi - lo))
+    on = (np.abs(x - lo) < tol) | (np.abs(x - hi) < tol)
+    flag = np.where(on.any(axis=1), WALL, 0).astype(np.int32)
+    if open_top:
+        top = np.abs(x[:, -1] - hi[-1]) < tol
+        others = (on[:, :-1]).any(axis=1) | (np.abs(x[:, -1] - lo[-1]) < tol)
+        flag[top & ~others] = OPEN
+    return flag
+
+
+def _face_flag_box(lo, hi, open_top):
+    tol = 1e-9 * float(np.max(np.asarray(hi) - np.asarray(lo)))
+
+    def f(c):
+        flag = np.full(len(c), WALL, dtype=np.int32)
+        if open_top:
+            flag[np.abs(c[:, -1] - hi[-1]) < tol] = OPEN
+        return flag
+    return f
+
+
+def channel_tri(nx: int = 64, ny: int = 32, Lx: float = 2.0, Ly: float = 1.0) -> Mesh:
+    """Structured channel, each quad split into two counter-clockwise triangles.
+    Walls (flag 5) at y = 0 and y = Ly; inflow/outflow ends (flag 2) at x = 0, Lx."""
+    xs, ys = np.linspace(0.0, Lx, nx + 1), np.linspace(0.0, Ly, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    coords = np.stack([X.ravel(), Y.ravel()], axis=1)
+    idx = np.arange((nx + 1) * (ny + 1)).reshape(ny + 1, nx + 1)
+    n00, n10 = idx[:-1, :-1].ravel(), idx[:-1, 1:].ravel()
+    n11, n01 = idx[1:, 1:].ravel(), idx[1:, :-1].ravel()
+    t1 = np.stack([n00, n10, n11], axis=1)
+    t2 = np.stack([n00, n11, n01], axis=1)
+    conn = np.stack([t1, t2], axis=1).reshape(-1, 3).astype(np.int32)
+    tol = 1e-12
+    wall = (np.abs(coords[:, 1]) < tol) | (np.abs(coords[:, 1] - Ly) < tol)
+    end = (np.abs(coords[:, 0]) < tol) | (np.abs(coords[:, 0] - Lx) < tol)
+    node_flag = np.where(wall, WALL, np.where(end, OPEN, 0)).astype(np.int32)
+
+    def ff(c):
+        return np.where((np.abs(c[:, 1]) < tol) | (np.abs(c[:, 1] - Ly) < tol), WALL, OPEN)
+    return _finish(coords, conn, node_flag, ff, f"channel_tri_{nx}x{ny}")
+
+
+def channel_quad(nx: int = 16, ny: int = 8, Lx: float = 2.0, Ly: float = 1.0, jitter: float = 0.0,
+                 seed: int = 0) -> Mesh:
+    xs, ys = np.linspace(0.0, Lx, nx + 1), np.linspace(0.0, Ly, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    coords = np.stack([X.ravel(), Y.ravel()], axis=1)
+    if jitter:
+        rng = np.random.default_rng(seed)
+        inner = (X.ravel() > 0) & (X.ravel() < Lx) & (Y.ravel() > 0) & (Y.ravel() < Ly)
+        h = min(Lx / nx, Ly / ny)
+        coords[inner] += rng.uniform(-jitter * h, jitter * h, size=(inner.sum(), 2))
+    idx = np.arange((nx + 1) * (ny + 1)).reshape(ny + 1, nx + 1)
+    conn = np.stack([idx[:-1, :-1].ravel(), idx[:-1, 1:].ravel(), idx[1:, 1:].ravel(), idx[1:, :-1].ravel()],
+                    axis=1).astype(np.int32)
+    tol = 1e-12
+    wall = (np.abs(coords[:, 1]) < tol) | (np.abs(coords[:, 1] - Ly) < tol)
+    end = (np.abs(coords[:, 0]) < tol) | (np.abs(coords[:, 0] - Lx) < tol)
+    node_flag = np.where(wall, WALL, np.where(end, OPEN, 0)).astype(np.int32)
+
+    def ff(c):
+        return np.where((np.abs(c[:, 1]) < tol) | (np.abs(c[:, 1] - Ly) < tol), WALL, OPEN)
+    return _finish(coords, conn, node_flag, ff, f"channel_quad_{nx}x{ny}")
+
+
+def _jittered_lattice(n, jitter, rng, dim):
+    g = np.linspace(0.0, 1.0, n)
+    grids = np.meshgrid(*([g] * dim), indexing="ij")
+    pts = np.stack([x.ravel() for x in grids], axis=1)
+    h = 1.0 / (n - 1)
+    d = rng.uniform(-jitter * h, jitter * h, size=pts.shape)
+    on_face = (pts < 1e-12) | (pts > 1 - 1e-12)
+    d[on_face] = 0.0          # boundary points move only within their faces
+    return pts + d
+
+
+def box_tet_delaunay(n: int = 56, jitter: float = 0.3, seed: int = 1, min_quality: float = 1e-3) -> Mesh:
+    """Delaunay tetrahedra of an n^3 jittered lattice in the unit box, oriented so
+    that J > 0 (quad.hpp:549).  Near-flat tets (volume below min_quality * h^3 / 6)
+    are dropped.  Walls (flag 5) everywhere except the open top z = 1 (flag 2)."""
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    pts = _jittered_lattice(n, jitter, rng, 3)
+    tri = Delaunay(pts, qhull_options="Qbb Qc Qz Q12")
+    conn = tri.simplices.astype(np.int64)
+    x = pts[conn]
+    vol = np.einsum("ij,ij->i", np.cross(x[:, 1] - x[:, 0], x[:, 2] - x[:, 0]), x[:, 3] - x[:, 0])
+    flip = vol < 0
+    conn[flip, 1], conn[flip, 2] = conn[flip, 2].copy(), conn[flip, 1].copy()
+    h = 1.0 / (n - 1)
+    keep = np.abs(vol) > min_quality * h ** 3
+    conn = conn[keep]
+    used = np.zeros(len(pts), dtype=bool)
+    used[conn.ravel()] = True
+    remap = -np.ones(len(pts), dtype=np.int64)
+    remap[used] = np.arange(used.sum())
+    pts = pts[used]
+    conn = remap[conn].astype(np.int32)
+    lo, hi = np.zeros(3), np.ones(3)
+    node_flag = _box_flags(pts, lo, hi, open_top=True)
+    return _finish(pts, conn, node_flag, _face_flag_box(lo, hi, True), f"box_tet_delaunay_n{n}")
+
+
+def box_hex(nx: int, ny: int, nz: int, jitter: float = 0.1, seed: int = 4) -> Mesh:
+    """Structured hexahedra of the unit box with interior-node jitter (fraction of h)."""
+    rng = np.random.default_rng(seed)
+    xs, ys, zs = np.linspace(0, 1, nx + 1), np.linspace(0, 1, ny + 1), np.linspace(0, 1, nz + 1)
+    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    h = np.array([1.0 / nx, 1.0 / ny, 1.0 / nz])
+    d = rng.uniform(-1.0, 1.0, size=pts.shape) * jitter * h
+    d[(pts < 1e-12) | (pts > 1 - 1e-12)] = 0.0
+    pts = pts + d
+    idx = np.arange(pts.shape[0]).reshape(nx + 1, ny + 1, nz + 1)
+
+    def c(i0, j0, k0):
+        return idx[i0:i0 + nx, j0:j0 + ny, k0:k0 + nz].ravel()
+    conn = np.stack([c(0, 0, 0), c(1, 0, 0), c(1, 1, 0), c(0, 1, 0),
+                     c(0, 0, 1), c(1, 0, 1), c(1, 1, 1), c(0, 1, 1)], axis=1).astype(np.int32)
+    lo, hi = np.zeros(3), np.ones(3)
+    node_flag = _box_flags(pts, lo, hi, open_top=True)
+    return _finish(pts, conn, node_flag, _face_flag_box(lo, hi, True), f"box_hex_{nx}x{ny}x{nz}")
+
+
+# ---------------------------------------------------------------------------
+# Materials
+
+def melt(rng) -> "object":
+    """Weakly compressible melt: rho 2400, bulk modulus 1e10 (beta 1e-10), viscosity
+    log-uniform in [1e2, 1e4] (one seeded value), alpha 3e-5, cp 1200, kappa 1.5."""
+    mu = float(10.0 ** rng.uniform(2.0, 4.0))
+    return custom_chemical(rho=2400.0, mu=mu, cp=1200.0, kappa=1.5, alpha=3.0e-5, beta=1.0e-10)
+
+
+def material_for(nb_comp: int, seed: int = 0) -> Material:
+    rng = np.random.default_rng(seed)
+    if nb_comp == 1:
+        return Material([melt(rng)])
+    if nb_comp == 2:
+        return Material([melt(rng), ideal_gas(8.314462 / 461.0, 1.4)])
+    if nb_comp == 3:
+        return Material([melt(rng), ideal_gas_named("H2O"), ideal_gas_named("CO2")])
+    return Material([melt(rng), ideal_gas_named("H2O"), ideal_gas_named("CO2"), ideal_gas_named("AIR")])
+
+
+def setup_for(dim: int, nb_comp: int, dirichlet_T_everywhere: bool = False, **kw) -> Setup:
+    """Shipped-case flags (tau 2019, dc_2006, dc_sharp 2) with the P0 wall policy.
+    3D uses gravity (0, 0, -9.81)."""
+    if dim == 3 and "gravity" not in kw:
+        kw["gravity"] = (0.0, 0.0, -9.81)
+    s = Setup(dim, **kw)
+    return p0_policy(s, nb_comp, dirichlet_T_everywhere=dirichlet_T_everywhere)
+
+
+# ---------------------------------------------------------------------------
+# States
+
+def _fourier(x: np.ndarray, rng, modes: int = 8, kmax: int = 3) -> np.ndarray:
+    dim = x.shape[1]
+    f = np.zeros(len(x))
+    for _ in range(modes):
+        k = rng.integers(-kmax, kmax + 1, size=dim)
+        if not k.any():
+            k[0] = 1
+        phi = rng.uniform(0, 2 * np.pi)
+        a = rng.normal()
+        f += a * np.sin(2 * np.pi * (x @ k) + phi)
+    m = np.max(np.abs(f))
+    return f / m if m > 0 else f
+
+
+def state_for(mesh: Mesh, nb_comp: int, seed: int = 0, perturb: float = 1e-4, no_slip_flag: int = WALL):
+    """Seeded (I, P) nodal states, AoS float64 of shape (n_nodes*nd,)."""
+    rng = np.random.default_rng(seed)
+    x = mesh.coords
+    dim = x.shape[1]
+    nd = nb_dofs(dim, nb_comp)
+    n = len(x)
+    ext = x.max(axis=0) - x.min(axis=0)
+    xn = (x - x.min(axis=0)) / np.where(ext > 0, ext, 1.0)
+    height = xn[:, -1]
+    S = np.zeros((n, nd))
+    S[:, 0] = (1e5 + (1e8 - 1e5) * (1.0 - height)) * (1.0 + 0.01 * rng.normal(size=n))
+    for k in range(dim):
+        S[:, 1 + k] = 0.1 * _fourier(xn, rng)
+    S[node_flag_mask(mesh, no_slip_flag), 1:1 + dim] = 0.0
+    S[:, dim + 1] = 1273.0 + 50.0 * _fourier(xn, rng)
+    if nb_comp == 2:
+        S[:, dim + 2] = np.clip(0.5 + 0.7 * _fourier(xn, rng), 0.0, 1.0)
+    elif nb_comp > 2:
+        w = np.stack([np.exp(1.5 * _fourier(xn, rng)) for _ in range(nb_comp)], axis=1)
+        w[:, 0] *= 6.0    # melt-dominated mixture
+        Y = w / w.sum(axis=1, keepdims=True)
+        S[:, dim + 2:] = Y[:, :nb_comp - 1]
+    I = S.ravel().copy()
+    P = I.copy()
+    if perturb:
+        scale = np.abs(S).max(axis=0)
+        dP = perturb * rng.normal(size=S.shape) * scale
+        dP[:, 1:1 + dim] *= 1.0
+        P = (S + dP).ravel()
+    return I, P
+
+
+def node_flag_mask(mesh: Mesh, flag: int) -> np.ndarray:
+    return mesh.node_flag == flag
+
+
+def workload(name: str, seed: int = 0):
+    """(mesh, material, setup, I, P, dt) of a named workload."""
+    if name == "c0_tri":
+        mesh = channel_tri()
+        nc = 2
+    elif name == "c1_tet":
+        mesh = box_tet_delaunay(56, seed=seed + 1)
+        nc = 3
+    elif name == "c3_tet":
+        mesh = box_tet_delaunay(33, seed=seed + 3)
+        nc = 3
+    elif name == "c4_hex":
+        mesh = box_hex(160, 160, 156, seed=seed + 4)
+        nc = 4
+    else:
+        raise KeyError(name)
+    mat = material_for(nc, seed)
+    setup = setup_for(mesh.dim, nc)
+    I, P = state_for(mesh, nc, seed)
+    return mesh, mat, setup, I, P, 1e-3

@@ -1,0 +1,223 @@
+/*
+ * gales_asm.h — C ABI of the GB300 assembly library for the compressible
+ * multicomponent fluid_mc equations of GALES-multi-fluid.
+ *
+ * One call fills the global CSR tangent matrix A and the right-hand side b of
+ * one Newton iteration, exactly what the reference's
+ *   fluid_assembly<fluid<ic_bc,dim>, scatter<dofs_ic_bc>, dim>::execute()
+ * (sim/fluid_mc/P0/fluid_assembly.hpp:39-68) fills into its Epetra
+ * linear_system (src/fem/ls/linear_system.hpp:35-105).  The element-level
+ * plugin points of the reference (fluid::execute_i / execute_b,
+ * sim/fluid_mc/P0/fluid_2d.hpp:171,209, and scatter::execute,
+ * src/fem/ls/scatter.hpp:37) are too fine-grained for a GPU, so the whole
+ * assembly driver is the replaced unit.
+ *
+ * Conventions (all taken from the reference):
+ *   - dofs per node nd = 2 + dim + nb_comp - 1, ordered
+ *     (p, v_1..v_dim, T, Y_1..Y_{nb_comp-1})        (main.cpp:82, fluid_2d.hpp:86-92)
+ *   - nodal state is AoS FP64, index node*nd + k; slot I = current iterate,
+ *     slot P = previous time level                 (dof_state.hpp:43-49)
+ *   - global dof id = node*nd + k                   (node.hpp:73)
+ *   - the matrix is scalar CSR with sorted global column ids per row; every
+ *     element contributes a dense (nen*nd)^2 block (linear_system.hpp:46-63)
+ *   - b = -R (the element returns r = -r_, fluid_2d.hpp:200-201) and
+ *     Dirichlet rows are replaced as in scatter.hpp:62-78.
+ *
+ * Errors: every entry point returns an int status (0 = OK, otherwise an OR of
+ * GALES_ERR_* bits).  Kernels never trap; a device status word records the
+ * first offending element.  The reference aborts through MPI_Abort instead
+ * (src/fem/base/algorithm.hpp:37-44).
+ *
+ * Pointers passed to assemble/residual/vjp may be host or device memory; the
+ * library detects which with cudaPointerGetAttributes.  A handle is
+ * single-threaded and stream-ordered; distinct handles are independent.
+ */
+#ifndef GALES_ASM_H_
+#define GALES_ASM_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GALES_MAX_DIM 3
+#define GALES_MAX_COMP 8
+#define GALES_MAX_ND (2 + GALES_MAX_DIM + GALES_MAX_COMP - 1)
+#define GALES_MAX_FLAGS 32
+
+/* status bits */
+#define GALES_OK 0
+#define GALES_ERR_BAD_INPUT 1
+#define GALES_ERR_NEG_JACOBIAN 2   /* quad.hpp:215-218, 549-552 */
+#define GALES_ERR_SINGULAR 4       /* algorithm.hpp:406-410 (LU of DUDY) */
+#define GALES_ERR_NONFINITE 8
+#define GALES_ERR_CUDA 16
+#define GALES_ERR_UNSUPPORTED 32
+#define GALES_ERR_NO_MEMORY 64
+
+/* numerical forms */
+#define GALES_FORM_FP64 0    /* every operation in FP64 (the reference's arithmetic) */
+#define GALES_FORM_MIXED 1   /* FP32 element integrals; FP64 EOS, tau, accumulation */
+
+/* chemical kinds (src/fem/physical_props/fluid/chemicals.hpp) */
+#define GALES_CH_CUSTOM 0     /* custom_chemical, chemicals.hpp:19-49 */
+#define GALES_CH_IDEAL_GAS 1  /* ideal_gas, chemicals.hpp:198-271 */
+
+/* stabilisation parameter variants (fluid_2d.hpp:877-1022) */
+#define GALES_TAU_NONE 0
+#define GALES_TAU_NON_DIAG_COMP_2001 2001
+#define GALES_TAU_NON_DIAG_COMP_2019 2019
+#define GALES_TAU_DIAG_INCOMP_2007 2007
+#define GALES_TAU_DIAG_2014 2014
+
+/* VJP modes */
+#define GALES_VJP_EXACT 0    /* lambda^T dB/dI of the assembled rhs, all coefficients differentiated */
+#define GALES_VJP_FROZEN 1   /* A^T lambda with the frozen-coefficient tangent A */
+
+/* scatter strategies */
+#define GALES_SCATTER_ATOMIC 0
+#define GALES_SCATTER_COLOURED 1
+
+/* Mesh on one rank.  Node ids are 0..n_nodes-1 and equal the node gid.
+ * Element node order and side numbering follow element.hpp:63-176 (2D) and
+ * element.hpp:360-477 (3D).  Supported (dim, nen): (2,3) tri, (2,4) quad,
+ * (3,4) tet, (3,8) hex. */
+typedef struct gales_mesh_desc {
+  int32_t dim;
+  int32_t nen;
+  int64_t n_nodes;
+  int64_t n_elements;
+  const double* coords;          /* [n_nodes][dim] */
+  const int32_t* conn;           /* [n_elements][nen] */
+  const int32_t* node_flag;      /* [n_nodes], node.hpp flag (0 interior) */
+  const uint8_t* el_on_boundary; /* [n_elements], element flag > 0 (mesh.hpp:224-225); NULL = none */
+  int64_t n_bd_sides;            /* sides with side flag > 0 (mesh.hpp:409-446) */
+  const int32_t* bd_side_el;     /* [n_bd_sides] element index */
+  const int32_t* bd_side_local;  /* [n_bd_sides] local side index of that element */
+  const int32_t* bd_side_flag;   /* [n_bd_sides] side flag (1..GALES_MAX_FLAGS-1) */
+} gales_mesh_desc;
+
+/* Stored constants of one chemical after construction (base_chemical.hpp:80-90).
+ * custom: rho, mu, cp, kappa, alpha, beta are constants; cv is derived per call
+ *         as cp - T*alpha^2/(rho*beta) (cp if beta == 0), c = 1/sqrt(rho*beta).
+ * ideal gas: R (specific gas constant), gamma, cv, cp, mu, kappa are constants;
+ *         rho = p/(R T), beta = 1/p, alpha = 1/T, c = sqrt(gamma R T). */
+typedef struct gales_chemical_desc {
+  int32_t kind;
+  int32_t reserved;
+  double rho, mu, cp, cv, kappa, alpha, beta;
+  double R, gamma;
+  double chemical_diffusivity; /* base_chemical.hpp:86 default 1e-10 */
+} gales_chemical_desc;
+
+/* mix_of_ch mixture (fluid_properties.hpp:199-227) */
+typedef struct gales_material_desc {
+  int32_t nb_comp;
+  int32_t reserved;
+  gales_chemical_desc comp[GALES_MAX_COMP];
+} gales_material_desc;
+
+/* Neumann / prescribed mass flux data of one side flag, the data form of the
+ * policy calls fluid_ic_bc::neumann_* and mass_flux* (fluid_ic_bc.hpp:133-211)
+ * consumed by fluid_2d.hpp:610-868.  Stress override tau_kj (k <= j) is bit
+ * k*3+j of tau_mask with value tau[k*3+j]; heat flux q_k is bit k; species
+ * flux J_k of component i is bit k*8+i; mass flux rho*v_k is bit k. */
+typedef struct gales_side_bc {
+  uint32_t tau_mask;
+  uint32_t q_mask;
+  uint32_t J_mask;
+  uint32_t mass_flux_mask;
+  double tau[9];
+  double q[3];
+  double J[3][8];
+  double mass_flux[3];
+} gales_side_bc;
+
+/* Run-time flags (read_setup.hpp; sim/fluid_mc/P0/setup.txt:24-31) plus the
+ * ic_bc policy as data. */
+typedef struct gales_setup_desc {
+  int32_t tau;            /* GALES_TAU_* */
+  int32_t dc_2006;        /* discontinuity capturing on/off */
+  int32_t steady_state;
+  int32_t reserved;
+  double dc_sharp;        /* 1, 1.5 or 2 (fluid_2d.hpp:1055-1057) */
+  double dc_scale_fact;
+  double gravity[3];      /* fluid_ic_bc::body_force, fluid_ic_bc.hpp:44-56 */
+  double p_ref, T_ref;    /* dc_2006 reference state, fluid_ic_bc.hpp:33 */
+  double v_ref[3];
+  /* per node flag: bit k set = dof k Dirichlet-constrained
+   * (fluid_dofs_ic_bc::dof_constraint, fluid_dofs_ic_bc.hpp:86-117) */
+  uint32_t dirichlet_mask[GALES_MAX_FLAGS];
+  gales_side_bc side_bc[GALES_MAX_FLAGS];
+} gales_setup_desc;
+
+typedef struct gales_asm gales_asm;
+
+/* Fill a chemical descriptor the way the reference constructors do. */
+void gales_chemical_custom(gales_chemical_desc* c, double rho, double mu, double cp, double kappa,
+                           double alpha, double beta);               /* chemicals.hpp:23-33 */
+void gales_chemical_ideal_gas(gales_chemical_desc* c, double molar_mass, double gamma); /* chemicals.hpp:237-246 */
+/* Defaults of the shipped case: tau 2019, dc_2006 on, dc_sharp 2, scale 1,
+ * unsteady, gravity (0,-9.81) in 2D and 0 in 3D, p_ref 70e6, T_ref 1300,
+ * v_ref 0, no Dirichlet, no Neumann overrides. */
+void gales_setup_default(gales_setup_desc* s, int32_t dim);
+
+/* Create a handle: uploads the mesh, builds the CSR graph (linear_system.hpp:40-66),
+ * the element colouring and the per-element CSR slot table.  Replaces
+ * linear_system's constructor and fluid's constructor (u_ref_inv, fluid_2d.hpp:123-135). */
+int gales_asm_create(const gales_mesh_desc* mesh, const gales_material_desc* mat,
+                     const gales_setup_desc* setup, int device, gales_asm** out);
+void gales_asm_destroy(gales_asm* h);
+
+/* CSR pattern on the host (owned by the handle): n_rows = n_nodes*nd,
+ * row_ptr[n_rows+1] (int64), col[nnz] (int32, sorted per row). */
+int gales_asm_pattern(gales_asm* h, int64_t* n_rows, int64_t* nnz, const int64_t** row_ptr,
+                      const int32_t** col);
+/* Node-level graph (the CSR is this graph with every entry expanded to an nd x nd block). */
+int gales_asm_node_graph(gales_asm* h, int64_t* n_nodes, int64_t* nnz_nodes,
+                         const int64_t** node_row_ptr, const int32_t** node_col);
+/* Greedy element colouring: no two elements of one colour share a node. */
+int gales_asm_colouring(gales_asm* h, int32_t* n_colours, const int32_t** colour);
+int gales_asm_set_scatter(gales_asm* h, int32_t mode); /* GALES_SCATTER_* */
+
+/* One assembly: vals[nnz] and rhs[n_rows] are overwritten (linear_system::clear
+ * is part of the call, linear_system.hpp:90-94).  stream: cudaStream_t or NULL. */
+int gales_asm_assemble(gales_asm* h, const double* I, const double* P, double dt, int32_t form,
+                       double* vals, double* rhs, void* stream);
+/* Residual only (rhs), no matrix. */
+int gales_asm_residual(gales_asm* h, const double* I, const double* P, double dt, int32_t form,
+                       double* rhs, void* stream);
+/* Vector-Jacobian product of the assembled rhs b(I; theta):
+ *   g_state[n_rows]  = (db/dI)^T lambda           (mode EXACT)
+ *                    = A^T lambda                  (mode FROZEN, A the assembled tangent)
+ *   g_params[3*nb_comp] = (db/dtheta)^T lambda, theta_c = (density parameter, mu, cp) of
+ *                    component c (density parameter = rho for custom chemicals, molar mass
+ *                    for ideal gases).  Only in mode EXACT; may be NULL. */
+int gales_asm_vjp(gales_asm* h, const double* I, const double* P, double dt, const double* lambda,
+                  int32_t mode, double* g_state, double* g_params, void* stream);
+/* Element-level blocks, the batched form of the reference's integral plugin call
+ *   fluid::execute_i(el, dofs, m, r)   (which = 0, fluid_2d.hpp:171-202)
+ *   fluid::execute_b(el, dofs, m, r)   (which = 1, fluid_2d.hpp:209-245)
+ * for the n listed elements: m_out[n][(nen*nd)^2] (row-major, row nd*b+jb) and
+ * r_out[n][nen*nd] with r = -r_, before Dirichlet rows and scatter.  m_out may be
+ * NULL (residual only).  elements is a host array. */
+int gales_asm_element_blocks(gales_asm* h, const double* I, const double* P, double dt, int32_t form,
+                             int32_t which, const int32_t* elements, int64_t n, double* m_out,
+                             double* r_out, void* stream);
+/* ||b||_2 of a rhs vector (residual_check.hpp:48-51). */
+int gales_asm_norm2(gales_asm* h, const double* rhs, double* out, void* stream);
+
+/* Status of the last call: error bits and the first offending element (-1 if none). */
+int gales_asm_status(gales_asm* h, int64_t* first_bad_element);
+const char* gales_asm_last_error(gales_asm* h);
+/* Device time in ms of the last assemble/residual/vjp call (CUDA events on its stream). */
+double gales_asm_last_ms(gales_asm* h);
+/* Number of kernel launches made by the library since the handle was created. */
+int64_t gales_asm_launch_count(gales_asm* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GALES_ASM_H_ */

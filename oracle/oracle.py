@@ -1,0 +1,166 @@
+"""TEST INFRASTRUCTURE — ctypes binding of the CPU oracle (gales_oracle.cpp).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this,
+as the checker.  PARITY UNPINNED: the reference itself cannot be built here
+(Boost, MPI and Trilinos are absent) and ships no golden data; see the header
+of gales_oracle.cpp.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import importlib
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+if str(HERE) not in sys.path:
+    sys.path.insert(0, str(HERE))
+
+import build as _build  # noqa: E402  (oracle/build.py)
+
+gm = importlib.import_module("gales-multi-fluid_gb300")
+abi = gm.abi
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        vp, dp, i64p, i32p = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int32)
+        L.gor_properties.argtypes = [C.POINTER(abi.MaterialDesc), C.c_double, C.c_double, dp, dp]
+        L.gor_inverse.argtypes = [C.c_int, dp, dp]
+        L.gor_quad.argtypes = [C.c_int, C.c_int, dp, dp, C.c_int, dp]
+        L.gor_gauss.argtypes = [C.c_int, C.c_int, dp, i32p, dp, i32p]
+        L.gor_pattern_count.argtypes = [C.POINTER(abi.MeshDesc), C.c_int, i64p]
+        L.gor_pattern_count.restype = C.c_int64
+        L.gor_pattern.argtypes = [C.POINTER(abi.MeshDesc), C.c_int, i64p, i32p, i64p, i32p]
+        L.gor_colouring.argtypes = [C.POINTER(abi.MeshDesc), i32p, i32p]
+        L.gor_element.argtypes = [C.POINTER(abi.MeshDesc), C.POINTER(abi.MaterialDesc), C.POINTER(abi.SetupDesc),
+                                  dp, dp, C.c_double, C.c_int64, C.c_int, dp, dp]
+        L.gor_assemble.argtypes = [C.POINTER(abi.MeshDesc), C.POINTER(abi.MaterialDesc), C.POINTER(abi.SetupDesc),
+                                   dp, dp, C.c_double, i64p, i32p, dp, dp, C.c_int, i32p, C.c_int32, i64p]
+        for f in ("gor_properties", "gor_inverse", "gor_quad", "gor_gauss", "gor_pattern", "gor_colouring",
+                  "gor_element", "gor_assemble"):
+            getattr(L, f).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i64(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def _i32(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def properties(material, p, T, Y):
+    nc = material.nb_comp
+    out = np.zeros(9 + 3 * nc)
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    lib().gor_properties(C.byref(material.desc), p, T, _d(Y), _d(out))
+    keys = ["rho", "mu", "cp", "cv", "kappa", "D", "c", "alpha", "beta"]
+    d = dict(zip(keys, out[:9]))
+    d["rho_c"] = out[9::3].copy()
+    d["e_c"] = out[10::3].copy()
+    d["D_c"] = out[11::3].copy()
+    return d
+
+
+def inverse(A):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    n = A.shape[0]
+    inv = np.zeros_like(A)
+    s = lib().gor_inverse(n, _d(A), _d(inv))
+    return inv, s
+
+
+def quad(dim, nen, xe, pt, boundary=False):
+    xe = np.ascontiguousarray(xe, dtype=np.float64)
+    pt = np.ascontiguousarray(pt, dtype=np.float64)
+    out = np.zeros(nen + dim * nen + 2 + dim * dim + 2 * dim)
+    rc = lib().gor_quad(dim, nen, _d(xe), _d(pt), int(boundary), _d(out))
+    o = 0
+    sh = out[o:o + nen]; o += nen
+    ds = out[o:o + dim * nen].reshape(dim, nen); o += dim * nen
+    J, JxW = out[o], out[o + 1]; o += 2
+    G = out[o:o + dim * dim].reshape(dim, dim); o += dim * dim
+    g = out[o:o + dim]; o += dim
+    JNxW = out[o:o + dim]
+    return dict(sh=sh, ds=ds, J=J, JxW=JxW, G=G, g=g, JNxW=JNxW, status=rc)
+
+
+def gauss(dim, nen):
+    gp = np.zeros(8 * 3)
+    sides = np.zeros(6 * 4, dtype=np.int32)
+    sgp = np.zeros(6 * 4 * 3)
+    cnt = np.zeros(4, dtype=np.int32)
+    lib().gor_gauss(dim, nen, _d(gp), _i32(sides), _d(sgp), _i32(cnt))
+    nq, ns, nsn, nqs = (int(x) for x in cnt)
+    return dict(gp=gp[:nq * 3].reshape(nq, 3), sides=sides[:ns * nsn].reshape(ns, nsn),
+                sgp=sgp[:ns * nqs * 3].reshape(ns, nqs, 3))
+
+
+def pattern(mesh, nd, scalar=True):
+    nnz_nodes = C.c_int64()
+    nnz = lib().gor_pattern_count(C.byref(mesh.desc()), nd, C.byref(nnz_nodes))
+    nrp = np.zeros(mesh.n_nodes + 1, dtype=np.int64)
+    ncol = np.zeros(nnz_nodes.value, dtype=np.int32)
+    if scalar:
+        rp = np.zeros(mesh.n_nodes * nd + 1, dtype=np.int64)
+        col = np.zeros(nnz, dtype=np.int32)
+        lib().gor_pattern(C.byref(mesh.desc()), nd, _i64(nrp), _i32(ncol), _i64(rp), _i32(col))
+        return nrp, ncol, rp, col
+    lib().gor_pattern(C.byref(mesh.desc()), nd, _i64(nrp), _i32(ncol), None, None)
+    return nrp, ncol, None, None
+
+
+def colouring(mesh):
+    colour = np.zeros(mesh.n_elements, dtype=np.int32)
+    nc = C.c_int32()
+    lib().gor_colouring(C.byref(mesh.desc()), _i32(colour), C.byref(nc))
+    return colour, nc.value
+
+
+def element(mesh, material, setup, I, P, dt, e, which=0, want_matrix=True):
+    nd = gm.nb_dofs(mesh.dim, material.nb_comp)
+    n = mesh.nen * nd
+    m = np.zeros((n, n)) if want_matrix else None
+    r = np.zeros(n)
+    I = np.ascontiguousarray(I, dtype=np.float64)
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    s = lib().gor_element(C.byref(mesh.desc()), C.byref(material.desc), C.byref(setup.desc), _d(I), _d(P), dt, e,
+                          which, _d(m) if want_matrix else None, _d(r))
+    return m, r, s
+
+
+def assemble(mesh, material, setup, I, P, dt, row_ptr, col, want_matrix=True, nthreads=1, colour=None,
+             n_colours=0):
+    """fluid_assembly::execute on the CPU: returns (vals, rhs, status, first_bad)."""
+    I = np.ascontiguousarray(I, dtype=np.float64)
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    vals = np.zeros(int(row_ptr[-1])) if want_matrix else None
+    rhs = np.zeros(len(row_ptr) - 1)
+    fb = C.c_int64(-1)
+    colour_p = None
+    if colour is not None:
+        colour = np.ascontiguousarray(colour, dtype=np.int32)
+        colour_p = _i32(colour)
+    s = lib().gor_assemble(C.byref(mesh.desc()), C.byref(material.desc), C.byref(setup.desc), _d(I), _d(P), dt,
+                           _i64(row_ptr), _i32(col), _d(vals) if want_matrix else None, _d(rhs), nthreads, colour_p,
+                           n_colours, C.byref(fb))
+    return vals, rhs, s, fb.value
