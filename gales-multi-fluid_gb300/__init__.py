@@ -428,6 +428,10 @@ class FluidAssembly:
     def device_ms(self) -> float:
         return self._L.gales_asm_last_ms(self._h)
 
+    def phase_ms(self, phase: int) -> float:
+        """0 = clear, 1 = interior kernel(s), 2 = boundary pass (CUDA events, last call)."""
+        return self._L.gales_asm_last_phase_ms(self._h, phase)
+
     def launch_count(self) -> int:
         return self._L.gales_asm_launch_count(self._h)
 

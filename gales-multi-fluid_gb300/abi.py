@@ -130,6 +130,8 @@ def lib() -> C.CDLL:
     L.gales_asm_last_error.restype = C.c_char_p
     L.gales_asm_last_ms.argtypes = [vp]
     L.gales_asm_last_ms.restype = C.c_double
+    L.gales_asm_last_phase_ms.argtypes = [vp, i32]
+    L.gales_asm_last_phase_ms.restype = C.c_double
     L.gales_asm_launch_count.argtypes = [vp]
     L.gales_asm_launch_count.restype = C.c_int64
     _lib = L
@@ -141,5 +143,5 @@ EXPORTED = [
     "gales_asm_create", "gales_asm_destroy", "gales_asm_pattern", "gales_asm_node_graph",
     "gales_asm_colouring", "gales_asm_set_scatter", "gales_asm_assemble", "gales_asm_residual",
     "gales_asm_vjp", "gales_asm_element_blocks", "gales_asm_norm2", "gales_asm_status", "gales_asm_last_error",
-    "gales_asm_last_ms", "gales_asm_launch_count",
+    "gales_asm_last_ms", "gales_asm_last_phase_ms", "gales_asm_launch_count",
 ]

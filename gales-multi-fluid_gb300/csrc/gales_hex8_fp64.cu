@@ -4,14 +4,12 @@
 
 namespace gales {
 
-using D_hex8 = ElementDispatch<3, 8, 8, 6, 4>;
-
-LaunchResult interior_hex8_fp64(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
-  return D_hex8::interior<GALES_FORM_FP64>(k, nc, want_m, n, st);
-}
+InteriorOps interior_ops_hex8_fp64() { return InteriorDispatch<3, 8, 8, GALES_FORM_FP64>::ops(); }
 
 LaunchResult boundary_hex8(const KParams& k, int nc, long long n, cudaStream_t st) {
-  return D_hex8::boundary(k, nc, n, st);
+  return boundary_dispatch<3, 8, 6, 4>(k, nc, n, st);
 }
+
+GeometryOps geometry_ops_hex8() { return GeometryDispatch<3, 8, 8>::ops(); }
 
 }  // namespace gales

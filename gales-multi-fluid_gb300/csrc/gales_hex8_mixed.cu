@@ -4,10 +4,6 @@
 
 namespace gales {
 
-using D_hex8 = ElementDispatch<3, 8, 8, 6, 4>;
-
-LaunchResult interior_hex8_mixed(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
-  return D_hex8::interior<GALES_FORM_MIXED>(k, nc, want_m, n, st);
-}
+InteriorOps interior_ops_hex8_mixed() { return InteriorDispatch<3, 8, 8, GALES_FORM_MIXED>::ops(); }
 
 }  // namespace gales

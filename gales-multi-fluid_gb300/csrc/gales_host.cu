@@ -142,6 +142,51 @@ void parallel_for(int64_t n, F f) {
   for (auto& x : th) x.join();
 }
 
+// Each point-record chunk buffer holds this many bytes; two of them stay resident
+// in L2 (about a quarter of the 129 MB) while the CSR values stream through it.
+constexpr size_t kChunkBytes = size_t(32) << 20;
+
+GeometryOps geometry_ops(int dim, int nen) {
+  if (dim == 2 && nen == 3) return geometry_ops_tri3();
+  if (dim == 2 && nen == 4) return geometry_ops_quad4();
+  if (dim == 3 && nen == 4) return geometry_ops_tet4();
+  return geometry_ops_hex8();
+}
+
+// Shape functions at a reference point (quad.hpp:153-187, 476-514); products and sums
+// only, so host and device evaluate them identically.
+void shape_values(int dim, int nen, const double* pt, double* sh) {
+  const double xi = pt[0], eta = pt[1], zeta = pt[2];
+  if (dim == 2 && nen == 3) {
+    sh[0] = 1.0 - xi - eta; sh[1] = xi; sh[2] = eta;
+  } else if (dim == 2 && nen == 4) {
+    sh[0] = 0.25 * (1.0 - xi) * (1.0 - eta);
+    sh[1] = 0.25 * (1.0 + xi) * (1.0 - eta);
+    sh[2] = 0.25 * (1.0 + xi) * (1.0 + eta);
+    sh[3] = 0.25 * (1.0 - xi) * (1.0 + eta);
+  } else if (dim == 3 && nen == 4) {
+    sh[0] = 1.0 - xi - eta - zeta; sh[1] = xi; sh[2] = eta; sh[3] = zeta;
+  } else {
+    const double sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+    const double sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+    const double sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+    for (int i = 0; i < 8; ++i) {
+      const double ax = sx[i] < 0 ? (1.0 - xi) : (1.0 + xi);
+      const double ay = sy[i] < 0 ? (1.0 - eta) : (1.0 + eta);
+      const double az = sz[i] < 0 ? (1.0 - zeta) : (1.0 + zeta);
+      sh[i] = 0.125 * ax * ay * az;
+    }
+  }
+}
+
+InteriorOps interior_ops(int dim, int nen, int form) {
+  const bool f64 = form == GALES_FORM_FP64;
+  if (dim == 2 && nen == 3) return f64 ? interior_ops_tri3_fp64() : interior_ops_tri3_mixed();
+  if (dim == 2 && nen == 4) return f64 ? interior_ops_quad4_fp64() : interior_ops_quad4_mixed();
+  if (dim == 3 && nen == 4) return f64 ? interior_ops_tet4_fp64() : interior_ops_tet4_mixed();
+  return f64 ? interior_ops_hex8_fp64() : interior_ops_hex8_mixed();
+}
+
 }  // namespace
 
 struct gales_asm {
@@ -179,7 +224,14 @@ struct gales_asm {
   unsigned int* h_status = nullptr;              // pinned
   unsigned long long* h_first_bad = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t evp[4] = {nullptr, nullptr, nullptr, nullptr};  // clear | interior | boundary | end
   int32_t scatter_mode = GALES_SCATTER_ATOMIC;
+  // interior pipeline: point-record chunk buffers (scratch) and two internal streams
+  InteriorOps ops[2];
+  DevBuf<unsigned char> qpbuf[2];
+  DevBuf<unsigned char> d_geo;   // element geometry at the interior points (mesh.hpp:468-495)
+  cudaStream_t ist[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
   int status = 0;
   int64_t first_bad = -1;
   double last_ms = 0.0;
@@ -372,6 +424,10 @@ int validate(gales_asm* h, const gales_mesh_desc* m, const gales_material_desc* 
 
 }  // namespace
 
+namespace {
+KParams base_params(gales_asm* h, double dt);
+}  // namespace
+
 extern "C" {
 
 void gales_chemical_custom(gales_chemical_desc* c, double rho, double mu, double cp, double kappa,
@@ -508,6 +564,36 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   if ((ce = cudaMallocHost(&h->h_first_bad, sizeof(unsigned long long))) != cudaSuccess) return bail(ce, "pinned");
   if ((ce = cudaEventCreate(&h->ev0)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(ce, "event");
+  for (int i = 0; i < 4; ++i)
+    if ((ce = cudaEventCreate(&h->evp[i])) != cudaSuccess) return bail(ce, "event");
+  if ((ce = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+  for (int i = 0; i < 2; ++i) {
+    if ((ce = cudaEventCreateWithFlags(&h->ev_join[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+    if ((ce = cudaStreamCreateWithFlags(&h->ist[i], cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
+    if ((ce = h->qpbuf[i].alloc(kChunkBytes)) != cudaSuccess) return bail(ce, "point-record buffer");
+  }
+  h->ops[GALES_FORM_FP64] = interior_ops(h->dim, h->nen, GALES_FORM_FP64);
+  h->ops[GALES_FORM_MIXED] = interior_ops(h->dim, h->nen, GALES_FORM_MIXED);
+  {  // element geometry, once per mesh; an inverted element fails here as it does at mesh load
+    GeometryOps g = geometry_ops(h->dim, h->nen);
+    if ((ce = h->d_geo.alloc(g.bytes_per_element * (size_t)h->n_el)) != cudaSuccess) return bail(ce, "geometry");
+    KParams k = base_params(h, 1.0);
+    if ((ce = cudaMemset(h->d_status.p, 0, sizeof(unsigned int))) != cudaSuccess) return bail(ce, "status");
+    if ((ce = cudaMemset(h->d_first_bad.p, 0xff, sizeof(unsigned long long))) != cudaSuccess) return bail(ce, "status");
+    LaunchResult r = g.launch(h->d_coords.p, h->d_conn.p, k, h->d_geo.p, h->n_el, 0);
+    if (r.err != cudaSuccess) return bail(r.err, "geometry kernel");
+    h->launches += r.launches;
+    if ((ce = cudaDeviceSynchronize()) != cudaSuccess) return bail(ce, "geometry kernel");
+    unsigned int st = 0;
+    unsigned long long fb = 0;
+    cudaMemcpy(&st, h->d_status.p, sizeof(st), cudaMemcpyDeviceToHost);
+    cudaMemcpy(&fb, h->d_first_bad.p, sizeof(fb), cudaMemcpyDeviceToHost);
+    if (st) {
+      fprintf(stderr, "gales_asm_create: Jacobian is not positive at element %llu (quad.hpp:215-218)\n", fb);
+      gales_asm_destroy(h);
+      return (int)st;
+    }
+  }
   *out = h;
   return 0;
 }
@@ -518,12 +604,20 @@ void gales_asm_destroy(gales_asm* h) {
   h->d_coords.release(); h->d_conn.release(); h->d_node_flag.release();
   h->d_colour_order.release(); h->d_bd_list.release(); h->d_node_rp.release();
   h->d_slot.release(); h->d_bd_sides.release(); h->d_side_bc.release();
-  h->d_status.release(); h->d_first_bad.release();
+  h->d_status.release(); h->d_first_bad.release(); h->d_geo.release();
   h->s_I.release(); h->s_P.release(); h->s_vals.release(); h->s_rhs.release(); h->s_aux.release();
   if (h->h_status) cudaFreeHost(h->h_status);
   if (h->h_first_bad) cudaFreeHost(h->h_first_bad);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  for (int i = 0; i < 4; ++i)
+    if (h->evp[i]) cudaEventDestroy(h->evp[i]);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  for (int i = 0; i < 2; ++i) {
+    if (h->ev_join[i]) cudaEventDestroy(h->ev_join[i]);
+    if (h->ist[i]) cudaStreamDestroy(h->ist[i]);
+    h->qpbuf[i].release();
+  }
   delete h;
 }
 
@@ -604,6 +698,8 @@ KParams base_params(gales_asm* h, double dt) {
   memcpy(k.gp, h->ei.gp, sizeof(k.gp));
   memcpy(k.sgp, h->ei.sgp, sizeof(k.sgp));
   k.W_in = h->ei.W_in;
+  for (int q = 0; q < h->ei.nq; ++q) shape_values(h->dim, h->nen, h->ei.gp[q], k.sh_tab[q]);
+  k.geo = h->d_geo.p;
   k.W_bd = h->ei.W_bd;
   k.tau = h->setup.tau;
   k.dc_2006 = h->setup.dc_2006;
@@ -624,16 +720,40 @@ KParams base_params(gales_asm* h, double dt) {
   return k;
 }
 
-LaunchResult dispatch_interior(gales_asm* h, const KParams& k, int form, bool want_m, long long n,
-                               cudaStream_t st) {
-  const bool f64 = form == GALES_FORM_FP64;
-  if (h->dim == 2 && h->nen == 3)
-    return f64 ? interior_tri3_fp64(k, h->nc, want_m, n, st) : interior_tri3_mixed(k, h->nc, want_m, n, st);
-  if (h->dim == 2 && h->nen == 4)
-    return f64 ? interior_quad4_fp64(k, h->nc, want_m, n, st) : interior_quad4_mixed(k, h->nc, want_m, n, st);
-  if (h->dim == 3 && h->nen == 4)
-    return f64 ? interior_tet4_fp64(k, h->nc, want_m, n, st) : interior_tet4_mixed(k, h->nc, want_m, n, st);
-  return f64 ? interior_hex8_fp64(k, h->nc, want_m, n, st) : interior_hex8_mixed(k, h->nc, want_m, n, st);
+// Interior pass over n listed elements (k.el_list, or elements 0..n-1): point stage then
+// matrix stage per chunk.  With atomics the chunks alternate between two internal
+// streams so that one chunk's FP64 point stage overlaps the previous chunk's matrix
+// stage; plain read-modify-write (coloured batches) keeps them on the caller's stream.
+int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long long n, cudaStream_t st,
+                 bool concurrent) {
+  const InteriorOps& ops = h->ops[form];
+  const size_t rb = ops.rec_bytes(h->nc);
+  if (rb == 0) return fail(h, GALES_ERR_UNSUPPORTED, "no interior kernel for this element/component count");
+  const long long chunk = std::max<long long>(1, (long long)(kChunkBytes / rb));
+  const long long nchunks = (n + chunk - 1) / chunk;
+  if (nchunks == 0) return 0;
+  if (concurrent) {
+    CK(h, cudaEventRecord(h->ev_fork, st), "event");
+    for (int i = 0; i < 2; ++i) CK(h, cudaStreamWaitEvent(h->ist[i], h->ev_fork, 0), "stream wait");
+  }
+  for (long long c = 0; c < nchunks; ++c) {
+    const long long first = c * chunk, cnt = std::min(chunk, n - first);
+    cudaStream_t s = concurrent ? h->ist[c & 1] : st;
+    void* buf = h->qpbuf[concurrent ? (c & 1) : 0].p;
+    LaunchResult r = ops.point(k, h->nc, buf, first, cnt, s);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "point kernel");
+    h->launches += r.launches;
+    r = ops.matrix(k, h->nc, want_m, buf, first, cnt, s);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "matrix kernel");
+    h->launches += r.launches;
+  }
+  if (concurrent) {
+    for (int i = 0; i < 2; ++i) {
+      CK(h, cudaEventRecord(h->ev_join[i], h->ist[i]), "event");
+      CK(h, cudaStreamWaitEvent(st, h->ev_join[i], 0), "stream wait");
+    }
+  }
+  return 0;
 }
 
 LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, long long n, cudaStream_t st) {
@@ -653,25 +773,26 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
   k.rhs = drhs;
   k.scatter_mode = (h->scatter_mode == GALES_SCATTER_COLOURED) ? 1 : 0;
   const bool want_m = dvals != nullptr;
+  CK(h, cudaEventRecord(h->evp[0], st), "event");
   CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
   CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
   if (dvals) CK(h, cudaMemsetAsync(dvals, 0, (size_t)h->nnz * sizeof(double), st), "memset vals");
   CK(h, cudaMemsetAsync(drhs, 0, (size_t)h->n_rows * sizeof(double), st), "memset rhs");
+  CK(h, cudaEventRecord(h->evp[1], st), "event");
   h->launches += 0;
   if (h->scatter_mode == GALES_SCATTER_COLOURED) {
     for (int c = 0; c < h->n_colours; ++c) {
       KParams kc = k;
       kc.el_list = h->d_colour_order.p + h->colour_off[c];
       kc.n_list = h->colour_off[c + 1] - h->colour_off[c];
-      LaunchResult r = dispatch_interior(h, kc, form, want_m, kc.n_list, st);
-      if (r.err != cudaSuccess) return cuda_fail(h, r.err, "interior kernel");
-      h->launches += r.launches;
+      int rc = run_interior(h, kc, form, want_m, kc.n_list, st, false);
+      if (rc) return rc;
     }
   } else {
-    LaunchResult r = dispatch_interior(h, k, form, want_m, h->n_el, st);
-    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "interior kernel");
-    h->launches += r.launches;
+    int rc = run_interior(h, k, form, want_m, h->n_el, st, true);
+    if (rc) return rc;
   }
+  CK(h, cudaEventRecord(h->evp[2], st), "event");
   if (!h->bd_list.empty()) {
     // the boundary pass always uses atomics: boundary elements of one colour may
     // still be scattered twice, but its own elements may share nodes
@@ -684,6 +805,7 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
     h->launches += r.launches;
   }
+  CK(h, cudaEventRecord(h->evp[3], st), "event");
   return 0;
 }
 
@@ -815,7 +937,9 @@ int gales_asm_element_blocks(gales_asm* h, const double* I, const double* P, dou
   CK(h, cudaMemsetAsync(dr, 0, (size_t)n * N * sizeof(double), st), "memset r");
   LaunchResult r;
   if (which == 0) {
-    r = dispatch_interior(h, k, form, dm != nullptr, n, st);
+    int rc0 = run_interior(h, k, form, dm != nullptr, n, st, false);
+    if (rc0) return rc0;
+    r = {cudaSuccess, 0};
   } else {
     std::vector<int8_t> sides((size_t)n * h->ei.nsides);
     for (int64_t i = 0; i < n; ++i)
@@ -855,6 +979,16 @@ int gales_asm_status(gales_asm* h, int64_t* first_bad_element) {
 const char* gales_asm_last_error(gales_asm* h) { return h ? h->err.c_str() : "null handle"; }
 
 double gales_asm_last_ms(gales_asm* h) { return h ? h->last_ms : 0.0; }
+
+double gales_asm_last_phase_ms(gales_asm* h, int32_t phase) {
+  if (!h || phase < 0 || phase > 2) return -1.0;
+  float ms = -1.f;
+  if (cudaEventElapsedTime(&ms, h->evp[phase], h->evp[phase + 1]) != cudaSuccess) {
+    cudaGetLastError();
+    return -1.0;
+  }
+  return ms;
+}
 
 int64_t gales_asm_launch_count(gales_asm* h) { return h ? h->launches : 0; }
 

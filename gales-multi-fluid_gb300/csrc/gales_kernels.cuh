@@ -21,6 +21,8 @@
 
 #include <cstdint>
 
+#include <type_traits>
+
 #include "gales_physics.cuh"
 
 namespace gales {
@@ -57,6 +59,8 @@ struct KParams {
   unsigned int* status;
   unsigned long long* first_bad;
   int32_t scatter_mode;        // 0 atomics, 1 plain read-modify-write (coloured batches)
+  const void* geo;             // ElemGeo records (per element, or per element and point)
+  double sh_tab[8][8];         // shape functions at the interior points [q][node]
   double* local_m;             // element-level output [n_list][(nen*nd)^2] (no scatter) or null
   double* local_r;             // element-level output [n_list][nen*nd] (r = -r_) or null
 };
@@ -268,7 +272,7 @@ __device__ __forceinline__ void geometry(const double (&X)[NEN][DIM], const doub
 // ---------------------------------------------------------------------------
 // Per-quadrature-point record written by the point phase.
 template <int DIM, int NEN, int NC, typename S>
-struct QP {
+struct alignas(16) QP {
   using L = Layout<DIM, NC>;
   static constexpr int ND = L::ND;
   S sh[NEN], ds[DIM][NEN], JxW;
@@ -281,44 +285,135 @@ struct QP {
   S res[ND];        // least-squares residual Res (fluid_2d.hpp:282)
 };
 
-// Point phase for one (element, quadrature point).  FORM selects the tau inverse:
-// GALES_FORM_FP64 uses the uBLAS-faithful LU; GALES_FORM_MIXED the closed form.
+// Element geometry at the interior quadrature points, computed once at handle
+// creation as the reference does at mesh load (mesh.hpp:468-495 builds a quad
+// object per Gauss point): one record per element for simplices (affine map, the
+// gradients, J and metrics are the same at every point), one per point otherwise.
+template <int DIM, int NEN>
+struct alignas(16) ElemGeo {
+  double ds[DIM][NEN];
+  double J;
+  double G[DIM][DIM];
+  double g[DIM];
+};
+
+template <int DIM, int NEN>
+__host__ __device__ constexpr int geo_per_element(int nq) { return NEN == DIM + 1 ? 1 : nq; }
+
+template <int DIM, int NEN, int NQ>
+__global__ void __launch_bounds__(128) geometry_kernel(const double* __restrict__ coords,
+                                                        const int32_t* __restrict__ conn, KParams k,
+                                                        ElemGeo<DIM, NEN>* __restrict__ out, long long n_el) {
+  constexpr int NG = geo_per_element<DIM, NEN>(NQ);
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long e = t / NG;
+  const int iq = (int)(t % NG);
+  if (e >= n_el) return;
+  double X[NEN][DIM];
+#pragma unroll
+  for (int a = 0; a < NEN; ++a) {
+    const int nd_ = conn[e * NEN + a];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) X[a][d] = coords[(long long)nd_ * DIM + d];
+  }
+  Geo<DIM, NEN> q;
+  geometry<DIM, NEN>(X, k.gp[iq], true, q);
+  ElemGeo<DIM, NEN>& o = out[e * NG + iq];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d)
+#pragma unroll
+    for (int i = 0; i < NEN; ++i) o.ds[d][i] = q.ds[d][i];
+  o.J = q.J;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
+    o.g[i] = q.g[i];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) o.G[i][j] = q.G[i][j];
+  }
+  if (!(q.J > 0.0)) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
+}
+
+// Point phase for one (element, quadrature point).
+//   GALES_FORM_FP64 : every step in FP64 with the reference's operations; tau uses
+//                     the uBLAS-faithful LU inverse.
+//   GALES_FORM_MIXED: FP64 for the mixture EOS and its derivatives, U - U_P, the
+//                     element size h and tau with the closed-form DUDY inverse; the
+//                     fluxes, least-squares residual and dc viscosity in FP32.
 template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
 __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, NC, S>& out) {
   using L = Layout<DIM, NC>;
   constexpr int ND = L::ND;
+  constexpr int NG = geo_per_element<DIM, NEN>(NQ);
+  using R = typename std::conditional<FORM == GALES_FORM_FP64, double, float>::type;
   int nodes[NEN];
-  double X[NEN][DIM];
 #pragma unroll
-  for (int a = 0; a < NEN; ++a) {
-    nodes[a] = __ldg(k.conn + e * NEN + a);
+  for (int a = 0; a < NEN; ++a) nodes[a] = __ldg(k.conn + e * NEN + a);
+  const ElemGeo<DIM, NEN>& q = reinterpret_cast<const ElemGeo<DIM, NEN>*>(k.geo)[e * NG + (NG == 1 ? 0 : iq)];
+  double sh[NEN];
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) X[a][d] = __ldg(k.coords + (long long)nodes[a] * DIM + d);
-  }
-  Geo<DIM, NEN> q;
-  geometry<DIM, NEN>(X, k.gp[iq], true, q);
-  if (!(q.J > 0.0)) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
+  for (int i = 0; i < NEN; ++i) sh[i] = k.sh_tab[iq][i];
   const double JxW = q.J * k.W_in;
-  double Pq[ND], Iq[ND], dI[DIM][ND];
+  double Ie[NEN][ND], Pq[ND], Iq[ND];
+#pragma unroll
+  for (int i = 0; i < NEN; ++i)
+#pragma unroll
+    for (int j = 0; j < ND; ++j) Ie[i][j] = __ldg(k.I + (long long)nodes[i] * ND + j);
 #pragma unroll
   for (int j = 0; j < ND; ++j) {
-    Pq[j] = 0.0; Iq[j] = 0.0;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) dI[d][j] = 0.0;
+    Pq[j] = 0.0;
+    Iq[j] = 0.0;
   }
 #pragma unroll
   for (int i = 0; i < NEN; ++i) {
     const double* pi = k.P + (long long)nodes[i] * ND;
-    const double* ii = k.I + (long long)nodes[i] * ND;
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
-      const double pv = __ldg(pi + j), iv = __ldg(ii + j);
-      Pq[j] += q.sh[i] * pv;
-      Iq[j] += q.sh[i] * iv;
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) dI[d][j] += q.ds[d][i] * iv;
+      Pq[j] += sh[i] * __ldg(pi + j);
+      Iq[j] += sh[i] * Ie[i][j];
     }
   }
+  // gradients: FP64 in the FP64 form; FP32 of nodal differences in the mixed form
+  // (sum_i dN_i/dx = 0, so sum_i dN_i (I_i - I_0) is the same gradient)
+  R dI[DIM][ND];
+  if constexpr (FORM == GALES_FORM_FP64) {
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+      for (int j = 0; j < ND; ++j) {
+        double b = 0.0;
+#pragma unroll
+        for (int i = 0; i < NEN; ++i) b += q.ds[d][i] * Ie[i][j];
+        dI[d][j] = b;
+      }
+  } else {
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+      for (int j = 0; j < ND; ++j) dI[d][j] = 0.f;
+#pragma unroll
+    for (int i = 1; i < NEN; ++i)
+#pragma unroll
+      for (int j = 0; j < ND; ++j) {
+        const float dif = float(Ie[i][j] - Ie[0][j]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) dI[d][j] = fmaf(float(q.ds[d][i]), dif, dI[d][j]);
+      }
+  }
+  // velocity gradient in FP64 with the reference's operations (input of compute_h)
+  double dv[DIM][DIM];
+#pragma unroll
+  for (int a = 0; a < DIM; ++a)
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      if constexpr (FORM == GALES_FORM_FP64) {
+        dv[a][d] = dI[d][1 + a];
+      } else {
+        double b = 0.0;
+#pragma unroll
+        for (int i = 0; i < NEN; ++i) b += q.ds[d][i] * Ie[i][1 + a];
+        dv[a][d] = b;
+      }
+    }
   // previous-level conservative vector U_P (props at P with shear rate 0)
   double p, v[DIM], T, Y[NC];
   assign<DIM, NC>(Pq, p, v, T, Y);
@@ -335,7 +430,6 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
   double U[ND];
   conservative<DIM, NC>(pr.rho, pr.cv, v, T, Y, U);
   const double dt = k.dt;
-  // source S (fluid_2d.hpp:597-599)
   double Sv[ND];
 #pragma unroll
   for (int r = 0; r < ND; ++r) Sv[r] = 0.0;
@@ -348,28 +442,9 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
     }
     Sv[L::iT] = pr.rho * (gv);
   }
-  // residual pieces
-  double Res[ND], AdI[ND], t[ND];
-  {
-    double dd[ND];
-#pragma unroll
-    for (int j = 0; j < ND; ++j) dd[j] = (Iq[j] - Pq[j]) / dt;
-    dudy_mv<DIM, NC>(c, dd, Res);
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      a_mv<DIM, NC>(c, d, dI[d], t);
-#pragma unroll
-      for (int j = 0; j < ND; ++j) {
-        Res[j] = Res[j] + t[j];
-        AdI[j] = (d == 0) ? t[j] : AdI[j] + t[j];
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < ND; ++j) Res[j] = Res[j] - Sv[j];
-  }
 #pragma unroll
   for (int j = 0; j < ND; ++j) out.rv[j] = S((U[j] - UP[j]) / dt - Sv[j]);
-  // tau
+  // tau (fluid_2d.hpp:877-1022)
   double tau[ND][ND];
 #pragma unroll
   for (int r = 0; r < ND; ++r)
@@ -377,11 +452,6 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
     for (int cc = 0; cc < ND; ++cc) tau[r][cc] = 0.0;
   const double v_nrm = sqrt(vsq<DIM>(v));
   if (v_nrm >= kEps && k.tau != GALES_TAU_NONE) {
-    double dv[DIM][DIM];
-#pragma unroll
-    for (int i = 0; i < DIM; ++i)
-#pragma unroll
-      for (int j = 0; j < DIM; ++j) dv[i][j] = dI[j][1 + i];
     const double h = compute_h<DIM>(q.G, v, dv);
     double trG = 0.0;
 #pragma unroll
@@ -491,35 +561,60 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       }
     }
   }
-  // discontinuity capturing (fluid_2d.hpp:1027-1065)
-  double nu = 0.0;
-  double dU[DIM][ND];
+  // fluxes, least-squares residual and dc in the form's type R
+  using CR = Coef<DIM, NC, R>;
+  CR cr;
+  if constexpr (FORM == GALES_FORM_FP64) cr = c;
+  else cr = narrow<DIM, NC>(c);
+  R SvR[ND], Res[ND], AdI[ND], t[ND];
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) dudy_mv<DIM, NC>(c, dI[d], dU[d]);
+  for (int j = 0; j < ND; ++j) SvR[j] = R(Sv[j]);
+  {
+    R dd[ND];
+#pragma unroll
+    for (int j = 0; j < ND; ++j) dd[j] = R((Iq[j] - Pq[j]) / dt);
+    dudy_mv<DIM, NC, R>(cr, dd, Res);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      a_mv<DIM, NC, R>(cr, d, dI[d], t);
+#pragma unroll
+      for (int j = 0; j < ND; ++j) {
+        Res[j] = Res[j] + t[j];
+        AdI[j] = (d == 0) ? t[j] : AdI[j] + t[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < ND; ++j) Res[j] = Res[j] - SvR[j];
+  }
+  // discontinuity capturing (fluid_2d.hpp:1027-1065)
+  R nu = R(0);
+  R dU[DIM][ND];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) dudy_mv<DIM, NC, R>(cr, dI[d], dU[d]);
   if (k.dc_2006) {
-    double s = 0.0;
+    R s = R(0);
 #pragma unroll
     for (int d = 0; d < DIM; ++d) s += dU[d][0] * dU[d][0];
-    const double del_rho_nrm = sqrt(s);
-    if (!(del_rho_nrm < kEps)) {
-      double Jv[DIM];
+    const R del_rho_nrm = sqrt(s);
+    if (!(del_rho_nrm < R(kEps))) {
+      R Jv[DIM];
 #pragma unroll
       for (int d = 0; d < DIM; ++d) Jv[d] = dU[d][0] / del_rho_nrm;
-      double h = 0.0;
+      R h = R(0);
 #pragma unroll
       for (int i = 0; i < NEN; ++i) {
-        double tt = Jv[0] * q.ds[0][i];
+        R tt = Jv[0] * R(q.ds[0][i]);
 #pragma unroll
-        for (int d = 1; d < DIM; ++d) tt = tt + Jv[d] * q.ds[d][i];
+        for (int d = 1; d < DIM; ++d) tt = tt + Jv[d] * R(q.ds[d][i]);
         h += fabs(tt);
       }
-      if (h > kEps) {
-        h = 1.0 / h;
-        double Zn = 0.0, Un = 0.0, use1 = 0.0;
+      if (h > R(kEps)) {
+        h = R(1) / h;
+        R Zn = R(0), Un = R(0), use1 = R(0);
 #pragma unroll
         for (int j = 0; j < ND; ++j) {
-          const double z = k.u_ref_inv[j] * (AdI[j] - Sv[j]);
-          const double u = k.u_ref_inv[j] * U[j];
+          const R z = R(k.u_ref_inv[j]) * (AdI[j] - SvR[j]);
+          const R u = R(k.u_ref_inv[j]) * R(U[j]);
           Zn += z * z;
           Un += u * u;
         }
@@ -529,50 +624,51 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
         if (a == 1.0 || a == 1.5) {
 #pragma unroll
           for (int d = 0; d < DIM; ++d) {
-            double n2 = 0.0;
+            R n2 = R(0);
 #pragma unroll
             for (int j = 0; j < ND; ++j) {
-              const double u = k.u_ref_inv[j] * dU[d][j];
+              const R u = R(k.u_ref_inv[j]) * dU[d][j];
               n2 += u * u;
             }
-            const double n = sqrt(n2);
+            const R n = sqrt(n2);
             use1 += n * n;
           }
         }
-        if (a == 1.0) nu = Zn * h * (1.0 / sqrt(use1));
+        if (a == 1.0) nu = Zn * h * (R(1) / sqrt(use1));
         else if (a == 2.0) nu = Zn * h * h / Un;
-        else if (a == 1.5) nu = Zn * h * ((1.0 / sqrt(use1)) + h / Un) / 2.0;
-        nu = k.dc_scale * nu;
+        else if (a == 1.5) nu = Zn * h * ((R(1) / sqrt(use1)) + h / Un) / R(2);
+        nu = R(k.dc_scale) * nu;
       }
     }
   }
   // F_dif - F_adv + shock dI (fluid_2d.hpp:253-262, 311-318)
+  const R rhoR = cr.rho, pR = cr.p, ER = cr.E;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    double fd[ND];
+    R fd[ND];
 #pragma unroll
-    for (int j = 0; j < ND; ++j) fd[j] = 0.0;
+    for (int j = 0; j < ND; ++j) fd[j] = R(0);
 #pragma unroll
     for (int l = 0; l < DIM; ++l) {
-      k_mv<DIM, NC>(c, d, l, dI[l], t);
+      k_mv<DIM, NC, R>(cr, d, l, dI[l], t);
 #pragma unroll
       for (int j = 0; j < ND; ++j) fd[j] = (l == 0) ? t[j] : fd[j] + t[j];
     }
-    const double vk = v[d];
-    double fa[ND];
-    fa[0] = pr.rho * vk;
+    const R vk = cr.v[d];
+    R fa[ND];
+    fa[0] = rhoR * vk;
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) fa[1 + j] = (j == d) ? pr.rho * vk * vk + p : pr.rho * vk * v[j];
-    fa[L::iT] = vk * (pr.rho * c.E + p);
+    for (int j = 0; j < DIM; ++j) fa[1 + j] = (j == d) ? rhoR * vk * vk + pR : rhoR * vk * cr.v[j];
+    fa[L::iT] = vk * (rhoR * ER + pR);
 #pragma unroll
-    for (int i = 0; i < NC - 1; ++i) fa[L::iY + i] = pr.rho * vk * Y[i];
+    for (int i = 0; i < NC - 1; ++i) fa[L::iY + i] = rhoR * vk * cr.Y[i];
 #pragma unroll
     for (int j = 0; j < ND; ++j) out.rf[d][j] = S(fd[j] - fa[j] + nu * dU[d][j]);
   }
   // write the record
 #pragma unroll
   for (int i = 0; i < NEN; ++i) {
-    out.sh[i] = S(q.sh[i]);
+    out.sh[i] = S(sh[i]);
 #pragma unroll
     for (int d = 0; d < DIM; ++d) out.ds[d][i] = S(q.ds[d][i]);
   }
@@ -598,230 +694,326 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
   out.nu = S(nu);
 #pragma unroll
   for (int j = 0; j < ND; ++j) out.res[j] = S(Res[j]);
-  if (!isfinite(JxW) || !isfinite(pr.rho) || !isfinite(nu)) flag_error(k, GALES_ERR_NONFINITE, e);
+  if (!isfinite(JxW) || !isfinite(pr.rho) || !isfinite((double)nu)) flag_error(k, GALES_ERR_NONFINITE, e);
 }
 
-// Viscous/diffusive tangent contracted with the two shape gradients:
-// sum_kl dN_b/dx_k K_kl(jb,ja) dN_a/dx_l, in closed form (fluid_2d.hpp:531-571).
+// Viscous/diffusive tangent contracted with the test-function gradient gb:
+// sum_k gb_k K_kl(r, col), in closed form from the entries of K_kl
+// (fluid_2d.hpp:531-571): K_kl(1+j, v_m) = mu d_lk d_mj + mu d_lj d_mk + lambda d_kj d_lm,
+// K_kl(E, v_m) = sum_j v_j K_kl(1+j, v_m), K_kk(E, T) = kappa, K_kk(E, Y_i) = rho D_i H_i,
+// K_kk(Y_i, Y_i) = rho D_i.  gbv = gb . v.
 template <int DIM, int NC, typename S, typename C>
-__device__ __forceinline__ S kk_entry(const C& c, const S* gb, const S* ga, int jb, int ja) {
+__device__ __forceinline__ S kd_entry(const C& c, const S* gb, S gbv, int l, int r, int col) {
   using L = Layout<DIM, NC>;
-  if (jb == 0 || ja == 0) return S(0);
-  S gg = gb[0] * ga[0];
-#pragma unroll
-  for (int d = 1; d < DIM; ++d) gg += gb[d] * ga[d];
-  if (jb < L::iT) {
-    if (ja >= L::iT) return S(0);
-    const int j = jb - 1, m = ja - 1;
-    S x = c.mu * gb[m] * ga[j] + c.lambda * gb[j] * ga[m];
-    if (j == m) x += c.mu * gg;
+  if (r == 0 || col == 0) return S(0);
+  if (r < L::iT) {
+    if (col >= L::iT) return S(0);
+    const int j = r - 1, m = col - 1;
+    S x = S(0);
+    if (m == j) x += c.mu * gb[l];
+    if (l == j) x += c.mu * gb[m];
+    if (l == m) x += c.lambda * gb[j];
     return x;
   }
-  if (jb == L::iT) {
-    if (ja < L::iT) {
-      const int m = ja - 1;
-      S gav = ga[0] * c.v[0], gbv = gb[0] * c.v[0];
-#pragma unroll
-      for (int d = 1; d < DIM; ++d) { gav += ga[d] * c.v[d]; gbv += gb[d] * c.v[d]; }
-      return c.mu * gg * c.v[m] + c.mu * gb[m] * gav + c.lambda * gbv * ga[m];
+  if (r == L::iT) {
+    if (col < L::iT) {
+      const int m = col - 1;
+      S x = c.mu * (gb[l] * c.v[m] + c.v[l] * gb[m]);
+      if (l == m) x += c.lambda * gbv;
+      return x;
     }
-    if (ja == L::iT) return c.kappa * gg;
-    return c.rhoDH[ja - L::iY] * gg;
+    if (col == L::iT) return c.kappa * gb[l];
+    return c.rhoDH[col - L::iY] * gb[l];
   }
-  return (ja == jb) ? c.rhoD[jb - L::iY] * gg : S(0);
+  return (col == r) ? c.rhoD[r - L::iY] * gb[l] : S(0);
 }
 
+// Exact widening of an IEEE binary32 value to binary64 with integer operations
+// (sign, exponent rebias 127 -> 1023, mantissa shifted into the top of the 52-bit
+// field).  Zeros, subnormals, infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int ex = (u >> 23) & 0xffu;
+  if (ex == 0u || ex == 0xffu) return (double)f;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const unsigned long long e64 = (unsigned long long)(ex + (1023u - 127u)) << 52;
+  const unsigned long long m64 = (unsigned long long)(u & 0x7fffffu) << 29;
+  return __longlong_as_double((long long)(sign | e64 | m64));
+}
+__device__ __forceinline__ double widen(double d) { return d; }
+
 // ---------------------------------------------------------------------------
-// Shared-memory layout of the interior kernel.
-template <int DIM, int NEN, int NC, int NQ, int EB, typename S>
-struct InteriorSmem {
+// Interior pass, stage 1: one thread per (element, quadrature point) writes the
+// point record of that point to a chunk buffer (L2-resident).
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
+__global__ void __launch_bounds__(128) point_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ out,
+                                                     long long first, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long li = t / NQ;
+  const int iq = (int)(t % NQ);
+  if (li >= n) return;
+  const long long g = first + li;
+  const long long e = k.el_list ? (long long)k.el_list[g] : g;
+  point_phase<DIM, NEN, NC, NQ, FORM, S>(k, e, iq, out[li * NQ + iq]);
+}
+
+// Interior pass, stage 2: element matrices.  Lanes are mapped to (test node b,
+// trial node a, half of the rows): each lane owns an RH x ND register tile of the
+// (b, a) block and accumulates, per quadrature point,
+//   JxW [ FPT_b RM_a + N_a X_b + sum_l dN_a/dx_l KD_bl ]
+// with (fluid_2d.hpp:264-331)
+//   WA_b  = sum_k dN_b/dx_k A_k
+//   FPT_b = (WA_b - N_b S0) tau                       least-squares weight
+//   RM_a  = N_a DUDY/dt + WA_a - N_a S0               least-squares operator
+//   X_b   = N_b (DUDY/dt - S0) - WA_b                 Galerkin mass, source, advection
+//   KD_bl = sum_k dN_b/dx_k K_kl + nu dN_b/dx_l DUDY  viscous/diffusive and dc terms
+template <int DIM, int NEN, int NC>
+struct MatShape {
   static constexpr int ND = Layout<DIM, NC>::ND;
-  QP<DIM, NEN, NC, S> qp[EB][NQ];
-  struct Warp {
-    S D[ND][ND];           // DUDY
-    S WA[NEN][ND][ND];     // sum_k dN_b/dx_k A_k
-    S FPT[NEN][ND][ND];    // (WA_b - N_b S0) tau
-    S RM[NEN][ND][ND];     // N_a DUDY/dt + WA_a - N_a S0
-    double diag[NEN * ND];
-    int nodes[NEN];
-    int64_t rowbase[NEN];
-    int32_t rowlen[NEN];
-    uint32_t blocked[NEN];
-  } w[EB];
+  static constexpr int NDP = (ND + 1) & ~1;
+  static constexpr int RH = NDP / 2;
+  static constexpr int NP = NEN * NEN;
+  static constexpr int WPE = (2 * NP + 31) / 32;       // warps per element
+  static constexpr int EPC = WPE == 1 ? 4 : 1;        // elements per CTA
+  static constexpr int N = NEN * ND;
 };
 
-template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, bool WANT_M>
-__global__ void __launch_bounds__(256) interior_kernel(const KParams k) {
+template <int DIM, int NEN, int NC, int NQ, typename S>
+struct ElemSmem {
+  using M = MatShape<DIM, NEN, NC>;
+  static constexpr int ND = M::ND, NDP = M::NDP, N = M::N;
+  QP<DIM, NEN, NC, S> qp[NQ];
+  struct Work {
+    S A[DIM][ND][NDP];
+    S D[ND][NDP];
+    S WA[NEN][ND][NDP];
+    S FPT[NEN][NDP][ND];
+    S RM[NEN][ND][NDP];
+    S X[NEN][NDP][ND];
+    S KD[NEN][DIM][NDP][ND];
+  };
+  union {
+    Work w;
+    double stage[N * N];
+  } u;
+  double diag[N];
+  int nodes[NEN];
+  int64_t rowbase[NEN];
+  int32_t rowlen[NEN];
+  uint32_t blocked[NEN];
+};
+
+template <int WPE>
+__device__ __forceinline__ void elem_sync(int el_in_cta) {
+  if constexpr (WPE == 1) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(el_in_cta + 1), "r"(WPE * 32) : "memory");
+  }
+}
+
+template <int DIM, int NEN, int NC, int NQ, typename S, bool WANT_M>
+__global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<DIM, NEN, NC, S>* __restrict__ in,
+                                                      long long first, long long n) {
   using L = Layout<DIM, NC>;
-  constexpr int ND = L::ND;
-  constexpr int EB = 8;
-  constexpr int N = NEN * ND;
-  constexpr int NT = N * N;
-  constexpr int NPL = (NT + 31) / 32;
-  using SM = InteriorSmem<DIM, NEN, NC, NQ, EB, S>;
+  using M = MatShape<DIM, NEN, NC>;
+  using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
+  constexpr int ND = M::ND, NDP = M::NDP, RH = M::RH, N = M::N, NT = N * N, WPE = M::WPE, EPC = M::EPC;
+  constexpr int ET = WPE * 32;  // threads per element
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SM& sm = *reinterpret_cast<SM*>(smem_raw);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long nlist = k.el_list ? k.n_list : k.n_elements;
-  const long long base = (long long)blockIdx.x * EB;
-
-  // ---- point phase
-  if (tid < EB * NQ) {
-    const int le = tid / NQ, iq = tid % NQ;
-    const long long li = base + le;
-    if (li < nlist) {
-      const long long e = k.el_list ? (long long)k.el_list[li] : li;
-      point_phase<DIM, NEN, NC, NQ, FORM, S>(k, e, iq, sm.qp[le][iq]);
-    }
+  const int tid = threadIdx.x;
+  const int ec = tid / ET;      // element slot in the CTA
+  const int gl = tid % ET;      // thread index within the element
+  ES& E = reinterpret_cast<ES*>(smem_raw)[ec];
+  const long long li = (long long)blockIdx.x * EPC + ec;
+  if (li >= n) return;          // whole element groups exit together
+  const long long g = first + li;
+  const long long e = k.el_list ? (long long)k.el_list[g] : g;
+  // stage the element's point records
+  {
+    constexpr int W4 = sizeof(QP<DIM, NEN, NC, S>) * NQ / 16;
+    const int4* src = reinterpret_cast<const int4*>(in + li * NQ);
+    int4* dst = reinterpret_cast<int4*>(E.qp);
+    for (int i = gl; i < W4; i += ET) dst[i] = src[i];
   }
-  __syncthreads();
-
-  // ---- matrix phase: warp per element
-  const long long li = base + warp;
-  if (li >= nlist) return;
-  const long long e = k.el_list ? (long long)k.el_list[li] : li;
-  auto& W = sm.w[warp];
-  if (lane < NEN) {
-    const int nd_ = __ldg(k.conn + e * NEN + lane);
-    W.nodes[lane] = nd_;
+  if (gl < NEN) {
+    const int nd_ = __ldg(k.conn + e * NEN + gl);
+    E.nodes[gl] = nd_;
     const int64_t r0 = __ldg(k.node_rp + nd_), r1 = __ldg(k.node_rp + nd_ + 1);
-    W.rowbase[lane] = r0 * (int64_t)(ND * ND);
-    W.rowlen[lane] = (int32_t)((r1 - r0) * ND);
+    E.rowbase[gl] = r0 * (int64_t)(ND * ND);
+    E.rowlen[gl] = (int32_t)((r1 - r0) * ND);
     const int fl = k.node_flag ? __ldg(k.node_flag + nd_) : 0;
-    W.blocked[lane] = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
+    E.blocked[gl] = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
   }
-  constexpr int RPL = (N + 31) / 32;
-  S macc[NPL];
+  // padding rows of FPT, X and KD stay zero
+  if constexpr (NDP > ND) {
+    for (int t = gl; t < NEN * (NDP - ND) * ND; t += ET) {
+      const int b = t / ((NDP - ND) * ND), r = ND + (t / ND) % (NDP - ND), c = t % ND;
+      E.u.w.FPT[b][r][c] = S(0);
+      E.u.w.X[b][r][c] = S(0);
 #pragma unroll
-  for (int i = 0; i < NPL; ++i) macc[i] = S(0);
-  S racc[RPL];
+      for (int l = 0; l < DIM; ++l) E.u.w.KD[b][l][r][c] = S(0);
+    }
+  }
+  const int pr = gl >> 1, half = gl & 1;
+  const bool has_pair = pr < M::NP;
+  const int pb = has_pair ? pr / NEN : 0, pa = has_pair ? pr % NEN : 0;
+  const int r0 = half * RH;
+  S acc[RH][ND];
 #pragma unroll
-  for (int i = 0; i < RPL; ++i) racc[i] = S(0);
+  for (int i = 0; i < RH; ++i)
+#pragma unroll
+    for (int j = 0; j < ND; ++j) acc[i][j] = S(0);
+  S racc = S(0);
   const S dt = S(k.dt);
+  const S idt = S(1) / dt;
+  auto s0 = [&](const QP<DIM, NEN, NC, S>& c, int r, int col) -> S {
+    return (r == L::iT && col >= 1 && col <= DIM) ? c.rho * S(k.gravity[col - 1]) : S(0);
+  };
+  elem_sync<WPE>(ec);
   for (int iq = 0; iq < NQ; ++iq) {
-    const auto& c = sm.qp[warp][iq];
-    __syncwarp();
-    for (int t = lane; t < ND * ND; t += 32) {
-      const int r = t / ND, col = t % ND;
-      W.D[r][col] = dudy_entry<DIM, NC, S>(c, r, col);
+    const QP<DIM, NEN, NC, S>& c = E.qp[iq];
+    auto& w = E.u.w;
+    // (1) A_k and DUDY
+    for (int t = gl; t < (DIM + 1) * ND * NDP; t += ET) {
+      const int kk = t / (ND * NDP), r = (t / NDP) % ND, col = t % NDP;
+      if (kk < DIM) w.A[kk][r][col] = col < ND ? a_entry<DIM, NC, S>(c, kk, r, col) : S(0);
+      else w.D[r][col] = col < ND ? dudy_entry<DIM, NC, S>(c, r, col) : S(0);
     }
-    for (int t = lane; t < NEN * ND * ND; t += 32) {
+    elem_sync<WPE>(ec);
+    // (2) WA, RM, X, KD
+    for (int t = gl; t < NEN * ND * ND; t += ET) {
       const int b = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
-      S x = c.ds[0][b] * a_entry<DIM, NC, S>(c, 0, r, col);
+      S wa = c.ds[0][b] * w.A[0][r][col];
 #pragma unroll
-      for (int d = 1; d < DIM; ++d) x = madd(c.ds[d][b], a_entry<DIM, NC, S>(c, d, r, col), x);
-      W.WA[b][r][col] = x;
+      for (int d = 1; d < DIM; ++d) wa = madd(c.ds[d][b], w.A[d][r][col], wa);
+      const S Dv = w.D[r][col], sv = s0(c, r, col), shb = c.sh[b];
+      w.WA[b][r][col] = wa;
+      w.RM[b][r][col] = Dv * shb * idt + wa - sv * shb;
+      if constexpr (WANT_M) {
+        w.X[b][r][col] = shb * (Dv * idt - sv) - wa;
+        S gb[DIM];
+        S gbv = S(0);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          gb[d] = c.ds[d][b];
+          gbv = madd(gb[d], c.v[d], gbv);
+        }
+#pragma unroll
+        for (int l = 0; l < DIM; ++l)
+          w.KD[b][l][r][col] = madd(c.nu * gb[l], Dv, kd_entry<DIM, NC, S>(c, gb, gbv, l, r, col));
+      }
     }
-    __syncwarp();
-    for (int t = lane; t < NEN * ND * ND; t += 32) {
+    elem_sync<WPE>(ec);
+    // (3) FPT
+    for (int t = gl; t < NEN * ND * ND; t += ET) {
       const int b = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
-      // S0 has entries only in row rho E: S0(iT, 1+k) = rho g_k
+      const S shb = c.sh[b];
       S x = S(0);
 #pragma unroll
-      for (int m = 0; m < ND; ++m) {
-        S w = W.WA[b][r][m];
-        if (r == L::iT && m >= 1 && m <= DIM) w = w - c.sh[b] * (c.rho * S(k.gravity[m - 1]));
-        x = madd(w, c.tau[m][col], x);
-      }
-      W.FPT[b][r][col] = x;
-      S s0 = S(0);
-      if (r == L::iT && col >= 1 && col <= DIM) s0 = c.rho * S(k.gravity[col - 1]);
-      W.RM[b][r][col] = W.D[r][col] * c.sh[b] / dt + W.WA[b][r][col] - s0 * c.sh[b];
+      for (int m = 0; m < ND; ++m) x = madd(w.WA[b][r][m] - shb * s0(c, r, m), c.tau[m][col], x);
+      w.FPT[b][r][col] = x;
     }
-    __syncwarp();
+    elem_sync<WPE>(ec);
+    // (4) block tiles and residual
     if constexpr (WANT_M) {
+      if (has_pair) {
+        S tt[RH][ND];
 #pragma unroll
-      for (int i = 0; i < NPL; ++i) {
-        const int t = lane + 32 * i;
-        if (NT % 32 != 0 && t >= NT) break;
-        const int row = t / N, colx = t % N;
-        const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-        S lsq = S(0);
+        for (int i = 0; i < RH; ++i)
 #pragma unroll
-        for (int m = 0; m < ND; ++m) lsq = madd(W.FPT[b][jb][m], W.RM[a][m][ja], lsq);
-        S gb[DIM], ga[DIM];
+          for (int j = 0; j < ND; ++j) tt[i][j] = S(0);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) { gb[d] = c.ds[d][b]; ga[d] = c.ds[d][a]; }
-        S gg = gb[0] * ga[0];
+        for (int m = 0; m < ND; ++m) {
+          S fr[RH], rr[ND];
 #pragma unroll
-        for (int d = 1; d < DIM; ++d) gg += gb[d] * ga[d];
-        const S Dv = W.D[jb][ja];
-        S s0 = S(0);
-        if (jb == L::iT && ja >= 1 && ja <= DIM) s0 = c.rho * S(k.gravity[ja - 1]);
-        S gal = c.sh[b] * Dv * c.sh[a] / dt - c.sh[a] * W.WA[b][jb][ja] - c.sh[b] * s0 * c.sh[a];
-        gal += kk_entry<DIM, NC, S>(c, gb, ga, jb, ja);
-        gal += c.nu * gg * Dv;
-        macc[i] = madd(c.JxW, gal + lsq, macc[i]);
+          for (int i = 0; i < RH; ++i) fr[i] = w.FPT[pb][r0 + i][m];
+#pragma unroll
+          for (int j = 0; j < ND; ++j) rr[j] = w.RM[pa][m][j];
+#pragma unroll
+          for (int i = 0; i < RH; ++i)
+#pragma unroll
+            for (int j = 0; j < ND; ++j) tt[i][j] = madd(fr[i], rr[j], tt[i][j]);
+        }
+        const S sa = c.sh[pa];
+        S dsa[DIM];
+#pragma unroll
+        for (int l = 0; l < DIM; ++l) dsa[l] = c.ds[l][pa];
+#pragma unroll
+        for (int i = 0; i < RH; ++i)
+#pragma unroll
+          for (int j = 0; j < ND; ++j) {
+            S x = madd(sa, w.X[pb][r0 + i][j], tt[i][j]);
+#pragma unroll
+            for (int l = 0; l < DIM; ++l) x = madd(dsa[l], w.KD[pb][l][r0 + i][j], x);
+            acc[i][j] = madd(c.JxW, x, acc[i][j]);
+          }
       }
     }
+    if (gl < N) {
+      const int b = gl / ND, jb = gl % ND;
+      S x = c.sh[b] * c.rv[jb];
 #pragma unroll
-    for (int i = 0; i < RPL; ++i) {
-      const int t = lane + 32 * i;
-      if (t < N) {
-        const int b = t / ND, jb = t % ND;
-        S x = c.sh[b] * c.rv[jb];
+      for (int d = 0; d < DIM; ++d) x = madd(c.ds[d][b], c.rf[d][jb], x);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) x = madd(c.ds[d][b], c.rf[d][jb], x);
-#pragma unroll
-        for (int m = 0; m < ND; ++m) x = madd(W.FPT[b][jb][m], c.res[m], x);
-        racc[i] = madd(c.JxW, x, racc[i]);
-      }
+      for (int m = 0; m < ND; ++m) x = madd(w.FPT[b][jb][m], c.res[m], x);
+      racc = madd(c.JxW, x, racc);
     }
+    elem_sync<WPE>(ec);
   }
-  __syncwarp();
-  if (k.local_r) {  // element-level output of execute_i (fluid_2d.hpp:200-201): m = m_, r = -r_
-#pragma unroll
-    for (int i = 0; i < RPL; ++i) {
-      const int t = lane + 32 * i;
-      if (t < N) k.local_r[li * N + t] = -(double)racc[i];
-    }
-    if (WANT_M && k.local_m) {
-#pragma unroll
-      for (int i = 0; i < NPL; ++i) {
-        const int t = lane + 32 * i;
-        if (NT % 32 != 0 && t >= NT) break;
-        k.local_m[li * NT + t] = (double)macc[i];
-      }
-    }
-    return;
-  }
-  // ---- Dirichlet rows (scatter.hpp:62-78) and scatter (scatter.hpp:96-97)
+  // Dirichlet rows (scatter.hpp:62-78) and scatter (scatter.hpp:96-97)
   double avg = 0.0;
   if constexpr (WANT_M) {
+    if (has_pair && pb == pa) {
 #pragma unroll
-    for (int i = 0; i < NPL; ++i) {
-      const int t = lane + 32 * i;
-      if (NT % 32 != 0 && t >= NT) break;
-      const int row = t / N, colx = t % N;
-      if (row == colx) W.diag[row] = (double)macc[i];
+      for (int i = 0; i < RH; ++i)
+        if (r0 + i < ND) E.diag[pb * ND + r0 + i] = widen(acc[i][r0 + i]);
     }
-    __syncwarp();
-    avg = 1.0;
-    for (int i = 0; i < N; ++i) avg += W.diag[i];
-    avg /= N;
+    elem_sync<WPE>(ec);
+    // avg_val = (1 + trace)/n (scatter.hpp:65-68); trace summed by a warp tree
+    double tr = 0.0;
+    for (int i = gl & 31; i < N; i += 32) tr += E.diag[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    avg = (1.0 + tr) / N;
+    const bool local = k.local_r != nullptr;
+    if (has_pair) {
+#pragma unroll
+      for (int i = 0; i < RH; ++i) {
+        const int jb = r0 + i;
+        if (jb < ND) {
+          const bool blk = !local && ((E.blocked[pb] >> jb) & 1u);
+          const int row = pb * ND + jb;
+#pragma unroll
+          for (int j = 0; j < ND; ++j) {
+            const int col = pa * ND + j;
+            E.u.stage[row * N + col] = blk ? (row == col ? avg : 0.0) : widen(acc[i][j]);
+          }
+        }
+      }
+    }
+    elem_sync<WPE>(ec);
+  }
+  if (k.local_r) {  // element-level output of execute_i (fluid_2d.hpp:200-201): m = m_, r = -r_
+    if (gl < N) k.local_r[g * N + gl] = -(double)racc;
+    if (WANT_M && k.local_m)
+      for (int t = gl; t < NT; t += ET) k.local_m[g * NT + t] = E.u.stage[t];
+    return;
   }
   const int mode = k.scatter_mode;
-#pragma unroll
-  for (int i = 0; i < RPL; ++i) {
-    const int t = lane + 32 * i;
-    if (t < N) {
-      const int b = t / ND, jb = t % ND;
-      const bool blk = (W.blocked[b] >> jb) & 1u;
-      const double rv = blk ? avg * 0.0 : -(double)racc[i];
-      add_to(k.rhs + (long long)W.nodes[b] * ND + jb, rv, mode);
-    }
+  if (gl < N) {
+    const int b = gl / ND, jb = gl % ND;
+    const bool blk = (E.blocked[b] >> jb) & 1u;
+    const double rv = blk ? avg * 0.0 : -(double)racc;
+    add_to(k.rhs + (long long)E.nodes[b] * ND + jb, rv, mode);
   }
   if constexpr (WANT_M) {
-#pragma unroll
-    for (int i = 0; i < NPL; ++i) {
-      const int t = lane + 32 * i;
-      if (NT % 32 != 0 && t >= NT) break;
-      const int row = t / N, colx = t % N;
-      const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-      double val = (double)macc[i];
-      if ((W.blocked[b] >> jb) & 1u) val = (row == colx) ? avg : 0.0;
+    for (int t = gl; t < NT; t += ET) {
+      const double val = E.u.stage[t];
       if (val != 0.0) {
-        const int64_t off = W.rowbase[b] + (int64_t)jb * W.rowlen[b] +
+        const int row = t / N, colx = t % N;
+        const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
+        const int64_t off = E.rowbase[b] + (int64_t)jb * E.rowlen[b] +
                             (int64_t)__ldg(k.slot + (e * NEN + b) * NEN + a) * ND + ja;
         add_to(k.vals + off, val, mode);
       }
@@ -886,46 +1078,78 @@ __device__ __forceinline__ double a_entry_bd(const Coef<DIM, NC>& c, const gales
   return 0.0;
 }
 
+// Per boundary point data (one side quadrature point): the state coefficients, the
+// area vector, shape data and the boundary residual vector
+//   rb = sum_k (F_adv,k - F_dif,k) JNxW_k                       (fluid_2d.hpp:343-349)
+template <int DIM, int NEN, int NC>
+struct BPoint {
+  using L = Layout<DIM, NC>;
+  static constexpr int ND = L::ND;
+  Coef<DIM, NC> c;
+  double sh[NEN], ds[DIM][NEN], JNxW[DIM], rb[ND];
+  int flag;
+};
+
+template <int DIM, int NEN, int NC, int NS, int NSQ>
+struct BoundarySmem {
+  static constexpr int ND = Layout<DIM, NC>::ND, N = NEN * ND;
+  BPoint<DIM, NEN, NC> pt[NS * NSQ];
+  double BA[ND][ND];          // sum_k A'_k JNxW_k
+  double BK[DIM][ND][ND];     // sum_k K'_kl JNxW_k
+  double m[N * N];            // element block accumulator
+  double r[N];
+};
+
+// Boundary pass, one warp per listed boundary element (FP64 in both forms).
+// Lanes first evaluate one side quadrature point each (thread per point), then
+// build BA and BK entry-parallel per point and accumulate
+//   m_ba += N_b (N_a BA - sum_l dN_a/dx_l BK_l)                 (fluid_2d.hpp:351-363)
+// before the element's own Dirichlet pass and scatter (fluid_assembly.hpp:57-63).
 template <int DIM, int NEN, int NC, int NS, int NSQ>
 __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   using L = Layout<DIM, NC>;
   constexpr int ND = L::ND;
   constexpr int N = NEN * ND;
   constexpr int NT = N * N;
-  constexpr int NPL = (NT + 31) / 32;
+  using BS = BoundarySmem<DIM, NEN, NC, NS, NSQ>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  BS& B = *reinterpret_cast<BS*>(smem_raw);
   const int lane = threadIdx.x;
   const long long li = blockIdx.x;
   if (li >= k.n_list) return;
   const long long e = k.el_list[li];
-  __shared__ double diag[N];
   int nodes[NEN];
-  double X[NEN][DIM], Ie[NEN][ND];
 #pragma unroll
-  for (int a = 0; a < NEN; ++a) {
-    nodes[a] = __ldg(k.conn + e * NEN + a);
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) X[a][d] = __ldg(k.coords + (long long)nodes[a] * DIM + d);
-#pragma unroll
-    for (int j = 0; j < ND; ++j) Ie[a][j] = __ldg(k.I + (long long)nodes[a] * ND + j);
-  }
-  constexpr int RPL = (N + 31) / 32;
-  double macc[NPL];
-#pragma unroll
-  for (int i = 0; i < NPL; ++i) macc[i] = 0.0;
-  double racc[RPL];
-#pragma unroll
-  for (int i = 0; i < RPL; ++i) racc[i] = 0.0;
-  for (int s = 0; s < NS; ++s) {
+  for (int a = 0; a < NEN; ++a) nodes[a] = __ldg(k.conn + e * NEN + a);
+  for (int t = lane; t < NT; t += 32) B.m[t] = 0.0;
+  for (int t = lane; t < N; t += 32) B.r[t] = 0.0;
+  // (1) point physics, one lane per (side, point)
+  if (lane < NS * NSQ) {
+    const int s = lane / NSQ, iq = lane % NSQ;
     const int flag = k.bd_sides[li * NS + s];
-    if (flag <= 0) continue;
-    const gales_side_bc& bc = k.side_bc[flag < GALES_MAX_FLAGS ? flag : 0];
-    for (int iq = 0; iq < NSQ; ++iq) {
+    BPoint<DIM, NEN, NC>& P = B.pt[lane];
+    P.flag = flag;
+    if (flag > 0) {
+      const gales_side_bc& bc = k.side_bc[flag < GALES_MAX_FLAGS ? flag : 0];
+      double X[NEN][DIM], Ie[NEN][ND];
+#pragma unroll
+      for (int a = 0; a < NEN; ++a) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) X[a][d] = __ldg(k.coords + (long long)nodes[a] * DIM + d);
+#pragma unroll
+        for (int j = 0; j < ND; ++j) Ie[a][j] = __ldg(k.I + (long long)nodes[a] * ND + j);
+      }
       Geo<DIM, NEN> q;
       geometry<DIM, NEN>(X, k.sgp[s][iq], false, q);
-      if (!(q.J > 0.0) && lane == 0) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
-      double JNxW[DIM];
+      if (!(q.J > 0.0)) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) JNxW[d] = q.JN[d] * k.W_bd;
+      for (int d = 0; d < DIM; ++d) P.JNxW[d] = q.JN[d] * k.W_bd;
+#pragma unroll
+      for (int i = 0; i < NEN; ++i) {
+        P.sh[i] = q.sh[i];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) P.ds[d][i] = q.ds[d][i];
+      }
       double Iq[ND], dI[DIM][ND];
 #pragma unroll
       for (int j = 0; j < ND; ++j) {
@@ -945,8 +1169,8 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
       assign<DIM, NC>(Iq, p, v, T, Y);
       Props<NC> pr;
       mixture<NC>(k.ch, p, T, Y, pr);
-      Coef<DIM, NC> c;
-      make_coef<DIM, NC>(pr, p, v, T, Y, c);
+      make_coef<DIM, NC>(pr, p, v, T, Y, P.c);
+      const Coef<DIM, NC>& c = P.c;
       // advective flux (fluid_2d.hpp:581-595), mass-flux override (fluid_2d.hpp:674-680, 732-738)
       double Fa[DIM][ND], Fd[DIM][ND];
 #pragma unroll
@@ -1025,60 +1249,57 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
         }
       }
 #pragma unroll
-      for (int i = 0; i < RPL; ++i) {
-        const int t = lane + 32 * i;
-        if (t < N) {
-          const int b = t / ND, j = t % ND;
-          double x = 0.0;
+      for (int j = 0; j < ND; ++j) {
+        double x = Fa[0][j] * P.JNxW[0];
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) x += q.sh[b] * Fa[d][j] * JNxW[d];
+        for (int d = 1; d < DIM; ++d) x = madd(Fa[d][j], P.JNxW[d], x);
 #pragma unroll
-          for (int d = 0; d < DIM; ++d) x -= q.sh[b] * Fd[d][j] * JNxW[d];
-          racc[i] += x;
-        }
-      }
-#pragma unroll 1
-      for (int i = 0; i < NPL; ++i) {
-        const int t = lane + 32 * i;
-        if (t >= NT) break;
-        const int row = t / N, colx = t % N;
-        const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-        double x = 0.0;
-        for (int d = 0; d < DIM; ++d) x += q.sh[b] * a_entry_bd<DIM, NC>(c, bc, d, jb, ja) * JNxW[d] * q.sh[a];
-        for (int d = 0; d < DIM; ++d)
-          for (int l = 0; l < DIM; ++l)
-            x -= q.sh[b] * k_entry_bd<DIM, NC>(c, bc, d, l, jb, ja) * JNxW[d] * q.ds[l][a];
-        macc[i] += x;
+        for (int d = 0; d < DIM; ++d) x = madd(-Fd[d][j], P.JNxW[d], x);
+        P.rb[j] = x;
       }
     }
-  }
-  if (k.local_r) {  // element-level output of execute_b: m = m_, r = -r_
-#pragma unroll
-    for (int i = 0; i < RPL; ++i) {
-      const int t = lane + 32 * i;
-      if (t < N) k.local_r[li * N + t] = -racc[i];
-    }
-    if (k.local_m) {
-#pragma unroll 1
-      for (int i = 0; i < NPL; ++i) {
-        const int t = lane + 32 * i;
-        if (t >= NT) break;
-        k.local_m[li * NT + t] = macc[i];
-      }
-    }
-    return;
-  }
-  // second scatter pass with its own Dirichlet average
-#pragma unroll
-  for (int i = 0; i < NPL; ++i) {
-    const int t = lane + 32 * i;
-    if (t >= NT) break;
-    const int row = t / N, colx = t % N;
-    if (row == colx) diag[row] = macc[i];
   }
   __syncwarp();
+  // (2) per flagged point: BA, BK entry-parallel, then the block and residual
+  for (int ip = 0; ip < NS * NSQ; ++ip) {
+    const BPoint<DIM, NEN, NC>& P = B.pt[ip];
+    if (P.flag <= 0) continue;
+    const gales_side_bc& bc = k.side_bc[P.flag < GALES_MAX_FLAGS ? P.flag : 0];
+    for (int t = lane; t < (1 + DIM) * ND * ND; t += 32) {
+      const int w = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
+      double x = 0.0;
+      if (w == 0) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) x = madd(a_entry_bd<DIM, NC>(P.c, bc, d, r, col), P.JNxW[d], x);
+        B.BA[r][col] = x;
+      } else {
+        const int l = w - 1;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) x = madd(k_entry_bd<DIM, NC>(P.c, bc, d, l, r, col), P.JNxW[d], x);
+        B.BK[l][r][col] = x;
+      }
+    }
+    __syncwarp();
+    for (int t = lane; t < NT; t += 32) {
+      const int row = t / N, colx = t % N;
+      const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
+      double x = P.sh[a] * B.BA[jb][ja];
+#pragma unroll
+      for (int l = 0; l < DIM; ++l) x = madd(-P.ds[l][a], B.BK[l][jb][ja], x);
+      B.m[t] = madd(P.sh[b], x, B.m[t]);
+    }
+    for (int t = lane; t < N; t += 32) B.r[t] = madd(P.sh[t / ND], P.rb[t % ND], B.r[t]);
+    __syncwarp();
+  }
+  if (k.local_r) {  // element-level output of execute_b: m = m_, r = -r_
+    for (int t = lane; t < N; t += 32) k.local_r[li * N + t] = -B.r[t];
+    if (k.local_m)
+      for (int t = lane; t < NT; t += 32) k.local_m[li * NT + t] = B.m[t];
+    return;
+  }
+  // second scatter pass with its own Dirichlet average (scatter.hpp:62-78)
   double avg = 1.0;
-  for (int i = 0; i < N; ++i) avg += diag[i];
+  for (int i = 0; i < N; ++i) avg += B.m[i * N + i];
   avg /= N;
   uint32_t blocked[NEN];
   int64_t rowbase[NEN];
@@ -1092,24 +1313,17 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
     rowlen[a] = (int32_t)((r1 - r0) * ND);
   }
   const int mode = k.scatter_mode;
-#pragma unroll
-  for (int i = 0; i < RPL; ++i) {
-    const int t = lane + 32 * i;
-    if (t < N) {
-      const int b = t / ND, jb = t % ND;
-      const bool blk = (blocked[b] >> jb) & 1u;
-      const double rv = blk ? avg * 0.0 : -racc[i];
-      add_to(k.rhs + (long long)nodes[b] * ND + jb, rv, mode);
-    }
+  for (int t = lane; t < N; t += 32) {
+    const int b = t / ND, jb = t % ND;
+    const bool blk = (blocked[b] >> jb) & 1u;
+    const double rv = blk ? avg * 0.0 : -B.r[t];
+    add_to(k.rhs + (long long)nodes[b] * ND + jb, rv, mode);
   }
   if (k.vals) {
-#pragma unroll 1
-    for (int i = 0; i < NPL; ++i) {
-      const int t = lane + 32 * i;
-      if (t >= NT) break;
+    for (int t = lane; t < NT; t += 32) {
       const int row = t / N, colx = t % N;
       const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-      double val = macc[i];
+      double val = B.m[t];
       if ((blocked[b] >> jb) & 1u) val = (row == colx) ? avg : 0.0;
       if (val != 0.0) {
         const int64_t off = rowbase[b] + (int64_t)jb * rowlen[b] +

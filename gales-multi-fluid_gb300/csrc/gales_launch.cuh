@@ -1,7 +1,7 @@
 // Kernel dispatch for one element type (DIM, NEN): picks the template instance for
-// the number of components and the numerical form.  Each element type lives in
-// its own translation unit (gales_tri3.cu, gales_quad4.cu, gales_tet4.cu,
-// gales_hex8.cu) so the library builds in parallel.
+// the number of components and the numerical form.  Each (element type, form)
+// pair lives in its own translation unit (gales_<type>_<form>.cu) so the library
+// builds in parallel; the boundary kernels are in the FP64 unit.
 #pragma once
 
 #include <type_traits>
@@ -15,70 +15,139 @@ struct LaunchResult {
   int launches;
 };
 
-template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, bool WANT_M>
-LaunchResult launch_interior_inst(const KParams& k, long long n_items, cudaStream_t st) {
-  constexpr int EB = 8;
-  using SM = InteriorSmem<DIM, NEN, NC, NQ, EB, S>;
-  const size_t smem = sizeof(SM);
-  auto fn = interior_kernel<DIM, NEN, NC, NQ, FORM, S, WANT_M>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return {e, 0};
-  const long long blocks = (n_items + EB - 1) / EB;
-  if (blocks == 0) return {cudaSuccess, 0};
-  fn<<<(unsigned)blocks, 256, smem, st>>>(k);
-  return {cudaGetLastError(), 1};
-}
-
 template <int DIM, int NEN, int NC, int NQ, int FORM>
-LaunchResult launch_interior_nc(const KParams& k, bool want_m, long long n_items, cudaStream_t st) {
+struct InteriorInst {
   using S = typename std::conditional<FORM == GALES_FORM_FP64, double, float>::type;
-  if (want_m) return launch_interior_inst<DIM, NEN, NC, NQ, FORM, S, true>(k, n_items, st);
-  return launch_interior_inst<DIM, NEN, NC, NQ, FORM, S, false>(k, n_items, st);
-}
+  using Rec = QP<DIM, NEN, NC, S>;
+  using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
+  using M = MatShape<DIM, NEN, NC>;
+  static size_t rec_bytes() { return sizeof(Rec) * NQ; }
+  static LaunchResult point(const KParams& k, void* buf, long long first, long long n, cudaStream_t st) {
+    if (n <= 0) return {cudaSuccess, 0};
+    const long long threads = n * NQ;
+    point_kernel<DIM, NEN, NC, NQ, FORM, S><<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(
+        k, reinterpret_cast<Rec*>(buf), first, n);
+    return {cudaGetLastError(), 1};
+  }
+  static LaunchResult matrix(const KParams& k, bool want_m, const void* buf, long long first, long long n,
+                             cudaStream_t st) {
+    if (n <= 0) return {cudaSuccess, 0};
+    const size_t smem = sizeof(ES) * M::EPC;
+    const unsigned blocks = (unsigned)((n + M::EPC - 1) / M::EPC);
+    const Rec* in = reinterpret_cast<const Rec*>(buf);
+    if (want_m) {
+      auto fn = matrix_kernel<DIM, NEN, NC, NQ, S, true>;
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return {e, 0};
+      fn<<<blocks, 128, smem, st>>>(k, in, first, n);
+    } else {
+      auto fn = matrix_kernel<DIM, NEN, NC, NQ, S, false>;
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return {e, 0};
+      fn<<<blocks, 128, smem, st>>>(k, in, first, n);
+    }
+    return {cudaGetLastError(), 1};
+  }
+};
 
 template <int DIM, int NEN, int NC, int NS, int NSQ>
 LaunchResult launch_boundary_nc(const KParams& k, long long n_items, cudaStream_t st) {
   if (n_items == 0) return {cudaSuccess, 0};
-  boundary_kernel<DIM, NEN, NC, NS, NSQ><<<(unsigned)n_items, 32, 0, st>>>(k);
+  const size_t smem = sizeof(BoundarySmem<DIM, NEN, NC, NS, NSQ>);
+  auto fn = boundary_kernel<DIM, NEN, NC, NS, NSQ>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return {e, 0};
+  fn<<<(unsigned)n_items, 32, smem, st>>>(k);
   return {cudaGetLastError(), 1};
 }
 
-template <int DIM, int NEN, int NQ, int NS, int NSQ>
-struct ElementDispatch {
-  template <int FORM>
-  static LaunchResult interior(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
-    switch (nc) {
-      case 1: return launch_interior_nc<DIM, NEN, 1, NQ, FORM>(k, want_m, n, st);
-      case 2: return launch_interior_nc<DIM, NEN, 2, NQ, FORM>(k, want_m, n, st);
-      case 3: return launch_interior_nc<DIM, NEN, 3, NQ, FORM>(k, want_m, n, st);
-      case 4: return launch_interior_nc<DIM, NEN, 4, NQ, FORM>(k, want_m, n, st);
-      default: return {cudaErrorInvalidValue, 0};
-    }
-  }
-  static LaunchResult boundary(const KParams& k, int nc, long long n, cudaStream_t st) {
-    switch (nc) {
-      case 1: return launch_boundary_nc<DIM, NEN, 1, NS, NSQ>(k, n, st);
-      case 2: return launch_boundary_nc<DIM, NEN, 2, NS, NSQ>(k, n, st);
-      case 3: return launch_boundary_nc<DIM, NEN, 3, NS, NSQ>(k, n, st);
-      case 4: return launch_boundary_nc<DIM, NEN, 4, NS, NSQ>(k, n, st);
-      default: return {cudaErrorInvalidValue, 0};
-    }
-  }
+// Interior operations of one (element type, form): record bytes per element, point
+// stage and matrix stage, for 1..4 components.
+struct InteriorOps {
+  size_t (*rec_bytes)(int nc);
+  LaunchResult (*point)(const KParams&, int nc, void* buf, long long first, long long n, cudaStream_t);
+  LaunchResult (*matrix)(const KParams&, int nc, bool want_m, const void* buf, long long first, long long n,
+                         cudaStream_t);
 };
 
-// Entry points defined by the per-element translation units (<type>_fp64.cu holds the
-// FP64 interior and the boundary kernels, <type>_mixed.cu the mixed interior kernels).
-LaunchResult interior_tri3_fp64(const KParams&, int nc, bool want_m, long long n, cudaStream_t);
-LaunchResult interior_tri3_mixed(const KParams&, int nc, bool want_m, long long n, cudaStream_t);
+#define GALES_NC_SWITCH(expr_nc, CALL) \
+  switch (expr_nc) {                   \
+    case 1: CALL(1);                   \
+    case 2: CALL(2);                   \
+    case 3: CALL(3);                   \
+    case 4: CALL(4);                   \
+    default: break;                    \
+  }
+
+template <int DIM, int NEN, int NQ, int FORM>
+struct InteriorDispatch {
+  static size_t rec_bytes(int nc) {
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::rec_bytes()
+    GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+    return 0;
+  }
+  static LaunchResult point(const KParams& k, int nc, void* buf, long long first, long long n, cudaStream_t st) {
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::point(k, buf, first, n, st)
+    GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+    return {cudaErrorInvalidValue, 0};
+  }
+  static LaunchResult matrix(const KParams& k, int nc, bool want_m, const void* buf, long long first, long long n,
+                             cudaStream_t st) {
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::matrix(k, want_m, buf, first, n, st)
+    GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+    return {cudaErrorInvalidValue, 0};
+  }
+  static InteriorOps ops() { return {&rec_bytes, &point, &matrix}; }
+};
+
+template <int DIM, int NEN, int NS, int NSQ>
+LaunchResult boundary_dispatch(const KParams& k, int nc, long long n, cudaStream_t st) {
+#define GALES_C(NC) return launch_boundary_nc<DIM, NEN, NC, NS, NSQ>(k, n, st)
+  GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+  return {cudaErrorInvalidValue, 0};
+}
+
+// Element geometry precompute (handle creation).
+struct GeometryOps {
+  size_t bytes_per_element;
+  LaunchResult (*launch)(const double* coords, const int32_t* conn, const KParams& k, void* out, long long n_el,
+                         cudaStream_t st);
+};
+
+template <int DIM, int NEN, int NQ>
+struct GeometryDispatch {
+  static constexpr int NG = geo_per_element<DIM, NEN>(NQ);
+  static LaunchResult launch(const double* coords, const int32_t* conn, const KParams& k, void* out, long long n_el,
+                             cudaStream_t st) {
+    if (n_el <= 0) return {cudaSuccess, 0};
+    const long long threads = n_el * NG;
+    geometry_kernel<DIM, NEN, NQ><<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(
+        coords, conn, k, reinterpret_cast<ElemGeo<DIM, NEN>*>(out), n_el);
+    return {cudaGetLastError(), 1};
+  }
+  static GeometryOps ops() { return {sizeof(ElemGeo<DIM, NEN>) * NG, &launch}; }
+};
+
+// Entry points defined by the per-element translation units.
+InteriorOps interior_ops_tri3_fp64();
+InteriorOps interior_ops_tri3_mixed();
 LaunchResult boundary_tri3(const KParams&, int nc, long long n, cudaStream_t);
-LaunchResult interior_quad4_fp64(const KParams&, int nc, bool want_m, long long n, cudaStream_t);
-LaunchResult interior_quad4_mixed(const KParams&, int nc, bool want_m, long long n, cudaStream_t);
+GeometryOps geometry_ops_tri3();
+InteriorOps interior_ops_quad4_fp64();
+InteriorOps interior_ops_quad4_mixed();
 LaunchResult boundary_quad4(const KParams&, int nc, long long n, cudaStream_t);
-LaunchResult interior_tet4_fp64(const KParams&, int nc, bool want_m, long long n, cudaStream_t);
-LaunchResult interior_tet4_mixed(const KParams&, int nc, bool want_m, long long n, cudaStream_t);
+GeometryOps geometry_ops_quad4();
+InteriorOps interior_ops_tet4_fp64();
+InteriorOps interior_ops_tet4_mixed();
 LaunchResult boundary_tet4(const KParams&, int nc, long long n, cudaStream_t);
-LaunchResult interior_hex8_fp64(const KParams&, int nc, bool want_m, long long n, cudaStream_t);
-LaunchResult interior_hex8_mixed(const KParams&, int nc, bool want_m, long long n, cudaStream_t);
+GeometryOps geometry_ops_tet4();
+InteriorOps interior_ops_hex8_fp64();
+InteriorOps interior_ops_hex8_mixed();
 LaunchResult boundary_hex8(const KParams&, int nc, long long n, cudaStream_t);
+GeometryOps geometry_ops_hex8();
 
 }  // namespace gales

@@ -120,13 +120,33 @@ __device__ __forceinline__ void mixture_rho_cv(const DevChem* ch, double p, doub
 
 // Scalars from which every frozen-coefficient matrix of the point is built
 // (fluid_2d.hpp:393-404, 531-533).
-template <int DIM, int NC>
+template <int DIM, int NC, typename T = double>
 struct Coef {
   using L = Layout<DIM, NC>;
-  double p, v[DIM], T, Y[NC];
-  double rho, E, drho_dp, drho_dT, de_dp, de_dT, mu, lambda, kappa, c, cv;
-  double drho_dY[L::NYA], dE_dY[L::NYA], rhoD[L::NYA], rhoDH[L::NYA];
+  T p, v[DIM], T_, Y[NC];
+  T rho, E, drho_dp, drho_dT, de_dp, de_dT, mu, lambda, kappa, c, cv;
+  T drho_dY[L::NYA], dE_dY[L::NYA], rhoD[L::NYA], rhoDH[L::NYA];
 };
+
+template <int DIM, int NC>
+__device__ __forceinline__ Coef<DIM, NC, float> narrow(const Coef<DIM, NC, double>& c) {
+  using L = Layout<DIM, NC>;
+  Coef<DIM, NC, float> f;
+  f.p = float(c.p); f.T_ = float(c.T_);
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) f.v[k] = float(c.v[k]);
+#pragma unroll
+  for (int i = 0; i < NC; ++i) f.Y[i] = float(c.Y[i]);
+  f.rho = float(c.rho); f.E = float(c.E); f.drho_dp = float(c.drho_dp); f.drho_dT = float(c.drho_dT);
+  f.de_dp = float(c.de_dp); f.de_dT = float(c.de_dT); f.mu = float(c.mu); f.lambda = float(c.lambda);
+  f.kappa = float(c.kappa); f.c = float(c.c); f.cv = float(c.cv);
+#pragma unroll
+  for (int i = 0; i < L::NYA; ++i) {
+    f.drho_dY[i] = float(c.drho_dY[i]); f.dE_dY[i] = float(c.dE_dY[i]);
+    f.rhoD[i] = float(c.rhoD[i]); f.rhoDH[i] = float(c.rhoDH[i]);
+  }
+  return f;
+}
 
 // assign(): fluid_2d.hpp:112-121
 template <int DIM, int NC>
@@ -170,7 +190,7 @@ __device__ __forceinline__ void conservative(double rho, double cv, const double
 template <int DIM, int NC>
 __device__ __forceinline__ void make_coef(const Props<NC>& pr, double p, const double* v, double T,
                                           const double* Y, Coef<DIM, NC>& c) {
-  c.p = p; c.T = T;
+  c.p = p; c.T_ = T;
 #pragma unroll
   for (int k = 0; k < DIM; ++k) c.v[k] = v[k];
 #pragma unroll
@@ -318,42 +338,75 @@ __device__ __forceinline__ T k_entry(const C& c, int k, int l, int r, int col) {
   return T(0);
 }
 
-// y = DUDY x, in ascending column order (the order of a dense uBLAS prod()).
+// Structural nonzeros of DUDY, A_k and K_kl (the entries fluid_2d.hpp:407-571 sets).
+// Evaluated at compile time inside fully unrolled loops, so products with structural
+// zeros are never issued; dropping exact-zero terms leaves every finite sum unchanged.
 template <int DIM, int NC>
-__device__ __forceinline__ void dudy_mv(const Coef<DIM, NC>& c, const double* x, double* y) {
+__host__ __device__ constexpr bool dudy_nz(int r, int col) {
+  using L = Layout<DIM, NC>;
+  if (r == L::iT) return true;
+  if (col == 0 || col == L::iT || col >= L::iY) return true;
+  return r >= 1 && r < L::iT && col == r;
+}
+
+template <int DIM, int NC>
+__host__ __device__ constexpr bool a_nz(int k, int r, int col) {
+  using L = Layout<DIM, NC>;
+  if (r == L::iT) return true;
+  if (col == 0 || col == L::iT || col >= L::iY || col == 1 + k) return true;
+  return r >= 1 && r < L::iT && col == r;
+}
+
+template <int DIM, int NC>
+__host__ __device__ constexpr bool k_nz(int k, int l, int r, int col) {
+  using L = Layout<DIM, NC>;
+  if (r == 0 || col == 0) return false;
+  if (k == l) {
+    if (r < L::iT) return col == r;
+    if (r == L::iT) return true;
+    return col == r;
+  }
+  return (r == 1 + k && col == 1 + l) || (r == 1 + l && col == 1 + k) ||
+         (r == L::iT && (col == 1 + k || col == 1 + l));
+}
+
+// y = DUDY x (and A_k x, K_kl x) in ascending column order, the order of a dense
+// uBLAS prod(), skipping structural zeros.
+template <int DIM, int NC, typename T, typename C>
+__device__ __forceinline__ void dudy_mv(const C& c, const T* x, T* y) {
   using L = Layout<DIM, NC>;
 #pragma unroll
   for (int r = 0; r < L::ND; ++r) {
-    double t = 0.0;
+    T t = T(0);
 #pragma unroll
-    for (int col = 0; col < L::ND; ++col) {
-      const double a = dudy_entry<DIM, NC, double>(c, r, col);
-      t += a * x[col];
-    }
+    for (int col = 0; col < L::ND; ++col)
+      if (dudy_nz<DIM, NC>(r, col)) t += dudy_entry<DIM, NC, T>(c, r, col) * x[col];
     y[r] = t;
   }
 }
 
-template <int DIM, int NC>
-__device__ __forceinline__ void a_mv(const Coef<DIM, NC>& c, int k, const double* x, double* y) {
+template <int DIM, int NC, typename T, typename C>
+__device__ __forceinline__ void a_mv(const C& c, int k, const T* x, T* y) {
   using L = Layout<DIM, NC>;
 #pragma unroll
   for (int r = 0; r < L::ND; ++r) {
-    double t = 0.0;
+    T t = T(0);
 #pragma unroll
-    for (int col = 0; col < L::ND; ++col) t += a_entry<DIM, NC, double>(c, k, r, col) * x[col];
+    for (int col = 0; col < L::ND; ++col)
+      if (a_nz<DIM, NC>(k, r, col)) t += a_entry<DIM, NC, T>(c, k, r, col) * x[col];
     y[r] = t;
   }
 }
 
-template <int DIM, int NC>
-__device__ __forceinline__ void k_mv(const Coef<DIM, NC>& c, int k, int l, const double* x, double* y) {
+template <int DIM, int NC, typename T, typename C>
+__device__ __forceinline__ void k_mv(const C& c, int k, int l, const T* x, T* y) {
   using L = Layout<DIM, NC>;
 #pragma unroll
   for (int r = 0; r < L::ND; ++r) {
-    double t = 0.0;
+    T t = T(0);
 #pragma unroll
-    for (int col = 0; col < L::ND; ++col) t += k_entry<DIM, NC, double>(c, k, l, r, col) * x[col];
+    for (int col = 0; col < L::ND; ++col)
+      if (k_nz<DIM, NC>(k, l, r, col)) t += k_entry<DIM, NC, T>(c, k, l, r, col) * x[col];
     y[r] = t;
   }
 }

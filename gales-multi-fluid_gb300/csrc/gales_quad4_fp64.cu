@@ -4,14 +4,12 @@
 
 namespace gales {
 
-using D_quad4 = ElementDispatch<2, 4, 4, 4, 2>;
-
-LaunchResult interior_quad4_fp64(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
-  return D_quad4::interior<GALES_FORM_FP64>(k, nc, want_m, n, st);
-}
+InteriorOps interior_ops_quad4_fp64() { return InteriorDispatch<2, 4, 4, GALES_FORM_FP64>::ops(); }
 
 LaunchResult boundary_quad4(const KParams& k, int nc, long long n, cudaStream_t st) {
-  return D_quad4::boundary(k, nc, n, st);
+  return boundary_dispatch<2, 4, 4, 2>(k, nc, n, st);
 }
+
+GeometryOps geometry_ops_quad4() { return GeometryDispatch<2, 4, 4>::ops(); }
 
 }  // namespace gales

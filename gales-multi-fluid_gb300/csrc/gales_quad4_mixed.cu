@@ -4,10 +4,6 @@
 
 namespace gales {
 
-using D_quad4 = ElementDispatch<2, 4, 4, 4, 2>;
-
-LaunchResult interior_quad4_mixed(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
-  return D_quad4::interior<GALES_FORM_MIXED>(k, nc, want_m, n, st);
-}
+InteriorOps interior_ops_quad4_mixed() { return InteriorDispatch<2, 4, 4, GALES_FORM_MIXED>::ops(); }
 
 }  // namespace gales

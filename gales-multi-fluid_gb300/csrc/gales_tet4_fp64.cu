@@ -4,14 +4,12 @@
 
 namespace gales {
 
-using D_tet4 = ElementDispatch<3, 4, 4, 4, 3>;
-
-LaunchResult interior_tet4_fp64(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
-  return D_tet4::interior<GALES_FORM_FP64>(k, nc, want_m, n, st);
-}
+InteriorOps interior_ops_tet4_fp64() { return InteriorDispatch<3, 4, 4, GALES_FORM_FP64>::ops(); }
 
 LaunchResult boundary_tet4(const KParams& k, int nc, long long n, cudaStream_t st) {
-  return D_tet4::boundary(k, nc, n, st);
+  return boundary_dispatch<3, 4, 4, 3>(k, nc, n, st);
 }
+
+GeometryOps geometry_ops_tet4() { return GeometryDispatch<3, 4, 4>::ops(); }
 
 }  // namespace gales

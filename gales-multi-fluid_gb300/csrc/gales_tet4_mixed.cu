@@ -4,10 +4,6 @@
 
 namespace gales {
 
-using D_tet4 = ElementDispatch<3, 4, 4, 4, 3>;
-
-LaunchResult interior_tet4_mixed(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
-  return D_tet4::interior<GALES_FORM_MIXED>(k, nc, want_m, n, st);
-}
+InteriorOps interior_ops_tet4_mixed() { return InteriorDispatch<3, 4, 4, GALES_FORM_MIXED>::ops(); }
 
 }  // namespace gales

@@ -4,14 +4,12 @@
 
 namespace gales {
 
-using D_tri3 = ElementDispatch<2, 3, 3, 3, 2>;
-
-LaunchResult interior_tri3_fp64(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
-  return D_tri3::interior<GALES_FORM_FP64>(k, nc, want_m, n, st);
-}
+InteriorOps interior_ops_tri3_fp64() { return InteriorDispatch<2, 3, 3, GALES_FORM_FP64>::ops(); }
 
 LaunchResult boundary_tri3(const KParams& k, int nc, long long n, cudaStream_t st) {
-  return D_tri3::boundary(k, nc, n, st);
+  return boundary_dispatch<2, 3, 3, 2>(k, nc, n, st);
 }
+
+GeometryOps geometry_ops_tri3() { return GeometryDispatch<2, 3, 3>::ops(); }
 
 }  // namespace gales

@@ -4,10 +4,6 @@
 
 namespace gales {
 
-using D_tri3 = ElementDispatch<2, 3, 3, 3, 2>;
-
-LaunchResult interior_tri3_mixed(const KParams& k, int nc, bool want_m, long long n, cudaStream_t st) {
-  return D_tri3::interior<GALES_FORM_MIXED>(k, nc, want_m, n, st);
-}
+InteriorOps interior_ops_tri3_mixed() { return InteriorDispatch<2, 3, 3, GALES_FORM_MIXED>::ops(); }
 
 }  // namespace gales

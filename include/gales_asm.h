@@ -213,6 +213,9 @@ int gales_asm_status(gales_asm* h, int64_t* first_bad_element);
 const char* gales_asm_last_error(gales_asm* h);
 /* Device time in ms of the last assemble/residual/vjp call (CUDA events on its stream). */
 double gales_asm_last_ms(gales_asm* h);
+/* Device time in ms of one phase of the last assemble/residual call, CUDA events on
+ * its stream: 0 = clearing A and b, 1 = interior element kernel(s), 2 = boundary pass. */
+double gales_asm_last_phase_ms(gales_asm* h, int32_t phase);
 /* Number of kernel launches made by the library since the handle was created. */
 int64_t gales_asm_launch_count(gales_asm* h);
 
