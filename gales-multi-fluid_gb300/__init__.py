@@ -402,6 +402,15 @@ class FluidAssembly:
         self.last_seconds = time.perf_counter() - t0
         return self.last_seconds
 
+    def execute_noalloc(self, I, P, dt: float, lp: LinearSystem, form: int = FORM_FP64, stream: int = 0) -> float:
+        """Same as execute() but allocates nothing: for callers that must keep a fixed
+        device-memory footprint.  All buffers must be CUDA tensors; calls share one
+        library-wide scratch array, so calls that overlap on the GPU must be ordered."""
+        t0 = time.perf_counter()
+        self._check(self._L.gales_asm_assemble_noalloc(self._h, _addr(I), _addr(P), float(dt), form,
+                                                       _addr(lp.vals), _addr(lp.rhs), stream or None))
+        return time.perf_counter() - t0
+
     def residual(self, I, P, dt: float, rhs, form: int = FORM_FP64, stream: int = 0) -> float:
         t0 = time.perf_counter()
         self._check(self._L.gales_asm_residual(self._h, _addr(I), _addr(P), float(dt), form, _addr(rhs),

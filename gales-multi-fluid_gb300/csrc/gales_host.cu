@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -993,3 +994,103 @@ double gales_asm_last_phase_ms(gales_asm* h, int32_t phase) {
 int64_t gales_asm_launch_count(gales_asm* h) { return h ? h->launches : 0; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Assembly without any allocation.
+//
+// Some callers cannot allocate device memory while they assemble: programs whose
+// device memory is owned by another allocator (a framework's caching pool, a
+// fixed per-process quota) where a raw cudaMalloc would overrun the budget or
+// fragment the pool, and time-stepping loops that must keep a fixed memory
+// footprint and never meet allocator latency or an out-of-memory failure in the
+// middle of a run.  gales_asm_assemble may allocate staging buffers on first use
+// (host pointers); the entry point below never does.  Its interior pass runs the
+// same point and matrix kernels, with the per-point records in this file-scope
+// device array instead of handle-owned buffers.  Every GPU that loads the library
+// holds the array until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GALES_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+// Device address of g_noalloc_scratch per device.  In host code the array's name
+// is only a host-side stand-in, so the address is looked up once per device, with
+// that device current, by the first gales_asm_assemble_noalloc call on it.
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {nullptr};
+
+int noalloc_scratch(gales_asm* h, void** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (h->device < 0 || h->device >= 64) return fail(h, GALES_ERR_BAD_INPUT, "device index out of range");
+  if (!g_noalloc_ptr[h->device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_ptr[h->device] = p;
+  }
+  *out = g_noalloc_ptr[h->device];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int gales_asm_assemble_noalloc(gales_asm* h, const double* I, const double* P, double dt,
+                                          int32_t form, double* vals, double* rhs, void* stream) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (!I || !P || !vals || !rhs) return fail(h, GALES_ERR_BAD_INPUT, "null state or output pointer");
+  if (form != GALES_FORM_FP64 && form != GALES_FORM_MIXED) return fail(h, GALES_ERR_BAD_INPUT, "unknown form");
+  if (!(dt > 0.0)) return fail(h, GALES_ERR_BAD_INPUT, "dt must be positive");
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (!is_device_ptr(I) || !is_device_ptr(P) || !is_device_ptr(vals) || !is_device_ptr(rhs))
+    return fail(h, GALES_ERR_BAD_INPUT,
+                "gales_asm_assemble_noalloc needs device pointers for I, P, vals and rhs "
+                "(host buffers would need staging allocations)");
+  const InteriorOps& ops = h->ops[form];
+  const size_t rb = ops.rec_bytes(h->nc);
+  if (rb == 0) return fail(h, GALES_ERR_UNSUPPORTED, "no interior kernel for this element/component count");
+  if (rb > GALES_NOALLOC_SCRATCH_BYTES)
+    return fail(h, GALES_ERR_UNSUPPORTED,
+                "one element's point records (" + std::to_string(rb) + " bytes) exceed the " +
+                    std::to_string((long long)GALES_NOALLOC_SCRATCH_BYTES) + "-byte no-allocation scratch");
+  void* scratch = nullptr;
+  int rc = noalloc_scratch(h, &scratch);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  KParams k = base_params(h, dt);
+  k.I = I;
+  k.P = P;
+  k.vals = vals;
+  k.rhs = rhs;
+  k.scatter_mode = 0;
+  CK(h, cudaEventRecord(h->ev0, st), "event");
+  CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
+  CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  CK(h, cudaMemsetAsync(vals, 0, (size_t)h->nnz * sizeof(double), st), "memset vals");
+  CK(h, cudaMemsetAsync(rhs, 0, (size_t)h->n_rows * sizeof(double), st), "memset rhs");
+  // The point records of a chunk are written in full by the point kernel before the
+  // matrix kernel reads them, so nothing in the scratch has to start at zero.
+  const long long chunk = (long long)(GALES_NOALLOC_SCRATCH_BYTES / rb);
+  for (long long first = 0; first < h->n_el; first += chunk) {
+    const long long cnt = std::min(chunk, h->n_el - first);
+    LaunchResult r = ops.point(k, h->nc, scratch, first, cnt, st);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "point kernel");
+    h->launches += r.launches;
+    r = ops.matrix(k, h->nc, true, scratch, first, cnt, st);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "matrix kernel");
+    h->launches += r.launches;
+  }
+  if (!h->bd_list.empty()) {
+    KParams kb = k;
+    kb.el_list = h->d_bd_list.p;
+    kb.n_list = (int64_t)h->bd_list.size();
+    kb.bd_sides = h->d_bd_sides.p;
+    LaunchResult r = dispatch_boundary(h, kb, kb.n_list, st);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
+    h->launches += r.launches;
+  }
+  CK(h, cudaEventRecord(h->ev1, st), "event");
+  rc = finish(h, st);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  return rc;
+}

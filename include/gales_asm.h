@@ -185,6 +185,23 @@ int gales_asm_set_scatter(gales_asm* h, int32_t mode); /* GALES_SCATTER_* */
  * is part of the call, linear_system.hpp:90-94).  stream: cudaStream_t or NULL. */
 int gales_asm_assemble(gales_asm* h, const double* I, const double* P, double dt, int32_t form,
                        double* vals, double* rhs, void* stream);
+/* Assembly that allocates nothing (no counterpart in the reference).  For callers
+ * that must not allocate device memory during the call: programs whose device
+ * memory belongs to another allocator or to a fixed quota, and loops that keep a
+ * fixed memory footprint after set-up.  Same result as gales_asm_assemble, but
+ * I, P, vals and rhs must be device pointers (host buffers are rejected with
+ * GALES_ERR_BAD_INPUT since staging them would allocate), the work runs on the
+ * caller's stream only, and the per-point records live in one library-wide
+ * device array of GALES_NOALLOC_SCRATCH_BYTES, which every GPU that loads the
+ * library keeps until exit.  An element whose point records exceed that size is
+ * rejected with GALES_ERR_UNSUPPORTED; larger meshes are processed in chunks.
+ * The first call on a device looks up the array's device address (once per
+ * device); make that first call before any stream capture.  All calls, from every
+ * handle, share the one array and it keeps the last call's contents: calls that
+ * overlap on the GPU (concurrent streams or threads) race on it, so order them. */
+#define GALES_NOALLOC_SCRATCH_BYTES (8u << 20)
+int gales_asm_assemble_noalloc(gales_asm* h, const double* I, const double* P, double dt, int32_t form,
+                               double* vals, double* rhs, void* stream);
 /* Residual only (rhs), no matrix. */
 int gales_asm_residual(gales_asm* h, const double* I, const double* P, double dt, int32_t form,
                        double* rhs, void* stream);
