@@ -759,14 +759,21 @@ __global__ void __launch_bounds__(128) point_kernel(const KParams k, QP<DIM, NEN
 
 // Interior pass, stage 2: element matrices.  Lanes are mapped to (test node b,
 // trial node a, half of the rows): each lane owns an RH x ND register tile of the
-// (b, a) block and accumulates, per quadrature point,
-//   JxW [ FPT_b RM_a + N_a X_b + sum_l dN_a/dx_l KD_bl ]
-// with (fluid_2d.hpp:264-331)
+// (b, a) block and accumulates, per quadrature point (fluid_2d.hpp:264-331),
+//   JxW [ FPT_b RM_a + N_a X_b ]   with
 //   WA_b  = sum_k dN_b/dx_k A_k
 //   FPT_b = (WA_b - N_b S0) tau                       least-squares weight
 //   RM_a  = N_a DUDY/dt + WA_a - N_a S0               least-squares operator
 //   X_b   = N_b (DUDY/dt - S0) - WA_b                 Galerkin mass, source, advection
-//   KD_bl = sum_k dN_b/dx_k K_kl + nu dN_b/dx_l DUDY  viscous/diffusive and dc terms
+// plus the viscous/diffusive and dc terms sum_kl dN_b/dx_k K'_kl dN_a/dx_l with
+// K'_kl = K_kl + nu d_kl DUDY.  K'_kl is linear in a few point scalars (mu, lambda,
+// mu v, lambda v, kappa, rho D_i, rho D_i H_i) and in nu DUDY, so it is applied in
+// closed form: per point for non-affine elements, once from JxW-weighted sums for
+// simplices (their shape gradients do not depend on the point).
+// DUDY and A_k are built branch-free from their structure: DUDY = w r0^T + rho M
+// (w = (1, v, E, Y), r0 its first row, M zero but for the velocity and mass-fraction
+// diagonal and the energy row), and A_k = v_k DUDY + (U + p e_E) e_{v_k}^T +
+// (e_{v_k} + v_k e_E) e_p^T (fluid_2d.hpp:407-524).
 template <int DIM, int NEN, int NC>
 struct MatShape {
   static constexpr int ND = Layout<DIM, NC>::ND;
@@ -776,11 +783,20 @@ struct MatShape {
   static constexpr int WPE = (2 * NP + 31) / 32;       // warps per element
   static constexpr int EPC = WPE == 1 ? 4 : 1;        // elements per CTA
   static constexpr int N = NEN * ND;
+  static constexpr bool AFFINE = NEN == DIM + 1;
+};
+
+// Point scalars entering K'_kl, JxW-weighted when summed over an element's points.
+template <int DIM, int NC, typename S>
+struct KSums {
+  using L = Layout<DIM, NC>;
+  S mu, lambda, kappa, muv[DIM], lamv[DIM], rhoD[L::NYA], rhoDH[L::NYA];
 };
 
 template <int DIM, int NEN, int NC, int NQ, typename S>
 struct ElemSmem {
   using M = MatShape<DIM, NEN, NC>;
+  using L = Layout<DIM, NC>;
   static constexpr int ND = M::ND, NDP = M::NDP, N = M::N;
   QP<DIM, NEN, NC, S> qp[NQ];
   struct Work {
@@ -790,7 +806,8 @@ struct ElemSmem {
     S FPT[NEN][NDP][ND];
     S RM[NEN][ND][NDP];
     S X[NEN][NDP][ND];
-    S KD[NEN][DIM][NDP][ND];
+    S Dnu[NDP][ND];          // sum_q JxW nu DUDY (simplices)
+    S w[ND], r0[ND], mE[ND], U[ND];
   };
   union {
     Work w;
@@ -812,6 +829,51 @@ __device__ __forceinline__ void elem_sync(int el_in_cta) {
   }
 }
 
+// Adds JxW * sum_kl gb_k K_kl(r, c) ga_l for the lane's tile rows r0..r0+RH-1 (the
+// closed form of the contraction; fluid_2d.hpp:531-571), with point scalars ks.
+template <int DIM, int NC, int RH, int ND, typename S>
+__device__ __forceinline__ void add_viscous_tile(S (&acc)[RH][ND], int r0, const KSums<DIM, NC, S>& ks,
+                                                 const S* gb, const S* ga) {
+  using L = Layout<DIM, NC>;
+  S gg = gb[0] * ga[0];
+  S gamv = ga[0] * ks.muv[0], gblv = gb[0] * ks.lamv[0];
+#pragma unroll
+  for (int d = 1; d < DIM; ++d) {
+    gg = madd(gb[d], ga[d], gg);
+    gamv = madd(ga[d], ks.muv[d], gamv);
+    gblv = madd(gb[d], ks.lamv[d], gblv);
+  }
+#pragma unroll
+  for (int i = 0; i < RH; ++i) {
+    const int r = r0 + i;
+    if (r >= 1 && r < L::iT) {
+      const int jj = r - 1;
+      S gbj = gb[0], gaj = ga[0];
+#pragma unroll
+      for (int d = 1; d < DIM; ++d) {
+        gbj = (jj == d) ? gb[d] : gbj;
+        gaj = (jj == d) ? ga[d] : gaj;
+      }
+#pragma unroll
+      for (int m = 0; m < DIM; ++m) {
+        S x = ks.mu * gb[m] * gaj + ks.lambda * gbj * ga[m];
+        if (m == jj) x = madd(ks.mu, gg, x);
+        acc[i][1 + m] += x;
+      }
+    } else if (r == L::iT) {
+#pragma unroll
+      for (int m = 0; m < DIM; ++m) acc[i][1 + m] += ks.muv[m] * gg + gb[m] * gamv + ga[m] * gblv;
+      acc[i][L::iT] = madd(ks.kappa, gg, acc[i][L::iT]);
+#pragma unroll
+      for (int y = 0; y < NC - 1; ++y) acc[i][L::iY + y] = madd(ks.rhoDH[y], gg, acc[i][L::iY + y]);
+    } else if (r >= L::iY && r < ND) {
+#pragma unroll
+      for (int y = 0; y < NC - 1; ++y)
+        if (r == L::iY + y) acc[i][L::iY + y] = madd(ks.rhoD[y], gg, acc[i][L::iY + y]);
+    }
+  }
+}
+
 template <int DIM, int NEN, int NC, int NQ, typename S, bool WANT_M>
 __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<DIM, NEN, NC, S>* __restrict__ in,
                                                       long long first, long long n) {
@@ -820,6 +882,7 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
   using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
   constexpr int ND = M::ND, NDP = M::NDP, RH = M::RH, N = M::N, NT = N * N, WPE = M::WPE, EPC = M::EPC;
   constexpr int ET = WPE * 32;  // threads per element
+  constexpr bool AFF = M::AFFINE;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x;
   const int ec = tid / ET;      // element slot in the CTA
@@ -829,7 +892,6 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
   if (li >= n) return;          // whole element groups exit together
   const long long g = first + li;
   const long long e = k.el_list ? (long long)k.el_list[g] : g;
-  // stage the element's point records
   {
     constexpr int W4 = sizeof(QP<DIM, NEN, NC, S>) * NQ / 16;
     const int4* src = reinterpret_cast<const int4*>(in + li * NQ);
@@ -839,22 +901,21 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
   if (gl < NEN) {
     const int nd_ = __ldg(k.conn + e * NEN + gl);
     E.nodes[gl] = nd_;
-    const int64_t r0 = __ldg(k.node_rp + nd_), r1 = __ldg(k.node_rp + nd_ + 1);
-    E.rowbase[gl] = r0 * (int64_t)(ND * ND);
-    E.rowlen[gl] = (int32_t)((r1 - r0) * ND);
+    const int64_t rr0 = __ldg(k.node_rp + nd_), rr1 = __ldg(k.node_rp + nd_ + 1);
+    E.rowbase[gl] = rr0 * (int64_t)(ND * ND);
+    E.rowlen[gl] = (int32_t)((rr1 - rr0) * ND);
     const int fl = k.node_flag ? __ldg(k.node_flag + nd_) : 0;
     E.blocked[gl] = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
   }
-  // padding rows of FPT, X and KD stay zero
+  auto& w = E.u.w;
   if constexpr (NDP > ND) {
     for (int t = gl; t < NEN * (NDP - ND) * ND; t += ET) {
       const int b = t / ((NDP - ND) * ND), r = ND + (t / ND) % (NDP - ND), c = t % ND;
-      E.u.w.FPT[b][r][c] = S(0);
-      E.u.w.X[b][r][c] = S(0);
-#pragma unroll
-      for (int l = 0; l < DIM; ++l) E.u.w.KD[b][l][r][c] = S(0);
+      w.FPT[b][r][c] = S(0);
+      w.X[b][r][c] = S(0);
     }
   }
+  for (int t = gl; t < NDP * ND; t += ET) (&w.Dnu[0][0])[t] = S(0);
   const int pr = gl >> 1, half = gl & 1;
   const bool has_pair = pr < M::NP;
   const int pb = has_pair ? pr / NEN : 0, pa = has_pair ? pr % NEN : 0;
@@ -865,43 +926,66 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
 #pragma unroll
     for (int j = 0; j < ND; ++j) acc[i][j] = S(0);
   S racc = S(0);
+  KSums<DIM, NC, S> ksum;
+  if constexpr (AFF) {
+    ksum.mu = ksum.lambda = ksum.kappa = S(0);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ksum.muv[d] = ksum.lamv[d] = S(0);
+#pragma unroll
+    for (int y = 0; y < L::NYA; ++y) ksum.rhoD[y] = ksum.rhoDH[y] = S(0);
+  }
   const S dt = S(k.dt);
   const S idt = S(1) / dt;
-  auto s0 = [&](const QP<DIM, NEN, NC, S>& c, int r, int col) -> S {
-    return (r == L::iT && col >= 1 && col <= DIM) ? c.rho * S(k.gravity[col - 1]) : S(0);
-  };
+  S grav[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) grav[d] = S(k.gravity[d]);
   elem_sync<WPE>(ec);
   for (int iq = 0; iq < NQ; ++iq) {
     const QP<DIM, NEN, NC, S>& c = E.qp[iq];
-    auto& w = E.u.w;
-    // (1) A_k and DUDY
-    for (int t = gl; t < (DIM + 1) * ND * NDP; t += ET) {
-      const int kk = t / (ND * NDP), r = (t / NDP) % ND, col = t % NDP;
-      if (kk < DIM) w.A[kk][r][col] = col < ND ? a_entry<DIM, NC, S>(c, kk, r, col) : S(0);
-      else w.D[r][col] = col < ND ? dudy_entry<DIM, NC, S>(c, r, col) : S(0);
+    // (0) structure vectors of DUDY: w, r0, energy row of M, U
+    for (int t = gl; t < ND; t += ET) {
+      S wv, r0v, mv;
+      if (t == 0) { wv = S(1); r0v = c.drho_dp; mv = c.de_dp; }
+      else if (t < L::iT) { wv = c.v[t - 1]; r0v = S(0); mv = c.v[t - 1]; }
+      else if (t == L::iT) { wv = c.E; r0v = c.drho_dT; mv = c.de_dT; }
+      else { wv = c.Y[t - L::iY]; r0v = c.drho_dY[t - L::iY]; mv = c.dE_dY[t - L::iY]; }
+      w.w[t] = wv; w.r0[t] = r0v; w.mE[t] = mv; w.U[t] = c.rho * wv;
     }
     elem_sync<WPE>(ec);
-    // (2) WA, RM, X, KD
+    // (1) DUDY and A_k, branch-free
+    for (int t = gl; t < ND * ND; t += ET) {
+      const int r = t / ND, col = t % ND;
+      const S Mrc = (r == L::iT) ? w.mE[col] : ((r == col && r != 0) ? S(1) : S(0));
+      const S Dv = madd(w.w[r], w.r0[col], c.rho * Mrc);
+      w.D[r][col] = Dv;
+      const S isE = (r == L::iT) ? S(1) : S(0);
+      const S Ur = w.U[r];
+#pragma unroll
+      for (int kk = 0; kk < DIM; ++kk) {
+        const S vk = c.v[kk];
+        S a = vk * Dv;
+        a += (col == 1 + kk) ? madd(isE, c.p, Ur) : S(0);
+        a += (col == 0) ? madd(isE, vk, (r == 1 + kk) ? S(1) : S(0)) : S(0);
+        w.A[kk][r][col] = a;
+      }
+    }
+    elem_sync<WPE>(ec);
+    // (2) WA, RM, X
     for (int t = gl; t < NEN * ND * ND; t += ET) {
       const int b = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
       S wa = c.ds[0][b] * w.A[0][r][col];
 #pragma unroll
       for (int d = 1; d < DIM; ++d) wa = madd(c.ds[d][b], w.A[d][r][col], wa);
-      const S Dv = w.D[r][col], sv = s0(c, r, col), shb = c.sh[b];
+      const S Dv = w.D[r][col], shb = c.sh[b];
+      const S sv = (r == L::iT && col >= 1 && col <= DIM) ? c.rho * grav[(col - 1) % DIM] : S(0);
       w.WA[b][r][col] = wa;
       w.RM[b][r][col] = Dv * shb * idt + wa - sv * shb;
-      if constexpr (WANT_M) {
-        w.X[b][r][col] = shb * (Dv * idt - sv) - wa;
-        S gb[DIM];
-        S gbv = S(0);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          gb[d] = c.ds[d][b];
-          gbv = madd(gb[d], c.v[d], gbv);
-        }
-#pragma unroll
-        for (int l = 0; l < DIM; ++l)
-          w.KD[b][l][r][col] = madd(c.nu * gb[l], Dv, kd_entry<DIM, NC, S>(c, gb, gbv, l, r, col));
+      if constexpr (WANT_M) w.X[b][r][col] = shb * (Dv * idt - sv) - wa;
+    }
+    if constexpr (WANT_M && AFF) {
+      for (int t = gl; t < ND * ND; t += ET) {
+        const int r = t / ND, col = t % ND;
+        w.Dnu[r][col] = madd(c.JxW * c.nu, w.D[r][col], w.Dnu[r][col]);
       }
     }
     elem_sync<WPE>(ec);
@@ -911,7 +995,10 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
       const S shb = c.sh[b];
       S x = S(0);
 #pragma unroll
-      for (int m = 0; m < ND; ++m) x = madd(w.WA[b][r][m] - shb * s0(c, r, m), c.tau[m][col], x);
+      for (int m = 0; m < ND; ++m) {
+        const S sv = (r == L::iT && m >= 1 && m <= DIM) ? c.rho * grav[(m - 1) % DIM] : S(0);
+        x = madd(w.WA[b][r][m] - shb * sv, c.tau[m][col], x);
+      }
       w.FPT[b][r][col] = x;
     }
     elem_sync<WPE>(ec);
@@ -936,18 +1023,52 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
             for (int j = 0; j < ND; ++j) tt[i][j] = madd(fr[i], rr[j], tt[i][j]);
         }
         const S sa = c.sh[pa];
-        S dsa[DIM];
-#pragma unroll
-        for (int l = 0; l < DIM; ++l) dsa[l] = c.ds[l][pa];
 #pragma unroll
         for (int i = 0; i < RH; ++i)
 #pragma unroll
-          for (int j = 0; j < ND; ++j) {
-            S x = madd(sa, w.X[pb][r0 + i][j], tt[i][j]);
+          for (int j = 0; j < ND; ++j) tt[i][j] = madd(sa, w.X[pb][r0 + i][j], tt[i][j]);
+        if constexpr (!AFF) {
+          // viscous, diffusive and dc terms at this point
+          S gb[DIM], ga[DIM];
 #pragma unroll
-            for (int l = 0; l < DIM; ++l) x = madd(dsa[l], w.KD[pb][l][r0 + i][j], x);
-            acc[i][j] = madd(c.JxW, x, acc[i][j]);
-          }
+          for (int d = 0; d < DIM; ++d) { gb[d] = c.ds[d][pb]; ga[d] = c.ds[d][pa]; }
+          KSums<DIM, NC, S> ks;
+          ks.mu = c.mu; ks.lambda = c.lambda; ks.kappa = c.kappa;
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) { ks.muv[d] = c.mu * c.v[d]; ks.lamv[d] = c.lambda * c.v[d]; }
+#pragma unroll
+          for (int y = 0; y < L::NYA; ++y) { ks.rhoD[y] = c.rhoD[y]; ks.rhoDH[y] = c.rhoDH[y]; }
+          add_viscous_tile<DIM, NC, RH, ND, S>(tt, r0, ks, gb, ga);
+          S gg = gb[0] * ga[0];
+#pragma unroll
+          for (int d = 1; d < DIM; ++d) gg = madd(gb[d], ga[d], gg);
+          const S gn = gg * c.nu;
+#pragma unroll
+          for (int i = 0; i < RH; ++i)
+#pragma unroll
+            for (int j = 0; j < ND; ++j)
+              if (r0 + i < ND) tt[i][j] = madd(gn, w.D[r0 + i][j], tt[i][j]);
+        }
+#pragma unroll
+        for (int i = 0; i < RH; ++i)
+#pragma unroll
+          for (int j = 0; j < ND; ++j) acc[i][j] = madd(c.JxW, tt[i][j], acc[i][j]);
+      }
+      if constexpr (AFF) {
+        const S jx = c.JxW;
+        ksum.mu = madd(jx, c.mu, ksum.mu);
+        ksum.lambda = madd(jx, c.lambda, ksum.lambda);
+        ksum.kappa = madd(jx, c.kappa, ksum.kappa);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          ksum.muv[d] = madd(jx * c.mu, c.v[d], ksum.muv[d]);
+          ksum.lamv[d] = madd(jx * c.lambda, c.v[d], ksum.lamv[d]);
+        }
+#pragma unroll
+        for (int y = 0; y < L::NYA; ++y) {
+          ksum.rhoD[y] = madd(jx, c.rhoD[y], ksum.rhoD[y]);
+          ksum.rhoDH[y] = madd(jx, c.rhoDH[y], ksum.rhoDH[y]);
+        }
       }
     }
     if (gl < N) {
@@ -960,6 +1081,23 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
       racc = madd(c.JxW, x, racc);
     }
     elem_sync<WPE>(ec);
+  }
+  if constexpr (WANT_M && AFF) {
+    // viscous/diffusive and dc terms of a simplex, from the point sums
+    if (has_pair) {
+      const QP<DIM, NEN, NC, S>& c = E.qp[0];
+      S gb[DIM], ga[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) { gb[d] = c.ds[d][pb]; ga[d] = c.ds[d][pa]; }
+      add_viscous_tile<DIM, NC, RH, ND, S>(acc, r0, ksum, gb, ga);
+      S gg = gb[0] * ga[0];
+#pragma unroll
+      for (int d = 1; d < DIM; ++d) gg = madd(gb[d], ga[d], gg);
+#pragma unroll
+      for (int i = 0; i < RH; ++i)
+#pragma unroll
+        for (int j = 0; j < ND; ++j) acc[i][j] = madd(gg, w.Dnu[r0 + i][j], acc[i][j]);
+    }
   }
   // Dirichlet rows (scatter.hpp:62-78) and scatter (scatter.hpp:96-97)
   double avg = 0.0;
@@ -1004,7 +1142,7 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
   if (gl < N) {
     const int b = gl / ND, jb = gl % ND;
     const bool blk = (E.blocked[b] >> jb) & 1u;
-    const double rv = blk ? avg * 0.0 : -(double)racc;
+    const double rv = blk ? avg * 0.0 : -widen(racc);
     add_to(k.rhs + (long long)E.nodes[b] * ND + jb, rv, mode);
   }
   if constexpr (WANT_M) {
@@ -1022,8 +1160,7 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
 }
 
 // ---------------------------------------------------------------------------
-// Boundary pass (fluid_2d.hpp:209-245, 341-364, 610-868), one warp per listed
-// boundary element, FP64.  Each lane evaluates the point physics redundantly.
+// Boundary pass helpers (fluid_2d.hpp:610-868): boundary-modified A_k and K_kl.
 
 // Entry of the boundary-modified K_kl (fluid_2d.hpp:819-867).
 template <int DIM>
