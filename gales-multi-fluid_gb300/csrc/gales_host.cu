@@ -690,8 +690,17 @@ KParams base_params(gales_asm* h, double dt) {
     d.kind = q.kind;
     d.rho = q.rho; d.mu = q.mu; d.cp = q.cp; d.cv = q.cv; d.kappa = q.kappa;
     d.alpha = q.alpha; d.beta = q.beta; d.R = q.R; d.gamma = q.gamma; d.D = q.chemical_diffusivity;
+    // ratios used by the mixed form's EOS
+    d.inv_rho = q.kind == GALES_CH_CUSTOM ? 1.0 / q.rho : 0.0;
+    d.beta_over_rho = q.kind == GALES_CH_CUSTOM ? q.beta / q.rho : 0.0;
+    d.alpha_over_rho = q.kind == GALES_CH_CUSTOM ? q.alpha / q.rho : 0.0;
+    d.cv_shift = (q.kind == GALES_CH_CUSTOM && q.beta != 0.0) ? q.alpha * q.alpha / (q.rho * q.beta) : 0.0;
+    d.inv_R = q.kind == GALES_CH_IDEAL_GAS ? 1.0 / q.R : 0.0;
+    d.R_over_gamma = q.kind == GALES_CH_IDEAL_GAS ? q.R / q.gamma : 0.0;
+    d.inv_D = 1.0 / q.chemical_diffusivity;
   }
   k.dt = dt;
+  k.inv_dt = 1.0 / dt;
   k.dc_sharp = h->setup.dc_sharp;
   k.dc_scale = h->setup.dc_scale_fact;
   for (int d = 0; d < 3; ++d) k.gravity[d] = h->setup.gravity[d];

@@ -56,6 +56,7 @@ struct KParams {
   const double* P;
   double* vals;
   double* rhs;
+  double inv_dt;
   unsigned int* status;
   unsigned long long* first_bad;
   int32_t scatter_mode;        // 0 atomics, 1 plain read-modify-write (coloured batches)
@@ -368,8 +369,20 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
     const double* pi = k.P + (long long)nodes[i] * ND;
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
-      Pq[j] += sh[i] * __ldg(pi + j);
-      Iq[j] += sh[i] * Ie[i][j];
+      if constexpr (FORM == GALES_FORM_FP64) {
+        Pq[j] += sh[i] * __ldg(pi + j);
+        Iq[j] += sh[i] * Ie[i][j];
+      } else {
+        // the velocity keeps the reference's operations (it enters compute_h); P and I
+        // are interpolated alike so that P == I gives U == U_P exactly
+        if (j >= 1 && j <= DIM) {
+          Pq[j] += sh[i] * __ldg(pi + j);
+          Iq[j] += sh[i] * Ie[i][j];
+        } else {
+          Pq[j] = fma(sh[i], __ldg(pi + j), Pq[j]);
+          Iq[j] = fma(sh[i], Ie[i][j], Iq[j]);
+        }
+      }
     }
   }
   // gradients: FP64 in the FP64 form; FP32 of nodal differences in the mixed form
@@ -394,9 +407,9 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
     for (int i = 1; i < NEN; ++i)
 #pragma unroll
       for (int j = 0; j < ND; ++j) {
-        const float dif = float(Ie[i][j] - Ie[0][j]);
+        const float dif = narrow_rn(Ie[i][j] - Ie[0][j]);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) dI[d][j] = fmaf(float(q.ds[d][i]), dif, dI[d][j]);
+        for (int d = 0; d < DIM; ++d) dI[d][j] = fmaf(narrow_rn(q.ds[d][i]), dif, dI[d][j]);
       }
   }
   // velocity gradient in FP64 with the reference's operations (input of compute_h)
@@ -418,15 +431,21 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
   double p, v[DIM], T, Y[NC];
   assign<DIM, NC>(Pq, p, v, T, Y);
   double rhoP, cvP;
-  mixture_rho_cv<NC>(k.ch, p, T, Y, rhoP, cvP);
+  if constexpr (FORM == GALES_FORM_FP64) mixture_rho_cv<NC>(k.ch, p, T, Y, rhoP, cvP);
+  else mixture_rho_cv_fast<NC>(k.ch, p, T, Y, rhoP, cvP);
   double UP[ND];
   conservative<DIM, NC>(rhoP, cvP, v, T, Y, UP);
   // current iterate
   assign<DIM, NC>(Iq, p, v, T, Y);
   Props<NC> pr;
-  mixture<NC>(k.ch, p, T, Y, pr);
   Coef<DIM, NC> c;
-  make_coef<DIM, NC>(pr, p, v, T, Y, c);
+  if constexpr (FORM == GALES_FORM_FP64) {
+    mixture<NC>(k.ch, p, T, Y, pr);
+    make_coef<DIM, NC>(pr, p, v, T, Y, c);
+  } else {
+    mixture_fast<NC>(k.ch, p, T, Y, pr);
+    make_coef_fast<DIM, NC>(pr, p, v, T, Y, c);
+  }
   double U[ND];
   conservative<DIM, NC>(pr.rho, pr.cv, v, T, Y, U);
   const double dt = k.dt;
@@ -443,7 +462,10 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
     Sv[L::iT] = pr.rho * (gv);
   }
 #pragma unroll
-  for (int j = 0; j < ND; ++j) out.rv[j] = S((U[j] - UP[j]) / dt - Sv[j]);
+  for (int j = 0; j < ND; ++j) {
+    if constexpr (FORM == GALES_FORM_FP64) out.rv[j] = (U[j] - UP[j]) / dt - Sv[j];
+    else out.rv[j] = to_s<S>(fma(U[j] - UP[j], k.inv_dt, -Sv[j]));
+  }
   // tau (fluid_2d.hpp:877-1022)
   double tau[ND][ND];
 #pragma unroll
@@ -470,6 +492,19 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       tau[L::iT][L::iT] = fmin(use, rho * h * h * cv / (kappa * 12));
 #pragma unroll
       for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = fmin(use, h * h / (pr.D_c[i] * 12));
+      nondiag = true;
+    } else if (FORM == GALES_FORM_MIXED && k.tau == GALES_TAU_NON_DIAG_COMP_2019) {
+      // the same parameters with reciprocals (mixed form)
+      const double hv = h * (0.5 / (v_nrm + cs) + 0.5 / v_nrm);
+      const double use = k.steady ? hv : fmin(dt * 0.5, hv);
+      const double hh12 = h * h * (1.0 / 12.0);
+      tau[0][0] = use;
+      const double tm = fmin(use, hh12 * rho / mu);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) tau[1 + d][1 + d] = tm;
+      tau[L::iT][L::iT] = fmin(use, hh12 * rho * cv / kappa);
+#pragma unroll
+      for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = fmin(use, hh12 * k.ch[i].inv_D);
       nondiag = true;
     } else if (k.tau == GALES_TAU_NON_DIAG_COMP_2019) {
       double use;
@@ -568,11 +603,14 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
   else cr = narrow<DIM, NC>(c);
   R SvR[ND], Res[ND], AdI[ND], t[ND];
 #pragma unroll
-  for (int j = 0; j < ND; ++j) SvR[j] = R(Sv[j]);
+  for (int j = 0; j < ND; ++j) SvR[j] = to_s<R>(Sv[j]);
   {
     R dd[ND];
 #pragma unroll
-    for (int j = 0; j < ND; ++j) dd[j] = R((Iq[j] - Pq[j]) / dt);
+    for (int j = 0; j < ND; ++j) {
+      if constexpr (FORM == GALES_FORM_FP64) dd[j] = (Iq[j] - Pq[j]) / dt;
+      else dd[j] = narrow_rn((Iq[j] - Pq[j]) * k.inv_dt);
+    }
     dudy_mv<DIM, NC, R>(cr, dd, Res);
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
@@ -603,9 +641,9 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       R h = R(0);
 #pragma unroll
       for (int i = 0; i < NEN; ++i) {
-        R tt = Jv[0] * R(q.ds[0][i]);
+        R tt = Jv[0] * to_s<R>(q.ds[0][i]);
 #pragma unroll
-        for (int d = 1; d < DIM; ++d) tt = tt + Jv[d] * R(q.ds[d][i]);
+        for (int d = 1; d < DIM; ++d) tt = tt + Jv[d] * to_s<R>(q.ds[d][i]);
         h += fabs(tt);
       }
       if (h > R(kEps)) {
@@ -613,8 +651,9 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
         R Zn = R(0), Un = R(0), use1 = R(0);
 #pragma unroll
         for (int j = 0; j < ND; ++j) {
-          const R z = R(k.u_ref_inv[j]) * (AdI[j] - SvR[j]);
-          const R u = R(k.u_ref_inv[j]) * R(U[j]);
+          const R ui = to_s<R>(k.u_ref_inv[j]);
+          const R z = ui * (AdI[j] - SvR[j]);
+          const R u = ui * to_s<R>(U[j]);
           Zn += z * z;
           Un += u * u;
         }
@@ -627,7 +666,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
             R n2 = R(0);
 #pragma unroll
             for (int j = 0; j < ND; ++j) {
-              const R u = R(k.u_ref_inv[j]) * dU[d][j];
+              const R u = to_s<R>(k.u_ref_inv[j]) * dU[d][j];
               n2 += u * u;
             }
             const R n = sqrt(n2);
@@ -637,7 +676,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
         if (a == 1.0) nu = Zn * h * (R(1) / sqrt(use1));
         else if (a == 2.0) nu = Zn * h * h / Un;
         else if (a == 1.5) nu = Zn * h * ((R(1) / sqrt(use1)) + h / Un) / R(2);
-        nu = R(k.dc_scale) * nu;
+        nu = to_s<R>(k.dc_scale) * nu;
       }
     }
   }
@@ -668,29 +707,29 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
   // write the record
 #pragma unroll
   for (int i = 0; i < NEN; ++i) {
-    out.sh[i] = S(sh[i]);
+    out.sh[i] = to_s<S>(sh[i]);
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) out.ds[d][i] = S(q.ds[d][i]);
+    for (int d = 0; d < DIM; ++d) out.ds[d][i] = to_s<S>(q.ds[d][i]);
   }
-  out.JxW = S(JxW);
-  out.p = S(p);
+  out.JxW = to_s<S>(JxW);
+  out.p = to_s<S>(p);
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) out.v[d] = S(v[d]);
+  for (int d = 0; d < DIM; ++d) out.v[d] = to_s<S>(v[d]);
 #pragma unroll
-  for (int i = 0; i < NC; ++i) out.Y[i] = S(Y[i]);
-  out.rho = S(c.rho); out.E = S(c.E);
-  out.drho_dp = S(c.drho_dp); out.drho_dT = S(c.drho_dT);
-  out.de_dp = S(c.de_dp); out.de_dT = S(c.de_dT);
-  out.mu = S(c.mu); out.lambda = S(c.lambda); out.kappa = S(c.kappa);
+  for (int i = 0; i < NC; ++i) out.Y[i] = to_s<S>(Y[i]);
+  out.rho = to_s<S>(c.rho); out.E = to_s<S>(c.E);
+  out.drho_dp = to_s<S>(c.drho_dp); out.drho_dT = to_s<S>(c.drho_dT);
+  out.de_dp = to_s<S>(c.de_dp); out.de_dT = to_s<S>(c.de_dT);
+  out.mu = to_s<S>(c.mu); out.lambda = to_s<S>(c.lambda); out.kappa = to_s<S>(c.kappa);
 #pragma unroll
   for (int i = 0; i < L::NYA; ++i) {
-    out.drho_dY[i] = S(c.drho_dY[i]); out.dE_dY[i] = S(c.dE_dY[i]);
-    out.rhoD[i] = S(c.rhoD[i]); out.rhoDH[i] = S(c.rhoDH[i]);
+    out.drho_dY[i] = to_s<S>(c.drho_dY[i]); out.dE_dY[i] = to_s<S>(c.dE_dY[i]);
+    out.rhoD[i] = to_s<S>(c.rhoD[i]); out.rhoDH[i] = to_s<S>(c.rhoDH[i]);
   }
 #pragma unroll
   for (int r = 0; r < ND; ++r)
 #pragma unroll
-    for (int cc = 0; cc < ND; ++cc) out.tau[r][cc] = S(tau[r][cc]);
+    for (int cc = 0; cc < ND; ++cc) out.tau[r][cc] = to_s<S>(tau[r][cc]);
   out.nu = S(nu);
 #pragma unroll
   for (int j = 0; j < ND; ++j) out.res[j] = S(Res[j]);
@@ -734,6 +773,7 @@ __device__ __forceinline__ S kd_entry(const C& c, const S* gb, S gbv, int l, int
 __device__ __forceinline__ double widen(float f) {
   const unsigned int u = __float_as_uint(f);
   const unsigned int ex = (u >> 23) & 0xffu;
+  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(u >> 31) << 63));
   if (ex == 0u || ex == 0xffu) return (double)f;
   const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
   const unsigned long long e64 = (unsigned long long)(ex + (1023u - 127u)) << 52;
@@ -1105,7 +1145,9 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
     if (has_pair && pb == pa) {
 #pragma unroll
       for (int i = 0; i < RH; ++i)
-        if (r0 + i < ND) E.diag[pb * ND + r0 + i] = widen(acc[i][r0 + i]);
+#pragma unroll
+        for (int j = 0; j < ND; ++j)
+          if (j == r0 + i) E.diag[pb * ND + j] = widen(acc[i][j]);
     }
     elem_sync<WPE>(ec);
     // avg_val = (1 + trace)/n (scatter.hpp:65-68); trace summed by a warp tree
@@ -1148,7 +1190,7 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
   if constexpr (WANT_M) {
     for (int t = gl; t < NT; t += ET) {
       const double val = E.u.stage[t];
-      if (val != 0.0) {
+      if ((__double_as_longlong(val) << 1) != 0) {
         const int row = t / N, colx = t % N;
         const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
         const int64_t off = E.rowbase[b] + (int64_t)jb * E.rowlen[b] +

@@ -33,7 +33,30 @@ struct DevChem {
   int32_t kind;
   int32_t pad;
   double rho, mu, cp, cv, kappa, alpha, beta, R, gamma, D;
+  // reciprocals and ratios for the mixed form's EOS (filled on the host)
+  double inv_rho, beta_over_rho, alpha_over_rho, cv_shift, inv_R, R_over_gamma, inv_D;
 };
+
+// Round-to-nearest-even narrowing of binary64 to binary32 with integer operations
+// (52-bit mantissa cut to 23 bits, ties to even, carry into the exponent).  Values
+// whose binary32 result is zero, subnormal, infinite or NaN take the hardware path.
+__device__ __forceinline__ float narrow_rn(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  const unsigned int hi = (unsigned int)(u >> 32);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if (e <= 0 || e >= 255) return (float)d;
+  const unsigned int m = (unsigned int)((u >> 29) & 0x7fffffu);
+  const unsigned int rest = (unsigned int)(u & 0x1fffffffu);
+  unsigned int bits = (hi & 0x80000000u) | ((unsigned int)e << 23) | m;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
+  return __uint_as_float(bits);
+}
+
+template <typename S>
+__device__ __forceinline__ S to_s(double d) {
+  if constexpr (sizeof(S) == 4) return narrow_rn(d);
+  else return d;
+}
 
 template <int DIM, int NC>
 struct Layout {
@@ -49,6 +72,7 @@ template <int NC>
 struct Props {
   double rho, mu, cp, cv, kappa, c, alpha, beta;
   double rho_c[NC], e_c[NC], D_c[NC];
+  double irho_c[NC];  // 1/rho_c (mixed form only)
 };
 
 template <int NC>
@@ -95,6 +119,66 @@ __device__ __forceinline__ void mixture(const DevChem* ch, double p, double T, c
   o.alpha = alpha; o.beta = beta;
 }
 
+// The same mixture in FP64 for the mixed form, with per-chemical reciprocals and
+// ratios precomputed so that a point costs three divisions instead of about a dozen.
+template <int NC>
+__device__ __forceinline__ void mixture_fast(const DevChem* ch, double p, double T, const double* Y,
+                                             Props<NC>& o) {
+  const double ip = 1.0 / p, iT = 1.0 / T;
+  double irho = 0.0, mu = 0.0, cp = 0.0, cv = 0.0, kappa = 0.0, c2 = 0.0, al = 0.0, be = 0.0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const DevChem& q = ch[c];
+    double ir, v;
+    if (q.kind == GALES_CH_CUSTOM) {
+      ir = q.inv_rho;
+      v = fma(-T, q.cv_shift, q.cp);
+      c2 = fma(Y[c], q.beta == 0.0 ? 1.e-40 * ir * ir : q.beta_over_rho, c2);
+      al = fma(Y[c], q.alpha_over_rho, al);
+      be = fma(Y[c], q.beta_over_rho, be);
+    } else {
+      ir = q.R * T * ip;
+      v = q.cv;
+      c2 = fma(Y[c], q.R_over_gamma * T * ip * ip, c2);
+      al = fma(Y[c] * iT, ir, al);
+      be = fma(Y[c] * ip, ir, be);
+    }
+    o.irho_c[c] = ir;
+    irho = fma(Y[c], ir, irho);
+    mu = fma(Y[c], q.mu, mu);
+    cp = fma(Y[c], q.cp, cp);
+    cv = fma(Y[c], v, cv);
+    kappa = fma(Y[c], q.kappa, kappa);
+    o.e_c[c] = v * T;
+    o.D_c[c] = q.D;
+  }
+  const double rho = 1.0 / irho;
+  o.rho = rho; o.mu = mu; o.cp = cp; o.cv = cv; o.kappa = kappa;
+  o.c = sqrt(1.0 / c2) * irho;
+  o.alpha = rho * al;
+  o.beta = rho * be;
+}
+
+template <int NC>
+__device__ __forceinline__ void mixture_rho_cv_fast(const DevChem* ch, double p, double T, const double* Y,
+                                                    double& rho_out, double& cv_out) {
+  const double ip = 1.0 / p;
+  double irho = 0.0, cv = 0.0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const DevChem& q = ch[c];
+    if (q.kind == GALES_CH_CUSTOM) {
+      irho = fma(Y[c], q.inv_rho, irho);
+      cv = fma(Y[c], fma(-T, q.cv_shift, q.cp), cv);
+    } else {
+      irho = fma(Y[c], q.R * T * ip, irho);
+      cv = fma(Y[c], q.cv, cv);
+    }
+  }
+  rho_out = 1.0 / irho;
+  cv_out = cv;
+}
+
 // Only rho and cv (what U(P) needs); same operations as mixture().
 template <int NC>
 __device__ __forceinline__ void mixture_rho_cv(const DevChem* ch, double p, double T,
@@ -132,18 +216,18 @@ template <int DIM, int NC>
 __device__ __forceinline__ Coef<DIM, NC, float> narrow(const Coef<DIM, NC, double>& c) {
   using L = Layout<DIM, NC>;
   Coef<DIM, NC, float> f;
-  f.p = float(c.p); f.T_ = float(c.T_);
+  f.p = narrow_rn(c.p); f.T_ = narrow_rn(c.T_);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) f.v[k] = float(c.v[k]);
+  for (int k = 0; k < DIM; ++k) f.v[k] = narrow_rn(c.v[k]);
 #pragma unroll
-  for (int i = 0; i < NC; ++i) f.Y[i] = float(c.Y[i]);
-  f.rho = float(c.rho); f.E = float(c.E); f.drho_dp = float(c.drho_dp); f.drho_dT = float(c.drho_dT);
-  f.de_dp = float(c.de_dp); f.de_dT = float(c.de_dT); f.mu = float(c.mu); f.lambda = float(c.lambda);
-  f.kappa = float(c.kappa); f.c = float(c.c); f.cv = float(c.cv);
+  for (int i = 0; i < NC; ++i) f.Y[i] = narrow_rn(c.Y[i]);
+  f.rho = narrow_rn(c.rho); f.E = narrow_rn(c.E); f.drho_dp = narrow_rn(c.drho_dp); f.drho_dT = narrow_rn(c.drho_dT);
+  f.de_dp = narrow_rn(c.de_dp); f.de_dT = narrow_rn(c.de_dT); f.mu = narrow_rn(c.mu); f.lambda = narrow_rn(c.lambda);
+  f.kappa = narrow_rn(c.kappa); f.c = narrow_rn(c.c); f.cv = narrow_rn(c.cv);
 #pragma unroll
   for (int i = 0; i < L::NYA; ++i) {
-    f.drho_dY[i] = float(c.drho_dY[i]); f.dE_dY[i] = float(c.dE_dY[i]);
-    f.rhoD[i] = float(c.rhoD[i]); f.rhoDH[i] = float(c.rhoDH[i]);
+    f.drho_dY[i] = narrow_rn(c.drho_dY[i]); f.dE_dY[i] = narrow_rn(c.dE_dY[i]);
+    f.rhoD[i] = narrow_rn(c.rhoD[i]); f.rhoDH[i] = narrow_rn(c.rhoDH[i]);
   }
   return f;
 }
@@ -214,6 +298,37 @@ __device__ __forceinline__ void make_coef(const Props<NC>& pr, double p, const d
     const double H = pr.e_c[i] + p / pr.rho_c[i];
     c.rhoD[i] = rho * pr.D_c[i];
     c.rhoDH[i] = rho * pr.D_c[i] * H;
+  }
+}
+
+// make_coef for the mixed form, from mixture_fast's reciprocals.
+template <int DIM, int NC>
+__device__ __forceinline__ void make_coef_fast(const Props<NC>& pr, double p, const double* v, double T,
+                                               const double* Y, Coef<DIM, NC>& c) {
+  c.p = p; c.T_ = T;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) c.v[k] = v[k];
+#pragma unroll
+  for (int i = 0; i < NC; ++i) c.Y[i] = Y[i];
+  const double rho = pr.rho, irho = 1.0 / rho;
+  c.rho = rho;
+  c.cv = pr.cv;
+  c.E = fma(pr.cv, T, 0.5 * vsq<DIM>(v));
+  c.drho_dp = rho * pr.beta;
+  c.drho_dT = -rho * pr.alpha;
+  c.de_dp = fma(pr.beta, p, -pr.alpha * T) * irho;
+  c.de_dT = fma(-p * pr.alpha, irho, pr.cp);
+  c.mu = pr.mu;
+  c.lambda = (-2.0 / 3.0) * pr.mu;
+  c.kappa = pr.kappa;
+  c.c = pr.c;
+#pragma unroll
+  for (int i = 0; i < NC - 1; ++i) {
+    c.drho_dY[i] = -rho * rho * (pr.irho_c[i] - pr.irho_c[NC - 1]);
+    c.dE_dY[i] = pr.e_c[i] - pr.e_c[NC - 1];
+    const double H = fma(p, pr.irho_c[i], pr.e_c[i]);
+    c.rhoD[i] = rho * pr.D_c[i];
+    c.rhoDH[i] = c.rhoD[i] * H;
   }
 }
 
@@ -499,19 +614,19 @@ __device__ __forceinline__ void dydu_closed(const Coef<DIM, NC>& c, double (&X)[
     double xv[DIM], xy[L::NYA];
     double R1 = s, R2 = 0.0;
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) xv[j] = (((col == 1 + j) ? 1.0 : 0.0) - c.v[j] * s) * irho;
+    for (int j = 0; j < DIM; ++j) xv[j] = fma(-c.v[j], s, (col == 1 + j) ? 1.0 : 0.0) * irho;
 #pragma unroll
-    for (int i = 0; i < NC - 1; ++i) xy[i] = (((col == L::iY + i) ? 1.0 : 0.0) - c.Y[i] * s) * irho;
-    R2 = (((col == L::iT) ? 1.0 : 0.0) - c.E * s) * irho;
+    for (int i = 0; i < NC - 1; ++i) xy[i] = fma(-c.Y[i], s, (col == L::iY + i) ? 1.0 : 0.0) * irho;
+    R2 = fma(-c.E, s, (col == L::iT) ? 1.0 : 0.0) * irho;
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) R2 -= c.v[j] * xv[j];
+    for (int j = 0; j < DIM; ++j) R2 = fma(-c.v[j], xv[j], R2);
 #pragma unroll
     for (int i = 0; i < NC - 1; ++i) {
-      R1 -= c.drho_dY[i] * xy[i];
-      R2 -= c.dE_dY[i] * xy[i];
+      R1 = fma(-c.drho_dY[i], xy[i], R1);
+      R2 = fma(-c.dE_dY[i], xy[i], R2);
     }
-    X[0][col] = (R1 * c.de_dT - c.drho_dT * R2) * idet;
-    X[L::iT][col] = (c.drho_dp * R2 - c.de_dp * R1) * idet;
+    X[0][col] = fma(R1, c.de_dT, -c.drho_dT * R2) * idet;
+    X[L::iT][col] = fma(c.drho_dp, R2, -c.de_dp * R1) * idet;
 #pragma unroll
     for (int j = 0; j < DIM; ++j) X[1 + j][col] = xv[j];
 #pragma unroll
