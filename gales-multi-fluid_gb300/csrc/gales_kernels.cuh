@@ -1,17 +1,17 @@
 // Element assembly kernels for fluid_mc (interior and boundary passes).
 //
-// Interior kernel, one CTA per batch of EB elements (one warp per element):
-//   point phase  - one thread per (element, quadrature point), FP64: geometry
-//                  (quad.hpp:196-231, 523-571), interpolation (quad.hpp:817-885),
-//                  mixture EOS at P and I (fluid_2d.hpp:179-195), flux scalars
-//                  (fluid_2d.hpp:391-603), tau (fluid_2d.hpp:877-1022) and the dc
-//                  viscosity (fluid_2d.hpp:1027-1065).  Results go to shared memory
-//                  in the form's arithmetic type S.
-//   matrix phase - one warp per element, lanes over the (nen*nd)^2 block entries:
-//                  Galerkin, least-squares and dc terms of RM_i (fluid_2d.hpp:251-333)
-//                  accumulated in registers over the quadrature points, then the
-//                  Dirichlet row replacement of scatter::execute (scatter.hpp:62-78)
-//                  and FP64 atomic adds into the CSR values and rhs (scatter.hpp:96-97).
+// Interior pass, two kernels per chunk of elements:
+//   point_kernel  - one thread per (element, quadrature point): interpolation
+//                   (quad.hpp:817-885), mixture EOS at P and I (fluid_2d.hpp:179-195),
+//                   flux scalars (fluid_2d.hpp:391-603), tau (fluid_2d.hpp:877-1022)
+//                   and the dc viscosity (fluid_2d.hpp:1027-1065), written as a point
+//                   record in the form's arithmetic type S.
+//   matrix_kernel - one warp per element (more for hexahedra), one lane per row of
+//                   the element block: Galerkin, least-squares and dc terms of RM_i
+//                   (fluid_2d.hpp:251-333) accumulated in registers over the points,
+//                   then the Dirichlet row replacement of scatter::execute
+//                   (scatter.hpp:62-78) and FP64 adds into the CSR values and rhs
+//                   (scatter.hpp:96-97).
 // Boundary kernel, one warp per boundary element: execute_b/RM_b
 // (fluid_2d.hpp:209-245, 341-364, 610-868) and its own scatter pass
 // (fluid_assembly.hpp:57-63), all in FP64.
@@ -797,63 +797,66 @@ __global__ void __launch_bounds__(128) point_kernel(const KParams k, QP<DIM, NEN
   point_phase<DIM, NEN, NC, NQ, FORM, S>(k, e, iq, out[li * NQ + iq]);
 }
 
-// Interior pass, stage 2: element matrices.  Lanes are mapped to (test node b,
-// trial node a, half of the rows): each lane owns an RH x ND register tile of the
-// (b, a) block and accumulates, per quadrature point (fluid_2d.hpp:264-331),
+// Interior pass, stage 2: element matrices.  Lane (b, r, g) owns row (b, r) of the
+// element block (test node b, dof r) for the trial nodes of group g, and builds it
+// per quadrature point (fluid_2d.hpp:264-331) from
 //   JxW [ FPT_b RM_a + N_a X_b ]   with
 //   WA_b  = sum_k dN_b/dx_k A_k
 //   FPT_b = (WA_b - N_b S0) tau                       least-squares weight
 //   RM_a  = N_a DUDY/dt + WA_a - N_a S0               least-squares operator
 //   X_b   = N_b (DUDY/dt - S0) - WA_b                 Galerkin mass, source, advection
 // plus the viscous/diffusive and dc terms sum_kl dN_b/dx_k K'_kl dN_a/dx_l with
-// K'_kl = K_kl + nu d_kl DUDY.  K'_kl is linear in a few point scalars (mu, lambda,
-// mu v, lambda v, kappa, rho D_i, rho D_i H_i) and in nu DUDY, so it is applied in
-// closed form: per point for non-affine elements, once from JxW-weighted sums for
-// simplices (their shape gradients do not depend on the point).
-// DUDY and A_k are built branch-free from their structure: DUDY = w r0^T + rho M
-// (w = (1, v, E, Y), r0 its first row, M zero but for the velocity and mass-fraction
-// diagonal and the energy row), and A_k = v_k DUDY + (U + p e_E) e_{v_k}^T +
-// (e_{v_k} + v_k e_E) e_p^T (fluid_2d.hpp:407-524).
+// K'_kl = K_kl + nu d_kl DUDY.
+// None of the nd x nd matrices is formed.  DUDY = w r0^T + rho M (w = (1, v, E, Y),
+// r0 its first row, M zero but for the velocity and mass-fraction diagonal and the
+// energy row mE), A_k = v_k DUDY + u' e_{v_k}^T + (e_{v_k} + v_k e_E) e_p^T with
+// u' = U + p e_E, and S0 = e_E sigma^T with sigma = rho g on the velocity columns
+// (fluid_2d.hpp:407-575).  With s_b = dN_b/dx . v these give, row r of the lane,
+//   FPT_b[r]   = s_b (w_r z + rho Mtau[r]) + u'_r t_b + kappa_br tau[0] - N_b [r=E] rho t_g
+//   (FPT_b RM_a)[r] = alpha_a (FPT_b DUDY)[r] + (FPT_b[r].u') gamma_a
+//                     + (FPT_b[r].kappa_a) e_p - N_a FPT_b[r][E] sigma
+//   X_b[r]     = beta_b DUDY[r] - u'_r gamma_b - kappa_br e_p - N_b [r=E] sigma
+// where z = r0^T tau, Mtau = M tau, t_b = sum_k dN_b/dx_k tau[v_k], t_g = sum_k g_k
+// tau[v_k], gamma_a = dN_a/dx on the velocity columns, kappa_a = dN_a/dx on the
+// velocity rows + s_a e_E, alpha_a = N_a/dt + s_a, beta_b = N_b/dt - s_b.  K'_kl is
+// applied in closed form from a few point scalars (mu, lambda, mu v, lambda v, kappa,
+// rho D_i, rho D_i H_i) and nu DUDY: per point for non-affine elements, once from
+// JxW-weighted sums for simplices (their shape gradients do not depend on the point).
 template <int DIM, int NEN, int NC>
 struct MatShape {
   static constexpr int ND = Layout<DIM, NC>::ND;
-  static constexpr int NDP = (ND + 1) & ~1;
-  static constexpr int RH = NDP / 2;
-  static constexpr int NP = NEN * NEN;
-  static constexpr int WPE = (2 * NP + 31) / 32;       // warps per element
-  static constexpr int EPC = WPE == 1 ? 4 : 1;        // elements per CTA
-  static constexpr int N = NEN * ND;
+  static constexpr int N = NEN * ND;                  // rows (and columns) of the block
+  static constexpr int AG = NEN >= 8 ? 2 : 1;          // trial-node groups per row
+  static constexpr int NA = NEN / AG;                  // trial nodes per lane
+  static constexpr int LANES = N * AG;
+  static constexpr int WPE = (LANES + 31) / 32;        // warps per element
+  static constexpr int EPC = WPE == 1 ? 4 : (WPE == 2 ? 2 : 1);  // elements per CTA
+  static constexpr int ET = WPE * 32;                  // threads per element
+  static constexpr int CTA = EPC * ET;
+  static constexpr int NS = N + 1;                     // stage row stride (doubles)
   static constexpr bool AFFINE = NEN == DIM + 1;
 };
 
-// Point scalars entering K'_kl, JxW-weighted when summed over an element's points.
-template <int DIM, int NC, typename S>
-struct KSums {
-  using L = Layout<DIM, NC>;
-  S mu, lambda, kappa, muv[DIM], lamv[DIM], rhoD[L::NYA], rhoDH[L::NYA];
+// Per-point vectors shared by the lanes of an element: w, z = r0^T tau,
+// Mtau[E] = mE^T tau, t_g and t_b.
+template <int DIM, int NEN, int NC, int NQ, typename S>
+struct PointVecs {
+  static constexpr int ND = Layout<DIM, NC>::ND;
+  S w[NQ][ND], z[NQ][ND], y[NQ][ND], tg[NQ][ND], tb[NQ][NEN][ND];
 };
 
 template <int DIM, int NEN, int NC, int NQ, typename S>
 struct ElemSmem {
   using M = MatShape<DIM, NEN, NC>;
-  using L = Layout<DIM, NC>;
-  static constexpr int ND = M::ND, NDP = M::NDP, N = M::N;
-  QP<DIM, NEN, NC, S> qp[NQ];
-  struct Work {
-    S A[DIM][ND][NDP];
-    S D[ND][NDP];
-    S WA[NEN][ND][NDP];
-    S FPT[NEN][NDP][ND];
-    S RM[NEN][ND][NDP];
-    S X[NEN][NDP][ND];
-    S Dnu[NDP][ND];          // sum_q JxW nu DUDY (simplices)
-    S w[ND], r0[ND], mE[ND], U[ND];
+  struct In {
+    QP<DIM, NEN, NC, S> qp[NQ];
+    PointVecs<DIM, NEN, NC, NQ, S> pv;
   };
   union {
-    Work w;
-    double stage[N * N];
+    In in;
+    double stage[M::N * M::NS];
   } u;
-  double diag[N];
+  double wsum[M::WPE];
   int nodes[NEN];
   int64_t rowbase[NEN];
   int32_t rowlen[NEN];
@@ -869,14 +872,26 @@ __device__ __forceinline__ void elem_sync(int el_in_cta) {
   }
 }
 
-// Adds JxW * sum_kl gb_k K_kl(r, c) ga_l for the lane's tile rows r0..r0+RH-1 (the
-// closed form of the contraction; fluid_2d.hpp:531-571), with point scalars ks.
-template <int DIM, int NC, int RH, int ND, typename S>
-__device__ __forceinline__ void add_viscous_tile(S (&acc)[RH][ND], int r0, const KSums<DIM, NC, S>& ks,
-                                                 const S* gb, const S* ga) {
+// Point scalars entering K'_kl (JxW-weighted, summed over the points of a simplex).
+template <int DIM, int NC, typename S>
+struct KSums {
   using L = Layout<DIM, NC>;
-  S gg = gb[0] * ga[0];
-  S gamv = ga[0] * ks.muv[0], gblv = gb[0] * ks.lamv[0];
+  S mu, lambda, kappa, muv[DIM], lamv[DIM], rhoD[L::NYA], rhoDH[L::NYA];
+};
+
+// Adds sum_kl gb_k K_kl(r, :) ga_l to row r of one (b, a) block (the closed form of
+// the contraction; fluid_2d.hpp:531-571), branch-free in r:
+//   velocity row v_j: mu gb_m ga_j + lambda gb_j ga_m + mu (gb.ga) d_mj  on column v_m
+//   energy row      : mu v_m (gb.ga) + gb_m (ga.mu v) + ga_m (gb.lambda v) on v_m,
+//                     kappa (gb.ga) on T, rho D_i H_i (gb.ga) on Y_i
+//   mass-fraction row Y_i: rho D_i (gb.ga) on Y_i.
+template <int DIM, int NC, typename S>
+__device__ __forceinline__ void add_viscous_row(S (&acc)[Layout<DIM, NC>::ND], int r, const KSums<DIM, NC, S>& ks,
+                                                const S* gb, const S* ga) {
+  using L = Layout<DIM, NC>;
+  const bool cV = r >= 1 && r < L::iT, cE = r == L::iT;
+  S gg = gb[0] * ga[0], gamv = ga[0] * ks.muv[0], gblv = gb[0] * ks.lamv[0];
+  S gbj = S(0), gaj = S(0);
 #pragma unroll
   for (int d = 1; d < DIM; ++d) {
     gg = madd(gb[d], ga[d], gg);
@@ -884,44 +899,36 @@ __device__ __forceinline__ void add_viscous_tile(S (&acc)[RH][ND], int r0, const
     gblv = madd(gb[d], ks.lamv[d], gblv);
   }
 #pragma unroll
-  for (int i = 0; i < RH; ++i) {
-    const int r = r0 + i;
-    if (r >= 1 && r < L::iT) {
-      const int jj = r - 1;
-      S gbj = gb[0], gaj = ga[0];
+  for (int d = 0; d < DIM; ++d) {
+    gbj = (r == 1 + d) ? gb[d] : gbj;
+    gaj = (r == 1 + d) ? ga[d] : gaj;
+  }
+  const S p1 = cV ? ks.mu * gaj : (cE ? gamv : S(0));
+  const S p2 = cV ? ks.lambda * gbj : (cE ? gblv : S(0));
+  const S p3 = cV ? ks.mu * gg : S(0);
 #pragma unroll
-      for (int d = 1; d < DIM; ++d) {
-        gbj = (jj == d) ? gb[d] : gbj;
-        gaj = (jj == d) ? ga[d] : gaj;
-      }
+  for (int m = 0; m < DIM; ++m) {
+    S x = madd(gb[m], p1, ga[m] * p2);
+    if (cE) x = madd(ks.muv[m], gg, x);
+    if (r == 1 + m) x += p3;
+    acc[1 + m] += x;
+  }
+  acc[L::iT] = madd(cE ? ks.kappa : S(0), gg, acc[L::iT]);
 #pragma unroll
-      for (int m = 0; m < DIM; ++m) {
-        S x = ks.mu * gb[m] * gaj + ks.lambda * gbj * ga[m];
-        if (m == jj) x = madd(ks.mu, gg, x);
-        acc[i][1 + m] += x;
-      }
-    } else if (r == L::iT) {
-#pragma unroll
-      for (int m = 0; m < DIM; ++m) acc[i][1 + m] += ks.muv[m] * gg + gb[m] * gamv + ga[m] * gblv;
-      acc[i][L::iT] = madd(ks.kappa, gg, acc[i][L::iT]);
-#pragma unroll
-      for (int y = 0; y < NC - 1; ++y) acc[i][L::iY + y] = madd(ks.rhoDH[y], gg, acc[i][L::iY + y]);
-    } else if (r >= L::iY && r < ND) {
-#pragma unroll
-      for (int y = 0; y < NC - 1; ++y)
-        if (r == L::iY + y) acc[i][L::iY + y] = madd(ks.rhoD[y], gg, acc[i][L::iY + y]);
-    }
+  for (int y = 0; y < NC - 1; ++y) {
+    const S q = cE ? ks.rhoDH[y] : ((r == L::iY + y) ? ks.rhoD[y] : S(0));
+    acc[L::iY + y] = madd(q, gg, acc[L::iY + y]);
   }
 }
 
 template <int DIM, int NEN, int NC, int NQ, typename S, bool WANT_M>
-__global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<DIM, NEN, NC, S>* __restrict__ in,
-                                                      long long first, long long n) {
+__global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
+    matrix_kernel(const KParams k, const QP<DIM, NEN, NC, S>* __restrict__ in, long long first, long long n) {
   using L = Layout<DIM, NC>;
   using M = MatShape<DIM, NEN, NC>;
   using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
-  constexpr int ND = M::ND, NDP = M::NDP, RH = M::RH, N = M::N, NT = N * N, WPE = M::WPE, EPC = M::EPC;
-  constexpr int ET = WPE * 32;  // threads per element
+  constexpr int ND = M::ND, N = M::N, NA = M::NA, NT = N * N, WPE = M::WPE, EPC = M::EPC, ET = M::ET, NS = M::NS;
+  constexpr int iT = L::iT, iY = L::iY;
   constexpr bool AFF = M::AFFINE;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x;
@@ -935,7 +942,7 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
   {
     constexpr int W4 = sizeof(QP<DIM, NEN, NC, S>) * NQ / 16;
     const int4* src = reinterpret_cast<const int4*>(in + li * NQ);
-    int4* dst = reinterpret_cast<int4*>(E.qp);
+    int4* dst = reinterpret_cast<int4*>(E.u.in.qp);
     for (int i = gl; i < W4; i += ET) dst[i] = src[i];
   }
   if (gl < NEN) {
@@ -947,155 +954,179 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
     const int fl = k.node_flag ? __ldg(k.node_flag + nd_) : 0;
     E.blocked[gl] = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
   }
-  auto& w = E.u.w;
-  if constexpr (NDP > ND) {
-    for (int t = gl; t < NEN * (NDP - ND) * ND; t += ET) {
-      const int b = t / ((NDP - ND) * ND), r = ND + (t / ND) % (NDP - ND), c = t % ND;
-      w.FPT[b][r][c] = S(0);
-      w.X[b][r][c] = S(0);
+  S grav[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) grav[d] = S(k.gravity[d]);
+  elem_sync<WPE>(ec);
+  auto& pv = E.u.in.pv;
+  // per-point vectors
+  {
+    constexpr int NPV = (4 + NEN) * ND;
+    for (int t = gl; t < NQ * NPV; t += ET) {
+      const int q = t / NPV, u = t % NPV, kind = u / ND, col = u % ND;
+      const QP<DIM, NEN, NC, S>& c = E.u.in.qp[q];
+      S x;
+      if (kind == 0) {
+        x = col == 0 ? S(1) : (col < iT ? c.v[col - 1] : (col == iT ? c.E : c.Y[col - iY]));
+        pv.w[q][col] = x;
+      } else if (kind == 1) {
+        x = madd(c.drho_dp, c.tau[0][col], c.drho_dT * c.tau[iT][col]);
+#pragma unroll
+        for (int y = 0; y < NC - 1; ++y) x = madd(c.drho_dY[y], c.tau[iY + y][col], x);
+        pv.z[q][col] = x;
+      } else if (kind == 2) {
+        x = madd(c.de_dp, c.tau[0][col], c.de_dT * c.tau[iT][col]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) x = madd(c.v[d], c.tau[1 + d][col], x);
+#pragma unroll
+        for (int y = 0; y < NC - 1; ++y) x = madd(c.dE_dY[y], c.tau[iY + y][col], x);
+        pv.y[q][col] = x;
+      } else if (kind == 3) {
+        x = grav[0] * c.tau[1][col];
+#pragma unroll
+        for (int d = 1; d < DIM; ++d) x = madd(grav[d], c.tau[1 + d][col], x);
+        pv.tg[q][col] = x;
+      } else {
+        const int b = kind - 4;
+        x = c.ds[0][b] * c.tau[1][col];
+#pragma unroll
+        for (int d = 1; d < DIM; ++d) x = madd(c.ds[d][b], c.tau[1 + d][col], x);
+        pv.tb[q][b][col] = x;
+      }
     }
   }
-  for (int t = gl; t < NDP * ND; t += ET) (&w.Dnu[0][0])[t] = S(0);
-  const int pr = gl >> 1, half = gl & 1;
-  const bool has_pair = pr < M::NP;
-  const int pb = has_pair ? pr / NEN : 0, pa = has_pair ? pr % NEN : 0;
-  const int r0 = half * RH;
-  S acc[RH][ND];
+  elem_sync<WPE>(ec);
+  const bool active = gl < M::LANES;
+  const int row = active ? gl % N : 0;
+  const int grp = active ? gl / N : 0;
+  const int b = row / ND, r = row % ND;
+  const int a0 = grp * NA;
+  const bool cV = r >= 1 && r < iT, cE = r == iT, cvy = r >= 1 && r != iT;
+  S acc[NA][ND];
 #pragma unroll
-  for (int i = 0; i < RH; ++i)
+  for (int i = 0; i < NA; ++i)
 #pragma unroll
     for (int j = 0; j < ND; ++j) acc[i][j] = S(0);
   S racc = S(0);
+  S Dnu[ND];
   KSums<DIM, NC, S> ksum;
   if constexpr (AFF) {
+#pragma unroll
+    for (int j = 0; j < ND; ++j) Dnu[j] = S(0);
     ksum.mu = ksum.lambda = ksum.kappa = S(0);
 #pragma unroll
     for (int d = 0; d < DIM; ++d) ksum.muv[d] = ksum.lamv[d] = S(0);
 #pragma unroll
     for (int y = 0; y < L::NYA; ++y) ksum.rhoD[y] = ksum.rhoDH[y] = S(0);
   }
-  const S dt = S(k.dt);
-  const S idt = S(1) / dt;
-  S grav[DIM];
+  const S idt = S(k.inv_dt);
+  for (int q = 0; q < NQ; ++q) {
+    const QP<DIM, NEN, NC, S>& c = E.u.in.qp[q];
+    const S rho = c.rho, p = c.p, jx = c.JxW;
+    S gb[DIM];
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) grav[d] = S(k.gravity[d]);
-  elem_sync<WPE>(ec);
-  for (int iq = 0; iq < NQ; ++iq) {
-    const QP<DIM, NEN, NC, S>& c = E.qp[iq];
-    // (0) structure vectors of DUDY: w, r0, energy row of M, U
-    for (int t = gl; t < ND; t += ET) {
-      S wv, r0v, mv;
-      if (t == 0) { wv = S(1); r0v = c.drho_dp; mv = c.de_dp; }
-      else if (t < L::iT) { wv = c.v[t - 1]; r0v = S(0); mv = c.v[t - 1]; }
-      else if (t == L::iT) { wv = c.E; r0v = c.drho_dT; mv = c.de_dT; }
-      else { wv = c.Y[t - L::iY]; r0v = c.drho_dY[t - L::iY]; mv = c.dE_dY[t - L::iY]; }
-      w.w[t] = wv; w.r0[t] = r0v; w.mE[t] = mv; w.U[t] = c.rho * wv;
-    }
-    elem_sync<WPE>(ec);
-    // (1) DUDY and A_k, branch-free
-    for (int t = gl; t < ND * ND; t += ET) {
-      const int r = t / ND, col = t % ND;
-      const S Mrc = (r == L::iT) ? w.mE[col] : ((r == col && r != 0) ? S(1) : S(0));
-      const S Dv = madd(w.w[r], w.r0[col], c.rho * Mrc);
-      w.D[r][col] = Dv;
-      const S isE = (r == L::iT) ? S(1) : S(0);
-      const S Ur = w.U[r];
+    for (int d = 0; d < DIM; ++d) gb[d] = c.ds[d][b];
+    const S Nb = c.sh[b];
+    S sb = gb[0] * c.v[0];
 #pragma unroll
-      for (int kk = 0; kk < DIM; ++kk) {
-        const S vk = c.v[kk];
-        S a = vk * Dv;
-        a += (col == 1 + kk) ? madd(isE, c.p, Ur) : S(0);
-        a += (col == 0) ? madd(isE, vk, (r == 1 + kk) ? S(1) : S(0)) : S(0);
-        w.A[kk][r][col] = a;
-      }
-    }
-    elem_sync<WPE>(ec);
-    // (2) WA, RM, X
-    for (int t = gl; t < NEN * ND * ND; t += ET) {
-      const int b = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
-      S wa = c.ds[0][b] * w.A[0][r][col];
+    for (int d = 1; d < DIM; ++d) sb = madd(gb[d], c.v[d], sb);
+    const S wr = pv.w[q][r];
+    const S ur = madd(rho, wr, cE ? p : S(0));
+    S gsel = S(0);
 #pragma unroll
-      for (int d = 1; d < DIM; ++d) wa = madd(c.ds[d][b], w.A[d][r][col], wa);
-      const S Dv = w.D[r][col], shb = c.sh[b];
-      const S sv = (r == L::iT && col >= 1 && col <= DIM) ? c.rho * grav[(col - 1) % DIM] : S(0);
-      w.WA[b][r][col] = wa;
-      w.RM[b][r][col] = Dv * shb * idt + wa - sv * shb;
-      if constexpr (WANT_M) w.X[b][r][col] = shb * (Dv * idt - sv) - wa;
-    }
-    if constexpr (WANT_M && AFF) {
-      for (int t = gl; t < ND * ND; t += ET) {
-        const int r = t / ND, col = t % ND;
-        w.Dnu[r][col] = madd(c.JxW * c.nu, w.D[r][col], w.Dnu[r][col]);
-      }
-    }
-    elem_sync<WPE>(ec);
-    // (3) FPT
-    for (int t = gl; t < NEN * ND * ND; t += ET) {
-      const int b = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
-      const S shb = c.sh[b];
-      S x = S(0);
+    for (int d = 0; d < DIM; ++d) gsel = (r == 1 + d) ? gb[d] : gsel;
+    const S kap = (cE ? sb : S(0)) + gsel;
+    // row r of FPT_b
+    const S cz = sb * wr, cm = (r == 0) ? S(0) : sb * rho, cg = cE ? -Nb * rho : S(0);
+    const S* mrow = cvy ? &c.tau[r][0] : &pv.y[q][0];
+    const S* tb = &pv.tb[q][b][0];
+    S F[ND];
 #pragma unroll
-      for (int m = 0; m < ND; ++m) {
-        const S sv = (r == L::iT && m >= 1 && m <= DIM) ? c.rho * grav[(m - 1) % DIM] : S(0);
-        x = madd(w.WA[b][r][m] - shb * sv, c.tau[m][col], x);
-      }
-      w.FPT[b][r][col] = x;
+    for (int j = 0; j < ND; ++j) {
+      S x = cz * pv.z[q][j];
+      x = madd(cm, mrow[j], x);
+      x = madd(ur, tb[j], x);
+      x = madd(kap, c.tau[0][j], x);
+      F[j] = madd(cg, pv.tg[q][j], x);
     }
-    elem_sync<WPE>(ec);
-    // (4) block tiles and residual
+    // residual row: N_b rv + sum_k dN_b/dx_k rf_k + FPT_b Res (fluid_2d.hpp:253-262, 280-290)
+    {
+      S x = Nb * c.rv[r];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) x = madd(gb[d], c.rf[d][r], x);
+#pragma unroll
+      for (int j = 0; j < ND; ++j) x = madd(F[j], c.res[j], x);
+      racc = madd(jx, x, racc);
+    }
     if constexpr (WANT_M) {
-      if (has_pair) {
-        S tt[RH][ND];
+      // FPT_b DUDY, DUDY row r, and the a-independent velocity-column terms
+      S fw = F[0];
 #pragma unroll
-        for (int i = 0; i < RH; ++i)
+      for (int j = 1; j < ND; ++j) fw = madd(F[j], pv.w[q][j], fw);
+      const S fu = madd(rho, fw, p * F[iT]);
+      const S rF = rho * F[iT];
+      S FD[ND], Dr[ND];
 #pragma unroll
-          for (int j = 0; j < ND; ++j) tt[i][j] = S(0);
+      for (int j = 0; j < ND; ++j) {
+        S r0j, mEj;
+        if (j == 0) { r0j = c.drho_dp; mEj = c.de_dp; }
+        else if (j < iT) { r0j = S(0); mEj = c.v[j - 1]; }
+        else if (j == iT) { r0j = c.drho_dT; mEj = c.de_dT; }
+        else { r0j = c.drho_dY[j - iY]; mEj = c.dE_dY[j - iY]; }
+        S x = madd(rF, mEj, (j >= 1 && j != iT) ? rho * F[j] : S(0));
+        FD[j] = (j >= 1 && j < iT) ? x : madd(fw, r0j, x);
+        S dd = madd(cE ? rho : S(0), mEj, (cvy && r == j) ? rho : S(0));
+        Dr[j] = (j >= 1 && j < iT) ? dd : madd(wr, r0j, dd);
+      }
+      S hv[DIM];
+      const S fe = rho * (F[iT] + (cE ? Nb : S(0)));
 #pragma unroll
-        for (int m = 0; m < ND; ++m) {
-          S fr[RH], rr[ND];
+      for (int d = 0; d < DIM; ++d) hv[d] = -madd(ur, gb[d], fe * grav[d]);
+      const S beta = madd(Nb, idt, -sb);
+      KSums<DIM, NC, S> ks;
+      S nu_j = S(0);
+      if constexpr (!AFF) {
+        ks.mu = jx * c.mu; ks.lambda = jx * c.lambda; ks.kappa = jx * c.kappa;
 #pragma unroll
-          for (int i = 0; i < RH; ++i) fr[i] = w.FPT[pb][r0 + i][m];
+        for (int d = 0; d < DIM; ++d) { ks.muv[d] = ks.mu * c.v[d]; ks.lamv[d] = ks.lambda * c.v[d]; }
 #pragma unroll
-          for (int j = 0; j < ND; ++j) rr[j] = w.RM[pa][m][j];
+        for (int y = 0; y < L::NYA; ++y) { ks.rhoD[y] = jx * c.rhoD[y]; ks.rhoDH[y] = jx * c.rhoDH[y]; }
+        nu_j = jx * c.nu;
+      }
 #pragma unroll
-          for (int i = 0; i < RH; ++i)
+      for (int ai = 0; ai < NA; ++ai) {
+        const int a = a0 + ai;
+        S ga[DIM];
 #pragma unroll
-            for (int j = 0; j < ND; ++j) tt[i][j] = madd(fr[i], rr[j], tt[i][j]);
-        }
-        const S sa = c.sh[pa];
+        for (int d = 0; d < DIM; ++d) ga[d] = c.ds[d][a];
+        const S Na = c.sh[a];
+        S sa = ga[0] * c.v[0];
 #pragma unroll
-        for (int i = 0; i < RH; ++i)
+        for (int d = 1; d < DIM; ++d) sa = madd(ga[d], c.v[d], sa);
+        S fk = sa * F[iT];
 #pragma unroll
-          for (int j = 0; j < ND; ++j) tt[i][j] = madd(sa, w.X[pb][r0 + i][j], tt[i][j]);
+        for (int d = 0; d < DIM; ++d) fk = madd(ga[d], F[1 + d], fk);
+        const S A1 = jx * madd(Na, idt, sa), A4 = jx * Na, A2 = A4 * beta, A3 = jx * fu;
+        acc[ai][0] = madd(A1, FD[0], madd(A2, Dr[0], madd(jx, madd(-Na, kap, fk), acc[ai][0])));
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+          acc[ai][1 + d] = madd(A1, FD[1 + d], madd(A2, Dr[1 + d], madd(A3, ga[d], madd(A4, hv[d], acc[ai][1 + d]))));
+#pragma unroll
+        for (int j = iT; j < ND; ++j) acc[ai][j] = madd(A1, FD[j], madd(A2, Dr[j], acc[ai][j]));
         if constexpr (!AFF) {
-          // viscous, diffusive and dc terms at this point
-          S gb[DIM], ga[DIM];
-#pragma unroll
-          for (int d = 0; d < DIM; ++d) { gb[d] = c.ds[d][pb]; ga[d] = c.ds[d][pa]; }
-          KSums<DIM, NC, S> ks;
-          ks.mu = c.mu; ks.lambda = c.lambda; ks.kappa = c.kappa;
-#pragma unroll
-          for (int d = 0; d < DIM; ++d) { ks.muv[d] = c.mu * c.v[d]; ks.lamv[d] = c.lambda * c.v[d]; }
-#pragma unroll
-          for (int y = 0; y < L::NYA; ++y) { ks.rhoD[y] = c.rhoD[y]; ks.rhoDH[y] = c.rhoDH[y]; }
-          add_viscous_tile<DIM, NC, RH, ND, S>(tt, r0, ks, gb, ga);
+          add_viscous_row<DIM, NC, S>(acc[ai], r, ks, gb, ga);
           S gg = gb[0] * ga[0];
 #pragma unroll
           for (int d = 1; d < DIM; ++d) gg = madd(gb[d], ga[d], gg);
-          const S gn = gg * c.nu;
+          const S gn = gg * nu_j;
 #pragma unroll
-          for (int i = 0; i < RH; ++i)
-#pragma unroll
-            for (int j = 0; j < ND; ++j)
-              if (r0 + i < ND) tt[i][j] = madd(gn, w.D[r0 + i][j], tt[i][j]);
+          for (int j = 0; j < ND; ++j) acc[ai][j] = madd(gn, Dr[j], acc[ai][j]);
         }
-#pragma unroll
-        for (int i = 0; i < RH; ++i)
-#pragma unroll
-          for (int j = 0; j < ND; ++j) acc[i][j] = madd(c.JxW, tt[i][j], acc[i][j]);
       }
       if constexpr (AFF) {
-        const S jx = c.JxW;
+        const S jn = jx * c.nu;
+#pragma unroll
+        for (int j = 0; j < ND; ++j) Dnu[j] = madd(jn, Dr[j], Dnu[j]);
         ksum.mu = madd(jx, c.mu, ksum.mu);
         ksum.lambda = madd(jx, c.lambda, ksum.lambda);
         ksum.kappa = madd(jx, c.kappa, ksum.kappa);
@@ -1111,90 +1142,79 @@ __global__ void __launch_bounds__(128) matrix_kernel(const KParams k, const QP<D
         }
       }
     }
-    if (gl < N) {
-      const int b = gl / ND, jb = gl % ND;
-      S x = c.sh[b] * c.rv[jb];
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) x = madd(c.ds[d][b], c.rf[d][jb], x);
-#pragma unroll
-      for (int m = 0; m < ND; ++m) x = madd(w.FPT[b][jb][m], c.res[m], x);
-      racc = madd(c.JxW, x, racc);
-    }
-    elem_sync<WPE>(ec);
   }
   if constexpr (WANT_M && AFF) {
     // viscous/diffusive and dc terms of a simplex, from the point sums
-    if (has_pair) {
-      const QP<DIM, NEN, NC, S>& c = E.qp[0];
-      S gb[DIM], ga[DIM];
+    const QP<DIM, NEN, NC, S>& c = E.u.in.qp[0];
+    S gb[DIM];
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) { gb[d] = c.ds[d][pb]; ga[d] = c.ds[d][pa]; }
-      add_viscous_tile<DIM, NC, RH, ND, S>(acc, r0, ksum, gb, ga);
+    for (int d = 0; d < DIM; ++d) gb[d] = c.ds[d][b];
+#pragma unroll
+    for (int ai = 0; ai < NA; ++ai) {
+      S ga[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) ga[d] = c.ds[d][a0 + ai];
+      add_viscous_row<DIM, NC, S>(acc[ai], r, ksum, gb, ga);
       S gg = gb[0] * ga[0];
 #pragma unroll
       for (int d = 1; d < DIM; ++d) gg = madd(gb[d], ga[d], gg);
 #pragma unroll
-      for (int i = 0; i < RH; ++i)
-#pragma unroll
-        for (int j = 0; j < ND; ++j) acc[i][j] = madd(gg, w.Dnu[r0 + i][j], acc[i][j]);
+      for (int j = 0; j < ND; ++j) acc[ai][j] = madd(gg, Dnu[j], acc[ai][j]);
     }
   }
   // Dirichlet rows (scatter.hpp:62-78) and scatter (scatter.hpp:96-97)
+  const bool local = k.local_r != nullptr;
+  const bool blk = !local && ((E.blocked[b] >> r) & 1u);
   double avg = 0.0;
   if constexpr (WANT_M) {
-    if (has_pair && pb == pa) {
+    // avg_val = (1 + trace)/n (scatter.hpp:65-68)
+    S dg = S(0);
 #pragma unroll
-      for (int i = 0; i < RH; ++i)
+    for (int ai = 0; ai < NA; ++ai)
 #pragma unroll
-        for (int j = 0; j < ND; ++j)
-          if (j == r0 + i) E.diag[pb * ND + j] = widen(acc[i][j]);
-    }
-    elem_sync<WPE>(ec);
-    // avg_val = (1 + trace)/n (scatter.hpp:65-68); trace summed by a warp tree
-    double tr = 0.0;
-    for (int i = gl & 31; i < N; i += 32) tr += E.diag[i];
+      for (int j = 0; j < ND; ++j) dg = (a0 + ai == b && j == r) ? acc[ai][j] : dg;
+    double tr = active ? widen(dg) : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    if constexpr (WPE > 1) {
+      if ((gl & 31) == 0) E.wsum[gl >> 5] = tr;
+    }
+    elem_sync<WPE>(ec);  // the point records are dead from here on (stage aliases them)
+    if constexpr (WPE > 1) {
+      tr = E.wsum[0];
+#pragma unroll
+      for (int w = 1; w < WPE; ++w) tr += E.wsum[w];
+    }
     avg = (1.0 + tr) / N;
-    const bool local = k.local_r != nullptr;
-    if (has_pair) {
+    if (active) {
+      double* srow = E.u.stage + row * NS + a0 * ND;
 #pragma unroll
-      for (int i = 0; i < RH; ++i) {
-        const int jb = r0 + i;
-        if (jb < ND) {
-          const bool blk = !local && ((E.blocked[pb] >> jb) & 1u);
-          const int row = pb * ND + jb;
+      for (int ai = 0; ai < NA; ++ai)
 #pragma unroll
-          for (int j = 0; j < ND; ++j) {
-            const int col = pa * ND + j;
-            E.u.stage[row * N + col] = blk ? (row == col ? avg : 0.0) : widen(acc[i][j]);
-          }
-        }
-      }
+        for (int j = 0; j < ND; ++j)
+          srow[ai * ND + j] = blk ? ((a0 + ai == b && j == r) ? avg : 0.0) : widen(acc[ai][j]);
     }
     elem_sync<WPE>(ec);
   }
-  if (k.local_r) {  // element-level output of execute_i (fluid_2d.hpp:200-201): m = m_, r = -r_
-    if (gl < N) k.local_r[g * N + gl] = -(double)racc;
+  if (local) {  // element-level output of execute_i (fluid_2d.hpp:200-201): m = m_, r = -r_
+    if (active && grp == 0) k.local_r[g * N + row] = -widen(racc);
     if (WANT_M && k.local_m)
-      for (int t = gl; t < NT; t += ET) k.local_m[g * NT + t] = E.u.stage[t];
+      for (int t = gl; t < NT; t += ET) k.local_m[g * NT + t] = E.u.stage[(t / N) * NS + t % N];
     return;
   }
   const int mode = k.scatter_mode;
-  if (gl < N) {
-    const int b = gl / ND, jb = gl % ND;
-    const bool blk = (E.blocked[b] >> jb) & 1u;
+  if (active && grp == 0) {
     const double rv = blk ? avg * 0.0 : -widen(racc);
-    add_to(k.rhs + (long long)E.nodes[b] * ND + jb, rv, mode);
+    add_to(k.rhs + (long long)E.nodes[b] * ND + r, rv, mode);
   }
   if constexpr (WANT_M) {
     for (int t = gl; t < NT; t += ET) {
-      const double val = E.u.stage[t];
+      const int srw = t / N, colx = t - srw * N;
+      const double val = E.u.stage[srw * NS + colx];
       if ((__double_as_longlong(val) << 1) != 0) {
-        const int row = t / N, colx = t % N;
-        const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-        const int64_t off = E.rowbase[b] + (int64_t)jb * E.rowlen[b] +
-                            (int64_t)__ldg(k.slot + (e * NEN + b) * NEN + a) * ND + ja;
+        const int sb_ = srw / ND, jb = srw - sb_ * ND, a = colx / ND, ja = colx - a * ND;
+        const int64_t off = E.rowbase[sb_] + (int64_t)jb * E.rowlen[sb_] +
+                            (int64_t)__ldg(k.slot + (e * NEN + sb_) * NEN + a) * ND + ja;
         add_to(k.vals + off, val, mode);
       }
     }

@@ -39,12 +39,12 @@ struct InteriorInst {
       auto fn = matrix_kernel<DIM, NEN, NC, NQ, S, true>;
       cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return {e, 0};
-      fn<<<blocks, 128, smem, st>>>(k, in, first, n);
+      fn<<<blocks, M::CTA, smem, st>>>(k, in, first, n);
     } else {
       auto fn = matrix_kernel<DIM, NEN, NC, NQ, S, false>;
       cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return {e, 0};
-      fn<<<blocks, 128, smem, st>>>(k, in, first, n);
+      fn<<<blocks, M::CTA, smem, st>>>(k, in, first, n);
     }
     return {cudaGetLastError(), 1};
   }
