@@ -449,10 +449,14 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
   double U[ND];
   conservative<DIM, NC>(pr.rho, pr.cv, v, T, Y, U);
   const double dt = k.dt;
-  double Sv[ND];
+  // source S (gravity; fluid_2d.hpp:597-599) and the mass-term coefficient (U - U_P)/dt - S
+  R SvR[ND];
 #pragma unroll
-  for (int r = 0; r < ND; ++r) Sv[r] = 0.0;
-  {
+  for (int r = 0; r < ND; ++r) SvR[r] = R(0);
+  if constexpr (FORM == GALES_FORM_FP64) {
+    double Sv[ND];
+#pragma unroll
+    for (int r = 0; r < ND; ++r) Sv[r] = 0.0;
     double gv = 0.0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
@@ -460,11 +464,24 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       gv += k.gravity[d] * v[d];
     }
     Sv[L::iT] = pr.rho * (gv);
-  }
 #pragma unroll
-  for (int j = 0; j < ND; ++j) {
-    if constexpr (FORM == GALES_FORM_FP64) out.rv[j] = (U[j] - UP[j]) / dt - Sv[j];
-    else out.rv[j] = to_s<S>(fma(U[j] - UP[j], k.inv_dt, -Sv[j]));
+    for (int j = 0; j < ND; ++j) {
+      SvR[j] = Sv[j];
+      out.rv[j] = (U[j] - UP[j]) / dt - Sv[j];
+    }
+  } else {
+    const float rf = narrow_rn(pr.rho);
+    float gv = 0.f;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const float gd = narrow_rn(k.gravity[d]);
+      SvR[1 + d] = rf * gd;
+      gv = fmaf(gd, narrow_rn(v[d]), gv);
+    }
+    SvR[L::iT] = rf * gv;
+    const float idt = narrow_rn(k.inv_dt);
+#pragma unroll
+    for (int j = 0; j < ND; ++j) out.rv[j] = fmaf(narrow_rn(U[j] - UP[j]), idt, -SvR[j]);
   }
   // tau (fluid_2d.hpp:877-1022)
   double tau[ND][ND];
@@ -494,15 +511,16 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = fmin(use, h * h / (pr.D_c[i] * 12));
       nondiag = true;
     } else if (FORM == GALES_FORM_MIXED && k.tau == GALES_TAU_NON_DIAG_COMP_2019) {
-      // the same parameters with reciprocals (mixed form)
-      const double hv = h * (0.5 / (v_nrm + cs) + 0.5 / v_nrm);
+      // the same parameters with fewer divisions (mixed form)
+      const double hv = (0.5 * h) * fma(2.0, v_nrm, cs) / (v_nrm * (v_nrm + cs));
       const double use = k.steady ? hv : fmin(dt * 0.5, hv);
       const double hh12 = h * h * (1.0 / 12.0);
+      const double imk = 1.0 / (mu * kappa);
       tau[0][0] = use;
-      const double tm = fmin(use, hh12 * rho / mu);
+      const double tm = fmin(use, hh12 * rho * kappa * imk);
 #pragma unroll
       for (int d = 0; d < DIM; ++d) tau[1 + d][1 + d] = tm;
-      tau[L::iT][L::iT] = fmin(use, hh12 * rho * cv / kappa);
+      tau[L::iT][L::iT] = fmin(use, hh12 * rho * cv * mu * imk);
 #pragma unroll
       for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = fmin(use, hh12 * k.ch[i].inv_D);
       nondiag = true;
@@ -571,45 +589,53 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       tau[0][0] = 1.0 / (tau[0][0] + rho * tau[1][1] * (trG));
     }
     if (nondiag) {
-      double Xinv[ND][ND];
+      double td[ND];
+#pragma unroll
+      for (int i = 0; i < ND; ++i) td[i] = tau[i][i];
       if constexpr (FORM == GALES_FORM_FP64) {
-        double A0[ND][ND];
+        double A0[ND][ND], Xinv[ND][ND];
 #pragma unroll
         for (int r = 0; r < ND; ++r)
 #pragma unroll
           for (int cc = 0; cc < ND; ++cc) A0[r][cc] = dudy_entry<DIM, NC, double>(c, r, cc);
         if (lu_inverse<ND>(A0, Xinv)) flag_error(k, GALES_ERR_SINGULAR, e);
+#pragma unroll
+        for (int r = 0; r < ND; ++r)
+#pragma unroll
+          for (int cc = 0; cc < ND; ++cc) tau[r][cc] = Xinv[r][cc] * td[cc];
+        if (v_nrm / cs < 0.1) {
+          tau[0][0] = 1.0 / (1.0 / tau[0][0] + 1.0 / (rho * tau[1][1] * (trG)));
+#pragma unroll
+          for (int cc = 1; cc < ND; ++cc) tau[0][cc] = 0.0;
+        }
       } else {
-        dydu_closed<DIM, NC>(c, Xinv);
-      }
-      double td[ND];
+        tau_closed<DIM, NC>(c, pr.irho, td, tau);
+        if (v_nrm < 0.1 * cs) {
+          // 1/(1/a + 1/b) = a b/(a + b)
+          const double b = rho * tau[1][1] * trG;
+          tau[0][0] = tau[0][0] * b / (tau[0][0] + b);
 #pragma unroll
-      for (int i = 0; i < ND; ++i) td[i] = tau[i][i];
-#pragma unroll
-      for (int r = 0; r < ND; ++r)
-#pragma unroll
-        for (int cc = 0; cc < ND; ++cc) tau[r][cc] = Xinv[r][cc] * td[cc];
-      if (v_nrm / cs < 0.1) {
-        tau[0][0] = 1.0 / (1.0 / tau[0][0] + 1.0 / (rho * tau[1][1] * (trG)));
-#pragma unroll
-        for (int cc = 1; cc < ND; ++cc) tau[0][cc] = 0.0;
+          for (int cc = 1; cc < ND; ++cc) tau[0][cc] = 0.0;
+        }
       }
     }
   }
+#pragma unroll
+  for (int r = 0; r < ND; ++r)
+#pragma unroll
+    for (int cc = 0; cc < ND; ++cc) out.tau[r][cc] = to_s<S>(tau[r][cc]);
   // fluxes, least-squares residual and dc in the form's type R
   using CR = Coef<DIM, NC, R>;
   CR cr;
   if constexpr (FORM == GALES_FORM_FP64) cr = c;
   else cr = narrow<DIM, NC>(c);
-  R SvR[ND], Res[ND], AdI[ND], t[ND];
-#pragma unroll
-  for (int j = 0; j < ND; ++j) SvR[j] = to_s<R>(Sv[j]);
+  R Res[ND], AdI[ND], t[ND];
   {
     R dd[ND];
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
       if constexpr (FORM == GALES_FORM_FP64) dd[j] = (Iq[j] - Pq[j]) / dt;
-      else dd[j] = narrow_rn((Iq[j] - Pq[j]) * k.inv_dt);
+      else dd[j] = narrow_rn(Iq[j] - Pq[j]) * narrow_rn(k.inv_dt);
     }
     dudy_mv<DIM, NC, R>(cr, dd, Res);
 #pragma unroll
@@ -726,10 +752,6 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
     out.drho_dY[i] = to_s<S>(c.drho_dY[i]); out.dE_dY[i] = to_s<S>(c.dE_dY[i]);
     out.rhoD[i] = to_s<S>(c.rhoD[i]); out.rhoDH[i] = to_s<S>(c.rhoDH[i]);
   }
-#pragma unroll
-  for (int r = 0; r < ND; ++r)
-#pragma unroll
-    for (int cc = 0; cc < ND; ++cc) out.tau[r][cc] = to_s<S>(tau[r][cc]);
   out.nu = S(nu);
 #pragma unroll
   for (int j = 0; j < ND; ++j) out.res[j] = S(Res[j]);
@@ -784,9 +806,11 @@ __device__ __forceinline__ double widen(double d) { return d; }
 
 // ---------------------------------------------------------------------------
 // Interior pass, stage 1: one thread per (element, quadrature point) writes the
-// point record of that point to a chunk buffer (L2-resident).
+// point record of that point to a chunk buffer (L2-resident).  The mixed form is
+// held to 128 registers (4 CTAs per SM): more warps hide the FP64 latency better
+// than the spilled values cost.
 template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
-__global__ void __launch_bounds__(128) point_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ out,
+__global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1) point_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ out,
                                                      long long first, long long n) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long li = t / NQ;

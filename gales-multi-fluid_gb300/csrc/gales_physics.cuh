@@ -73,6 +73,7 @@ struct Props {
   double rho, mu, cp, cv, kappa, c, alpha, beta;
   double rho_c[NC], e_c[NC], D_c[NC];
   double irho_c[NC];  // 1/rho_c (mixed form only)
+  double irho;        // 1/rho = sum_c Y_c/rho_c (mixed form only)
 };
 
 template <int NC>
@@ -153,8 +154,8 @@ __device__ __forceinline__ void mixture_fast(const DevChem* ch, double p, double
     o.D_c[c] = q.D;
   }
   const double rho = 1.0 / irho;
-  o.rho = rho; o.mu = mu; o.cp = cp; o.cv = cv; o.kappa = kappa;
-  o.c = sqrt(1.0 / c2) * irho;
+  o.rho = rho; o.irho = irho; o.mu = mu; o.cp = cp; o.cv = cv; o.kappa = kappa;
+  o.c = rsqrt(c2) * irho;
   o.alpha = rho * al;
   o.beta = rho * be;
 }
@@ -310,7 +311,7 @@ __device__ __forceinline__ void make_coef_fast(const Props<NC>& pr, double p, co
   for (int k = 0; k < DIM; ++k) c.v[k] = v[k];
 #pragma unroll
   for (int i = 0; i < NC; ++i) c.Y[i] = Y[i];
-  const double rho = pr.rho, irho = 1.0 / rho;
+  const double rho = pr.rho, irho = pr.irho;
   c.rho = rho;
   c.cv = pr.cv;
   c.E = fma(pr.cv, T, 0.5 * vsq<DIM>(v));
@@ -597,40 +598,52 @@ __device__ __forceinline__ int lu_inverse(double (&A)[N][N], double (&X)[N][N]) 
   return singular;
 }
 
-// DUDY^{-1} in closed form.  DUDY = w r0^T + rho M with w = (1, v, E, Y),
-// r0 = its first row and M sparse, so DUDY x = y reduces to a 2x2 solve for
-// (x_p, x_T).  Used by the mixed form only.
+// tau = DUDY^{-1} diag(td) for the mixed form (fluid_2d.hpp:946-947), from the
+// structure of DUDY = w r0^T + rho M.  The velocity and mass-fraction rows of
+// DUDY^{-1} are (e_j - w_j e_p^T)/rho; the p and T rows come from the 2x2 system
+// [drho_dp drho_dT; de_dp de_dT] per column.  Every other entry is zero.  irho = 1/rho.
 template <int DIM, int NC>
-__device__ __forceinline__ void dydu_closed(const Coef<DIM, NC>& c, double (&X)[Layout<DIM, NC>::ND][Layout<DIM, NC>::ND]) {
+__device__ __forceinline__ void tau_closed(const Coef<DIM, NC>& c, double irho, const double* td,
+                                           double (&tau)[Layout<DIM, NC>::ND][Layout<DIM, NC>::ND]) {
   using L = Layout<DIM, NC>;
   constexpr int ND = L::ND;
-  const double irho = 1.0 / c.rho;
-  const double det = c.drho_dp * c.de_dT - c.drho_dT * c.de_dp;
-  const double idet = 1.0 / det;
 #pragma unroll
-  for (int col = 0; col < ND; ++col) {
-    // y = e_col
-    const double s = (col == 0) ? 1.0 : 0.0;
-    double xv[DIM], xy[L::NYA];
-    double R1 = s, R2 = 0.0;
+  for (int r = 0; r < ND; ++r)
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) xv[j] = fma(-c.v[j], s, (col == 1 + j) ? 1.0 : 0.0) * irho;
+    for (int cc = 0; cc < ND; ++cc) tau[r][cc] = 0.0;
+  const double idet = 1.0 / fma(c.drho_dp, c.de_dT, -c.drho_dT * c.de_dp);
+  const double q = irho * idet;
+  // column p: R1 = 1 + (sum_i drho_dY_i Y_i)/rho, R2 = (|v|^2 - E + sum_i dE_dY_i Y_i)/rho
+  double sY = 0.0, sE = -c.E;
 #pragma unroll
-    for (int i = 0; i < NC - 1; ++i) xy[i] = fma(-c.Y[i], s, (col == L::iY + i) ? 1.0 : 0.0) * irho;
-    R2 = fma(-c.E, s, (col == L::iT) ? 1.0 : 0.0) * irho;
+  for (int j = 0; j < DIM; ++j) sE = fma(c.v[j], c.v[j], sE);
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) R2 = fma(-c.v[j], xv[j], R2);
+  for (int i = 0; i < NC - 1; ++i) {
+    sY = fma(c.drho_dY[i], c.Y[i], sY);
+    sE = fma(c.dE_dY[i], c.Y[i], sE);
+  }
+  const double R1 = fma(irho, sY, 1.0), R2 = irho * sE;
+  const double t0 = td[0] * idet, ti = td[0] * irho;
+  tau[0][0] = fma(R1, c.de_dT, -c.drho_dT * R2) * t0;
+  tau[L::iT][0] = fma(c.drho_dp, R2, -c.de_dp * R1) * t0;
 #pragma unroll
-    for (int i = 0; i < NC - 1; ++i) {
-      R1 = fma(-c.drho_dY[i], xy[i], R1);
-      R2 = fma(-c.dE_dY[i], xy[i], R2);
-    }
-    X[0][col] = fma(R1, c.de_dT, -c.drho_dT * R2) * idet;
-    X[L::iT][col] = fma(c.drho_dp, R2, -c.de_dp * R1) * idet;
+  for (int j = 0; j < DIM; ++j) {
+    tau[1 + j][0] = -c.v[j] * ti;
+    tau[1 + j][1 + j] = irho * td[1 + j];
+    const double a = q * td[1 + j] * c.v[j];
+    tau[0][1 + j] = c.drho_dT * a;
+    tau[L::iT][1 + j] = -c.drho_dp * a;
+  }
+  tau[0][L::iT] = -c.drho_dT * q * td[L::iT];
+  tau[L::iT][L::iT] = c.drho_dp * q * td[L::iT];
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) X[1 + j][col] = xv[j];
-#pragma unroll
-    for (int i = 0; i < NC - 1; ++i) X[L::iY + i][col] = xy[i];
+  for (int i = 0; i < NC - 1; ++i) {
+    const int y = L::iY + i;
+    tau[y][0] = -c.Y[i] * ti;
+    tau[y][y] = irho * td[y];
+    const double a = q * td[y];
+    tau[0][y] = fma(c.drho_dT, c.dE_dY[i], -c.drho_dY[i] * c.de_dT) * a;
+    tau[L::iT][y] = fma(c.de_dp, c.drho_dY[i], -c.drho_dp * c.dE_dY[i]) * a;
   }
 }
 
