@@ -6,8 +6,9 @@ namespace gales {
 
 InteriorOps interior_ops_hex8_fp64() { return InteriorDispatch<3, 8, 8, GALES_FORM_FP64>::ops(); }
 
-LaunchResult boundary_hex8(const KParams& k, int nc, long long n, cudaStream_t st) {
-  return boundary_dispatch<3, 8, 6, 4>(k, nc, n, st);
+LaunchResult boundary_hex8(const KParams& k, int nc, int form, long long n, cudaStream_t st) {
+  if (form == GALES_FORM_MIXED) return boundary_hex8_mixed(k, nc, n, st);
+  return boundary_dispatch<3, 8, 6, 4, double>(k, nc, n, st);
 }
 
 GeometryOps geometry_ops_hex8() { return GeometryDispatch<3, 8, 8>::ops(); }

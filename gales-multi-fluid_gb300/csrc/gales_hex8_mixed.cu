@@ -6,4 +6,8 @@ namespace gales {
 
 InteriorOps interior_ops_hex8_mixed() { return InteriorDispatch<3, 8, 8, GALES_FORM_MIXED>::ops(); }
 
+LaunchResult boundary_hex8_mixed(const KParams& k, int nc, long long n, cudaStream_t st) {
+  return boundary_dispatch<3, 8, 6, 4, float>(k, nc, n, st);
+}
+
 }  // namespace gales

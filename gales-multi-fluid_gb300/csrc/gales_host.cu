@@ -823,11 +823,11 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
   return 0;
 }
 
-LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, long long n, cudaStream_t st) {
-  if (h->dim == 2 && h->nen == 3) return boundary_tri3(k, h->nc, n, st);
-  if (h->dim == 2 && h->nen == 4) return boundary_quad4(k, h->nc, n, st);
-  if (h->dim == 3 && h->nen == 4) return boundary_tet4(k, h->nc, n, st);
-  return boundary_hex8(k, h->nc, n, st);
+LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, int form, long long n, cudaStream_t st) {
+  if (h->dim == 2 && h->nen == 3) return boundary_tri3(k, h->nc, form, n, st);
+  if (h->dim == 2 && h->nen == 4) return boundary_quad4(k, h->nc, form, n, st);
+  if (h->dim == 3 && h->nen == 4) return boundary_tet4(k, h->nc, form, n, st);
+  return boundary_hex8(k, h->nc, form, n, st);
 }
 
 // Device-side body of one assembly on device pointers (no host synchronisation).
@@ -872,7 +872,7 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
     kb.el_list = h->d_bd_list.p;
     kb.n_list = (int64_t)h->bd_list.size();
     kb.bd_sides = h->d_bd_sides.p;
-    LaunchResult r = dispatch_boundary(h, kb, kb.n_list, st);
+    LaunchResult r = dispatch_boundary(h, kb, form, kb.n_list, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
     h->launches += r.launches;
   }
@@ -1019,7 +1019,7 @@ int gales_asm_element_blocks(gales_asm* h, const double* I, const double* P, dou
     CK(h, d_sides.alloc(sides.size()), "sides");
     CK(h, cudaMemcpy(d_sides.p, sides.data(), sides.size(), cudaMemcpyHostToDevice), "copy sides");
     k.bd_sides = d_sides.p;
-    r = dispatch_boundary(h, k, n, st);
+    r = dispatch_boundary(h, k, form, n, st);
   }
   if (r.err != cudaSuccess) return cuda_fail(h, r.err, "element kernel");
   h->launches += r.launches;
@@ -1155,7 +1155,7 @@ extern "C" int gales_asm_assemble_noalloc(gales_asm* h, const double* I, const d
     kb.el_list = h->d_bd_list.p;
     kb.n_list = (int64_t)h->bd_list.size();
     kb.bd_sides = h->d_bd_sides.p;
-    LaunchResult r = dispatch_boundary(h, kb, kb.n_list, st);
+    LaunchResult r = dispatch_boundary(h, kb, form, kb.n_list, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
     h->launches += r.launches;
   }

@@ -1258,38 +1258,37 @@ __device__ __forceinline__ int energy_source(int a, int l, int m) {
   return -1;
 }
 
-template <int DIM, int NC>
-__device__ __forceinline__ double k_entry_bd(const Coef<DIM, NC>& c, const gales_side_bc& bc, int k,
+template <int DIM, int NC, typename T>
+__device__ __forceinline__ T k_entry_bd(const Coef<DIM, NC, T>& c, const gales_side_bc& bc, int k,
                                              int l, int r, int col) {
   using L = Layout<DIM, NC>;
-  double x = k_entry<DIM, NC, double>(c, k, l, r, col);
-  if (x == 0.0) return x;
+  T x = k_entry<DIM, NC, T>(c, k, l, r, col);
+  if (x == T(0)) return x;
   auto tau_set = [&](int i, int j) {
     const int lo = i < j ? i : j, hi = i < j ? j : i;
     return (bc.tau_mask >> (lo * 3 + hi)) & 1u;
   };
   if (r >= 1 && r < L::iT && col >= 1 && col < L::iT) {
-    if (tau_set(k, r - 1)) return 0.0;
+    if (tau_set(k, r - 1)) return T(0);
   }
   if (r == L::iT && col >= 1 && col < L::iT) {
     const int j = energy_source<DIM>(k, l, col - 1);
-    if (j >= 0 && tau_set(k, j)) return 0.0;
+    if (j >= 0 && tau_set(k, j)) return T(0);
   }
-  if (k == l && r == L::iT && col == L::iT && ((bc.q_mask >> k) & 1u)) return 0.0;
+  if (k == l && r == L::iT && col == L::iT && ((bc.q_mask >> k) & 1u)) return T(0);
   if (k == l && col >= L::iY) {
     const int i = col - L::iY;
-    if (((bc.J_mask >> (k * 8 + i)) & 1u) && (r == col || r == L::iT)) return 0.0;
+    if (((bc.J_mask >> (k * 8 + i)) & 1u) && (r == col || r == L::iT)) return T(0);
   }
   return x;
 }
 
-template <int DIM, int NC>
-__device__ __forceinline__ double a_entry_bd(const Coef<DIM, NC>& c, const gales_side_bc& bc, int k,
-                                             int r, int col) {
+template <int DIM, int NC, typename T>
+__device__ __forceinline__ T a_entry_bd(const Coef<DIM, NC, T>& c, const gales_side_bc& bc, int k, int r, int col) {
   using L = Layout<DIM, NC>;
-  if (!((bc.mass_flux_mask >> k) & 1u)) return a_entry<DIM, NC, double>(c, k, r, col);
-  const double mf = bc.mass_flux[k];
-  if (r == 1 + k && col == 0) return 1.0;
+  if (!((bc.mass_flux_mask >> k) & 1u)) return a_entry<DIM, NC, T>(c, k, r, col);
+  const T mf = T(bc.mass_flux[k]);
+  if (r == 1 + k && col == 0) return T(1);
   if (r >= 1 && r < L::iT && col == r) return mf;
   if (r == L::iT) {
     if (col == 0) return c.v[k] + mf * c.de_dp;
@@ -1298,43 +1297,45 @@ __device__ __forceinline__ double a_entry_bd(const Coef<DIM, NC>& c, const gales
     return mf * c.dE_dY[col - L::iY];
   }
   if (r >= L::iY && col == r) return mf;
-  return 0.0;
+  return T(0);
 }
 
 // Per boundary point data (one side quadrature point): the state coefficients, the
 // area vector, shape data and the boundary residual vector
 //   rb = sum_k (F_adv,k - F_dif,k) JNxW_k                       (fluid_2d.hpp:343-349)
-template <int DIM, int NEN, int NC>
+template <int DIM, int NEN, int NC, typename S>
 struct BPoint {
   using L = Layout<DIM, NC>;
   static constexpr int ND = L::ND;
-  Coef<DIM, NC> c;
-  double sh[NEN], ds[DIM][NEN], JNxW[DIM], rb[ND];
+  Coef<DIM, NC, S> c;
+  S sh[NEN], ds[DIM][NEN], JNxW[DIM];
+  double shr[NEN], rb[ND];
   int flag;
 };
 
-template <int DIM, int NEN, int NC, int NS, int NSQ>
+template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
 struct BoundarySmem {
   static constexpr int ND = Layout<DIM, NC>::ND, N = NEN * ND;
-  BPoint<DIM, NEN, NC> pt[NS * NSQ];
-  double BA[ND][ND];          // sum_k A'_k JNxW_k
-  double BK[DIM][ND][ND];     // sum_k K'_kl JNxW_k
-  double m[N * N];            // element block accumulator
+  BPoint<DIM, NEN, NC, S> pt[NS * NSQ];
+  S BA[ND][ND];          // sum_k A'_k JNxW_k
+  S BK[DIM][ND][ND];     // sum_k K'_kl JNxW_k
+  S m[N * N];            // element block accumulator
   double r[N];
 };
 
-// Boundary pass, one warp per listed boundary element (FP64 in both forms).
-// Lanes first evaluate one side quadrature point each (thread per point), then
-// build BA and BK entry-parallel per point and accumulate
+// Boundary pass, one warp per listed boundary element.  Lanes first evaluate one
+// side quadrature point each (thread per point, FP64: geometry, EOS, fluxes and the
+// boundary residual), then build BA and BK entry-parallel per point in the form's
+// matrix type S and accumulate
 //   m_ba += N_b (N_a BA - sum_l dN_a/dx_l BK_l)                 (fluid_2d.hpp:351-363)
 // before the element's own Dirichlet pass and scatter (fluid_assembly.hpp:57-63).
-template <int DIM, int NEN, int NC, int NS, int NSQ>
+template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
 __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   using L = Layout<DIM, NC>;
   constexpr int ND = L::ND;
   constexpr int N = NEN * ND;
   constexpr int NT = N * N;
-  using BS = BoundarySmem<DIM, NEN, NC, NS, NSQ>;
+  using BS = BoundarySmem<DIM, NEN, NC, NS, NSQ, S>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BS& B = *reinterpret_cast<BS*>(smem_raw);
   const int lane = threadIdx.x;
@@ -1344,13 +1345,13 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   int nodes[NEN];
 #pragma unroll
   for (int a = 0; a < NEN; ++a) nodes[a] = __ldg(k.conn + e * NEN + a);
-  for (int t = lane; t < NT; t += 32) B.m[t] = 0.0;
+  for (int t = lane; t < NT; t += 32) B.m[t] = S(0);
   for (int t = lane; t < N; t += 32) B.r[t] = 0.0;
   // (1) point physics, one lane per (side, point)
   if (lane < NS * NSQ) {
     const int s = lane / NSQ, iq = lane % NSQ;
     const int flag = k.bd_sides[li * NS + s];
-    BPoint<DIM, NEN, NC>& P = B.pt[lane];
+    BPoint<DIM, NEN, NC, S>& P = B.pt[lane];
     P.flag = flag;
     if (flag > 0) {
       const gales_side_bc& bc = k.side_bc[flag < GALES_MAX_FLAGS ? flag : 0];
@@ -1365,13 +1366,18 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
       Geo<DIM, NEN> q;
       geometry<DIM, NEN>(X, k.sgp[s][iq], false, q);
       if (!(q.J > 0.0)) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
+      double JNxW[DIM];
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) P.JNxW[d] = q.JN[d] * k.W_bd;
+      for (int d = 0; d < DIM; ++d) {
+        JNxW[d] = q.JN[d] * k.W_bd;
+        P.JNxW[d] = to_s<S>(JNxW[d]);
+      }
 #pragma unroll
       for (int i = 0; i < NEN; ++i) {
-        P.sh[i] = q.sh[i];
+        P.sh[i] = to_s<S>(q.sh[i]);
+        P.shr[i] = q.sh[i];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) P.ds[d][i] = q.ds[d][i];
+        for (int d = 0; d < DIM; ++d) P.ds[d][i] = to_s<S>(q.ds[d][i]);
       }
       double Iq[ND], dI[DIM][ND];
 #pragma unroll
@@ -1392,8 +1398,10 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
       assign<DIM, NC>(Iq, p, v, T, Y);
       Props<NC> pr;
       mixture<NC>(k.ch, p, T, Y, pr);
-      make_coef<DIM, NC>(pr, p, v, T, Y, P.c);
-      const Coef<DIM, NC>& c = P.c;
+      Coef<DIM, NC> c;
+      make_coef<DIM, NC>(pr, p, v, T, Y, c);
+      if constexpr (sizeof(S) == 4) P.c = narrow<DIM, NC>(c);
+      else P.c = c;
       // advective flux (fluid_2d.hpp:581-595), mass-flux override (fluid_2d.hpp:674-680, 732-738)
       double Fa[DIM][ND], Fd[DIM][ND];
 #pragma unroll
@@ -1473,11 +1481,11 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
       }
 #pragma unroll
       for (int j = 0; j < ND; ++j) {
-        double x = Fa[0][j] * P.JNxW[0];
+        double x = Fa[0][j] * JNxW[0];
 #pragma unroll
-        for (int d = 1; d < DIM; ++d) x = madd(Fa[d][j], P.JNxW[d], x);
+        for (int d = 1; d < DIM; ++d) x = madd(Fa[d][j], JNxW[d], x);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) x = madd(-Fd[d][j], P.JNxW[d], x);
+        for (int d = 0; d < DIM; ++d) x = madd(-Fd[d][j], JNxW[d], x);
         P.rb[j] = x;
       }
     }
@@ -1485,20 +1493,20 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   __syncwarp();
   // (2) per flagged point: BA, BK entry-parallel, then the block and residual
   for (int ip = 0; ip < NS * NSQ; ++ip) {
-    const BPoint<DIM, NEN, NC>& P = B.pt[ip];
+    const BPoint<DIM, NEN, NC, S>& P = B.pt[ip];
     if (P.flag <= 0) continue;
     const gales_side_bc& bc = k.side_bc[P.flag < GALES_MAX_FLAGS ? P.flag : 0];
     for (int t = lane; t < (1 + DIM) * ND * ND; t += 32) {
       const int w = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
-      double x = 0.0;
+      S x = S(0);
       if (w == 0) {
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) x = madd(a_entry_bd<DIM, NC>(P.c, bc, d, r, col), P.JNxW[d], x);
+        for (int d = 0; d < DIM; ++d) x = madd(a_entry_bd<DIM, NC, S>(P.c, bc, d, r, col), P.JNxW[d], x);
         B.BA[r][col] = x;
       } else {
         const int l = w - 1;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) x = madd(k_entry_bd<DIM, NC>(P.c, bc, d, l, r, col), P.JNxW[d], x);
+        for (int d = 0; d < DIM; ++d) x = madd(k_entry_bd<DIM, NC, S>(P.c, bc, d, l, r, col), P.JNxW[d], x);
         B.BK[l][r][col] = x;
       }
     }
@@ -1506,23 +1514,23 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
     for (int t = lane; t < NT; t += 32) {
       const int row = t / N, colx = t % N;
       const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-      double x = P.sh[a] * B.BA[jb][ja];
+      S x = P.sh[a] * B.BA[jb][ja];
 #pragma unroll
       for (int l = 0; l < DIM; ++l) x = madd(-P.ds[l][a], B.BK[l][jb][ja], x);
       B.m[t] = madd(P.sh[b], x, B.m[t]);
     }
-    for (int t = lane; t < N; t += 32) B.r[t] = madd(P.sh[t / ND], P.rb[t % ND], B.r[t]);
+    for (int t = lane; t < N; t += 32) B.r[t] = madd(P.shr[t / ND], P.rb[t % ND], B.r[t]);
     __syncwarp();
   }
   if (k.local_r) {  // element-level output of execute_b: m = m_, r = -r_
     for (int t = lane; t < N; t += 32) k.local_r[li * N + t] = -B.r[t];
     if (k.local_m)
-      for (int t = lane; t < NT; t += 32) k.local_m[li * NT + t] = B.m[t];
+      for (int t = lane; t < NT; t += 32) k.local_m[li * NT + t] = widen(B.m[t]);
     return;
   }
   // second scatter pass with its own Dirichlet average (scatter.hpp:62-78)
   double avg = 1.0;
-  for (int i = 0; i < N; ++i) avg += B.m[i * N + i];
+  for (int i = 0; i < N; ++i) avg += widen(B.m[i * N + i]);
   avg /= N;
   uint32_t blocked[NEN];
   int64_t rowbase[NEN];
@@ -1546,7 +1554,7 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
     for (int t = lane; t < NT; t += 32) {
       const int row = t / N, colx = t % N;
       const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-      double val = B.m[t];
+      double val = widen(B.m[t]);
       if ((blocked[b] >> jb) & 1u) val = (row == colx) ? avg : 0.0;
       if (val != 0.0) {
         const int64_t off = rowbase[b] + (int64_t)jb * rowlen[b] +

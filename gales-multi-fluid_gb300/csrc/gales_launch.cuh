@@ -50,11 +50,11 @@ struct InteriorInst {
   }
 };
 
-template <int DIM, int NEN, int NC, int NS, int NSQ>
+template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
 LaunchResult launch_boundary_nc(const KParams& k, long long n_items, cudaStream_t st) {
   if (n_items == 0) return {cudaSuccess, 0};
-  const size_t smem = sizeof(BoundarySmem<DIM, NEN, NC, NS, NSQ>);
-  auto fn = boundary_kernel<DIM, NEN, NC, NS, NSQ>;
+  const size_t smem = sizeof(BoundarySmem<DIM, NEN, NC, NS, NSQ, S>);
+  auto fn = boundary_kernel<DIM, NEN, NC, NS, NSQ, S>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return {e, 0};
   fn<<<(unsigned)n_items, 32, smem, st>>>(k);
@@ -103,9 +103,10 @@ struct InteriorDispatch {
   static InteriorOps ops() { return {&rec_bytes, &point, &matrix}; }
 };
 
-template <int DIM, int NEN, int NS, int NSQ>
+// Boundary pass of one element type; S is the matrix arithmetic type of the form.
+template <int DIM, int NEN, int NS, int NSQ, typename S>
 LaunchResult boundary_dispatch(const KParams& k, int nc, long long n, cudaStream_t st) {
-#define GALES_C(NC) return launch_boundary_nc<DIM, NEN, NC, NS, NSQ>(k, n, st)
+#define GALES_C(NC) return launch_boundary_nc<DIM, NEN, NC, NS, NSQ, S>(k, n, st)
   GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
   return {cudaErrorInvalidValue, 0};
@@ -135,19 +136,23 @@ struct GeometryDispatch {
 // Entry points defined by the per-element translation units.
 InteriorOps interior_ops_tri3_fp64();
 InteriorOps interior_ops_tri3_mixed();
-LaunchResult boundary_tri3(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult boundary_tri3(const KParams&, int nc, int form, long long n, cudaStream_t);
+LaunchResult boundary_tri3_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_tri3();
 InteriorOps interior_ops_quad4_fp64();
 InteriorOps interior_ops_quad4_mixed();
-LaunchResult boundary_quad4(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult boundary_quad4(const KParams&, int nc, int form, long long n, cudaStream_t);
+LaunchResult boundary_quad4_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_quad4();
 InteriorOps interior_ops_tet4_fp64();
 InteriorOps interior_ops_tet4_mixed();
-LaunchResult boundary_tet4(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult boundary_tet4(const KParams&, int nc, int form, long long n, cudaStream_t);
+LaunchResult boundary_tet4_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_tet4();
 InteriorOps interior_ops_hex8_fp64();
 InteriorOps interior_ops_hex8_mixed();
-LaunchResult boundary_hex8(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult boundary_hex8(const KParams&, int nc, int form, long long n, cudaStream_t);
+LaunchResult boundary_hex8_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_hex8();
 
 }  // namespace gales

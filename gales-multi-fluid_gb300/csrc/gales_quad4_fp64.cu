@@ -6,8 +6,9 @@ namespace gales {
 
 InteriorOps interior_ops_quad4_fp64() { return InteriorDispatch<2, 4, 4, GALES_FORM_FP64>::ops(); }
 
-LaunchResult boundary_quad4(const KParams& k, int nc, long long n, cudaStream_t st) {
-  return boundary_dispatch<2, 4, 4, 2>(k, nc, n, st);
+LaunchResult boundary_quad4(const KParams& k, int nc, int form, long long n, cudaStream_t st) {
+  if (form == GALES_FORM_MIXED) return boundary_quad4_mixed(k, nc, n, st);
+  return boundary_dispatch<2, 4, 4, 2, double>(k, nc, n, st);
 }
 
 GeometryOps geometry_ops_quad4() { return GeometryDispatch<2, 4, 4>::ops(); }

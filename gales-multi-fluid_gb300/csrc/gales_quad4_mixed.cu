@@ -6,4 +6,8 @@ namespace gales {
 
 InteriorOps interior_ops_quad4_mixed() { return InteriorDispatch<2, 4, 4, GALES_FORM_MIXED>::ops(); }
 
+LaunchResult boundary_quad4_mixed(const KParams& k, int nc, long long n, cudaStream_t st) {
+  return boundary_dispatch<2, 4, 4, 2, float>(k, nc, n, st);
+}
+
 }  // namespace gales

@@ -6,8 +6,9 @@ namespace gales {
 
 InteriorOps interior_ops_tet4_fp64() { return InteriorDispatch<3, 4, 4, GALES_FORM_FP64>::ops(); }
 
-LaunchResult boundary_tet4(const KParams& k, int nc, long long n, cudaStream_t st) {
-  return boundary_dispatch<3, 4, 4, 3>(k, nc, n, st);
+LaunchResult boundary_tet4(const KParams& k, int nc, int form, long long n, cudaStream_t st) {
+  if (form == GALES_FORM_MIXED) return boundary_tet4_mixed(k, nc, n, st);
+  return boundary_dispatch<3, 4, 4, 3, double>(k, nc, n, st);
 }
 
 GeometryOps geometry_ops_tet4() { return GeometryDispatch<3, 4, 4>::ops(); }

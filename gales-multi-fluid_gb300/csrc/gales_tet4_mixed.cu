@@ -6,4 +6,8 @@ namespace gales {
 
 InteriorOps interior_ops_tet4_mixed() { return InteriorDispatch<3, 4, 4, GALES_FORM_MIXED>::ops(); }
 
+LaunchResult boundary_tet4_mixed(const KParams& k, int nc, long long n, cudaStream_t st) {
+  return boundary_dispatch<3, 4, 4, 3, float>(k, nc, n, st);
+}
+
 }  // namespace gales

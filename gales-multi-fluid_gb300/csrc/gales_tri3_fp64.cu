@@ -6,8 +6,9 @@ namespace gales {
 
 InteriorOps interior_ops_tri3_fp64() { return InteriorDispatch<2, 3, 3, GALES_FORM_FP64>::ops(); }
 
-LaunchResult boundary_tri3(const KParams& k, int nc, long long n, cudaStream_t st) {
-  return boundary_dispatch<2, 3, 3, 2>(k, nc, n, st);
+LaunchResult boundary_tri3(const KParams& k, int nc, int form, long long n, cudaStream_t st) {
+  if (form == GALES_FORM_MIXED) return boundary_tri3_mixed(k, nc, n, st);
+  return boundary_dispatch<2, 3, 3, 2, double>(k, nc, n, st);
 }
 
 GeometryOps geometry_ops_tri3() { return GeometryDispatch<2, 3, 3>::ops(); }
