@@ -38,18 +38,40 @@ struct DevChem {
 };
 
 // Round-to-nearest-even narrowing of binary64 to binary32 with integer operations
-// (52-bit mantissa cut to 23 bits, ties to even, carry into the exponent).  Values
-// whose binary32 result is zero, subnormal, infinite or NaN take the hardware path.
+// only (52-bit significand cut to 23 bits, ties to even, carry into the exponent;
+// overflow to infinity, gradual underflow to subnormals and zero, NaN kept quiet).
+// On this GPU the hardware conversion issues on the FP64 pipe, which the point
+// stage already saturates; every special case is integer work too, so no path
+// falls back to the conversion instruction.
 __device__ __forceinline__ float narrow_rn(double d) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(d);
-  const unsigned int hi = (unsigned int)(u >> 32);
-  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-  if (e <= 0 || e >= 255) return (float)d;
-  const unsigned int m = (unsigned int)((u >> 29) & 0x7fffffu);
-  const unsigned int rest = (unsigned int)(u & 0x1fffffffu);
-  unsigned int bits = (hi & 0x80000000u) | ((unsigned int)e << 23) | m;
-  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
-  return __uint_as_float(bits);
+  const unsigned int sign = (unsigned int)(u >> 32) & 0x80000000u;
+  const int e64 = (int)((u >> 52) & 0x7ffu);
+  const unsigned long long m52 = u & 0xfffffffffffffull;
+  const int e = e64 - (1023 - 127);
+  unsigned int bits;
+  if (e64 == 0x7ff) {
+    bits = 0x7f800000u | (unsigned int)(m52 >> 29) | (m52 ? 0x400000u : 0u);
+  } else if (e >= 255) {
+    bits = 0x7f800000u;
+  } else if (e > 0) {
+    const unsigned int m = (unsigned int)(m52 >> 29);
+    const unsigned int rest = (unsigned int)(u & 0x1fffffffu);
+    bits = ((unsigned int)e << 23) | m;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
+  } else {
+    // binary32 subnormal or zero: significand (with its leading one) >> (30 - e)
+    const int r = 30 - e;
+    if (r > 54 || e64 == 0) {
+      bits = 0u;
+    } else {
+      const unsigned long long M = m52 | (1ull << 52);
+      const unsigned long long q = M >> r, rem = M & ((1ull << r) - 1ull), half = 1ull << (r - 1);
+      bits = (unsigned int)q;
+      if (rem > half || (rem == half && (q & 1ull))) bits += 1u;
+    }
+  }
+  return __uint_as_float(sign | bits);
 }
 
 template <typename S>
