@@ -422,6 +422,12 @@ class FluidAssembly:
                                           _addr(g_state), _addr(g_params) if g_params is not None else None,
                                           stream or None))
 
+    def norm2(self, rhs) -> float:
+        """||b||_2 on the device (residual_check.hpp:48-51)."""
+        out = C.c_double()
+        self._check(self._L.gales_asm_norm2(self._h, _addr(rhs), C.byref(out), None))
+        return out.value
+
     def element_blocks(self, I, P, dt: float, elements, which: int = 0, form: int = FORM_FP64,
                        want_matrix: bool = True):
         """Batched fluid::execute_i (which=0) / execute_b (which=1): local (m, r) per element."""

@@ -17,7 +17,8 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = HERE / "libgales_asm.so"
-SOURCES = ["gales_host.cu"] + [f"gales_{t}_{f}.cu" for t in ("hex8", "tet4", "tri3", "quad4") for f in ("fp64", "mixed")]
+SOURCES = (["gales_host.cu"] + [f"gales_{t}_{f}.cu" for t in ("hex8", "tet4", "tri3", "quad4") for f in ("fp64", "mixed")]
+           + [f"gales_vjp_{t}.cu" for t in ("hex8", "tet4", "tri3", "quad4")])
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no implicit contraction (see gales_physics.cuh); hot loops use explicit fma
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

@@ -145,6 +145,7 @@ void parallel_for(int64_t n, F f) {
 
 // Each point-record chunk buffer holds this many bytes; two of them stay resident
 // in L2 (about a quarter of the 129 MB) while the CSR values stream through it.
+constexpr int kVjpAux = 3 * GALES_MAX_COMP + GALES_MAX_ND;
 constexpr size_t kChunkBytes = size_t(32) << 20;
 
 GeometryOps geometry_ops(int dim, int nen) {
@@ -222,9 +223,12 @@ struct gales_asm {
   DevBuf<gales_side_bc> d_side_bc;
   DevBuf<unsigned int> d_status;
   DevBuf<unsigned long long> d_first_bad;
-  DevBuf<double> s_I, s_P, s_vals, s_rhs, s_aux;  // staging for host pointers
+  DevBuf<double> s_I, s_P, s_vals, s_rhs, s_aux, s_lam, s_th;  // staging for host pointers
+  DevBuf<double> d_vjp;                          // theta and u_ref_inv cotangents of the exact VJP
+  double* h_vjp = nullptr;                       // pinned copy of d_vjp
   unsigned int* h_status = nullptr;              // pinned
   unsigned long long* h_first_bad = nullptr;
+  double* h_aux = nullptr;                       // pinned scalar
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t evp[4] = {nullptr, nullptr, nullptr, nullptr};  // clear | interior | boundary | end
   int32_t scatter_mode = GALES_SCATTER_ATOMIC;
@@ -302,6 +306,59 @@ void compute_u_ref_inv(gales_asm* h) {
   u[dim + 1] = rho * E;
   for (int i = 0; i < nc - 1; ++i) u[dim + 2 + i] = rho * 0.5;
   for (int i = 0; i < h->nd; ++i) h->u_ref_inv[i] = (u[i] < DBL_EPSILON) ? 0.0 : 1.0 / u[i];
+}
+
+// Reverse of compute_u_ref_inv: the cotangents urib of u_ref_inv = 1/U_ref, with U_ref
+// the conservative vector of the mixture at (p_ref, T_ref, v_ref, Y_ref = 0.5), folded
+// into the parameter cotangents th (theta_c = (density parameter, mu_c, cp_c); the
+// density parameter of an ideal gas is its molar mass, R = R_u/M, cv = cp - R).
+void u_ref_inv_reverse(const gales_asm* h, const double* urib, double* th) {
+  if (!h->setup.dc_2006) return;
+  const int nc = h->nc, dim = h->dim;
+  const double p = h->setup.p_ref, T = h->setup.T_ref;
+  double irho = 0.0, cv = 0.0, r[GALES_MAX_COMP], vc[GALES_MAX_COMP];
+  for (int c = 0; c < nc; ++c) {
+    const gales_chemical_desc& q = h->mat.comp[c];
+    if (q.kind == GALES_CH_CUSTOM) {
+      r[c] = q.rho;
+      vc[c] = (q.beta == 0.0) ? q.cp : q.cp - T * q.alpha * q.alpha / (r[c] * q.beta);
+    } else {
+      r[c] = p / (q.R * T);
+      vc[c] = q.cv;
+    }
+    irho += 0.5 / r[c];
+    cv += 0.5 * vc[c];
+  }
+  const double rho = 1.0 / irho;
+  double v2 = 0.0;
+  for (int k = 0; k < dim; ++k) v2 += h->setup.v_ref[k] * h->setup.v_ref[k];
+  const double E = cv * T + 0.5 * v2;
+  // u = (rho, rho v_ref, rho E, rho/2 ...); u_ref_inv = 1/u where u >= eps
+  double rhob = 0.0, Eb = 0.0;
+  for (int j = 0; j < h->nd; ++j) {
+    const double uri = h->u_ref_inv[j];
+    if (uri == 0.0) continue;
+    const double ub = -urib[j] * uri * uri;
+    if (j == 0) rhob += ub;
+    else if (j <= dim) rhob += ub * h->setup.v_ref[j - 1];
+    else if (j == dim + 1) { rhob += ub * E; Eb += ub * rho; }
+    else rhob += ub * 0.5;
+  }
+  const double cvb = Eb * T;
+  for (int c = 0; c < nc; ++c) {
+    const gales_chemical_desc& q = h->mat.comp[c];
+    const double rb = rhob * rho * rho * 0.5 / (r[c] * r[c]);
+    const double vb = 0.5 * cvb;
+    if (q.kind == GALES_CH_CUSTOM) {
+      th[3 * c + 0] += rb;
+      if (q.beta != 0.0) th[3 * c + 0] += vb * T * q.alpha * q.alpha / (r[c] * r[c] * q.beta);
+      th[3 * c + 2] += vb;
+    } else {
+      double Rb = rb * (-r[c] / q.R) - vb;
+      th[3 * c + 2] += vb;
+      th[3 * c + 0] += Rb * (-q.R * q.R / 8.314462);
+    }
+  }
 }
 
 // Node graph of linear_system.hpp:46-63 on one rank: sorted unique neighbours.
@@ -620,6 +677,8 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   if ((ce = h->d_first_bad.alloc(1)) != cudaSuccess) return bail(ce, "first_bad");
   if ((ce = cudaMallocHost(&h->h_status, sizeof(unsigned int))) != cudaSuccess) return bail(ce, "pinned");
   if ((ce = cudaMallocHost(&h->h_first_bad, sizeof(unsigned long long))) != cudaSuccess) return bail(ce, "pinned");
+  if ((ce = cudaMallocHost(&h->h_aux, sizeof(double))) != cudaSuccess) return bail(ce, "pinned");
+  if ((ce = cudaMallocHost(&h->h_vjp, kVjpAux * sizeof(double))) != cudaSuccess) return bail(ce, "pinned");
   if ((ce = cudaEventCreate(&h->ev0)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(ce, "event");
   for (int i = 0; i < 4; ++i)
@@ -664,8 +723,12 @@ void gales_asm_destroy(gales_asm* h) {
   h->d_slot.release(); h->d_bd_sides.release(); h->d_side_bc.release();
   h->d_status.release(); h->d_first_bad.release(); h->d_geo.release();
   h->s_I.release(); h->s_P.release(); h->s_vals.release(); h->s_rhs.release(); h->s_aux.release();
+  h->s_lam.release(); h->s_th.release();
   if (h->h_status) cudaFreeHost(h->h_status);
   if (h->h_first_bad) cudaFreeHost(h->h_first_bad);
+  if (h->h_aux) cudaFreeHost(h->h_aux);
+  if (h->h_vjp) cudaFreeHost(h->h_vjp);
+  h->d_vjp.release();
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (int i = 0; i < 4; ++i)
@@ -828,6 +891,50 @@ LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, int form, long lo
   if (h->dim == 2 && h->nen == 4) return boundary_quad4(k, h->nc, form, n, st);
   if (h->dim == 3 && h->nen == 4) return boundary_tet4(k, h->nc, form, n, st);
   return boundary_hex8(k, h->nc, form, n, st);
+}
+
+LaunchResult dispatch_vjp(gales_asm* h, const KParams& k, bool boundary, long long n, cudaStream_t st) {
+  if (h->dim == 2 && h->nen == 3) return boundary ? vjp_boundary_tri3(k, h->nc, n, st) : vjp_interior_tri3(k, h->nc, n, st);
+  if (h->dim == 2 && h->nen == 4)
+    return boundary ? vjp_boundary_quad4(k, h->nc, n, st) : vjp_interior_quad4(k, h->nc, n, st);
+  if (h->dim == 3 && h->nen == 4) return boundary ? vjp_boundary_tet4(k, h->nc, n, st) : vjp_interior_tet4(k, h->nc, n, st);
+  return boundary ? vjp_boundary_hex8(k, h->nc, n, st) : vjp_interior_hex8(k, h->nc, n, st);
+}
+
+// ||b||_2 of a vector (residual_check.hpp:48-51): per-block sums of squares in a fixed
+// order, then one block adds the partials, so the result does not depend on timing.
+constexpr int kNormBlocks = 256;
+
+__global__ void __launch_bounds__(256) norm_partial_kernel(const double* __restrict__ x, long long n,
+                                                            double* __restrict__ part) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * 256 + threadIdx.x; i < n; i += (long long)gridDim.x * 256)
+    s = fma(x[i], x[i], s);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(256) norm_final_kernel(double* part) {
+  __shared__ double sh[256];
+  sh[threadIdx.x] = part[threadIdx.x];
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[kNormBlocks] = sqrt(sh[0]);
+}
+
+cudaError_t launch_norm2(const double* x, long long n, double* part, cudaStream_t st) {
+  norm_partial_kernel<<<kNormBlocks, 256, 0, st>>>(x, n, part);
+  norm_final_kernel<<<1, 256, 0, st>>>(part);
+  return cudaGetLastError();
 }
 
 // Device-side body of one assembly on device pointers (no host synchronisation).
@@ -1030,15 +1137,128 @@ int gales_asm_element_blocks(gales_asm* h, const double* I, const double* P, dou
   return rc;
 }
 
-int gales_asm_vjp(gales_asm* h, const double*, const double*, double, const double*, int32_t, double*, double*,
-                  void*) {
-  return fail(h, GALES_ERR_UNSUPPORTED, "vjp not available in this build");
+int gales_asm_vjp(gales_asm* h, const double* I, const double* P, double dt, const double* lambda, int32_t mode,
+                  double* g_state, double* g_params, void* stream) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (!I || !P || !lambda || !g_state) return fail(h, GALES_ERR_BAD_INPUT, "null argument");
+  if (mode != GALES_VJP_EXACT && mode != GALES_VJP_FROZEN) return fail(h, GALES_ERR_BAD_INPUT, "unknown VJP mode");
+  if (!(dt > 0.0)) return fail(h, GALES_ERR_BAD_INPUT, "dt must be positive");
+  if (mode == GALES_VJP_EXACT && h->setup.tau != GALES_TAU_NON_DIAG_COMP_2019 && h->setup.tau != GALES_TAU_NONE)
+    return fail(h, GALES_ERR_UNSUPPORTED, "the exact VJP is available for tau 2019 and tau none");
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t sb = (size_t)h->n_rows * sizeof(double);
+  const int npar = 3 * h->nc;
+  const double* dI = I;
+  const double* dP = P;
+  const double* dlam = lambda;
+  double* dg = g_state;
+  double* dth = g_params;
+  const bool hI = !is_device_ptr(I), hP = !is_device_ptr(P), hL = !is_device_ptr(lambda);
+  const bool hG = !is_device_ptr(g_state), hT = g_params && !is_device_ptr(g_params);
+  CK(h, cudaEventRecord(h->ev0, st), "event");
+  if (hI) {
+    CK(h, h->s_I.alloc(h->n_rows), "staging I");
+    CK(h, cudaMemcpyAsync(h->s_I.p, I, sb, cudaMemcpyHostToDevice, st), "copy I");
+    dI = h->s_I.p;
+  }
+  if (hP) {
+    CK(h, h->s_P.alloc(h->n_rows), "staging P");
+    CK(h, cudaMemcpyAsync(h->s_P.p, P, sb, cudaMemcpyHostToDevice, st), "copy P");
+    dP = h->s_P.p;
+  }
+  if (hL) {
+    CK(h, h->s_lam.alloc(h->n_rows), "staging lambda");
+    CK(h, cudaMemcpyAsync(h->s_lam.p, lambda, sb, cudaMemcpyHostToDevice, st), "copy lambda");
+    dlam = h->s_lam.p;
+  }
+  if (hG) {
+    CK(h, h->s_rhs.alloc(h->n_rows), "staging g_state");
+    dg = h->s_rhs.p;
+  }
+  CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
+  CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  CK(h, cudaMemsetAsync(dg, 0, sb, st), "memset g_state");
+  const bool want_th = mode == GALES_VJP_EXACT && g_params != nullptr;
+  if (want_th) {
+    CK(h, h->d_vjp.alloc(kVjpAux), "vjp scratch");
+    CK(h, cudaMemsetAsync(h->d_vjp.p, 0, kVjpAux * sizeof(double), st), "memset vjp scratch");
+  }
+  KParams k = base_params(h, dt);
+  k.I = dI;
+  k.P = dP;
+  k.vjp_lam = dlam;
+  k.vjp_g = dg;
+  k.vjp_th = want_th ? h->d_vjp.p : nullptr;
+  k.scatter_mode = 0;
+  k.el_list = h->d_sweep.p;
+  k.n_list = h->n_el;
+  KParams kb = k;
+  kb.el_list = h->d_bd_list.p;
+  kb.n_list = (int64_t)h->bd_list.size();
+  kb.bd_sides = h->d_bd_sides.p;
+  if (mode == GALES_VJP_EXACT) {
+    LaunchResult r = dispatch_vjp(h, k, false, h->n_el, st);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "vjp interior kernel");
+    h->launches += r.launches;
+    if (kb.n_list > 0) {
+      r = dispatch_vjp(h, kb, true, kb.n_list, st);
+      if (r.err != cudaSuccess) return cuda_fail(h, r.err, "vjp boundary kernel");
+      h->launches += r.launches;
+    }
+  } else {
+    // the FP64 tangent, contracted with lambda by the matrix and boundary kernels
+    int rc = run_interior(h, k, GALES_FORM_FP64, true, h->n_el, st, true);
+    if (rc) return rc;
+    if (kb.n_list > 0) {
+      LaunchResult r = dispatch_boundary(h, kb, GALES_FORM_FP64, kb.n_list, st);
+      if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
+      h->launches += r.launches;
+    }
+  }
+  if (hG) CK(h, cudaMemcpyAsync(g_state, dg, sb, cudaMemcpyDeviceToHost, st), "copy g_state");
+  if (want_th) CK(h, cudaMemcpyAsync(h->h_vjp, h->d_vjp.p, kVjpAux * sizeof(double), cudaMemcpyDeviceToHost, st),
+                  "copy vjp scratch");
+  CK(h, cudaEventRecord(h->ev1, st), "event");
+  int rc = finish(h, st);
+  if (g_params) {
+    // theta cotangents plus the path through u_ref_inv (host arithmetic on nd values)
+    double th[3 * GALES_MAX_COMP];
+    for (int i = 0; i < npar; ++i) th[i] = want_th ? h->h_vjp[i] : 0.0;
+    if (want_th) u_ref_inv_reverse(h, h->h_vjp + npar, th);
+    if (hT) {
+      memcpy(g_params, th, npar * sizeof(double));
+    } else {
+      CK(h, cudaMemcpyAsync(dth, th, npar * sizeof(double), cudaMemcpyHostToDevice, st), "copy g_params");
+      CK(h, cudaStreamSynchronize(st), "synchronize");
+    }
+  }
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  return rc;
 }
 
 int gales_asm_norm2(gales_asm* h, const double* rhs, double* out, void* stream) {
-  (void)stream;
   if (!h || !rhs || !out) return GALES_ERR_BAD_INPUT;
-  return fail(h, GALES_ERR_UNSUPPORTED, "norm2 not available in this build");
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const double* d = rhs;
+  if (!is_device_ptr(rhs)) {
+    CK(h, h->s_aux.alloc(h->n_rows + kNormBlocks + 1), "staging rhs");
+    CK(h, cudaMemcpyAsync(h->s_aux.p, rhs, (size_t)h->n_rows * sizeof(double), cudaMemcpyHostToDevice, st),
+       "copy rhs");
+    d = h->s_aux.p;
+  }
+  CK(h, h->s_th.alloc(kNormBlocks + 1 > 3 * GALES_MAX_COMP ? kNormBlocks + 1 : 3 * GALES_MAX_COMP), "norm scratch");
+  CK(h, launch_norm2(d, h->n_rows, h->s_th.p, st), "norm kernel");
+  h->launches += 2;
+  double r = 0.0;
+  CK(h, cudaMemcpyAsync(h->h_aux, h->s_th.p + kNormBlocks, sizeof(double), cudaMemcpyDeviceToHost, st), "copy norm");
+  CK(h, cudaStreamSynchronize(st), "synchronize");
+  r = *h->h_aux;
+  *out = r;
+  return 0;
 }
 
 int gales_asm_status(gales_asm* h, int64_t* first_bad_element) {

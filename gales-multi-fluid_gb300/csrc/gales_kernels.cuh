@@ -64,6 +64,11 @@ struct KParams {
   double sh_tab[8][8];         // shape functions at the interior points [q][node]
   double* local_m;             // element-level output [n_list][(nen*nd)^2] (no scatter) or null
   double* local_r;             // element-level output [n_list][nen*nd] (r = -r_) or null
+  // vector-Jacobian products: lambda, g_state (+=) and g_params (+=); when vjp_lam is set
+  // the matrix and boundary kernels contract their blocks with lambda instead of scattering
+  const double* vjp_lam;
+  double* vjp_g;
+  double* vjp_th;
 };
 
 __device__ __forceinline__ void flag_error(const KParams& k, unsigned int bits, long long e) {
@@ -1230,6 +1235,16 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
     }
     elem_sync<WPE>(ec);
   }
+  if (WANT_M && k.vjp_lam) {
+    // frozen-tangent VJP: g += K^T lambda for this element's block (Dirichlet rows included)
+    for (int cx = gl; cx < N; cx += ET) {
+      double sum = 0.0;
+      for (int rw = 0; rw < N; ++rw)
+        sum += __ldg(k.vjp_lam + (long long)E.nodes[rw / ND] * ND + rw % ND) * E.u.stage[rw * NS + cx];
+      if (sum != 0.0) atomicAdd(k.vjp_g + (long long)E.nodes[cx / ND] * ND + cx % ND, sum);
+    }
+    return;
+  }
   if (local) {  // element-level output of execute_i (fluid_2d.hpp:200-201): m = m_, r = -r_
     if (active && grp == 0) k.local_r[g * N + row] = -widen(racc);
     if (WANT_M && k.local_m)
@@ -1552,6 +1567,19 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
     const int64_t r0 = __ldg(k.node_rp + nodes[a]), r1 = __ldg(k.node_rp + nodes[a] + 1);
     rowbase[a] = r0 * (int64_t)(ND * ND);
     rowlen[a] = (int32_t)((r1 - r0) * ND);
+  }
+  if (k.vjp_lam) {
+    // frozen-tangent VJP: g += K^T lambda for this element's boundary block
+    for (int cx = lane; cx < N; cx += 32) {
+      double sum = 0.0;
+      for (int rw = 0; rw < N; ++rw) {
+        const int b = rw / ND, jb = rw % ND;
+        const double val = ((blocked[b] >> jb) & 1u) ? (rw == cx ? avg : 0.0) : widen(B.m[rw * N + cx]);
+        sum += __ldg(k.vjp_lam + (long long)nodes[b] * ND + jb) * val;
+      }
+      if (sum != 0.0) atomicAdd(k.vjp_g + (long long)nodes[cx / ND] * ND + cx % ND, sum);
+    }
+    return;
   }
   const int mode = k.scatter_mode;
   for (int t = lane; t < N; t += 32) {

@@ -152,6 +152,15 @@ GeometryOps geometry_ops_tet4();
 InteriorOps interior_ops_hex8_fp64();
 InteriorOps interior_ops_hex8_mixed();
 LaunchResult boundary_hex8(const KParams&, int nc, int form, long long n, cudaStream_t);
+// exact VJP kernels (gales_vjp_<type>.cu)
+LaunchResult vjp_interior_tri3(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult vjp_boundary_tri3(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult vjp_interior_quad4(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult vjp_boundary_quad4(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult vjp_interior_tet4(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult vjp_boundary_tet4(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult vjp_interior_hex8(const KParams&, int nc, long long n, cudaStream_t);
+LaunchResult vjp_boundary_hex8(const KParams&, int nc, long long n, cudaStream_t);
 LaunchResult boundary_hex8_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_hex8();
 

@@ -11,7 +11,9 @@
 // point_reverse propagates cotangents (phi0_bar, phi_d_bar) back to Iq, dI and theta
 // by hand-written reverse mode through tau (with compute_h and the DUDY inverse),
 // the dc viscosity, the mixture EOS and U_P.  Nothing is stored between calls: the
-// caller recomputes the point from the state.
+// caller recomputes the point from the state.  The dc scaling u_ref_inv is itself a
+// function of theta (fluid_2d.hpp:123-135, the mixture at p_ref, T_ref, Y_ref); its
+// cotangent is returned in urib for the caller to fold into theta.
 //
 // Parameterisation (the derivative's meaning):
 //   custom chemical (chemicals.hpp:19-49): theta = (rho_c, mu_c, cp_c); alpha, beta,
@@ -853,7 +855,7 @@ GV_HD void point_reverse(const Ctx<DIM, NC>& x, const PGeo<DIM, NEN>& q, const d
                          const double (&dI)[DIM][Layout<DIM, NC>::ND], const double* Pq,
                          const PTape<DIM, NEN, NC>& t, const double* phi0b,
                          const double (&phib)[DIM][Layout<DIM, NC>::ND], double* Ib,
-                         double (&dIb)[DIM][Layout<DIM, NC>::ND], double* th) {
+                         double (&dIb)[DIM][Layout<DIM, NC>::ND], double* th, double* urib = nullptr) {
   using L = Layout<DIM, NC>;
   constexpr int ND = L::ND;
   const Cf<DIM, NC>& c = t.c;
@@ -995,18 +997,25 @@ GV_HD void point_reverse(const Ctx<DIM, NC>& x, const PGeo<DIM, NEN>& q, const d
         const double g = Znb * t.Z[j] / t.Zn * x.u_ref_inv[j];
         AdIb[j] += g;
         Sb[j] -= g;
+        if (urib) urib[j] += Znb * t.Z[j] / t.Zn * (t.AdI[j] - t.S[j]);
       }
     }
     // Un = |u_ref_inv U|
     if (t.Un > 0.0) {
 #pragma unroll
-      for (int j = 0; j < ND; ++j) Ub[j] += Unb * x.u_ref_inv[j] * x.u_ref_inv[j] * t.U[j] / t.Un;
+      for (int j = 0; j < ND; ++j) {
+        Ub[j] += Unb * x.u_ref_inv[j] * x.u_ref_inv[j] * t.U[j] / t.Un;
+        if (urib) urib[j] += Unb * x.u_ref_inv[j] * t.U[j] * t.U[j] / t.Un;
+      }
     }
     // use1 = sum_d |u_ref_inv dU_d|^2
 #pragma unroll
     for (int d = 0; d < DIM; ++d)
 #pragma unroll
-      for (int j = 0; j < ND; ++j) dUb[d][j] += use1b * 2.0 * x.u_ref_inv[j] * x.u_ref_inv[j] * t.dU[d][j];
+      for (int j = 0; j < ND; ++j) {
+        dUb[d][j] += use1b * 2.0 * x.u_ref_inv[j] * x.u_ref_inv[j] * t.dU[d][j];
+        if (urib) urib[j] += use1b * 2.0 * x.u_ref_inv[j] * t.dU[d][j] * t.dU[d][j];
+      }
     // hdc = 1/sJ, sJ = sum_i |J . dN_i|, J = grho/|grho|, grho_d = dU_d[0]
     const double sJb = -hdb / (t.sJ * t.sJ);
     double Jb[DIM];

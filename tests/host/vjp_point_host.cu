@@ -118,6 +118,7 @@ void brev(const DevChem* ch, const double* scal, const double* uri, const gales_
 GV_BINST(3, 3)
 GV_BINST(2, 2)
 GV_BINST(3, 4)
+GV_BINST(3, 1)
 
 #define GV_INST(DIM, NEN, NC)                                                                               \
   extern "C" void pt_forward_##DIM##_##NEN##_##NC(const DevChem* ch, const double* scal, const double* uri, \

@@ -183,11 +183,11 @@ def _side_bc(kind, dim, nc):
     return bc
 
 
-@pytest.mark.parametrize("dim,nc", [(3, 3), (2, 2), (3, 4)])
+@pytest.mark.parametrize("dim,nc", [(3, 3), (2, 2), (3, 4), (3, 1)])
 @pytest.mark.parametrize("kind", ["none", "tau", "q", "J", "mf"])
 def test_boundary_point_vjp_matches_central_differences(lib, dim, nc, kind):
     for seed in range(3):
-        pt = Point(lib, dim, {(3, 3): 4, (2, 2): 3, (3, 4): 8}[(dim, nc)], nc, seed)
+        pt = Point(lib, dim, {(3, 3): 4, (2, 2): 3, (3, 4): 8, (3, 1): 4}[(dim, nc)], nc, seed)
         bc = _side_bc(kind, dim, nc)
         rng = np.random.default_rng(7 + seed)
         JN = rng.normal(0, 1e-3, dim)
