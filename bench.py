@@ -145,6 +145,182 @@ def cpu_oracle_rate(mesh, mat, setup, I, P, dt, row_ptr, col, colour, n_colours,
     return rate, nthreads, n
 
 
+BYTES_PER_ELEM_HEX = 4 * 8 + 8 * 3 * 8 + 2 * 8 * 8 * 8 + 16 * (8 * 8) ** 2 + 16 * 8 * 8  # 67,808
+
+
+def top_gas_flux_lambda(mesh, mat, I, nd):
+    """lambda = dJ/dI of J = sum over top-face nodes of A_n rho (1 - Y_melt) v_z: the
+    gas mass flux through the top face (nodal quadrature, lumped quad areas), with rho
+    the mixture density (fluid_properties.hpp:199-227) at the node.  Complex-step
+    derivative per dof; nodes are independent, so one pass per dof covers them all."""
+    coords = mesh.coords
+    top = np.nonzero(np.abs(coords[:, 2] - coords[:, 2].max()) < 1e-12)[0]
+    # lumped areas of the top quads (sides 0 of the boundary elements with a top side)
+    bd = mesh.bd_sides[mesh.bd_sides[:, 1] == 0]
+    quad = mesh.conn[bd[:, 0]][:, [4, 5, 6, 7]]
+    x, y = coords[quad, 0], coords[quad, 1]
+    area = 0.5 * np.abs((x * np.roll(y, -1, axis=1) - np.roll(x, -1, axis=1) * y).sum(axis=1))
+    A = np.zeros(len(coords))
+    np.add.at(A, quad.ravel(), np.repeat(area / 4.0, 4))
+    S = I.reshape(-1, nd)[top]
+    chems = mat.chemicals
+
+    def J(Sc):
+        p, vz, T = Sc[:, 0], Sc[:, 3], Sc[:, 4]
+        Ys = [Sc[:, 5 + i] for i in range(len(chems) - 1)]
+        Ys.append(1.0 - sum(Ys))
+        irho = 0.0
+        for c, q in enumerate(chems):
+            r = q.rho if q.kind == 0 else p / (q.R * T)
+            irho = irho + Ys[c] / r
+        return A[top] * (1.0 / irho) * (1.0 - Ys[0]) * vz
+
+    lam = np.zeros((len(coords), nd))
+    h = 1e-30
+    for j in range(nd):
+        Sc = S.astype(np.complex128)
+        Sc[:, j] += 1j * h * max(1.0, float(np.abs(S[:, j]).max()))
+        lam[top, j] = J(Sc).imag / (h * max(1.0, float(np.abs(S[:, j]).max())))
+    return lam.ravel(), float(J(S.astype(np.complex128)).real.sum())
+
+
+def run_hex(args):
+    """Large hex workload: 160x160x156 trilinear hexahedra (3,993,600) with 10% node
+    jitter, 4 components, 8 dofs, 64x64 blocks; 10 mixed assemblies captured in one
+    CUDA graph, FP64 beside it, and the VJP of the top-face gas mass flux."""
+    import torch
+    dev = torch.device("cuda", 0)
+    gm = importlib.import_module("gales-multi-fluid_gb300")
+    syn = importlib.import_module("gales-multi-fluid_gb300.synthetic")
+    importlib.import_module("gales-multi-fluid_gb300.build").build()
+    nx, ny, nz = args.hex_dims
+    t0 = time.perf_counter()
+    mesh = syn.box_hex(nx, ny, nz, jitter=0.1, seed=4)
+    mat = syn.material_for(4, 0)
+    setup = syn.setup_for(3, 4)
+    I, P = syn.state_for(mesh, 4, 0)
+    t_mesh = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    fa = gm.FluidAssembly(mesh, mat, setup)
+    t_create = time.perf_counter() - t0
+    lp = fa.device_system(dev)
+    nnz = lp.vals.numel()
+    Id, Pd = torch.tensor(I, device=dev), torch.tensor(P, device=dev)
+    dt = 1e-3
+    s = torch.cuda.Stream(device=dev)
+    sh = s.cuda_stream
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def sync_timed(form, k, warm):
+        for _ in range(warm):
+            fa.execute(Id, Pd, dt, lp, form=form, stream=sh)
+        torch.cuda.synchronize(dev)
+        a, b = ev(), ev()
+        a.record(s)
+        for _ in range(k):
+            fa.execute(Id, Pd, dt, lp, form=form, stream=sh)
+        b.record(s)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / k, fa.phase_ms(1)
+
+    ms64, k64 = sync_timed(gm.FORM_FP64, max(1, args.fp64_steps), 1)
+    ms_sync, k_mx = sync_timed(gm.FORM_MIXED, 2, 1)
+    # 10 Newton-iteration assemblies in one CUDA graph
+    n_in_graph = 10
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s, capture_error_mode="thread_local"):
+        for _ in range(n_in_graph):
+            fa.enqueue(Id, Pd, dt, lp, form=gm.FORM_MIXED, stream=sh)
+    for _ in range(max(1, args.warmup // 3)):
+        g.replay()
+    torch.cuda.synchronize(dev)
+    reps = max(1, args.steps // 5)
+    with ClockSampler(0) as clk:
+        a, b = ev(), ev()
+        a.record(s)
+        with torch.cuda.stream(s):
+            for _ in range(reps):
+                g.replay()
+        b.record(s)
+        torch.cuda.synchronize(dev)
+    fa.sync(stream=sh)
+    ms_graph = a.elapsed_time(b) / (reps * n_in_graph)
+    # objective VJP: lambda = dJ/dI of the top-face gas mass flux, gradient w.r.t. theta
+    lam, Jval = top_gas_flux_lambda(mesh, mat, I, fa.nd)
+    lamd = torch.tensor(lam, device=dev)
+    gst = torch.zeros_like(Id)
+    th = torch.zeros(3 * 4, dtype=torch.float64, device=dev)
+    fa.vjp(Id, Pd, dt, lamd, gm.VJP_EXACT, gst, th, stream=sh)
+    torch.cuda.synchronize(dev)
+    vjp_ms = fa.device_ms()
+    ne = mesh.n_elements
+    pk = peaks()
+    hbm = pk.get("hbm_gbs")
+    ach = BYTES_PER_ELEM_HEX * ne / (k_mx * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": ne / (ms_graph * 1e-3), "unit": "elements/s", "n_gpus": 1,
+        "steps": reps * n_in_graph, "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 element integrals + f64 EOS/tau/accumulation (mixed)", "data": "synthetic",
+        "config": {"workload": f"3D hex assembly, {ne} trilinear hexahedra ({nx}x{ny}x{nz}, 10% jitter), "
+                               f"4 components, 8 dofs, 64x64 blocks, 10 mixed assemblies per CUDA graph",
+                   "n_elements": int(ne), "n_nodes": int(mesh.n_nodes), "dofs_per_node": 8, "nnz": int(nnz),
+                   "csr_values_gb": nnz * 8 / 1e9, "l2": "CSR values > L2", "seed": 0},
+        "mixed_sync_ms": ms_sync,
+        "fp64": {"value": ne / (ms64 * 1e-3), "unit": "elements/s", "ms_per_step": ms64, "interior_kernel_ms": k64},
+        "mixed_over_fp64": ms64 / ms_graph,
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                     "frac": ach / hbm if hbm else None, "traffic": None, "kernel": "interior_kernel (mixed form)",
+                     "kernel_ms": k_mx, "bytes_per_element": BYTES_PER_ELEM_HEX,
+                     "peak_source": "measured (MEASURED_PEAKS.json)"},
+        "objective_vjp": {"J": Jval, "ms": vjp_ms,
+                          "dJdmu_via_lambda": [float(th[3 * c + 1]) for c in range(4)],
+                          "note": "lambda = dJ/dU seeded VJP (the transpose solve is outside the path)"},
+        "host_setup_s": {"mesh": t_mesh, "create": t_create},
+        "device_memory_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def vjp_block(gm, syn, torch, dev, n=32):
+    """Adjoint workload: ~200k tets, 3 components.  Exact and frozen VJP against the
+    forward residual (FP64 and mixed), and the memory a stored-point design would need."""
+    mesh = syn.box_tet_delaunay(n, seed=3)
+    mat = syn.material_for(3, 0)
+    setup = syn.setup_for(3, 3)
+    I, P = syn.state_for(mesh, 3, 0)
+    fa = gm.FluidAssembly(mesh, mat, setup)
+    Id, Pd = torch.tensor(I, device=dev), torch.tensor(P, device=dev)
+    lam = torch.tensor(np.random.default_rng(1).normal(size=I.size), device=dev)
+    lam /= lam.norm()
+    b = torch.zeros_like(Id)
+    g = torch.zeros_like(Id)
+    th = torch.zeros(9, dtype=torch.float64, device=dev)
+
+    def t(f, k=5):
+        for _ in range(2):
+            f()
+        torch.cuda.synchronize(dev)
+        ms = []
+        for _ in range(k):
+            f()
+            ms.append(fa.device_ms())
+        return float(np.median(ms))
+
+    r64 = t(lambda: fa.residual(Id, Pd, 1e-3, b, form=gm.FORM_FP64))
+    rmx = t(lambda: fa.residual(Id, Pd, 1e-3, b, form=gm.FORM_MIXED))
+    ex = t(lambda: fa.vjp(Id, Pd, 1e-3, lam, gm.VJP_EXACT, g, th))
+    fr = t(lambda: fa.vjp(Id, Pd, 1e-3, lam, gm.VJP_FROZEN, g))
+    nq = 4
+    return {"workload": f"{mesh.n_elements} Delaunay tets ({n}^3 lattice), 3 components, lambda a seeded unit vector",
+            "exact_ms": ex, "frozen_ms": fr, "residual_fp64_ms": r64, "residual_mixed_ms": rmx,
+            "exact_over_residual_fp64": ex / r64, "exact_over_residual_mixed": ex / rmx,
+            "memory": {"recompute_extra_bytes": 0,
+                       "store_points_bytes": int(mesh.n_elements * nq * 8 * 360),
+                       "note": "recompute: no per-point storage; store: ~360 doubles of forward tape per point"}}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -179,9 +355,15 @@ def main():
     ap.add_argument("--lattice", type=int, default=LATTICE_N, help="lattice points per side (54 -> 1.0M tets)")
     ap.add_argument("--only", default="both", choices=["both", "mixed", "fp64"],
                     help="profiling aid: run only one form (no e2e, no CPU leg)")
+    ap.add_argument("--workload", default="tet", choices=["tet", "hex"],
+                    help="tet: 1.0M tets (default); hex: 4.0M hexahedra with a CUDA graph of 10 assemblies")
+    ap.add_argument("--hex-dims", type=int, nargs=3, default=[160, 160, 156])
+    ap.add_argument("--no-vjp", action="store_true", help="skip the adjoint block")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "hex":
+        return run_hex(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -296,6 +478,9 @@ def main():
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_vjp:
+        syn = importlib.import_module("gales-multi-fluid_gb300.synthetic")
+        line["vjp"] = vjp_block(gm, syn, torch, dev)
     if rank == 0 and not args.no_cpu:
         rate, cores, n = cpu_oracle_rate(mesh, mat, setup, I, P, dt, None, None, None, 0)
         line["cpu_baseline"] = {"value": rate, "unit": "elements/s", "cores": cores, "kind": "port",

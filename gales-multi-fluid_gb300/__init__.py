@@ -292,16 +292,17 @@ class LinearSystem:
     vals and rhs are float64 numpy arrays or torch tensors (host or cuda).
     """
 
-    def __init__(self, row_ptr: np.ndarray, col: np.ndarray, vals=None, rhs=None):
+    def __init__(self, row_ptr: Optional[np.ndarray], col: Optional[np.ndarray], vals=None, rhs=None):
         self.row_ptr = row_ptr
         self.col = col
-        n_rows = len(row_ptr) - 1
+        if row_ptr is None and (vals is None or rhs is None):
+            raise ValueError("without a pattern, vals and rhs must be given")
         self.vals = vals if vals is not None else np.zeros(int(row_ptr[-1]), dtype=np.float64)
-        self.rhs = rhs if rhs is not None else np.zeros(n_rows, dtype=np.float64)
+        self.rhs = rhs if rhs is not None else np.zeros(len(row_ptr) - 1, dtype=np.float64)
 
     @property
     def n_rows(self) -> int:
-        return len(self.row_ptr) - 1
+        return len(self.rhs)
 
     def matrix_scipy(self):
         import scipy.sparse as sp
@@ -390,6 +391,19 @@ class FluidAssembly:
         rhs = torch.zeros(len(row_ptr) - 1, dtype=torch.float64, device=device)
         return LinearSystem(row_ptr, col, vals, rhs)
 
+    def nnz_from_graph(self) -> int:
+        """nnz of the CSR pattern from the node graph (nd^2 entries per node pair)."""
+        rp, _ = self.node_graph()
+        return int(rp[-1]) * self.nd * self.nd
+
+    def device_system(self, device) -> LinearSystem:
+        """CSR values and rhs on the device without building the scalar pattern
+        (row_ptr/col stay None): for meshes whose pattern would not fit the host."""
+        import torch
+        vals = torch.zeros(self.nnz_from_graph(), dtype=torch.float64, device=device)
+        rhs = torch.zeros(self.n_rows, dtype=torch.float64, device=device)
+        return LinearSystem(None, None, vals, rhs)
+
     def set_scatter(self, mode: int):
         self._check(self._L.gales_asm_set_scatter(self._h, mode))
 
@@ -416,6 +430,18 @@ class FluidAssembly:
         self._check(self._L.gales_asm_residual(self._h, _addr(I), _addr(P), float(dt), form, _addr(rhs),
                                                stream or None))
         return time.perf_counter() - t0
+
+    def enqueue(self, I, P, dt: float, lp: "LinearSystem", form: int = FORM_MIXED, stream: int = 0,
+                want_matrix: bool = True):
+        """Enqueue one assembly (device tensors only) without synchronising: capture-safe,
+        so repeated calls can be recorded into a CUDA graph.  Check with sync()."""
+        self._check(self._L.gales_asm_enqueue(self._h, _addr(I), _addr(P), float(dt), form,
+                                              _addr(lp.vals) if want_matrix else None, _addr(lp.rhs),
+                                              stream or None))
+
+    def sync(self, stream: int = 0):
+        """Wait for the stream and raise if any enqueued assembly reported an error."""
+        self._check(self._L.gales_asm_sync(self._h, stream or None))
 
     def vjp(self, I, P, dt: float, lam, mode: int, g_state, g_params=None, stream: int = 0):
         self._check(self._L.gales_asm_vjp(self._h, _addr(I), _addr(P), float(dt), _addr(lam), mode,

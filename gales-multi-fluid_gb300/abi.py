@@ -121,6 +121,10 @@ def lib() -> C.CDLL:
     L.gales_asm_assemble_noalloc.restype = C.c_int
     L.gales_asm_residual.argtypes = [vp, vp, vp, C.c_double, i32, vp, vp]
     L.gales_asm_residual.restype = C.c_int
+    L.gales_asm_enqueue.argtypes = [vp, vp, vp, C.c_double, i32, vp, vp, vp]
+    L.gales_asm_enqueue.restype = C.c_int
+    L.gales_asm_sync.argtypes = [vp, vp]
+    L.gales_asm_sync.restype = C.c_int
     L.gales_asm_vjp.argtypes = [vp, vp, vp, C.c_double, vp, i32, vp, vp, vp]
     L.gales_asm_vjp.restype = C.c_int
     L.gales_asm_element_blocks.argtypes = [vp, vp, vp, C.c_double, i32, i32, _p(C.c_int32), i64, vp, vp, vp]
@@ -145,7 +149,7 @@ EXPORTED = [
     "gales_chemical_custom", "gales_chemical_ideal_gas", "gales_setup_default",
     "gales_asm_create", "gales_asm_destroy", "gales_asm_pattern", "gales_asm_node_graph",
     "gales_asm_colouring", "gales_asm_set_scatter", "gales_asm_assemble", "gales_asm_assemble_noalloc",
-    "gales_asm_residual",
+    "gales_asm_residual", "gales_asm_enqueue", "gales_asm_sync",
     "gales_asm_vjp", "gales_asm_element_blocks", "gales_asm_norm2", "gales_asm_status", "gales_asm_last_error",
     "gales_asm_last_ms", "gales_asm_last_phase_ms", "gales_asm_launch_count",
 ]

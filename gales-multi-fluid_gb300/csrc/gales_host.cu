@@ -539,6 +539,7 @@ int validate(gales_asm* h, const gales_mesh_desc* m, const gales_material_desc* 
 
 namespace {
 KParams base_params(gales_asm* h, double dt);
+LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, int form, long long n, cudaStream_t st);
 }  // namespace
 
 extern "C" {
@@ -691,6 +692,13 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   }
   h->ops[GALES_FORM_FP64] = interior_ops(h->dim, h->nen, GALES_FORM_FP64);
   h->ops[GALES_FORM_MIXED] = interior_ops(h->dim, h->nen, GALES_FORM_MIXED);
+  for (int f = 0; f < 2; ++f) {  // kernel attributes, once, outside any stream capture
+    if ((ce = h->ops[f].prepare(h->nc)) != cudaSuccess) return bail(ce, "kernel attributes");
+    KParams k0;
+    memset(&k0, 0, sizeof(k0));
+    LaunchResult r = dispatch_boundary(h, k0, f, -1, 0);
+    if (r.err != cudaSuccess) return bail(r.err, "kernel attributes");
+  }
   {  // element geometry, once per mesh; an inverted element fails here as it does at mesh load
     GeometryOps g = geometry_ops(h->dim, h->nen);
     if ((ce = h->d_geo.alloc(g.bytes_per_element * (size_t)h->n_el)) != cudaSuccess) return bail(ce, "geometry");
@@ -711,6 +719,8 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
       return (int)st;
     }
   }
+  cudaMemset(h->d_status.p, 0, sizeof(unsigned int));
+  cudaMemset(h->d_first_bad.p, 0xff, sizeof(unsigned long long));
   *out = h;
   return 0;
 }
@@ -938,8 +948,10 @@ cudaError_t launch_norm2(const double* x, long long n, double* part, cudaStream_
 }
 
 // Device-side body of one assembly on device pointers (no host synchronisation).
+// With enqueue_only the call records no timing events and leaves the status word
+// alone (it accumulates until gales_asm_sync), so it may be captured into a graph.
 int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, int form, double* dvals,
-                 double* drhs, cudaStream_t st) {
+                 double* drhs, cudaStream_t st, bool enqueue_only = false) {
   KParams k = base_params(h, dt);
   k.I = dI;
   k.P = dP;
@@ -947,12 +959,15 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
   k.rhs = drhs;
   k.scatter_mode = (h->scatter_mode == GALES_SCATTER_COLOURED) ? 1 : 0;
   const bool want_m = dvals != nullptr;
-  CK(h, cudaEventRecord(h->evp[0], st), "event");
-  CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
-  CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  const bool timed = !enqueue_only;
+  if (timed) CK(h, cudaEventRecord(h->evp[0], st), "event");
+  if (!enqueue_only) {
+    CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
+    CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  }
   if (dvals) CK(h, cudaMemsetAsync(dvals, 0, (size_t)h->nnz * sizeof(double), st), "memset vals");
   CK(h, cudaMemsetAsync(drhs, 0, (size_t)h->n_rows * sizeof(double), st), "memset rhs");
-  CK(h, cudaEventRecord(h->evp[1], st), "event");
+  if (timed) CK(h, cudaEventRecord(h->evp[1], st), "event");
   h->launches += 0;
   if (h->scatter_mode == GALES_SCATTER_COLOURED) {
     for (int c = 0; c < h->n_colours; ++c) {
@@ -968,7 +983,7 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
     int rc = run_interior(h, k, form, want_m, h->n_el, st, true);
     if (rc) return rc;
   }
-  CK(h, cudaEventRecord(h->evp[2], st), "event");
+  if (timed) CK(h, cudaEventRecord(h->evp[2], st), "event");
   k.el_list = nullptr;
   k.n_list = 0;
   if (!h->bd_list.empty()) {
@@ -983,7 +998,7 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
     h->launches += r.launches;
   }
-  CK(h, cudaEventRecord(h->evp[3], st), "event");
+  if (timed) CK(h, cudaEventRecord(h->evp[3], st), "event");
   return 0;
 }
 
@@ -1063,6 +1078,29 @@ int gales_asm_assemble(gales_asm* h, const double* I, const double* P, double dt
 int gales_asm_residual(gales_asm* h, const double* I, const double* P, double dt, int32_t form, double* rhs,
                        void* stream) {
   return assemble_impl(h, I, P, dt, form, nullptr, rhs, stream);
+}
+
+int gales_asm_enqueue(gales_asm* h, const double* I, const double* P, double dt, int32_t form, double* vals,
+                      double* rhs, void* stream) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (!I || !P || !rhs) return fail(h, GALES_ERR_BAD_INPUT, "null state or rhs pointer");
+  if (form != GALES_FORM_FP64 && form != GALES_FORM_MIXED) return fail(h, GALES_ERR_BAD_INPUT, "unknown form");
+  if (!(dt > 0.0)) return fail(h, GALES_ERR_BAD_INPUT, "dt must be positive");
+  if (!is_device_ptr(I) || !is_device_ptr(P) || !is_device_ptr(rhs) || (vals && !is_device_ptr(vals)))
+    return fail(h, GALES_ERR_BAD_INPUT, "gales_asm_enqueue takes device pointers only");
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  return run_assembly(h, I, P, dt, form, vals, rhs, (cudaStream_t)stream, true);
+}
+
+int gales_asm_sync(gales_asm* h, void* stream) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = finish(h, st);
+  CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
+  CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  CK(h, cudaStreamSynchronize(st), "synchronize");
+  return rc;
 }
 
 int gales_asm_element_blocks(gales_asm* h, const double* I, const double* P, double dt, int32_t form,

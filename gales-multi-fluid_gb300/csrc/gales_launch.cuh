@@ -29,41 +29,46 @@ struct InteriorInst {
         k, reinterpret_cast<Rec*>(buf), first, n);
     return {cudaGetLastError(), 1};
   }
+  // dynamic shared memory limits, set once per device before any launch (also before
+  // a stream capture)
+  static cudaError_t prepare() {
+    const int smem = (int)(sizeof(ES) * M::EPC);
+    cudaError_t e = cudaFuncSetAttribute(matrix_kernel<DIM, NEN, NC, NQ, S, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(matrix_kernel<DIM, NEN, NC, NQ, S, false>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  }
   static LaunchResult matrix(const KParams& k, bool want_m, const void* buf, long long first, long long n,
                              cudaStream_t st) {
     if (n <= 0) return {cudaSuccess, 0};
     const size_t smem = sizeof(ES) * M::EPC;
     const unsigned blocks = (unsigned)((n + M::EPC - 1) / M::EPC);
     const Rec* in = reinterpret_cast<const Rec*>(buf);
-    if (want_m) {
-      auto fn = matrix_kernel<DIM, NEN, NC, NQ, S, true>;
-      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return {e, 0};
-      fn<<<blocks, M::CTA, smem, st>>>(k, in, first, n);
-    } else {
-      auto fn = matrix_kernel<DIM, NEN, NC, NQ, S, false>;
-      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return {e, 0};
-      fn<<<blocks, M::CTA, smem, st>>>(k, in, first, n);
-    }
+    if (want_m) matrix_kernel<DIM, NEN, NC, NQ, S, true><<<blocks, M::CTA, smem, st>>>(k, in, first, n);
+    else matrix_kernel<DIM, NEN, NC, NQ, S, false><<<blocks, M::CTA, smem, st>>>(k, in, first, n);
     return {cudaGetLastError(), 1};
   }
 };
 
 template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
+cudaError_t prepare_boundary_nc() {
+  return cudaFuncSetAttribute(boundary_kernel<DIM, NEN, NC, NS, NSQ, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(BoundarySmem<DIM, NEN, NC, NS, NSQ, S>));
+}
+
+template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
 LaunchResult launch_boundary_nc(const KParams& k, long long n_items, cudaStream_t st) {
   if (n_items == 0) return {cudaSuccess, 0};
   const size_t smem = sizeof(BoundarySmem<DIM, NEN, NC, NS, NSQ, S>);
-  auto fn = boundary_kernel<DIM, NEN, NC, NS, NSQ, S>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return {e, 0};
-  fn<<<(unsigned)n_items, 32, smem, st>>>(k);
+  boundary_kernel<DIM, NEN, NC, NS, NSQ, S><<<(unsigned)n_items, 32, smem, st>>>(k);
   return {cudaGetLastError(), 1};
 }
 
 // Interior operations of one (element type, form): record bytes per element, point
 // stage and matrix stage, for 1..4 components.
 struct InteriorOps {
+  cudaError_t (*prepare)(int nc);
   size_t (*rec_bytes)(int nc);
   LaunchResult (*point)(const KParams&, int nc, void* buf, long long first, long long n, cudaStream_t);
   LaunchResult (*matrix)(const KParams&, int nc, bool want_m, const void* buf, long long first, long long n,
@@ -81,6 +86,12 @@ struct InteriorOps {
 
 template <int DIM, int NEN, int NQ, int FORM>
 struct InteriorDispatch {
+  static cudaError_t prepare(int nc) {
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::prepare()
+    GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+    return cudaErrorInvalidValue;
+  }
   static size_t rec_bytes(int nc) {
 #define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::rec_bytes()
     GALES_NC_SWITCH(nc, GALES_C)
@@ -100,12 +111,19 @@ struct InteriorDispatch {
 #undef GALES_C
     return {cudaErrorInvalidValue, 0};
   }
-  static InteriorOps ops() { return {&rec_bytes, &point, &matrix}; }
+  static InteriorOps ops() { return {&prepare, &rec_bytes, &point, &matrix}; }
 };
 
 // Boundary pass of one element type; S is the matrix arithmetic type of the form.
+// n < 0 only prepares the kernel (shared-memory limit) and launches nothing.
 template <int DIM, int NEN, int NS, int NSQ, typename S>
 LaunchResult boundary_dispatch(const KParams& k, int nc, long long n, cudaStream_t st) {
+  if (n < 0) {
+#define GALES_C(NC) return {prepare_boundary_nc<DIM, NEN, NC, NS, NSQ, S>(), 0}
+    GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+    return {cudaErrorInvalidValue, 0};
+  }
 #define GALES_C(NC) return launch_boundary_nc<DIM, NEN, NC, NS, NSQ, S>(k, n, st)
   GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C

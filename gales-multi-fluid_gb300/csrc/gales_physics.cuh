@@ -37,41 +37,36 @@ struct DevChem {
   double inv_rho, beta_over_rho, alpha_over_rho, cv_shift, inv_R, R_over_gamma, inv_D;
 };
 
-// Round-to-nearest-even narrowing of binary64 to binary32 with integer operations
-// only (52-bit significand cut to 23 bits, ties to even, carry into the exponent;
-// overflow to infinity, gradual underflow to subnormals and zero, NaN kept quiet).
-// On this GPU the hardware conversion issues on the FP64 pipe, which the point
-// stage already saturates; every special case is integer work too, so no path
-// falls back to the conversion instruction.
+// The hardware conversions between binary64 and binary32 issue on the FP64 pipe,
+// which the point stage already saturates.  narrow_rn/widen do the common case (a
+// normal result) with integer operations and keep the conversion instruction for
+// the rare rest (zero or subnormal results, overflow, infinities, NaN) behind a
+// branch: the instruction is volatile asm, so the compiler cannot hoist it out of
+// the branch and execute it for every value.
+__device__ __forceinline__ float hw_narrow(double d) {
+  float f;
+  asm volatile("cvt.rn.f32.f64 %0, %1;" : "=f"(f) : "d"(d));
+  return f;
+}
+
+__device__ __forceinline__ double hw_widen(float f) {
+  double d;
+  asm volatile("cvt.f64.f32 %0, %1;" : "=d"(d) : "f"(f));
+  return d;
+}
+
+// Round-to-nearest-even narrowing of binary64 to binary32 (52-bit significand cut to
+// 23 bits, ties to even, carry into the exponent).
 __device__ __forceinline__ float narrow_rn(double d) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(d);
-  const unsigned int sign = (unsigned int)(u >> 32) & 0x80000000u;
-  const int e64 = (int)((u >> 52) & 0x7ffu);
-  const unsigned long long m52 = u & 0xfffffffffffffull;
-  const int e = e64 - (1023 - 127);
-  unsigned int bits;
-  if (e64 == 0x7ff) {
-    bits = 0x7f800000u | (unsigned int)(m52 >> 29) | (m52 ? 0x400000u : 0u);
-  } else if (e >= 255) {
-    bits = 0x7f800000u;
-  } else if (e > 0) {
-    const unsigned int m = (unsigned int)(m52 >> 29);
-    const unsigned int rest = (unsigned int)(u & 0x1fffffffu);
-    bits = ((unsigned int)e << 23) | m;
-    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
-  } else {
-    // binary32 subnormal or zero: significand (with its leading one) >> (30 - e)
-    const int r = 30 - e;
-    if (r > 54 || e64 == 0) {
-      bits = 0u;
-    } else {
-      const unsigned long long M = m52 | (1ull << 52);
-      const unsigned long long q = M >> r, rem = M & ((1ull << r) - 1ull), half = 1ull << (r - 1);
-      bits = (unsigned int)q;
-      if (rem > half || (rem == half && (q & 1ull))) bits += 1u;
-    }
-  }
-  return __uint_as_float(sign | bits);
+  const unsigned int hi = (unsigned int)(u >> 32);
+  const int e = (int)((hi >> 20) & 0x7ffu) - (1023 - 127);
+  if (e <= 0 || e >= 255) return hw_narrow(d);
+  const unsigned int m = (unsigned int)((u >> 29) & 0x7fffffu);
+  const unsigned int rest = (unsigned int)(u & 0x1fffffffu);
+  unsigned int bits = (hi & 0x80000000u) | ((unsigned int)e << 23) | m;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
+  return __uint_as_float(bits);
 }
 
 template <typename S>

@@ -186,7 +186,27 @@ def box_hex(nx: int, ny: int, nz: int, jitter: float = 0.1, seed: int = 4) -> Me
                      c(0, 0, 1), c(1, 0, 1), c(1, 1, 1), c(0, 1, 1)], axis=1).astype(np.int32)
     lo, hi = np.zeros(3), np.ones(3)
     node_flag = _box_flags(pts, lo, hi, open_top=True)
-    return _finish(pts, conn, node_flag, _face_flag_box(lo, hi, True), f"box_hex_{nx}x{ny}x{nz}")
+    bd = box_hex_sides(nx, ny, nz, open_top=True)
+    el_bd = np.zeros(conn.shape[0], dtype=np.uint8)
+    el_bd[bd[:, 0]] = 1
+    return Mesh(pts, conn, node_flag, el_bd, bd, name=f"box_hex_{nx}x{ny}x{nz}")
+
+
+def box_hex_sides(nx: int, ny: int, nz: int, open_top: bool = True) -> np.ndarray:
+    """Boundary sides of box_hex's structured grid without a face search (the same
+    rows, in the same order, as boundary_sides): element (i, j, k) is i*ny*nz + j*nz + k;
+    local sides of SIDES[(3, 8)] are 0: z+, 1: z-, 2: x-, 3: x+, 4: y+, 5: y-."""
+    I, J, K = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    e = (I * ny * nz + J * nz + K).ravel()
+    I, J, K = I.ravel(), J.ravel(), K.ravel()
+    parts = []
+    for side, mask in ((0, K == nz - 1), (1, K == 0), (2, I == 0), (3, I == nx - 1), (4, J == ny - 1), (5, J == 0)):
+        flag = OPEN if (side == 0 and open_top) else WALL
+        el = e[mask]
+        parts.append(np.stack([el, np.full(el.shape, side), np.full(el.shape, flag)], axis=1))
+    bd = np.concatenate(parts).astype(np.int64)
+    bd = bd[np.lexsort((bd[:, 1], bd[:, 0]))]
+    return bd.astype(np.int32)
 
 
 # ---------------------------------------------------------------------------

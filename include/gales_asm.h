@@ -202,6 +202,17 @@ int gales_asm_assemble(gales_asm* h, const double* I, const double* P, double dt
 #define GALES_NOALLOC_SCRATCH_BYTES (8u << 20)
 int gales_asm_assemble_noalloc(gales_asm* h, const double* I, const double* P, double dt, int32_t form,
                                double* vals, double* rhs, void* stream);
+/* Enqueue one assembly on `stream` and return: device pointers only, no host
+ * synchronisation, no timing events and no allocation, so a sequence of calls can be
+ * captured into a CUDA graph and replayed (e.g. the Newton iterations of one time
+ * step).  vals may be NULL (residual only).  Errors found by the kernels accumulate
+ * in the status word until gales_asm_sync.  No reference counterpart: the reference
+ * assembles synchronously (fluid_assembly.hpp:39-68). */
+int gales_asm_enqueue(gales_asm* h, const double* I, const double* P, double dt, int32_t form, double* vals,
+                      double* rhs, void* stream);
+/* Wait for `stream`, return the status of the work enqueued since the last sync
+ * (0 or error bits, first offending element via gales_asm_status) and clear it. */
+int gales_asm_sync(gales_asm* h, void* stream);
 /* Residual only (rhs), no matrix. */
 int gales_asm_residual(gales_asm* h, const double* I, const double* P, double dt, int32_t form,
                        double* rhs, void* stream);

@@ -66,3 +66,11 @@ def test_state_generator_ranges(syn):
     Y = np.concatenate([S[:, 5:7], 1 - S[:, 5:7].sum(axis=1, keepdims=True)], axis=1)
     assert Y.min() > 0 and np.allclose(Y.sum(axis=1), 1.0)
     assert np.abs(P - I).max() > 0
+
+
+def test_box_hex_sides_match_the_face_search(syn):
+    """The structured shortcut for the hex workload's boundary equals the generic search."""
+    import numpy as np
+    m = syn.box_hex(5, 4, 3, jitter=0.1, seed=2)
+    ref = syn.boundary_sides(m.conn, 3, m.coords, syn._face_flag_box(np.zeros(3), np.ones(3), True))
+    assert np.array_equal(m.bd_sides, ref)

@@ -1,10 +1,11 @@
 """The integer-only binary64 <-> binary32 conversions of the kernels, checked on the host.
 
 narrow_rn (gales_physics.cuh) and widen (gales_kernels.cuh) replace the hardware
-conversion instructions in the mixed form.  Their source is compiled here with g++
-behind a small shim for the CUDA bit-cast intrinsics and compared with numpy's IEEE
-conversions on special values, both subnormal ranges, overflow, rounding ties and
-random bit patterns.
+conversion instructions for normal values in the mixed form and route the rest to
+the instruction.  Their source is compiled here with g++ behind a small shim for
+the CUDA bit-cast intrinsics (and the host's IEEE cast standing in for the
+instruction) and compared with numpy's IEEE conversions on special values, both
+subnormal ranges, overflow, rounding ties and random bit patterns.
 """
 import ctypes as C
 import pathlib
@@ -26,6 +27,9 @@ static inline double __longlong_as_double(long long x) { double d; std::memcpy(&
 static inline unsigned int __float_as_uint(float f) { unsigned int x; std::memcpy(&x, &f, 4); return x; }
 static inline float __uint_as_float(unsigned int x) { float f; std::memcpy(&f, &x, 4); return f; }
 static inline int __clz(int x) { return x == 0 ? 32 : __builtin_clz((unsigned int)x); }
+// the device code routes special values to the conversion instruction; the host's IEEE cast
+static inline float hw_narrow(double d) { return (float)d; }
+static inline double hw_widen(float f) { return (double)f; }
 """
 
 
