@@ -238,6 +238,8 @@ struct gales_asm {
   DevBuf<unsigned char> d_geo;   // element geometry at the interior points (mesh.hpp:468-495)
   cudaStream_t ist[2] = {nullptr, nullptr};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  cudaStream_t bst = nullptr;                  // boundary pass, concurrent with the interior
+  cudaEvent_t ev_bfork = nullptr, ev_bjoin = nullptr;
   int status = 0;
   int64_t first_bad = -1;
   double last_ms = 0.0;
@@ -685,6 +687,9 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   for (int i = 0; i < 4; ++i)
     if ((ce = cudaEventCreate(&h->evp[i])) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+  if ((ce = cudaEventCreateWithFlags(&h->ev_bfork, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+  if ((ce = cudaEventCreateWithFlags(&h->ev_bjoin, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+  if ((ce = cudaStreamCreateWithFlags(&h->bst, cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
   for (int i = 0; i < 2; ++i) {
     if ((ce = cudaEventCreateWithFlags(&h->ev_join[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
     if ((ce = cudaStreamCreateWithFlags(&h->ist[i], cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
@@ -744,6 +749,9 @@ void gales_asm_destroy(gales_asm* h) {
   for (int i = 0; i < 4; ++i)
     if (h->evp[i]) cudaEventDestroy(h->evp[i]);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_bfork) cudaEventDestroy(h->ev_bfork);
+  if (h->ev_bjoin) cudaEventDestroy(h->ev_bjoin);
+  if (h->bst) cudaStreamDestroy(h->bst);
   for (int i = 0; i < 2; ++i) {
     if (h->ev_join[i]) cudaEventDestroy(h->ev_join[i]);
     if (h->ist[i]) cudaStreamDestroy(h->ist[i]);
@@ -969,6 +977,24 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
   CK(h, cudaMemsetAsync(drhs, 0, (size_t)h->n_rows * sizeof(double), st), "memset rhs");
   if (timed) CK(h, cudaEventRecord(h->evp[1], st), "event");
   h->launches += 0;
+  // boundary pass (fluid_assembly.hpp:57-63): always atomics, since boundary elements
+  // of one colour may still share nodes.  With the atomic interior scatter the two
+  // passes only add into A and b, so the boundary pass runs on its own stream beside
+  // the interior chunks; with the coloured (plain read-modify-write) scatter it waits.
+  const bool has_bd = !h->bd_list.empty();
+  const bool bd_concurrent = has_bd && h->scatter_mode != GALES_SCATTER_COLOURED;
+  KParams kb = k;
+  kb.scatter_mode = 0;
+  kb.el_list = h->d_bd_list.p;
+  kb.n_list = (int64_t)h->bd_list.size();
+  kb.bd_sides = h->d_bd_sides.p;
+  if (bd_concurrent) {
+    CK(h, cudaEventRecord(h->ev_bfork, st), "event");
+    CK(h, cudaStreamWaitEvent(h->bst, h->ev_bfork, 0), "stream wait");
+    LaunchResult r = dispatch_boundary(h, kb, form, kb.n_list, h->bst);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
+    h->launches += r.launches;
+  }
   if (h->scatter_mode == GALES_SCATTER_COLOURED) {
     for (int c = 0; c < h->n_colours; ++c) {
       KParams kc = k;
@@ -984,16 +1010,10 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
     if (rc) return rc;
   }
   if (timed) CK(h, cudaEventRecord(h->evp[2], st), "event");
-  k.el_list = nullptr;
-  k.n_list = 0;
-  if (!h->bd_list.empty()) {
-    // the boundary pass always uses atomics: boundary elements of one colour may
-    // still be scattered twice, but its own elements may share nodes
-    KParams kb = k;
-    kb.scatter_mode = 0;
-    kb.el_list = h->d_bd_list.p;
-    kb.n_list = (int64_t)h->bd_list.size();
-    kb.bd_sides = h->d_bd_sides.p;
+  if (bd_concurrent) {
+    CK(h, cudaEventRecord(h->ev_bjoin, h->bst), "event");
+    CK(h, cudaStreamWaitEvent(st, h->ev_bjoin, 0), "stream wait");
+  } else if (has_bd) {
     LaunchResult r = dispatch_boundary(h, kb, form, kb.n_list, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
     h->launches += r.launches;

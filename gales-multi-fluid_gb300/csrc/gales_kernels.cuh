@@ -285,6 +285,9 @@ struct alignas(16) QP {
   S p, v[DIM], Y[NC], rho, E, drho_dp, drho_dT, de_dp, de_dT, mu, lambda, kappa;
   S drho_dY[L::NYA], dE_dY[L::NYA], rhoD[L::NYA], rhoDH[L::NYA];
   S tau[ND][ND];
+  // structure vectors of DUDY = w r0^T + rho M and their products with tau:
+  // w = (1, v, E, Y), z = r0^T tau, y = mE^T tau (mE: energy row of M), tg = g^T tau_v
+  S w[ND], z[ND], y[ND], tg[ND];
   S nu;             // dc_scale_fact * nu_shoc (0 when dc is off or inactive)
   S rv[ND];         // coefficient of N_b:    (U - U_P)/dt - S
   S rf[DIM][ND];    // coefficient of dN_b/dx_k:  F_dif,k - F_adv,k + shock dI/dx_k
@@ -488,6 +491,11 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
 #pragma unroll
     for (int j = 0; j < ND; ++j) out.rv[j] = fmaf(narrow_rn(U[j] - UP[j]), idt, -SvR[j]);
   }
+  // the coefficients in the form's type R
+  using CR = Coef<DIM, NC, R>;
+  CR cr;
+  if constexpr (FORM == GALES_FORM_FP64) cr = c;
+  else cr = narrow<DIM, NC>(c);
   // tau (fluid_2d.hpp:877-1022)
   double tau[ND][ND];
 #pragma unroll
@@ -496,7 +504,9 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
     for (int cc = 0; cc < ND; ++cc) tau[r][cc] = 0.0;
   const double v_nrm = sqrt(vsq<DIM>(v));
   if (v_nrm >= kEps && k.tau != GALES_TAU_NONE) {
-    const double h = compute_h<DIM>(q.G, v, dv);
+    double h;
+    if constexpr (FORM == GALES_FORM_FP64) h = compute_h<DIM>(q.G, v, dv);
+    else h = compute_h_mixed<DIM>(q.G, v, dv);
     double trG = 0.0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) trG += q.G[d][d];
@@ -625,15 +635,39 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       }
     }
   }
+  {
+    // z = r0^T tau, y = mE^T tau, tg = sum_d g_d tau[v_d] from the rounded tau (what the
+    // matrix stage multiplies with), and w
+    R zz[ND], yy[ND], gg[ND], gR[DIM];
 #pragma unroll
-  for (int r = 0; r < ND; ++r)
+    for (int d = 0; d < DIM; ++d) gR[d] = to_s<R>(k.gravity[d]);
 #pragma unroll
-    for (int cc = 0; cc < ND; ++cc) out.tau[r][cc] = to_s<S>(tau[r][cc]);
+    for (int cc = 0; cc < ND; ++cc) zz[cc] = yy[cc] = gg[cc] = R(0);
+#pragma unroll
+    for (int r = 0; r < ND; ++r) {
+      R r0r, mEr, gr;
+      if (r == 0) { r0r = cr.drho_dp; mEr = cr.de_dp; gr = R(0); }
+      else if (r < L::iT) { r0r = R(0); mEr = cr.v[r - 1]; gr = gR[(r - 1) % DIM]; }
+      else if (r == L::iT) { r0r = cr.drho_dT; mEr = cr.de_dT; gr = R(0); }
+      else { r0r = cr.drho_dY[r - L::iY]; mEr = cr.dE_dY[r - L::iY]; gr = R(0); }
+#pragma unroll
+      for (int cc = 0; cc < ND; ++cc) {
+        const R t = to_s<R>(tau[r][cc]);
+        out.tau[r][cc] = S(t);
+        if (r < 1 || r >= L::iT) zz[cc] = madd(r0r, t, zz[cc]);
+        yy[cc] = madd(mEr, t, yy[cc]);
+        if (r >= 1 && r < L::iT) gg[cc] = madd(gr, t, gg[cc]);
+      }
+    }
+#pragma unroll
+    for (int cc = 0; cc < ND; ++cc) {
+      out.z[cc] = S(zz[cc]);
+      out.y[cc] = S(yy[cc]);
+      out.tg[cc] = S(gg[cc]);
+      out.w[cc] = S(cc == 0 ? R(1) : (cc < L::iT ? cr.v[cc - 1] : (cc == L::iT ? cr.E : cr.Y[cc - L::iY])));
+    }
+  }
   // fluxes, least-squares residual and dc in the form's type R
-  using CR = Coef<DIM, NC, R>;
-  CR cr;
-  if constexpr (FORM == GALES_FORM_FP64) cr = c;
-  else cr = narrow<DIM, NC>(c);
   R Res[ND], AdI[ND], t[ND];
   {
     R dd[ND];
@@ -866,12 +900,12 @@ struct MatShape {
   static constexpr bool AFFINE = NEN == DIM + 1;
 };
 
-// Per-point vectors shared by the lanes of an element: w, z = r0^T tau,
-// Mtau[E] = mE^T tau, t_g and t_b.
+// Per-point vectors t_b = sum_k dN_b/dx_k tau[v_k] shared by the lanes of an element
+// (w, z, y and t_g come with the point record).
 template <int DIM, int NEN, int NC, int NQ, typename S>
 struct PointVecs {
   static constexpr int ND = Layout<DIM, NC>::ND;
-  S w[NQ][ND], z[NQ][ND], y[NQ][ND], tg[NQ][ND], tb[NQ][NEN][ND];
+  S tb[NQ][NEN][ND];
 };
 
 template <int DIM, int NEN, int NC, int NQ, typename S>
@@ -988,41 +1022,14 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
   for (int d = 0; d < DIM; ++d) grav[d] = S(k.gravity[d]);
   elem_sync<WPE>(ec);
   auto& pv = E.u.in.pv;
-  // per-point vectors
-  {
-    constexpr int NPV = (4 + NEN) * ND;
-    for (int t = gl; t < NQ * NPV; t += ET) {
-      const int q = t / NPV, u = t % NPV, kind = u / ND, col = u % ND;
-      const QP<DIM, NEN, NC, S>& c = E.u.in.qp[q];
-      S x;
-      if (kind == 0) {
-        x = col == 0 ? S(1) : (col < iT ? c.v[col - 1] : (col == iT ? c.E : c.Y[col - iY]));
-        pv.w[q][col] = x;
-      } else if (kind == 1) {
-        x = madd(c.drho_dp, c.tau[0][col], c.drho_dT * c.tau[iT][col]);
+  // t_b per point
+  for (int t = gl; t < NQ * NEN * ND; t += ET) {
+    const int q = t / (NEN * ND), u = t % (NEN * ND), b = u / ND, col = u % ND;
+    const QP<DIM, NEN, NC, S>& c = E.u.in.qp[q];
+    S x = c.ds[0][b] * c.tau[1][col];
 #pragma unroll
-        for (int y = 0; y < NC - 1; ++y) x = madd(c.drho_dY[y], c.tau[iY + y][col], x);
-        pv.z[q][col] = x;
-      } else if (kind == 2) {
-        x = madd(c.de_dp, c.tau[0][col], c.de_dT * c.tau[iT][col]);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) x = madd(c.v[d], c.tau[1 + d][col], x);
-#pragma unroll
-        for (int y = 0; y < NC - 1; ++y) x = madd(c.dE_dY[y], c.tau[iY + y][col], x);
-        pv.y[q][col] = x;
-      } else if (kind == 3) {
-        x = grav[0] * c.tau[1][col];
-#pragma unroll
-        for (int d = 1; d < DIM; ++d) x = madd(grav[d], c.tau[1 + d][col], x);
-        pv.tg[q][col] = x;
-      } else {
-        const int b = kind - 4;
-        x = c.ds[0][b] * c.tau[1][col];
-#pragma unroll
-        for (int d = 1; d < DIM; ++d) x = madd(c.ds[d][b], c.tau[1 + d][col], x);
-        pv.tb[q][b][col] = x;
-      }
-    }
+    for (int d = 1; d < DIM; ++d) x = madd(c.ds[d][b], c.tau[1 + d][col], x);
+    pv.tb[q][b][col] = x;
   }
   elem_sync<WPE>(ec);
   const bool active = gl < M::LANES;
@@ -1059,7 +1066,7 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
     S sb = gb[0] * c.v[0];
 #pragma unroll
     for (int d = 1; d < DIM; ++d) sb = madd(gb[d], c.v[d], sb);
-    const S wr = pv.w[q][r];
+    const S wr = c.w[r];
     const S ur = madd(rho, wr, cE ? p : S(0));
     S gsel = S(0);
 #pragma unroll
@@ -1067,16 +1074,16 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
     const S kap = (cE ? sb : S(0)) + gsel;
     // row r of FPT_b
     const S cz = sb * wr, cm = (r == 0) ? S(0) : sb * rho, cg = cE ? -Nb * rho : S(0);
-    const S* mrow = cvy ? &c.tau[r][0] : &pv.y[q][0];
+    const S* mrow = cvy ? &c.tau[r][0] : &c.y[0];
     const S* tb = &pv.tb[q][b][0];
     S F[ND];
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
-      S x = cz * pv.z[q][j];
+      S x = cz * c.z[j];
       x = madd(cm, mrow[j], x);
       x = madd(ur, tb[j], x);
       x = madd(kap, c.tau[0][j], x);
-      F[j] = madd(cg, pv.tg[q][j], x);
+      F[j] = madd(cg, c.tg[j], x);
     }
     // residual row: N_b rv + sum_k dN_b/dx_k rf_k + FPT_b Res (fluid_2d.hpp:253-262, 280-290)
     {
@@ -1091,7 +1098,7 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
       // FPT_b DUDY, DUDY row r, and the a-independent velocity-column terms
       S fw = F[0];
 #pragma unroll
-      for (int j = 1; j < ND; ++j) fw = madd(F[j], pv.w[q][j], fw);
+      for (int j = 1; j < ND; ++j) fw = madd(F[j], c.w[j], fw);
       const S fu = madd(rho, fw, p * F[iT]);
       const S rF = rho * F[iT];
       S FD[ND], Dr[ND];
@@ -1247,14 +1254,24 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
     add_to(k.rhs + (long long)E.nodes[b] * ND + r, rv, mode);
   }
   if constexpr (WANT_M) {
-    for (int t = gl; t < NT; t += ET) {
-      const int srw = t / N, colx = t - srw * N;
-      const double val = E.u.stage[srw * NS + colx];
-      if ((__double_as_longlong(val) << 1) != 0) {
-        const int sb_ = srw / ND, jb = srw - sb_ * ND, a = colx / ND, ja = colx - a * ND;
-        const int64_t off = E.rowbase[sb_] + (int64_t)jb * E.rowlen[sb_] +
-                            (int64_t)__ldg(k.slot + (e * NEN + sb_) * NEN + a) * ND + ja;
-        add_to(k.vals + off, val, mode);
+    // One block row per warp step: lane l covers columns l, l+32, ... of the row, whose
+    // offset within node b's CSR row (slot(b, a) nd + ja) is fixed per (b, column), so
+    // it is formed once per test node; consecutive lanes write the contiguous nd-runs.
+    constexpr int CH = (N + 31) / 32;   // column passes per row
+    const int lane = gl & 31, warp = gl >> 5;
+#pragma unroll
+    for (int h = 0; h < CH; ++h) {
+      const int cx = lane + 32 * h;
+      if (cx >= N) break;
+      const int a = cx / ND, ja = cx - a * ND;
+      for (int sb_ = 0; sb_ < NEN; ++sb_) {
+        const int64_t coff = (int64_t)__ldg(k.slot + (e * NEN + sb_) * NEN + a) * ND + ja;
+        for (int jb = warp; jb < ND; jb += WPE) {
+          const int srw = sb_ * ND + jb;
+          const double val = E.u.stage[srw * NS + cx];
+          if ((__double_as_longlong(val) << 1) != 0)
+            add_to(k.vals + E.rowbase[sb_] + (int64_t)jb * E.rowlen[sb_] + coff, val, mode);
+        }
       }
     }
   }

@@ -723,4 +723,76 @@ __device__ __forceinline__ double compute_h(const double (&G)[DIM][DIM], const d
   return 2 * sqrt(fabs(h));
 }
 
+// compute_h for the mixed form.  The steps that decide its branches (s0, the
+// cross-stream residual s1 and |s1| against DBL_EPSILON) keep the reference's IEEE
+// operations, so the same branch is taken as in the FP64 form.  When s1 is a
+// direction (the common case) the remaining steps are insensitive to rounding and
+// use fused operations and one reciprocal per normalisation; the rank-one case
+// (s1 rounding noise) and a near-degenerate third direction take compute_h itself.
+template <int DIM>
+__device__ __forceinline__ double qform_fma(const double (&G)[DIM][DIM], const double* s) {
+  double r = 0.0;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
+    double t = G[i][0] * s[0];
+#pragma unroll
+    for (int j = 1; j < DIM; ++j) t = fma(G[i][j], s[j], t);
+    r = fma(s[i], t, r);
+  }
+  return r;
+}
+
+template <int DIM>
+__device__ __forceinline__ double compute_h_mixed(const double (&G)[DIM][DIM], const double* v,
+                                                  const double (&dv)[DIM][DIM]) {
+  const double nrm_v = sqrt(vsq<DIM>(v));
+  double s0[DIM], acc[DIM], s1[DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) s0[i] = v[i] / nrm_v;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
+    double t = 0.0;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) t += dv[i][j] * v[j];
+    acc[i] = t;
+  }
+  double ip = 0.0;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) ip += acc[i] * s0[i];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) s1[i] = acc[i] - ip * s0[i];
+  const double nrm_s1 = sqrt(vsq<DIM>(s1));
+  if (!(nrm_s1 > kEps)) return compute_h<DIM>(G, v, dv);
+  const double i1 = 1.0 / nrm_s1;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) s1[i] *= i1;
+  double a[3];
+  a[0] = qform_fma<DIM>(G, s0);
+  a[1] = qform_fma<DIM>(G, s1);
+  a[2] = 0.0;
+  if constexpr (DIM == 3) {
+    double s2[3];
+    s2[0] = fma(s0[1], s1[2], -s0[2] * s1[1]);
+    s2[1] = fma(s1[0], s0[2], -s1[2] * s0[0]);
+    s2[2] = fma(s0[0], s1[1], -s0[1] * s1[0]);
+    const double n2 = sqrt(fma(s2[0], s2[0], fma(s2[1], s2[1], s2[2] * s2[2])));
+    if (!(n2 > 1.0e3 * kEps)) return compute_h<DIM>(G, v, dv);
+    const double i2 = 1.0 / n2;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) s2[i] *= i2;
+    a[2] = qform_fma<DIM>(G, s2);
+  }
+  double h;
+  if (DIM == 3 && a[0] != 0.0 && a[1] != 0.0 && a[2] != 0.0) {
+    // 1/a0 + 1/a1 + 1/a2 with one division
+    h = fma(a[0], a[1] + a[2], a[1] * a[2]) / (a[0] * a[1] * a[2]);
+  } else {
+    h = 0.0;
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+      if (a[i] != 0.0) h += 1.0 / a[i];
+  }
+  return 2 * sqrt(fabs(h));
+}
+
 }  // namespace gales
