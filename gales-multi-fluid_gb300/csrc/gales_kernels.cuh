@@ -828,18 +828,26 @@ __device__ __forceinline__ S kd_entry(const C& c, const S* gb, S gbv, int l, int
   return (col == r) ? c.rhoD[r - L::iY] * gb[l] : S(0);
 }
 
-// Exact widening of binary32 to binary64 (exponent rebias 127 -> 1023, significand
-// shifted into the top of the 52-bit field); zeros in integer form too, subnormals,
-// infinities and NaN through hw_widen (see narrow_rn).
+// Exact widening of binary32 to binary64 with integer operations only (see
+// narrow_rn): exponent rebias 127 -> 1023, significand shifted into the top of the
+// 52-bit field; subnormals normalised, infinities and NaN keep their payload.
 __device__ __forceinline__ double widen(float f) {
   const unsigned int u = __float_as_uint(f);
-  const unsigned int ex = (u >> 23) & 0xffu;
   const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sign);
-  if (ex == 0u || ex == 0xffu) return hw_widen(f);
-  const unsigned long long e64 = (unsigned long long)(ex + (1023u - 127u)) << 52;
-  const unsigned long long m64 = (unsigned long long)(u & 0x7fffffu) << 29;
-  return __longlong_as_double((long long)(sign | e64 | m64));
+  const unsigned int ex = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  unsigned long long bits;
+  if (ex - 1u < 254u) {
+    bits = ((unsigned long long)(ex + (1023u - 127u)) << 52) | ((unsigned long long)m << 29);
+  } else if (ex == 0xffu) {
+    bits = (0x7ffull << 52) | ((unsigned long long)m << 29);
+  } else if (m == 0u) {
+    bits = 0ull;
+  } else {
+    // subnormal m * 2^-149: leading one at bit p = 31 - clz(m)
+    const int p = 31 - __clz((int)m);
+    bits = ((unsigned long long)(p - 149 + 1023) << 52) | (((unsigned long long)m << (52 - p)) & 0xfffffffffffffull);
+  }
+  return __longlong_as_double((long long)(sign | bits));
 }
 __device__ __forceinline__ double widen(double d) { return d; }
 

@@ -38,34 +38,32 @@ struct DevChem {
 };
 
 // The hardware conversions between binary64 and binary32 issue on the FP64 pipe,
-// which the point stage already saturates.  narrow_rn/widen do the common case (a
-// normal result) with integer operations and keep the conversion instruction for
-// the rare rest (zero or subnormal results, overflow, infinities, NaN) behind a
-// branch: the instruction is volatile asm, so the compiler cannot hoist it out of
-// the branch and execute it for every value.
-__device__ __forceinline__ float hw_narrow(double d) {
-  float f;
-  asm volatile("cvt.rn.f32.f64 %0, %1;" : "=f"(f) : "d"(d));
-  return f;
-}
-
-__device__ __forceinline__ double hw_widen(float f) {
-  double d;
-  asm volatile("cvt.f64.f32 %0, %1;" : "=d"(d) : "f"(f));
-  return d;
-}
+// which the point stage already saturates, and a conversion kept for rare operands
+// behind a branch is still issued (predicated off) for every value.  narrow_rn and
+// widen are therefore integer-only.
 
 // Round-to-nearest-even narrowing of binary64 to binary32 (52-bit significand cut to
-// 23 bits, ties to even, carry into the exponent).
+// 23 bits, ties to even, carry into the exponent, overflow to infinity, NaN kept
+// quiet).  Results below the smallest normal binary32 (|x| < 2^-126) flush to a
+// signed zero instead of a subnormal.
 __device__ __forceinline__ float narrow_rn(double d) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(d);
   const unsigned int hi = (unsigned int)(u >> 32);
-  const int e = (int)((hi >> 20) & 0x7ffu) - (1023 - 127);
-  if (e <= 0 || e >= 255) return hw_narrow(d);
+  const unsigned int sign = hi & 0x80000000u;
+  const int e64 = (int)((hi >> 20) & 0x7ffu);
+  const int e = e64 - (1023 - 127);
   const unsigned int m = (unsigned int)((u >> 29) & 0x7fffffu);
-  const unsigned int rest = (unsigned int)(u & 0x1fffffffu);
-  unsigned int bits = (hi & 0x80000000u) | ((unsigned int)e << 23) | m;
-  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
+  unsigned int bits;
+  if (e >= 1 && e <= 254) {
+    const unsigned int rest = (unsigned int)(u & 0x1fffffffu);
+    bits = sign | ((unsigned int)e << 23) | m;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
+  } else if (e64 == 0x7ff) {
+    const bool nan = (u & 0xfffffffffffffull) != 0ull;
+    bits = sign | 0x7f800000u | (nan ? (m | 0x400000u) : 0u);
+  } else {
+    bits = sign | (e >= 255 ? 0x7f800000u : 0u);
+  }
   return __uint_as_float(bits);
 }
 

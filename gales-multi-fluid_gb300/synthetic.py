@@ -289,6 +289,22 @@ def state_for(mesh: Mesh, nb_comp: int, seed: int = 0, perturb: float = 1e-4, no
     return I, P
 
 
+def state_near_rest(mesh: Mesh, nb_comp: int, seed: int = 0, p_top: float = 7.0e7, rho: float = 2400.0,
+                    gravity: float = 9.81):
+    """A state Newton can converge from: state_for's velocity and temperature fields,
+    a hydrostatic pressure p_top + rho g (z_top - z) along the last axis, and mass
+    fractions mapped into [0.25, 0.75] so that the mass-fraction clamp of the
+    reference's driver (model.hpp:176-184) stays inactive.  I = P."""
+    I, _ = state_for(mesh, nb_comp, seed, perturb=0.0)
+    nd = nb_dofs(mesh.dim, nb_comp)
+    S = I.reshape(-1, nd)
+    z = mesh.coords[:, -1]
+    S[:, 0] = p_top + rho * gravity * (z.max() - z)
+    S[:, mesh.dim + 2:] = 0.25 + 0.5 * S[:, mesh.dim + 2:]
+    I = S.ravel().copy()
+    return I, I.copy()
+
+
 def node_flag_mask(mesh: Mesh, flag: int) -> np.ndarray:
     return mesh.node_flag == flag
 
