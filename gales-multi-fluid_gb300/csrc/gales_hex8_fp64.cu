@@ -13,4 +13,6 @@ LaunchResult boundary_hex8(const KParams& k, int nc, int form, long long n, cuda
 
 GeometryOps geometry_ops_hex8() { return GeometryDispatch<3, 8, 8>::ops(); }
 
+BoundaryInfo boundary_info_hex8(int nc) { return BoundaryInfoDispatch<3, 8, 6, 4>::info(nc); }
+
 }  // namespace gales

@@ -214,12 +214,16 @@ struct gales_asm {
   std::vector<int32_t> bd_list;
   std::vector<int8_t> bd_sides;
   std::vector<int8_t> el_sides;  // side flags of every element [n_el][nsides]
+  // flagged side points of the boundary elements, grouped by element
+  std::vector<int32_t> bpt_off, bpt_el, bpt_ip;
   // device
   DevBuf<double> d_coords;
   DevBuf<int32_t> d_conn, d_node_flag, d_colour_order, d_bd_list, d_sweep;
   DevBuf<int64_t> d_node_rp;
   DevBuf<uint16_t> d_slot;
   DevBuf<int8_t> d_bd_sides;
+  DevBuf<int32_t> d_bpt_off, d_bpt_el, d_bpt_ip;
+  DevBuf<unsigned char> d_bgeo, d_bpt_rec;
   DevBuf<gales_side_bc> d_side_bc;
   DevBuf<unsigned int> d_status;
   DevBuf<unsigned long long> d_first_bad;
@@ -542,6 +546,24 @@ int validate(gales_asm* h, const gales_mesh_desc* m, const gales_material_desc* 
 namespace {
 KParams base_params(gales_asm* h, double dt);
 LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, int form, long long n, cudaStream_t st);
+
+BoundaryInfo boundary_info(int dim, int nen, int nc) {
+  if (dim == 2 && nen == 3) return boundary_info_tri3(nc);
+  if (dim == 2 && nen == 4) return boundary_info_quad4(nc);
+  if (dim == 3 && nen == 4) return boundary_info_tet4(nc);
+  return boundary_info_hex8(nc);
+}
+
+// The boundary-point tables of the handle's boundary element list (k.el_list must be
+// the handle's boundary list).
+void set_boundary_points(gales_asm* h, KParams& k) {
+  k.bpt_off = h->d_bpt_off.p;
+  k.bpt_el = h->d_bpt_el.p;
+  k.bpt_ip = h->d_bpt_ip.p;
+  k.bgeo = h->d_bgeo.p;
+  k.bpt_rec = h->bpt_el.empty() ? nullptr : h->d_bpt_rec.p;
+  k.n_bpt = (int64_t)h->bpt_el.size();
+}
 }  // namespace
 
 extern "C" {
@@ -648,6 +670,16 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
       const int32_t e = m->bd_side_el[i];
       if (pos[e] >= 0) h->bd_sides[(size_t)pos[e] * h->ei.nsides + m->bd_side_local[i]] = (int8_t)m->bd_side_flag[i];
     }
+    h->bpt_off.assign(h->bd_list.size() + 1, 0);
+    for (size_t li = 0; li < h->bd_list.size(); ++li) {
+      for (int sd = 0; sd < h->ei.nsides; ++sd)
+        if (h->bd_sides[li * h->ei.nsides + sd] > 0)
+          for (int q = 0; q < h->ei.nqs; ++q) {
+            h->bpt_el.push_back((int32_t)li);
+            h->bpt_ip.push_back(sd * h->ei.nqs + q);
+          }
+      h->bpt_off[li + 1] = (int32_t)h->bpt_el.size();
+    }
   }
   cudaError_t ce = cudaSetDevice(device);
   auto bail = [&](cudaError_t e, const char* what) {
@@ -674,6 +706,9 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   UP(h->d_sweep, h->sweep.data(), h->sweep.size(), "sweep");
   UP(h->d_bd_list, h->bd_list.data(), h->bd_list.size(), "bd_list");
   UP(h->d_bd_sides, h->bd_sides.data(), h->bd_sides.size(), "bd_sides");
+  UP(h->d_bpt_off, h->bpt_off.data(), h->bpt_off.size(), "bpt_off");
+  UP(h->d_bpt_el, h->bpt_el.data(), h->bpt_el.size(), "bpt_el");
+  UP(h->d_bpt_ip, h->bpt_ip.data(), h->bpt_ip.size(), "bpt_ip");
   UP(h->d_side_bc, h->setup.side_bc, (size_t)GALES_MAX_FLAGS, "side_bc");
 #undef UP
   if ((ce = h->d_status.alloc(1)) != cudaSuccess) return bail(ce, "status");
@@ -724,6 +759,31 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
       return (int)st;
     }
   }
+  {  // boundary side-point geometry and the point-record buffer of the boundary pass
+    const BoundaryInfo bi = boundary_info(h->dim, h->nen, h->nc);
+    const size_t nb = h->bpt_el.size();
+    if ((ce = h->d_bgeo.alloc(bi.bgeo_bytes * nb)) != cudaSuccess) return bail(ce, "boundary geometry");
+    const size_t rec = std::max(bi.rec_bytes[0], bi.rec_bytes[1]);
+    if ((ce = h->d_bpt_rec.alloc(rec * nb)) != cudaSuccess) return bail(ce, "boundary records");
+    KParams k = base_params(h, 1.0);
+    k.el_list = h->d_bd_list.p;
+    k.n_list = (int64_t)h->bd_list.size();
+    k.bd_sides = h->d_bd_sides.p;
+    set_boundary_points(h, k);
+    LaunchResult r = bi.geometry(k, h->d_bgeo.p, 0);
+    if (r.err != cudaSuccess) return bail(r.err, "boundary geometry kernel");
+    h->launches += r.launches;
+    if ((ce = cudaDeviceSynchronize()) != cudaSuccess) return bail(ce, "boundary geometry kernel");
+    unsigned int st = 0;
+    unsigned long long fb = 0;
+    cudaMemcpy(&st, h->d_status.p, sizeof(st), cudaMemcpyDeviceToHost);
+    cudaMemcpy(&fb, h->d_first_bad.p, sizeof(fb), cudaMemcpyDeviceToHost);
+    if (st) {
+      fprintf(stderr, "gales_asm_create: boundary Jacobian is not positive at element %llu (quad.hpp:215-218)\n", fb);
+      gales_asm_destroy(h);
+      return (int)st;
+    }
+  }
   cudaMemset(h->d_status.p, 0, sizeof(unsigned int));
   cudaMemset(h->d_first_bad.p, 0xff, sizeof(unsigned long long));
   *out = h;
@@ -736,6 +796,7 @@ void gales_asm_destroy(gales_asm* h) {
   h->d_coords.release(); h->d_conn.release(); h->d_node_flag.release();
   h->d_colour_order.release(); h->d_bd_list.release(); h->d_node_rp.release(); h->d_sweep.release();
   h->d_slot.release(); h->d_bd_sides.release(); h->d_side_bc.release();
+  h->d_bpt_off.release(); h->d_bpt_el.release(); h->d_bpt_ip.release(); h->d_bgeo.release(); h->d_bpt_rec.release();
   h->d_status.release(); h->d_first_bad.release(); h->d_geo.release();
   h->s_I.release(); h->s_P.release(); h->s_vals.release(); h->s_rhs.release(); h->s_aux.release();
   h->s_lam.release(); h->s_th.release();
@@ -988,6 +1049,7 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
   kb.el_list = h->d_bd_list.p;
   kb.n_list = (int64_t)h->bd_list.size();
   kb.bd_sides = h->d_bd_sides.p;
+  set_boundary_points(h, kb);
   if (bd_concurrent) {
     CK(h, cudaEventRecord(h->ev_bfork, st), "event");
     CK(h, cudaStreamWaitEvent(h->bst, h->ev_bfork, 0), "stream wait");
@@ -1255,6 +1317,7 @@ int gales_asm_vjp(gales_asm* h, const double* I, const double* P, double dt, con
   kb.el_list = h->d_bd_list.p;
   kb.n_list = (int64_t)h->bd_list.size();
   kb.bd_sides = h->d_bd_sides.p;
+  set_boundary_points(h, kb);
   if (mode == GALES_VJP_EXACT) {
     LaunchResult r = dispatch_vjp(h, k, false, h->n_el, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "vjp interior kernel");
@@ -1433,6 +1496,7 @@ extern "C" int gales_asm_assemble_noalloc(gales_asm* h, const double* I, const d
     kb.el_list = h->d_bd_list.p;
     kb.n_list = (int64_t)h->bd_list.size();
     kb.bd_sides = h->d_bd_sides.p;
+    set_boundary_points(h, kb);
     LaunchResult r = dispatch_boundary(h, kb, form, kb.n_list, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
     h->launches += r.launches;

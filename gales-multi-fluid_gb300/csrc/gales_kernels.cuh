@@ -69,6 +69,15 @@ struct KParams {
   const double* vjp_lam;
   double* vjp_g;
   double* vjp_th;
+  // boundary points (flagged side points of the listed boundary elements): per-element
+  // offsets [n_list+1], element slot and (side, point) index, precomputed geometry and
+  // the point records of the boundary point stage; null for the fused boundary pass
+  const int32_t* bpt_off;
+  const int32_t* bpt_el;
+  const int32_t* bpt_ip;
+  const void* bgeo;
+  void* bpt_rec;
+  int64_t n_bpt;
 };
 
 __device__ __forceinline__ void flag_error(const KParams& k, unsigned int bits, long long e) {
@@ -1344,7 +1353,7 @@ __device__ __forceinline__ T a_entry_bd(const Coef<DIM, NC, T>& c, const gales_s
 // area vector, shape data and the boundary residual vector
 //   rb = sum_k (F_adv,k - F_dif,k) JNxW_k                       (fluid_2d.hpp:343-349)
 template <int DIM, int NEN, int NC, typename S>
-struct BPoint {
+struct alignas(16) BPoint {
   using L = Layout<DIM, NC>;
   static constexpr int ND = L::ND;
   Coef<DIM, NC, S> c;
@@ -1362,6 +1371,200 @@ struct BoundarySmem {
   S m[N * N];            // element block accumulator
   double r[N];
 };
+
+// Boundary point physics (fluid_2d.hpp:341-349, 610-817) at one side point with
+// the given geometry (shape values, gradients, JN W_bd): the coefficients, shape data
+// and the boundary residual rb = sum_k (F_adv,k - F_dif,k) JNxW_k, in FP64.
+template <int DIM, int NEN, int NC, typename S>
+__device__ __forceinline__ void bpoint_phase(const KParams& k, const int* nodes, int flag, const double* sh,
+                                             const double (&ds)[DIM][NEN], const double* JNxW,
+                                             BPoint<DIM, NEN, NC, S>& P) {
+  using L = Layout<DIM, NC>;
+  constexpr int ND = L::ND;
+  const gales_side_bc& bc = k.side_bc[flag < GALES_MAX_FLAGS ? flag : 0];
+  P.flag = flag;
+  double Ie[NEN][ND];
+#pragma unroll
+  for (int a = 0; a < NEN; ++a)
+#pragma unroll
+    for (int j = 0; j < ND; ++j) Ie[a][j] = __ldg(k.I + (long long)nodes[a] * ND + j);
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) P.JNxW[d] = to_s<S>(JNxW[d]);
+#pragma unroll
+  for (int i = 0; i < NEN; ++i) {
+    P.sh[i] = to_s<S>(sh[i]);
+    P.shr[i] = sh[i];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) P.ds[d][i] = to_s<S>(ds[d][i]);
+  }
+  double Iq[ND], dI[DIM][ND];
+#pragma unroll
+  for (int j = 0; j < ND; ++j) {
+    double a = 0.0;
+#pragma unroll
+    for (int i = 0; i < NEN; ++i) a += sh[i] * Ie[i][j];
+    Iq[j] = a;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      double b = 0.0;
+#pragma unroll
+      for (int i = 0; i < NEN; ++i) b += ds[d][i] * Ie[i][j];
+      dI[d][j] = b;
+    }
+  }
+  double p, v[DIM], T, Y[NC];
+  assign<DIM, NC>(Iq, p, v, T, Y);
+  Props<NC> pr;
+  mixture<NC>(k.ch, p, T, Y, pr);
+  Coef<DIM, NC> c;
+  make_coef<DIM, NC>(pr, p, v, T, Y, c);
+  if constexpr (sizeof(S) == 4) P.c = narrow<DIM, NC>(c);
+  else P.c = c;
+  // advective flux (fluid_2d.hpp:581-595), mass-flux override (fluid_2d.hpp:674-680, 732-738)
+  double Fa[DIM][ND], Fd[DIM][ND];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    const double vk = v[d];
+    if ((bc.mass_flux_mask >> d) & 1u) {
+      const double mf = bc.mass_flux[d];
+      Fa[d][0] = mf;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) Fa[d][1 + j] = (j == d) ? mf * v[j] + p : mf * v[j];
+      Fa[d][L::iT] = mf * c.E + p * v[d];
+#pragma unroll
+      for (int i = 0; i < NC - 1; ++i) Fa[d][L::iY + i] = mf * Y[i];
+    } else {
+      Fa[d][0] = pr.rho * vk;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) Fa[d][1 + j] = (j == d) ? pr.rho * vk * vk + p : pr.rho * vk * v[j];
+      Fa[d][L::iT] = vk * (pr.rho * c.E + p);
+#pragma unroll
+      for (int i = 0; i < NC - 1; ++i) Fa[d][L::iY + i] = pr.rho * vk * Y[i];
+    }
+  }
+  // diffusive flux from stresses with Neumann overrides (fluid_2d.hpp:761-817)
+  {
+    const double lambda = -2.0 * pr.mu / 3.0;
+    double div = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) div += dI[d][1 + d];
+    double ts[DIM][DIM], qf[DIM], Jf[DIM][L::NYA];
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) {
+        if (a == b) ts[a][b] = lambda * (div) + 2.0 * pr.mu * dI[a][1 + a];
+        else {
+          const int lo = a < b ? a : b, hi = a < b ? b : a;
+          ts[a][b] = pr.mu * (dI[hi][1 + lo] + dI[lo][1 + hi]);
+        }
+      }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) qf[d] = -pr.kappa * dI[d][L::iT];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+#pragma unroll
+      for (int i = 0; i < NC - 1; ++i) Jf[d][i] = pr.rho * pr.D_c[i] * dI[d][L::iY + i];
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+#pragma unroll
+      for (int b = a; b < DIM; ++b)
+        if ((bc.tau_mask >> (a * 3 + b)) & 1u) { ts[a][b] = bc.tau[a * 3 + b]; ts[b][a] = ts[a][b]; }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+      if ((bc.q_mask >> d) & 1u) qf[d] = bc.q[d];
+#pragma unroll
+    for (int i = 0; i < NC - 1; ++i)
+#pragma unroll
+      for (int d = 0; d < DIM; ++d)
+        if ((bc.J_mask >> (d * 8 + i)) & 1u) Jf[d][i] = bc.J[d][i];
+    double H[L::NYA];
+#pragma unroll
+    for (int i = 0; i < NC - 1; ++i) H[i] = pr.e_c[i] + p / pr.rho_c[i];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      double HJ = 0.0;
+#pragma unroll
+      for (int i = 0; i < NC - 1; ++i) HJ += H[i] * Jf[d][i];
+      Fd[d][0] = 0.0;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) Fd[d][1 + j] = ts[d][j];
+      double en = ts[d][0] * v[0];
+#pragma unroll
+      for (int j = 1; j < DIM; ++j) en = en + ts[d][j] * v[j];
+      Fd[d][L::iT] = en - qf[d] - HJ;
+#pragma unroll
+      for (int i = 0; i < NC - 1; ++i) Fd[d][L::iY + i] = Jf[d][i];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < ND; ++j) {
+    double x = Fa[0][j] * JNxW[0];
+#pragma unroll
+    for (int d = 1; d < DIM; ++d) x = madd(Fa[d][j], JNxW[d], x);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) x = madd(-Fd[d][j], JNxW[d], x);
+    P.rb[j] = x;
+  }
+}
+
+// Side-point geometry of the listed boundary elements' flagged sides, once per mesh.
+template <int DIM, int NEN>
+struct alignas(16) BGeo {
+  double sh[NEN], ds[DIM][NEN], JNxW[DIM];
+};
+
+template <int DIM, int NEN, int NS, int NSQ>
+__global__ void __launch_bounds__(128) bgeo_kernel(const KParams k, BGeo<DIM, NEN>* __restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= k.n_bpt) return;
+  const int li = k.bpt_el[t], ip = k.bpt_ip[t], s = ip / NSQ, iq = ip % NSQ;
+  const long long e = k.el_list[li];
+  double X[NEN][DIM];
+#pragma unroll
+  for (int a = 0; a < NEN; ++a) {
+    const int nd_ = __ldg(k.conn + e * NEN + a);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) X[a][d] = __ldg(k.coords + (long long)nd_ * DIM + d);
+  }
+  Geo<DIM, NEN> q;
+  geometry<DIM, NEN>(X, k.sgp[s][iq], false, q);
+  if (!(q.J > 0.0)) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
+  BGeo<DIM, NEN>& o = out[t];
+#pragma unroll
+  for (int i = 0; i < NEN; ++i) {
+    o.sh[i] = q.sh[i];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) o.ds[d][i] = q.ds[d][i];
+  }
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) o.JNxW[d] = q.JN[d] * k.W_bd;
+}
+
+// Boundary pass, stage 1: one thread per flagged side point writes its point record.
+template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
+__global__ void __launch_bounds__(128) bpoint_kernel(const KParams k) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= k.n_bpt) return;
+  const int li = k.bpt_el[t], ip = k.bpt_ip[t];
+  const long long e = k.el_list[li];
+  int nodes[NEN];
+#pragma unroll
+  for (int a = 0; a < NEN; ++a) nodes[a] = __ldg(k.conn + e * NEN + a);
+  const BGeo<DIM, NEN>& g = reinterpret_cast<const BGeo<DIM, NEN>*>(k.bgeo)[t];
+  double sh[NEN], ds[DIM][NEN], JN[DIM];
+#pragma unroll
+  for (int i = 0; i < NEN; ++i) {
+    sh[i] = g.sh[i];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ds[d][i] = g.ds[d][i];
+  }
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) JN[d] = g.JNxW[d];
+  BPoint<DIM, NEN, NC, S> P;
+  bpoint_phase<DIM, NEN, NC, S>(k, nodes, (int)k.bd_sides[li * NS + ip / NSQ], sh, ds, JN, P);
+  reinterpret_cast<BPoint<DIM, NEN, NC, S>*>(k.bpt_rec)[t] = P;
+}
 
 // Boundary pass, one warp per listed boundary element.  Lanes first evaluate one
 // side quadrature point each (thread per point, FP64: geometry, EOS, fluxes and the
@@ -1387,147 +1590,38 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   for (int a = 0; a < NEN; ++a) nodes[a] = __ldg(k.conn + e * NEN + a);
   for (int t = lane; t < NT; t += 32) B.m[t] = S(0);
   for (int t = lane; t < N; t += 32) B.r[t] = 0.0;
-  // (1) point physics, one lane per (side, point)
-  if (lane < NS * NSQ) {
+  // (1) point physics: from the boundary point records of this element when the
+  // boundary point stage ran (k.bpt_rec), otherwise one lane per (side, point)
+  if (k.bpt_rec) {
+    for (int t = lane; t < NS * NSQ; t += 32) B.pt[t].flag = 0;
+    __syncwarp();
+    const int p0 = k.bpt_off[li], p1 = k.bpt_off[li + 1];
+    using BP = BPoint<DIM, NEN, NC, S>;
+    static_assert(sizeof(BP) % 16 == 0, "point record must be int4-aligned");
+    constexpr int W4 = sizeof(BP) / 16;
+    for (int t = lane; t < (p1 - p0) * W4; t += 32) {
+      const int pt = p0 + t / W4, w = t % W4;
+      reinterpret_cast<int4*>(&B.pt[k.bpt_ip[pt]])[w] = reinterpret_cast<const int4*>(
+          reinterpret_cast<const BP*>(k.bpt_rec) + pt)[w];
+    }
+  } else if (lane < NS * NSQ) {
     const int s = lane / NSQ, iq = lane % NSQ;
     const int flag = k.bd_sides[li * NS + s];
     BPoint<DIM, NEN, NC, S>& P = B.pt[lane];
     P.flag = flag;
     if (flag > 0) {
-      const gales_side_bc& bc = k.side_bc[flag < GALES_MAX_FLAGS ? flag : 0];
-      double X[NEN][DIM], Ie[NEN][ND];
+      double X[NEN][DIM];
 #pragma unroll
-      for (int a = 0; a < NEN; ++a) {
+      for (int a = 0; a < NEN; ++a)
 #pragma unroll
         for (int d = 0; d < DIM; ++d) X[a][d] = __ldg(k.coords + (long long)nodes[a] * DIM + d);
-#pragma unroll
-        for (int j = 0; j < ND; ++j) Ie[a][j] = __ldg(k.I + (long long)nodes[a] * ND + j);
-      }
       Geo<DIM, NEN> q;
       geometry<DIM, NEN>(X, k.sgp[s][iq], false, q);
       if (!(q.J > 0.0)) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
       double JNxW[DIM];
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        JNxW[d] = q.JN[d] * k.W_bd;
-        P.JNxW[d] = to_s<S>(JNxW[d]);
-      }
-#pragma unroll
-      for (int i = 0; i < NEN; ++i) {
-        P.sh[i] = to_s<S>(q.sh[i]);
-        P.shr[i] = q.sh[i];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) P.ds[d][i] = to_s<S>(q.ds[d][i]);
-      }
-      double Iq[ND], dI[DIM][ND];
-#pragma unroll
-      for (int j = 0; j < ND; ++j) {
-        double a = 0.0;
-#pragma unroll
-        for (int i = 0; i < NEN; ++i) a += q.sh[i] * Ie[i][j];
-        Iq[j] = a;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          double b = 0.0;
-#pragma unroll
-          for (int i = 0; i < NEN; ++i) b += q.ds[d][i] * Ie[i][j];
-          dI[d][j] = b;
-        }
-      }
-      double p, v[DIM], T, Y[NC];
-      assign<DIM, NC>(Iq, p, v, T, Y);
-      Props<NC> pr;
-      mixture<NC>(k.ch, p, T, Y, pr);
-      Coef<DIM, NC> c;
-      make_coef<DIM, NC>(pr, p, v, T, Y, c);
-      if constexpr (sizeof(S) == 4) P.c = narrow<DIM, NC>(c);
-      else P.c = c;
-      // advective flux (fluid_2d.hpp:581-595), mass-flux override (fluid_2d.hpp:674-680, 732-738)
-      double Fa[DIM][ND], Fd[DIM][ND];
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        const double vk = v[d];
-        if ((bc.mass_flux_mask >> d) & 1u) {
-          const double mf = bc.mass_flux[d];
-          Fa[d][0] = mf;
-#pragma unroll
-          for (int j = 0; j < DIM; ++j) Fa[d][1 + j] = (j == d) ? mf * v[j] + p : mf * v[j];
-          Fa[d][L::iT] = mf * c.E + p * v[d];
-#pragma unroll
-          for (int i = 0; i < NC - 1; ++i) Fa[d][L::iY + i] = mf * Y[i];
-        } else {
-          Fa[d][0] = pr.rho * vk;
-#pragma unroll
-          for (int j = 0; j < DIM; ++j) Fa[d][1 + j] = (j == d) ? pr.rho * vk * vk + p : pr.rho * vk * v[j];
-          Fa[d][L::iT] = vk * (pr.rho * c.E + p);
-#pragma unroll
-          for (int i = 0; i < NC - 1; ++i) Fa[d][L::iY + i] = pr.rho * vk * Y[i];
-        }
-      }
-      // diffusive flux from stresses with Neumann overrides (fluid_2d.hpp:761-817)
-      {
-        const double lambda = -2.0 * pr.mu / 3.0;
-        double div = 0.0;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) div += dI[d][1 + d];
-        double ts[DIM][DIM], qf[DIM], Jf[DIM][L::NYA];
-#pragma unroll
-        for (int a = 0; a < DIM; ++a)
-#pragma unroll
-          for (int b = 0; b < DIM; ++b) {
-            if (a == b) ts[a][b] = lambda * (div) + 2.0 * pr.mu * dI[a][1 + a];
-            else {
-              const int lo = a < b ? a : b, hi = a < b ? b : a;
-              ts[a][b] = pr.mu * (dI[hi][1 + lo] + dI[lo][1 + hi]);
-            }
-          }
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) qf[d] = -pr.kappa * dI[d][L::iT];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d)
-#pragma unroll
-          for (int i = 0; i < NC - 1; ++i) Jf[d][i] = pr.rho * pr.D_c[i] * dI[d][L::iY + i];
-#pragma unroll
-        for (int a = 0; a < DIM; ++a)
-#pragma unroll
-          for (int b = a; b < DIM; ++b)
-            if ((bc.tau_mask >> (a * 3 + b)) & 1u) { ts[a][b] = bc.tau[a * 3 + b]; ts[b][a] = ts[a][b]; }
-#pragma unroll
-        for (int d = 0; d < DIM; ++d)
-          if ((bc.q_mask >> d) & 1u) qf[d] = bc.q[d];
-#pragma unroll
-        for (int i = 0; i < NC - 1; ++i)
-#pragma unroll
-          for (int d = 0; d < DIM; ++d)
-            if ((bc.J_mask >> (d * 8 + i)) & 1u) Jf[d][i] = bc.J[d][i];
-        double H[L::NYA];
-#pragma unroll
-        for (int i = 0; i < NC - 1; ++i) H[i] = pr.e_c[i] + p / pr.rho_c[i];
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          double HJ = 0.0;
-#pragma unroll
-          for (int i = 0; i < NC - 1; ++i) HJ += H[i] * Jf[d][i];
-          Fd[d][0] = 0.0;
-#pragma unroll
-          for (int j = 0; j < DIM; ++j) Fd[d][1 + j] = ts[d][j];
-          double en = ts[d][0] * v[0];
-#pragma unroll
-          for (int j = 1; j < DIM; ++j) en = en + ts[d][j] * v[j];
-          Fd[d][L::iT] = en - qf[d] - HJ;
-#pragma unroll
-          for (int i = 0; i < NC - 1; ++i) Fd[d][L::iY + i] = Jf[d][i];
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < ND; ++j) {
-        double x = Fa[0][j] * JNxW[0];
-#pragma unroll
-        for (int d = 1; d < DIM; ++d) x = madd(Fa[d][j], JNxW[d], x);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) x = madd(-Fd[d][j], JNxW[d], x);
-        P.rb[j] = x;
-      }
+      for (int d = 0; d < DIM; ++d) JNxW[d] = q.JN[d] * k.W_bd;
+      bpoint_phase<DIM, NEN, NC, S>(k, nodes, flag, q.sh, q.ds, JNxW, P);
     }
   }
   __syncwarp();

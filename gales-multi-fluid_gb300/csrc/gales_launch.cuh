@@ -57,12 +57,19 @@ cudaError_t prepare_boundary_nc() {
                               (int)sizeof(BoundarySmem<DIM, NEN, NC, NS, NSQ, S>));
 }
 
+// Boundary pass: with point records (k.bpt_rec) the point stage runs first, one thread
+// per flagged side point; the element stage then reads the records.
 template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
 LaunchResult launch_boundary_nc(const KParams& k, long long n_items, cudaStream_t st) {
   if (n_items == 0) return {cudaSuccess, 0};
+  int launches = 0;
+  if (k.bpt_rec && k.n_bpt > 0) {
+    bpoint_kernel<DIM, NEN, NC, NS, NSQ, S><<<(unsigned)((k.n_bpt + 127) / 128), 128, 0, st>>>(k);
+    ++launches;
+  }
   const size_t smem = sizeof(BoundarySmem<DIM, NEN, NC, NS, NSQ, S>);
   boundary_kernel<DIM, NEN, NC, NS, NSQ, S><<<(unsigned)n_items, 32, smem, st>>>(k);
-  return {cudaGetLastError(), 1};
+  return {cudaGetLastError(), launches + 1};
 }
 
 // Interior operations of one (element type, form): record bytes per element, point
@@ -130,6 +137,33 @@ LaunchResult boundary_dispatch(const KParams& k, int nc, long long n, cudaStream
   return {cudaErrorInvalidValue, 0};
 }
 
+// Boundary side-point geometry (handle creation) and record sizes.
+struct BoundaryInfo {
+  size_t bgeo_bytes;
+  size_t rec_bytes[2];   // per form (FP64, mixed)
+  LaunchResult (*geometry)(const KParams& k, void* out, cudaStream_t st);
+};
+
+template <int DIM, int NEN, int NS, int NSQ>
+struct BoundaryInfoDispatch {
+  static LaunchResult geometry(const KParams& k, void* out, cudaStream_t st) {
+    if (k.n_bpt <= 0) return {cudaSuccess, 0};
+    bgeo_kernel<DIM, NEN, NS, NSQ><<<(unsigned)((k.n_bpt + 127) / 128), 128, 0, st>>>(
+        k, reinterpret_cast<BGeo<DIM, NEN>*>(out));
+    return {cudaGetLastError(), 1};
+  }
+  static BoundaryInfo info(int nc) {
+    BoundaryInfo b{sizeof(BGeo<DIM, NEN>), {0, 0}, &geometry};
+#define GALES_C(NC)                                                      \
+  b.rec_bytes[0] = sizeof(BPoint<DIM, NEN, NC, double>);               \
+  b.rec_bytes[1] = sizeof(BPoint<DIM, NEN, NC, float>);                \
+  break
+    GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+    return b;
+  }
+};
+
 // Element geometry precompute (handle creation).
 struct GeometryOps {
   size_t bytes_per_element;
@@ -157,16 +191,19 @@ InteriorOps interior_ops_tri3_mixed();
 LaunchResult boundary_tri3(const KParams&, int nc, int form, long long n, cudaStream_t);
 LaunchResult boundary_tri3_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_tri3();
+BoundaryInfo boundary_info_tri3(int nc);
 InteriorOps interior_ops_quad4_fp64();
 InteriorOps interior_ops_quad4_mixed();
 LaunchResult boundary_quad4(const KParams&, int nc, int form, long long n, cudaStream_t);
 LaunchResult boundary_quad4_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_quad4();
+BoundaryInfo boundary_info_quad4(int nc);
 InteriorOps interior_ops_tet4_fp64();
 InteriorOps interior_ops_tet4_mixed();
 LaunchResult boundary_tet4(const KParams&, int nc, int form, long long n, cudaStream_t);
 LaunchResult boundary_tet4_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_tet4();
+BoundaryInfo boundary_info_tet4(int nc);
 InteriorOps interior_ops_hex8_fp64();
 InteriorOps interior_ops_hex8_mixed();
 LaunchResult boundary_hex8(const KParams&, int nc, int form, long long n, cudaStream_t);
@@ -181,5 +218,6 @@ LaunchResult vjp_interior_hex8(const KParams&, int nc, long long n, cudaStream_t
 LaunchResult vjp_boundary_hex8(const KParams&, int nc, long long n, cudaStream_t);
 LaunchResult boundary_hex8_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_hex8();
+BoundaryInfo boundary_info_hex8(int nc);
 
 }  // namespace gales

@@ -13,4 +13,6 @@ LaunchResult boundary_quad4(const KParams& k, int nc, int form, long long n, cud
 
 GeometryOps geometry_ops_quad4() { return GeometryDispatch<2, 4, 4>::ops(); }
 
+BoundaryInfo boundary_info_quad4(int nc) { return BoundaryInfoDispatch<2, 4, 4, 2>::info(nc); }
+
 }  // namespace gales

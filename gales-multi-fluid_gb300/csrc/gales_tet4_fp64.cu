@@ -13,4 +13,6 @@ LaunchResult boundary_tet4(const KParams& k, int nc, int form, long long n, cuda
 
 GeometryOps geometry_ops_tet4() { return GeometryDispatch<3, 4, 4>::ops(); }
 
+BoundaryInfo boundary_info_tet4(int nc) { return BoundaryInfoDispatch<3, 4, 4, 3>::info(nc); }
+
 }  // namespace gales

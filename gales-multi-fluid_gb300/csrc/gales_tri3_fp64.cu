@@ -13,4 +13,6 @@ LaunchResult boundary_tri3(const KParams& k, int nc, int form, long long n, cuda
 
 GeometryOps geometry_ops_tri3() { return GeometryDispatch<2, 3, 3>::ops(); }
 
+BoundaryInfo boundary_info_tri3(int nc) { return BoundaryInfoDispatch<2, 3, 3, 2>::info(nc); }
+
 }  // namespace gales
