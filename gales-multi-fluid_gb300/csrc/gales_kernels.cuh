@@ -351,6 +351,30 @@ __global__ void __launch_bounds__(128) geometry_kernel(const double* __restrict_
   if (!(q.J > 0.0)) flag_error(k, GALES_ERR_NEG_JACOBIAN, e);
 }
 
+// compute_h where its branches hang on rounding (rank-one velocity field): the point
+// velocity and its gradient formed with the reference's operations (quad.hpp:817-885),
+// then compute_h.  Rarely taken, so kept out of line.
+template <int DIM, int NEN, int ND>
+__device__ __noinline__ double compute_h_reference(const double* __restrict__ I, const int* nodes, const double* sh,
+                                                   const ElemGeo<DIM, NEN>& q) {
+  double ve[DIM], dve[DIM][DIM];
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) {
+    double x = 0.0;
+#pragma unroll
+    for (int i = 0; i < NEN; ++i) x += sh[i] * __ldg(I + (long long)nodes[i] * ND + 1 + a);
+    ve[a] = x;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      double b = 0.0;
+#pragma unroll
+      for (int i = 0; i < NEN; ++i) b += q.ds[d][i] * __ldg(I + (long long)nodes[i] * ND + 1 + a);
+      dve[a][d] = b;
+    }
+  }
+  return compute_h<DIM>(q.G, ve, dve);
+}
+
 // Point phase for one (element, quadrature point).
 //   GALES_FORM_FP64 : every step in FP64 with the reference's operations; tau uses
 //                     the uBLAS-faithful LU inverse.
@@ -390,15 +414,9 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
         Pq[j] += sh[i] * __ldg(pi + j);
         Iq[j] += sh[i] * Ie[i][j];
       } else {
-        // the velocity keeps the reference's operations (it enters compute_h); P and I
-        // are interpolated alike so that P == I gives U == U_P exactly
-        if (j >= 1 && j <= DIM) {
-          Pq[j] += sh[i] * __ldg(pi + j);
-          Iq[j] += sh[i] * Ie[i][j];
-        } else {
-          Pq[j] = fma(sh[i], __ldg(pi + j), Pq[j]);
-          Iq[j] = fma(sh[i], Ie[i][j], Iq[j]);
-        }
+        // P and I are interpolated alike so that P == I gives U == U_P exactly
+        Pq[j] = fma(sh[i], __ldg(pi + j), Pq[j]);
+        Iq[j] = fma(sh[i], Ie[i][j], Iq[j]);
       }
     }
   }
@@ -429,7 +447,8 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
         for (int d = 0; d < DIM; ++d) dI[d][j] = fmaf(narrow_rn(q.ds[d][i]), dif, dI[d][j]);
       }
   }
-  // velocity gradient in FP64 with the reference's operations (input of compute_h)
+  // velocity gradient in FP64 (input of compute_h; fused in the mixed form, whose
+  // compute_h falls back to the reference's operations where they matter)
   double dv[DIM][DIM];
 #pragma unroll
   for (int a = 0; a < DIM; ++a)
@@ -438,9 +457,9 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       if constexpr (FORM == GALES_FORM_FP64) {
         dv[a][d] = dI[d][1 + a];
       } else {
-        double b = 0.0;
+        double b = q.ds[d][0] * Ie[0][1 + a];
 #pragma unroll
-        for (int i = 0; i < NEN; ++i) b += q.ds[d][i] * Ie[i][1 + a];
+        for (int i = 1; i < NEN; ++i) b = fma(q.ds[d][i], Ie[i][1 + a], b);
         dv[a][d] = b;
       }
     }
@@ -514,8 +533,13 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
   const double v_nrm = sqrt(vsq<DIM>(v));
   if (v_nrm >= kEps && k.tau != GALES_TAU_NONE) {
     double h;
-    if constexpr (FORM == GALES_FORM_FP64) h = compute_h<DIM>(q.G, v, dv);
-    else h = compute_h_mixed<DIM>(q.G, v, dv);
+    if constexpr (FORM == GALES_FORM_FP64) {
+      h = compute_h<DIM>(q.G, v, dv);
+    } else {
+      bool decided;
+      h = compute_h_fast<DIM>(q.G, v, dv, decided);
+      if (!decided) h = compute_h_reference<DIM, NEN, ND>(k.I, nodes, sh, q);
+    }
     double trG = 0.0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) trG += q.G[d][d];

@@ -721,12 +721,6 @@ __device__ __forceinline__ double compute_h(const double (&G)[DIM][DIM], const d
   return 2 * sqrt(fabs(h));
 }
 
-// compute_h for the mixed form.  The steps that decide its branches (s0, the
-// cross-stream residual s1 and |s1| against DBL_EPSILON) keep the reference's IEEE
-// operations, so the same branch is taken as in the FP64 form.  When s1 is a
-// direction (the common case) the remaining steps are insensitive to rounding and
-// use fused operations and one reciprocal per normalisation; the rank-one case
-// (s1 rounding noise) and a near-degenerate third direction take compute_h itself.
 template <int DIM>
 __device__ __forceinline__ double qform_fma(const double (&G)[DIM][DIM], const double* s) {
   double r = 0.0;
@@ -740,28 +734,44 @@ __device__ __forceinline__ double qform_fma(const double (&G)[DIM][DIM], const d
   return r;
 }
 
+// compute_h for the mixed form, with fused operations and one reciprocal per
+// normalisation.  compute_h branches on |s1| > DBL_EPSILON, where s1 (the part of
+// dv v normal to v) is rounding noise for a rank-one velocity field (every node but
+// one at rest); there only the reference's exact operations take the reference's
+// branch.  This routine decides the branch only when |s1| exceeds 1e-10 |dv v| (and
+// 1e3 DBL_EPSILON), far above what rounding can move, and so does the third
+// direction |s0 x s1|; otherwise it returns with decided = false and the caller runs
+// compute_h on the velocity and gradient formed with the reference's operations.
 template <int DIM>
-__device__ __forceinline__ double compute_h_mixed(const double (&G)[DIM][DIM], const double* v,
-                                                  const double (&dv)[DIM][DIM]) {
-  const double nrm_v = sqrt(vsq<DIM>(v));
+__device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], const double* v,
+                                                 const double (&dv)[DIM][DIM], bool& decided) {
+  decided = false;
+  double vv = v[0] * v[0];
+#pragma unroll
+  for (int i = 1; i < DIM; ++i) vv = fma(v[i], v[i], vv);
+  const double iv = 1.0 / sqrt(vv);
   double s0[DIM], acc[DIM], s1[DIM];
 #pragma unroll
-  for (int i = 0; i < DIM; ++i) s0[i] = v[i] / nrm_v;
+  for (int i = 0; i < DIM; ++i) s0[i] = v[i] * iv;
+  double aa = 0.0, ip = 0.0;
 #pragma unroll
   for (int i = 0; i < DIM; ++i) {
-    double t = 0.0;
+    double t = dv[i][0] * v[0];
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) t += dv[i][j] * v[j];
+    for (int j = 1; j < DIM; ++j) t = fma(dv[i][j], v[j], t);
     acc[i] = t;
+    aa = fma(t, t, aa);
+    ip = fma(t, s0[i], ip);
   }
-  double ip = 0.0;
+  double n1 = 0.0;
 #pragma unroll
-  for (int i = 0; i < DIM; ++i) ip += acc[i] * s0[i];
-#pragma unroll
-  for (int i = 0; i < DIM; ++i) s1[i] = acc[i] - ip * s0[i];
-  const double nrm_s1 = sqrt(vsq<DIM>(s1));
-  if (!(nrm_s1 > kEps)) return compute_h<DIM>(G, v, dv);
-  const double i1 = 1.0 / nrm_s1;
+  for (int i = 0; i < DIM; ++i) {
+    s1[i] = fma(-ip, s0[i], acc[i]);
+    n1 = fma(s1[i], s1[i], n1);
+  }
+  n1 = sqrt(n1);
+  if (!(n1 > fmax(1.0e-10 * sqrt(aa), 1.0e3 * kEps))) return 0.0;
+  const double i1 = 1.0 / n1;
 #pragma unroll
   for (int i = 0; i < DIM; ++i) s1[i] *= i1;
   double a[3];
@@ -774,12 +784,13 @@ __device__ __forceinline__ double compute_h_mixed(const double (&G)[DIM][DIM], c
     s2[1] = fma(s1[0], s0[2], -s1[2] * s0[0]);
     s2[2] = fma(s0[0], s1[1], -s0[1] * s1[0]);
     const double n2 = sqrt(fma(s2[0], s2[0], fma(s2[1], s2[1], s2[2] * s2[2])));
-    if (!(n2 > 1.0e3 * kEps)) return compute_h<DIM>(G, v, dv);
+    if (!(n2 > 1.0e3 * kEps)) return 0.0;
     const double i2 = 1.0 / n2;
 #pragma unroll
     for (int i = 0; i < 3; ++i) s2[i] *= i2;
     a[2] = qform_fma<DIM>(G, s2);
   }
+  decided = true;
   double h;
   if (DIM == 3 && a[0] != 0.0 && a[1] != 0.0 && a[2] != 0.0) {
     // 1/a0 + 1/a1 + 1/a2 with one division
