@@ -861,26 +861,27 @@ __device__ __forceinline__ S kd_entry(const C& c, const S* gb, S gbv, int l, int
   return (col == r) ? c.rhoD[r - L::iY] * gb[l] : S(0);
 }
 
-// Exact widening of binary32 to binary64 with integer operations only (see
-// narrow_rn): exponent rebias 127 -> 1023, significand shifted into the top of the
-// 52-bit field; subnormals normalised, infinities and NaN keep their payload.
+// Exact widening of binary32 to binary64 with 32-bit integer operations only (see
+// narrow_rn): exponent rebias 127 -> 1023, the 23-bit significand split over the two
+// words; subnormals normalised, infinities and NaN keep their payload.
 __device__ __forceinline__ double widen(float f) {
   const unsigned int u = __float_as_uint(f);
-  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-  const unsigned int ex = (u >> 23) & 0xffu, m = u & 0x7fffffu;
-  unsigned long long bits;
+  const unsigned int sign = u & 0x80000000u;
+  const unsigned int ex = (u >> 23) & 0xffu;
+  unsigned int m = u & 0x7fffffu, e64;
   if (ex - 1u < 254u) {
-    bits = ((unsigned long long)(ex + (1023u - 127u)) << 52) | ((unsigned long long)m << 29);
+    e64 = ex + (1023u - 127u);
   } else if (ex == 0xffu) {
-    bits = (0x7ffull << 52) | ((unsigned long long)m << 29);
+    e64 = 0x7ffu;
   } else if (m == 0u) {
-    bits = 0ull;
+    return __hiloint2double((int)sign, 0);
   } else {
     // subnormal m * 2^-149: leading one at bit p = 31 - clz(m)
     const int p = 31 - __clz((int)m);
-    bits = ((unsigned long long)(p - 149 + 1023) << 52) | (((unsigned long long)m << (52 - p)) & 0xfffffffffffffull);
+    e64 = (unsigned int)(p - 149 + 1023);
+    m = (m << (23 - p)) & 0x7fffffu;
   }
-  return __longlong_as_double((long long)(sign | bits));
+  return __hiloint2double((int)(sign | (e64 << 20) | (m >> 3)), (int)(m << 29));
 }
 __device__ __forceinline__ double widen(double d) { return d; }
 
@@ -1306,12 +1307,12 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
       if (cx >= N) break;
       const int a = cx / ND, ja = cx - a * ND;
       for (int sb_ = 0; sb_ < NEN; ++sb_) {
-        const int64_t coff = (int64_t)__ldg(k.slot + (e * NEN + sb_) * NEN + a) * ND + ja;
-        for (int jb = warp; jb < ND; jb += WPE) {
-          const int srw = sb_ * ND + jb;
-          const double val = E.u.stage[srw * NS + cx];
-          if ((__double_as_longlong(val) << 1) != 0)
-            add_to(k.vals + E.rowbase[sb_] + (int64_t)jb * E.rowlen[sb_] + coff, val, mode);
+        double* row = k.vals + E.rowbase[sb_] + (int64_t)warp * E.rowlen[sb_] +
+                      (int64_t)__ldg(k.slot + (e * NEN + sb_) * NEN + a) * ND + ja;
+        const int64_t step = (int64_t)WPE * E.rowlen[sb_];
+        for (int jb = warp; jb < ND; jb += WPE, row += step) {
+          const double val = E.u.stage[(sb_ * ND + jb) * NS + cx];
+          if ((__double2hiint(val) & 0x7fffffff) | __double2loint(val)) add_to(row, val, mode);
         }
       }
     }

@@ -40,26 +40,25 @@ struct DevChem {
 // The hardware conversions between binary64 and binary32 issue on the FP64 pipe,
 // which the point stage already saturates, and a conversion kept for rare operands
 // behind a branch is still issued (predicated off) for every value.  narrow_rn and
-// widen are therefore integer-only.
+// widen are therefore integer-only, on the two 32-bit words of the binary64 value.
 
 // Round-to-nearest-even narrowing of binary64 to binary32 (52-bit significand cut to
 // 23 bits, ties to even, carry into the exponent, overflow to infinity, NaN kept
 // quiet).  Results below the smallest normal binary32 (|x| < 2^-126) flush to a
 // signed zero instead of a subnormal.
 __device__ __forceinline__ float narrow_rn(double d) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
-  const unsigned int hi = (unsigned int)(u >> 32);
+  const unsigned int hi = (unsigned int)__double2hiint(d), lo = (unsigned int)__double2loint(d);
   const unsigned int sign = hi & 0x80000000u;
   const int e64 = (int)((hi >> 20) & 0x7ffu);
   const int e = e64 - (1023 - 127);
-  const unsigned int m = (unsigned int)((u >> 29) & 0x7fffffu);
+  const unsigned int m = ((hi & 0xfffffu) << 3) | (lo >> 29);
   unsigned int bits;
   if (e >= 1 && e <= 254) {
-    const unsigned int rest = (unsigned int)(u & 0x1fffffffu);
+    const unsigned int rest = lo & 0x1fffffffu;
     bits = sign | ((unsigned int)e << 23) | m;
     if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
   } else if (e64 == 0x7ff) {
-    const bool nan = (u & 0xfffffffffffffull) != 0ull;
+    const bool nan = ((hi & 0xfffffu) | lo) != 0u;
     bits = sign | 0x7f800000u | (nan ? (m | 0x400000u) : 0u);
   } else {
     bits = sign | (e >= 255 ? 0x7f800000u : 0u);
