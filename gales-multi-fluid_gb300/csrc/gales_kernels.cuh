@@ -352,8 +352,9 @@ __global__ void __launch_bounds__(128) geometry_kernel(const double* __restrict_
 }
 
 // compute_h where its branches hang on rounding (rank-one velocity field): the point
-// velocity and its gradient formed with the reference's operations (quad.hpp:817-885),
-// then compute_h.  Rarely taken, so kept out of line.
+// velocity and its gradient formed with the reference's operations (quad.hpp:817-885,
+// unfused whatever the unit's contraction setting), then compute_h.  Rarely taken, so
+// kept out of line.
 template <int DIM, int NEN, int ND>
 __device__ __noinline__ double compute_h_reference(const double* __restrict__ I, const int* nodes, const double* sh,
                                                    const ElemGeo<DIM, NEN>& q) {
@@ -362,13 +363,13 @@ __device__ __noinline__ double compute_h_reference(const double* __restrict__ I,
   for (int a = 0; a < DIM; ++a) {
     double x = 0.0;
 #pragma unroll
-    for (int i = 0; i < NEN; ++i) x += sh[i] * __ldg(I + (long long)nodes[i] * ND + 1 + a);
+    for (int i = 0; i < NEN; ++i) x = add_rn(x, mul_rn(sh[i], __ldg(I + (long long)nodes[i] * ND + 1 + a)));
     ve[a] = x;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       double b = 0.0;
 #pragma unroll
-      for (int i = 0; i < NEN; ++i) b += q.ds[d][i] * __ldg(I + (long long)nodes[i] * ND + 1 + a);
+      for (int i = 0; i < NEN; ++i) b = add_rn(b, mul_rn(q.ds[d][i], __ldg(I + (long long)nodes[i] * ND + 1 + a)));
       dve[a][d] = b;
     }
   }

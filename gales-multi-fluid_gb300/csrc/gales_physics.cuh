@@ -662,10 +662,25 @@ __device__ __forceinline__ void tau_closed(const Coef<DIM, NC>& c, double irho, 
 }
 
 // compute_h: quad.hpp:356-383 (2D), 701-739 (3D).  dv[i][j] = d v_i / d x_j.
+// IEEE multiply/add/subtract that are never fused into a multiply-add, whatever the
+// translation unit's contraction setting: the steps of compute_h whose rounding
+// decides its branches use them.
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+template <int DIM>
+__device__ __forceinline__ double vsq_rn(const double* v) {
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) s = add_rn(s, mul_rn(v[k], v[k]));
+  return s;
+}
+
 template <int DIM>
 __device__ __forceinline__ double compute_h(const double (&G)[DIM][DIM], const double* v,
                                             const double (&dv)[DIM][DIM]) {
-  double nrm_v = sqrt(vsq<DIM>(v));
+  double nrm_v = sqrt(vsq_rn<DIM>(v));
   double s0[DIM], s1[DIM], alpha[DIM];
 #pragma unroll
   for (int i = 0; i < DIM; ++i) s0[i] = v[i] / nrm_v;
@@ -675,12 +690,12 @@ __device__ __forceinline__ double compute_h(const double (&G)[DIM][DIM], const d
     for (int i = 0; i < DIM; ++i) {
       double t = 0.0;
 #pragma unroll
-      for (int j = 0; j < DIM; ++j) t += G[i][j] * s[j];
+      for (int j = 0; j < DIM; ++j) t = add_rn(t, mul_rn(G[i][j], s[j]));
       Gs[i] = t;
     }
     double r = 0.0;
 #pragma unroll
-    for (int i = 0; i < DIM; ++i) r += s[i] * Gs[i];
+    for (int i = 0; i < DIM; ++i) r = add_rn(r, mul_rn(s[i], Gs[i]));
     return r;
   };
   alpha[0] = quadform(s0);
@@ -689,25 +704,25 @@ __device__ __forceinline__ double compute_h(const double (&G)[DIM][DIM], const d
   for (int i = 0; i < DIM; ++i) {
     double t = 0.0;
 #pragma unroll
-    for (int j = 0; j < DIM; ++j) t += dv[i][j] * v[j];
+    for (int j = 0; j < DIM; ++j) t = add_rn(t, mul_rn(dv[i][j], v[j]));
     acc[i] = t;
   }
   double ip = 0.0;
 #pragma unroll
-  for (int i = 0; i < DIM; ++i) ip += acc[i] * s0[i];
+  for (int i = 0; i < DIM; ++i) ip = add_rn(ip, mul_rn(acc[i], s0[i]));
 #pragma unroll
-  for (int i = 0; i < DIM; ++i) s1[i] = acc[i] - ip * s0[i];
-  const double nrm_s1 = sqrt(vsq<DIM>(s1));
+  for (int i = 0; i < DIM; ++i) s1[i] = sub_rn(acc[i], mul_rn(ip, s0[i]));
+  const double nrm_s1 = sqrt(vsq_rn<DIM>(s1));
   if (nrm_s1 > kEps)
 #pragma unroll
     for (int i = 0; i < DIM; ++i) s1[i] /= nrm_s1;
   alpha[1] = quadform(s1);
   if constexpr (DIM == 3) {
     double s2[3];
-    s2[0] = s0[1] * s1[2] - s0[2] * s1[1];
-    s2[1] = s1[0] * s0[2] - s1[2] * s0[0];
-    s2[2] = s0[0] * s1[1] - s0[1] * s1[0];
-    const double nrm_s2 = sqrt(vsq<3>(s2));
+    s2[0] = sub_rn(mul_rn(s0[1], s1[2]), mul_rn(s0[2], s1[1]));
+    s2[1] = sub_rn(mul_rn(s1[0], s0[2]), mul_rn(s1[2], s0[0]));
+    s2[2] = sub_rn(mul_rn(s0[0], s1[1]), mul_rn(s0[1], s1[0]));
+    const double nrm_s2 = sqrt(vsq_rn<3>(s2));
     if (nrm_s2 > kEps)
 #pragma unroll
       for (int i = 0; i < 3; ++i) s2[i] /= nrm_s2;
@@ -716,7 +731,7 @@ __device__ __forceinline__ double compute_h(const double (&G)[DIM][DIM], const d
   double h = 0.0;
 #pragma unroll
   for (int i = 0; i < DIM; ++i)
-    if (alpha[i] != 0.0) h += 1.0 / alpha[i];
+    if (alpha[i] != 0.0) h = add_rn(h, 1.0 / alpha[i]);
   return 2 * sqrt(fabs(h));
 }
 
