@@ -146,7 +146,10 @@ void parallel_for(int64_t n, F f) {
 // Each point-record chunk buffer holds this many bytes; two of them stay resident
 // in L2 (about a quarter of the 129 MB) while the CSR values stream through it.
 constexpr int kVjpAux = 3 * GALES_MAX_COMP + GALES_MAX_ND;
-constexpr size_t kChunkBytes = size_t(32) << 20;
+// Chunks of the interior pipeline: whole waves of the point kernel (every SM holding
+// as many of its CTAs as fit), kWaves waves per chunk.
+constexpr int kWaves = 1;
+constexpr int kRing = 3;    // point-record buffers in flight between the two stages
 
 GeometryOps geometry_ops(int dim, int nen) {
   if (dim == 2 && nen == 3) return geometry_ops_tri3();
@@ -238,10 +241,12 @@ struct gales_asm {
   int32_t scatter_mode = GALES_SCATTER_ATOMIC;
   // interior pipeline: point-record chunk buffers (scratch) and two internal streams
   InteriorOps ops[2];
-  DevBuf<unsigned char> qpbuf[2];
+  DevBuf<unsigned char> qpbuf[kRing];
+  long long chunk_elems[2] = {1, 1};   // elements per chunk, per form
   DevBuf<unsigned char> d_geo;   // element geometry at the interior points (mesh.hpp:468-495)
   cudaStream_t ist[2] = {nullptr, nullptr};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  cudaEvent_t ev_pt[kRing] = {}, ev_mx[kRing] = {};   // chunk in a buffer written / consumed
   cudaStream_t bst = nullptr;                  // boundary pass, concurrent with the interior
   cudaEvent_t ev_bfork = nullptr, ev_bjoin = nullptr;
   int status = 0;
@@ -722,16 +727,36 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   for (int i = 0; i < 4; ++i)
     if ((ce = cudaEventCreate(&h->evp[i])) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+  for (int i = 0; i < kRing; ++i) {
+    if ((ce = cudaEventCreateWithFlags(&h->ev_pt[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+    if ((ce = cudaEventCreateWithFlags(&h->ev_mx[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+  }
   if ((ce = cudaEventCreateWithFlags(&h->ev_bfork, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreateWithFlags(&h->ev_bjoin, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaStreamCreateWithFlags(&h->bst, cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
   for (int i = 0; i < 2; ++i) {
     if ((ce = cudaEventCreateWithFlags(&h->ev_join[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+    // ist[0] runs the point stage, ist[1] the matrix stage
     if ((ce = cudaStreamCreateWithFlags(&h->ist[i], cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
-    if ((ce = h->qpbuf[i].alloc(kChunkBytes)) != cudaSuccess) return bail(ce, "point-record buffer");
+
   }
   h->ops[GALES_FORM_FP64] = interior_ops(h->dim, h->nen, GALES_FORM_FP64);
   h->ops[GALES_FORM_MIXED] = interior_ops(h->dim, h->nen, GALES_FORM_MIXED);
+  {  // chunk size per form from the point kernel's occupancy; record buffers for the larger
+    int sms = 0;
+    if ((ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+      return bail(ce, "device attribute");
+    size_t bytes = 0;
+    for (int f = 0; f < 2; ++f) {
+      const size_t rb = h->ops[f].rec_bytes(h->nc);
+      if (rb == 0) continue;
+      const long long wave = (long long)sms * h->ops[f].point_occupancy(h->nc) * 128 / h->ei.nq;
+      h->chunk_elems[f] = std::max<long long>(1, std::min<long long>(kWaves * wave, std::max<int64_t>(h->n_el, 1)));
+      bytes = std::max(bytes, rb * (size_t)h->chunk_elems[f]);
+    }
+    for (int i = 0; i < kRing; ++i)
+      if ((ce = h->qpbuf[i].alloc(std::max<size_t>(bytes, 16))) != cudaSuccess) return bail(ce, "point-record buffer");
+  }
   for (int f = 0; f < 2; ++f) {  // kernel attributes, once, outside any stream capture
     if ((ce = h->ops[f].prepare(h->nc)) != cudaSuccess) return bail(ce, "kernel attributes");
     KParams k0;
@@ -813,10 +838,14 @@ void gales_asm_destroy(gales_asm* h) {
   if (h->ev_bfork) cudaEventDestroy(h->ev_bfork);
   if (h->ev_bjoin) cudaEventDestroy(h->ev_bjoin);
   if (h->bst) cudaStreamDestroy(h->bst);
+  for (int i = 0; i < kRing; ++i) {
+    h->qpbuf[i].release();
+    if (h->ev_pt[i]) cudaEventDestroy(h->ev_pt[i]);
+    if (h->ev_mx[i]) cudaEventDestroy(h->ev_mx[i]);
+  }
   for (int i = 0; i < 2; ++i) {
     if (h->ev_join[i]) cudaEventDestroy(h->ev_join[i]);
     if (h->ist[i]) cudaStreamDestroy(h->ist[i]);
-    h->qpbuf[i].release();
   }
   delete h;
 }
@@ -930,15 +959,17 @@ KParams base_params(gales_asm* h, double dt) {
 }
 
 // Interior pass over n listed elements (k.el_list, or elements 0..n-1): point stage then
-// matrix stage per chunk.  With atomics the chunks alternate between two internal
-// streams so that one chunk's FP64 point stage overlaps the previous chunk's matrix
-// stage; plain read-modify-write (coloured batches) keeps them on the caller's stream.
+// matrix stage per chunk.  Concurrent (atomic scatter): the point stage runs on ist[0]
+// and the matrix stage on ist[1], chunk c's matrix waiting on its
+// records (ev_pt) and chunk c+kRing's point stage waiting until chunk c's buffer has
+// been consumed (ev_mx).  Otherwise (plain read-modify-write of coloured batches)
+// both stages run on the caller's stream.
 int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long long n, cudaStream_t st,
                  bool concurrent) {
   const InteriorOps& ops = h->ops[form];
   const size_t rb = ops.rec_bytes(h->nc);
   if (rb == 0) return fail(h, GALES_ERR_UNSUPPORTED, "no interior kernel for this element/component count");
-  const long long chunk = std::max<long long>(1, (long long)(kChunkBytes / rb));
+  const long long chunk = h->chunk_elems[form];
   const long long nchunks = (n + chunk - 1) / chunk;
   if (nchunks == 0) return 0;
   if (concurrent) {
@@ -947,14 +978,21 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
   }
   for (long long c = 0; c < nchunks; ++c) {
     const long long first = c * chunk, cnt = std::min(chunk, n - first);
-    cudaStream_t s = concurrent ? h->ist[c & 1] : st;
-    void* buf = h->qpbuf[concurrent ? (c & 1) : 0].p;
-    LaunchResult r = ops.point(k, h->nc, buf, first, cnt, s);
+    const int slot = (int)(c % kRing);
+    void* buf = h->qpbuf[concurrent ? slot : 0].p;
+    cudaStream_t sp = concurrent ? h->ist[0] : st, sm = concurrent ? h->ist[1] : st;
+    if (concurrent && c >= kRing) CK(h, cudaStreamWaitEvent(sp, h->ev_mx[slot], 0), "stream wait");
+    LaunchResult r = ops.point(k, h->nc, buf, first, cnt, sp);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "point kernel");
     h->launches += r.launches;
-    r = ops.matrix(k, h->nc, want_m, buf, first, cnt, s);
+    if (concurrent) {
+      CK(h, cudaEventRecord(h->ev_pt[slot], sp), "event");
+      CK(h, cudaStreamWaitEvent(sm, h->ev_pt[slot], 0), "stream wait");
+    }
+    r = ops.matrix(k, h->nc, want_m, buf, first, cnt, sm);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "matrix kernel");
     h->launches += r.launches;
+    if (concurrent) CK(h, cudaEventRecord(h->ev_mx[slot], sm), "event");
   }
   if (concurrent) {
     for (int i = 0; i < 2; ++i) {

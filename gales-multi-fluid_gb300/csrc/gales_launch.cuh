@@ -22,6 +22,14 @@ struct InteriorInst {
   using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
   using M = MatShape<DIM, NEN, NC>;
   static size_t rec_bytes() { return sizeof(Rec) * NQ; }
+  // resident point-kernel CTAs (128 threads) per SM
+  static int point_occupancy() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, point_kernel<DIM, NEN, NC, NQ, FORM, S>, 128, 0) !=
+        cudaSuccess)
+      return 1;
+    return nb > 0 ? nb : 1;
+  }
   static LaunchResult point(const KParams& k, void* buf, long long first, long long n, cudaStream_t st) {
     if (n <= 0) return {cudaSuccess, 0};
     const long long threads = n * NQ;
@@ -76,6 +84,7 @@ LaunchResult launch_boundary_nc(const KParams& k, long long n_items, cudaStream_
 // stage and matrix stage, for 1..4 components.
 struct InteriorOps {
   cudaError_t (*prepare)(int nc);
+  int (*point_occupancy)(int nc);
   size_t (*rec_bytes)(int nc);
   LaunchResult (*point)(const KParams&, int nc, void* buf, long long first, long long n, cudaStream_t);
   LaunchResult (*matrix)(const KParams&, int nc, bool want_m, const void* buf, long long first, long long n,
@@ -99,6 +108,12 @@ struct InteriorDispatch {
 #undef GALES_C
     return cudaErrorInvalidValue;
   }
+  static int point_occupancy(int nc) {
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::point_occupancy()
+    GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+    return 1;
+  }
   static size_t rec_bytes(int nc) {
 #define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::rec_bytes()
     GALES_NC_SWITCH(nc, GALES_C)
@@ -118,7 +133,7 @@ struct InteriorDispatch {
 #undef GALES_C
     return {cudaErrorInvalidValue, 0};
   }
-  static InteriorOps ops() { return {&prepare, &rec_bytes, &point, &matrix}; }
+  static InteriorOps ops() { return {&prepare, &point_occupancy, &rec_bytes, &point, &matrix}; }
 };
 
 // Boundary pass of one element type; S is the matrix arithmetic type of the form.
