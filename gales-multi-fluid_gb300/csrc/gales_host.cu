@@ -926,6 +926,7 @@ KParams base_params(gales_asm* h, double dt) {
     d.inv_R = q.kind == GALES_CH_IDEAL_GAS ? 1.0 / q.R : 0.0;
     d.R_over_gamma = q.kind == GALES_CH_IDEAL_GAS ? q.R / q.gamma : 0.0;
     d.inv_D = 1.0 / q.chemical_diffusivity;
+    if (q.kind == GALES_CH_IDEAL_GAS) k.has_gas = 1;
   }
   k.dt = dt;
   k.inv_dt = 1.0 / dt;

@@ -37,6 +37,7 @@ struct KParams {
   double gp[8][3];
   double W_in, W_bd;
   int32_t tau, dc_2006, steady;
+  int32_t has_gas;             // some component is an ideal gas (mixed-form EOS)
   int32_t n_sides, n_side_nodes, n_side_q;
   uint32_t dirichlet_mask[GALES_MAX_FLAGS];
   double sgp[6][4][3];
@@ -421,6 +422,13 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       }
     }
   }
+  // (I - P)/dt at the point, in the form's type (the least-squares mass term)
+  R dd[ND];
+#pragma unroll
+  for (int j = 0; j < ND; ++j) {
+    if constexpr (FORM == GALES_FORM_FP64) dd[j] = (Iq[j] - Pq[j]) / k.dt;
+    else dd[j] = narrow_rn(Iq[j] - Pq[j]) * narrow_rn(k.inv_dt);
+  }
   // gradients: FP64 in the FP64 form; FP32 of nodal differences in the mixed form
   // (sum_i dN_i/dx = 0, so sum_i dN_i (I_i - I_0) is the same gradient)
   R dI[DIM][ND];
@@ -464,27 +472,43 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
         dv[a][d] = b;
       }
     }
-  // previous-level conservative vector U_P (props at P with shear rate 0)
+  // previous-level conservative vector U_P (props at P with shear rate 0) and the
+  // current iterate's properties and U
   double p, v[DIM], T, Y[NC];
-  assign<DIM, NC>(Pq, p, v, T, Y);
-  double rhoP, cvP;
-  if constexpr (FORM == GALES_FORM_FP64) mixture_rho_cv<NC>(k.ch, p, T, Y, rhoP, cvP);
-  else mixture_rho_cv_fast<NC>(k.ch, p, T, Y, rhoP, cvP);
-  double UP[ND];
-  conservative<DIM, NC>(rhoP, cvP, v, T, Y, UP);
-  // current iterate
-  assign<DIM, NC>(Iq, p, v, T, Y);
+  double UP[ND], U[ND];
   Props<NC> pr;
   Coef<DIM, NC> c;
+  double v_nrm, iv = 0.0;
   if constexpr (FORM == GALES_FORM_FP64) {
+    assign<DIM, NC>(Pq, p, v, T, Y);
+    double rhoP, cvP;
+    mixture_rho_cv<NC>(k.ch, p, T, Y, rhoP, cvP);
+    conservative<DIM, NC>(rhoP, cvP, v, T, Y, UP);
+    assign<DIM, NC>(Iq, p, v, T, Y);
     mixture<NC>(k.ch, p, T, Y, pr);
     make_coef<DIM, NC>(pr, p, v, T, Y, c);
+    conservative<DIM, NC>(pr.rho, pr.cv, v, T, Y, U);
+    v_nrm = sqrt(vsq<DIM>(v));
   } else {
-    mixture_fast<NC>(k.ch, p, T, Y, pr);
-    make_coef_fast<DIM, NC>(pr, p, v, T, Y, c);
+    double pP, vP[DIM], TP, YP[NC];
+    assign<DIM, NC>(Pq, pP, vP, TP, YP);
+    assign<DIM, NC>(Iq, p, v, T, Y);
+    double rhoP, cvP;
+    mixture_pair_fast<NC>(k.ch, k.has_gas != 0, pP, TP, YP, p, T, Y, rhoP, cvP, pr);
+    conservative<DIM, NC>(rhoP, cvP, vP, TP, YP, UP);
+    double vv = v[0] * v[0];
+#pragma unroll
+    for (int d = 1; d < DIM; ++d) vv = fma(v[d], v[d], vv);
+    make_coef_fast<DIM, NC>(pr, p, v, vv, T, Y, c);
+    U[0] = pr.rho;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) U[1 + d] = pr.rho * v[d];
+    U[L::iT] = pr.rho * c.E;
+#pragma unroll
+    for (int i = 0; i < NC - 1; ++i) U[L::iY + i] = pr.rho * Y[i];
+    iv = rsqrt(vv);
+    v_nrm = vv > 0.0 ? vv * iv : 0.0;
   }
-  double U[ND];
-  conservative<DIM, NC>(pr.rho, pr.cv, v, T, Y, U);
   const double dt = k.dt;
   // source S (gravity; fluid_2d.hpp:597-599) and the mass-term coefficient (U - U_P)/dt - S
   R SvR[ND];
@@ -520,31 +544,39 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
 #pragma unroll
     for (int j = 0; j < ND; ++j) out.rv[j] = fmaf(narrow_rn(U[j] - UP[j]), idt, -SvR[j]);
   }
+  R Ur[ND];  // U in the form's type (discontinuity capturing)
+#pragma unroll
+  for (int j = 0; j < ND; ++j) Ur[j] = to_s<R>(U[j]);
   // the coefficients in the form's type R
   using CR = Coef<DIM, NC, R>;
   CR cr;
   if constexpr (FORM == GALES_FORM_FP64) cr = c;
   else cr = narrow<DIM, NC>(c);
-  // tau (fluid_2d.hpp:877-1022)
-  double tau[ND][ND];
+  // tau (fluid_2d.hpp:877-1022).  The branches give its diagonal parameters td; the FP64
+  // form then forms DUDY^{-1} diag(td) by LU, the mixed form in closed form, narrowed to
+  // FP32 entry by entry and only where it can be nonzero (tau_nz).
+  R tau[ND][ND];
 #pragma unroll
   for (int r = 0; r < ND; ++r)
 #pragma unroll
-    for (int cc = 0; cc < ND; ++cc) tau[r][cc] = 0.0;
-  const double v_nrm = sqrt(vsq<DIM>(v));
+    for (int cc = 0; cc < ND; ++cc) tau[r][cc] = R(0);
   if (v_nrm >= kEps && k.tau != GALES_TAU_NONE) {
-    double h;
+    double h, idet = 0.0;
+    bool have_idet = false;
     if constexpr (FORM == GALES_FORM_FP64) {
       h = compute_h<DIM>(q.G, v, dv);
     } else {
       bool decided;
-      h = compute_h_fast<DIM>(q.G, v, dv, decided);
+      h = compute_h_fast<DIM>(q.G, v, iv, dv, decided);
       if (!decided) h = compute_h_reference<DIM, NEN, ND>(k.I, nodes, sh, q);
     }
     double trG = 0.0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) trG += q.G[d][d];
     const double cs = pr.c, rho = pr.rho, mu = pr.mu, cv = pr.cv, kappa = pr.kappa;
+    double td[ND];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) td[i] = 0.0;
     bool nondiag = false;
     if (k.tau == GALES_TAU_NON_DIAG_COMP_2001) {
       double lambda_sqr = 0.0 * (v_nrm * v_nrm + cs * cs) + (0.0) * 0.5 * cs * cs;
@@ -552,38 +584,43 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       if (!k.steady) lambda_sqr += 4 / (dt * dt);
       const double lam = 1.0 / sqrt(lambda_sqr) + h / (2 * v_nrm);
       const double use = k.steady ? lam : fmin(dt * 0.5, lam);
-      tau[0][0] = use;
+      td[0] = use;
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) tau[1 + d][1 + d] = fmin(use, rho * h * h / (mu * 12));
-      tau[L::iT][L::iT] = fmin(use, rho * h * h * cv / (kappa * 12));
+      for (int d = 0; d < DIM; ++d) td[1 + d] = fmin(use, rho * h * h / (mu * 12));
+      td[L::iT] = fmin(use, rho * h * h * cv / (kappa * 12));
 #pragma unroll
-      for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = fmin(use, h * h / (pr.D_c[i] * 12));
+      for (int i = 0; i < NC - 1; ++i) td[L::iY + i] = fmin(use, h * h / (pr.D_c[i] * 12));
       nondiag = true;
     } else if (FORM == GALES_FORM_MIXED && k.tau == GALES_TAU_NON_DIAG_COMP_2019) {
-      // the same parameters with fewer divisions (mixed form)
-      const double hv = (0.5 * h) * fma(2.0, v_nrm, cs) / (v_nrm * (v_nrm + cs));
+      // the same parameters with one division for 1/(|v|(|v|+c)), 1/(mu kappa) and
+      // tau_closed's 1/det (mixed form): r = 1/(a b d) gives 1/a = b d r, ...
+      const double a = v_nrm * (v_nrm + cs), bmk = mu * kappa, det = tau_det<DIM, NC>(c);
+      const double ab = a * bmk, rr = 1.0 / (ab * det);
+      const double ia = bmk * det * rr, imk = a * det * rr;
+      idet = ab * rr;
+      have_idet = true;
+      const double hv = (0.5 * h) * fma(2.0, v_nrm, cs) * ia;
       const double use = k.steady ? hv : fmin(dt * 0.5, hv);
       const double hh12 = h * h * (1.0 / 12.0);
-      const double imk = 1.0 / (mu * kappa);
-      tau[0][0] = use;
+      td[0] = use;
       const double tm = fmin(use, hh12 * rho * kappa * imk);
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) tau[1 + d][1 + d] = tm;
-      tau[L::iT][L::iT] = fmin(use, hh12 * rho * cv * mu * imk);
+      for (int d = 0; d < DIM; ++d) td[1 + d] = tm;
+      td[L::iT] = fmin(use, hh12 * rho * cv * mu * imk);
 #pragma unroll
-      for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = fmin(use, hh12 * k.ch[i].inv_D);
+      for (int i = 0; i < NC - 1; ++i) td[L::iY + i] = fmin(use, hh12 * k.ch[i].inv_D);
       nondiag = true;
     } else if (k.tau == GALES_TAU_NON_DIAG_COMP_2019) {
       double use;
       if (k.steady) use = h / (2.0 * (v_nrm + cs)) + h / (2.0 * v_nrm);
       else use = fmin(dt * 0.5, h / (2.0 * (v_nrm + cs)) + h / (2.0 * v_nrm));
-      tau[0][0] = use;
+      td[0] = use;
       const double tm = fmin(use, h * h * rho / (12.0 * mu));
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) tau[1 + d][1 + d] = tm;
-      tau[L::iT][L::iT] = fmin(use, h * h * rho * cv / (12.0 * kappa));
+      for (int d = 0; d < DIM; ++d) td[1 + d] = tm;
+      td[L::iT] = fmin(use, h * h * rho * cv / (12.0 * kappa));
 #pragma unroll
-      for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = fmin(use, h * h / (12.0 * pr.D_c[i]));
+      for (int i = 0; i < NC - 1; ++i) td[L::iY + i] = fmin(use, h * h / (12.0 * pr.D_c[i]));
       nondiag = true;
     } else if (k.tau == GALES_TAU_DIAG_INCOMP_2007) {
       double use = 0.0;
@@ -611,18 +648,18 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       double tau_e = vGv + 9.0 * use * (de * de);
       if (!k.steady) tau_e += 4.0 / (dt * dt);
       tau_e = 1.0 / sqrt(tau_e);
-      tau[0][0] = tau_c;
+      td[0] = tau_c;
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) tau[1 + d][1 + d] = tau_m / rho;
-      tau[L::iT][L::iT] = tau_e / (rho * cv);
+      for (int d = 0; d < DIM; ++d) td[1 + d] = tau_m / rho;
+      td[L::iT] = tau_e / (rho * cv);
 #pragma unroll
-      for (int i = 0; i < NC - 1; ++i) tau[L::iY + i][L::iY + i] = tau_m;
+      for (int i = 0; i < NC - 1; ++i) td[L::iY + i] = tau_m;
     } else if (k.tau == GALES_TAU_DIAG_2014) {
 #pragma unroll
       for (int i = 0; i < ND; ++i) {
         const double a0 = dudy_entry<DIM, NC, double>(c, i, i);
         const double tt = 4.0 / (dt * dt) * (a0 * a0);
-        double ta = 0.0, td = 0.0;
+        double ta = 0.0, tk = 0.0;
 #pragma unroll
         for (int kk = 0; kk < DIM; ++kk)
 #pragma unroll
@@ -631,42 +668,34 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
             const double al = a_entry<DIM, NC, double>(c, ll, i, i);
             const double kv = k_entry<DIM, NC, double>(c, kk, ll, i, i);
             ta += q.G[kk][ll] * (ak * al);
-            td += q.G[kk][ll] * q.G[kk][ll] * (kv * kv);
+            tk += q.G[kk][ll] * q.G[kk][ll] * (kv * kv);
           }
-        tau[i][i] = 1.0 / (sqrt(tt) + sqrt(ta) + sqrt(td) + 1.e-8);
+        td[i] = 1.0 / (sqrt(tt) + sqrt(ta) + sqrt(tk) + 1.e-8);
       }
-      tau[0][0] = 1.0 / (tau[0][0] + rho * tau[1][1] * (trG));
+      td[0] = 1.0 / (td[0] + rho * td[1] * (trG));
     }
-    if (nondiag) {
-      double td[ND];
+    if (!nondiag) {
 #pragma unroll
-      for (int i = 0; i < ND; ++i) td[i] = tau[i][i];
-      if constexpr (FORM == GALES_FORM_FP64) {
-        double A0[ND][ND], Xinv[ND][ND];
+      for (int i = 0; i < ND; ++i) tau[i][i] = to_s<R>(td[i]);
+    } else if constexpr (FORM == GALES_FORM_FP64) {
+      double A0[ND][ND], Xinv[ND][ND];
 #pragma unroll
-        for (int r = 0; r < ND; ++r)
+      for (int r = 0; r < ND; ++r)
 #pragma unroll
-          for (int cc = 0; cc < ND; ++cc) A0[r][cc] = dudy_entry<DIM, NC, double>(c, r, cc);
-        if (lu_inverse<ND>(A0, Xinv)) flag_error(k, GALES_ERR_SINGULAR, e);
+        for (int cc = 0; cc < ND; ++cc) A0[r][cc] = dudy_entry<DIM, NC, double>(c, r, cc);
+      if (lu_inverse<ND>(A0, Xinv)) flag_error(k, GALES_ERR_SINGULAR, e);
 #pragma unroll
-        for (int r = 0; r < ND; ++r)
+      for (int r = 0; r < ND; ++r)
 #pragma unroll
-          for (int cc = 0; cc < ND; ++cc) tau[r][cc] = Xinv[r][cc] * td[cc];
-        if (v_nrm / cs < 0.1) {
-          tau[0][0] = 1.0 / (1.0 / tau[0][0] + 1.0 / (rho * tau[1][1] * (trG)));
+        for (int cc = 0; cc < ND; ++cc) tau[r][cc] = Xinv[r][cc] * td[cc];
+      if (v_nrm / cs < 0.1) {
+        tau[0][0] = 1.0 / (1.0 / tau[0][0] + 1.0 / (rho * tau[1][1] * (trG)));
 #pragma unroll
-          for (int cc = 1; cc < ND; ++cc) tau[0][cc] = 0.0;
-        }
-      } else {
-        tau_closed<DIM, NC>(c, pr.irho, td, tau);
-        if (v_nrm < 0.1 * cs) {
-          // 1/(1/a + 1/b) = a b/(a + b)
-          const double b = rho * tau[1][1] * trG;
-          tau[0][0] = tau[0][0] * b / (tau[0][0] + b);
-#pragma unroll
-          for (int cc = 1; cc < ND; ++cc) tau[0][cc] = 0.0;
-        }
+        for (int cc = 1; cc < ND; ++cc) tau[0][cc] = 0.0;
       }
+    } else {
+      tau_closed<DIM, NC, R>(c, pr.irho, have_idet ? idet : 1.0 / tau_det<DIM, NC>(c), td,
+                             v_nrm < 0.1 * cs, rho * trG, tau);
     }
   }
   {
@@ -686,7 +715,11 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
       else { r0r = cr.drho_dY[r - L::iY]; mEr = cr.dE_dY[r - L::iY]; gr = R(0); }
 #pragma unroll
       for (int cc = 0; cc < ND; ++cc) {
-        const R t = to_s<R>(tau[r][cc]);
+        if (FORM == GALES_FORM_MIXED && !tau_nz<DIM, NC>(r, cc)) {
+          out.tau[r][cc] = S(0);
+          continue;
+        }
+        const R t = tau[r][cc];
         out.tau[r][cc] = S(t);
         if (r < 1 || r >= L::iT) zz[cc] = madd(r0r, t, zz[cc]);
         yy[cc] = madd(mEr, t, yy[cc]);
@@ -704,12 +737,6 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
   // fluxes, least-squares residual and dc in the form's type R
   R Res[ND], AdI[ND], t[ND];
   {
-    R dd[ND];
-#pragma unroll
-    for (int j = 0; j < ND; ++j) {
-      if constexpr (FORM == GALES_FORM_FP64) dd[j] = (Iq[j] - Pq[j]) / dt;
-      else dd[j] = narrow_rn(Iq[j] - Pq[j]) * narrow_rn(k.inv_dt);
-    }
     dudy_mv<DIM, NC, R>(cr, dd, Res);
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
@@ -752,7 +779,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
         for (int j = 0; j < ND; ++j) {
           const R ui = to_s<R>(k.u_ref_inv[j]);
           const R z = ui * (AdI[j] - SvR[j]);
-          const R u = ui * to_s<R>(U[j]);
+          const R u = ui * Ur[j];
           Zn += z * z;
           Un += u * u;
         }
@@ -1246,25 +1273,35 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
   const bool blk = !local && ((E.blocked[b] >> r) & 1u);
   double avg = 0.0;
   if constexpr (WANT_M) {
-    // avg_val = (1 + trace)/n (scatter.hpp:65-68)
-    S dg = S(0);
+    // avg_val = (1 + trace)/n (scatter.hpp:65-68), only where the element has a blocked
+    // row (the same for every lane of the element)
+    uint32_t any_blocked = 0u;
 #pragma unroll
-    for (int ai = 0; ai < NA; ++ai)
+    for (int i = 0; i < NEN; ++i) any_blocked |= E.blocked[i];
+    const bool need_avg = !local && any_blocked != 0u;
+    double tr = 0.0;
+    if (need_avg) {
+      S dg = S(0);
 #pragma unroll
-      for (int j = 0; j < ND; ++j) dg = (a0 + ai == b && j == r) ? acc[ai][j] : dg;
-    double tr = active ? widen(dg) : 0.0;
+      for (int ai = 0; ai < NA; ++ai)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
-    if constexpr (WPE > 1) {
-      if ((gl & 31) == 0) E.wsum[gl >> 5] = tr;
+        for (int j = 0; j < ND; ++j) dg = (a0 + ai == b && j == r) ? acc[ai][j] : dg;
+      tr = active ? widen(dg) : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+      if constexpr (WPE > 1) {
+        if ((gl & 31) == 0) E.wsum[gl >> 5] = tr;
+      }
     }
     elem_sync<WPE>(ec);  // the point records are dead from here on (stage aliases them)
-    if constexpr (WPE > 1) {
-      tr = E.wsum[0];
+    if (need_avg) {
+      if constexpr (WPE > 1) {
+        tr = E.wsum[0];
 #pragma unroll
-      for (int w = 1; w < WPE; ++w) tr += E.wsum[w];
+        for (int w = 1; w < WPE; ++w) tr += E.wsum[w];
+      }
+      avg = (1.0 + tr) / N;
     }
-    avg = (1.0 + tr) / N;
     if (active) {
       double* srow = E.u.stage + row * NS + a0 * ND;
 #pragma unroll

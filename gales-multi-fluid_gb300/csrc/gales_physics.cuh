@@ -134,32 +134,40 @@ __device__ __forceinline__ void mixture(const DevChem* ch, double p, double T, c
   o.alpha = alpha; o.beta = beta;
 }
 
-// The same mixture in FP64 for the mixed form, with per-chemical reciprocals and
-// ratios precomputed so that a point costs three divisions instead of about a dozen.
+// The mixture in FP64 for the mixed form: state I in full (Props) and state P's rho
+// and cv (what U(P) needs), from per-chemical ratios precomputed on the host and one
+// division for both states.  A gas has 1/rho_c = R_c T/p, so
+//   1/rho = (T G + p C)/p = D/p,   G = sum_gas Y_c R_c,  C = sum_custom Y_c/rho_c,
+// and with r = 1/(p D D_P):  1/p = D D_P r,  rho = p^2 D_P r,  rho_P = p_P p D r.
+// A gas's alpha_c/rho_c = R_c/p, beta_c/rho_c = R_c T/p^2 and 1/(rho_c^2 s_c^2) =
+// (R_c/gamma_c) T/p^2, so the gas sums need 1/p alone.  A material without a gas
+// (has_gas = 0) takes rho = 1/C, rho_P = 1/C_P and never divides by p.
 template <int NC>
-__device__ __forceinline__ void mixture_fast(const DevChem* ch, double p, double T, const double* Y,
-                                             Props<NC>& o) {
-  const double ip = 1.0 / p, iT = 1.0 / T;
-  double irho = 0.0, mu = 0.0, cp = 0.0, cv = 0.0, kappa = 0.0, c2 = 0.0, al = 0.0, be = 0.0;
+__device__ __forceinline__ void mixture_pair_fast(const DevChem* ch, bool has_gas, double pP, double TP,
+                                                  const double* YP, double p, double T, const double* Y,
+                                                  double& rhoP, double& cvP, Props<NC>& o) {
+  double GP = 0.0, CP = 0.0, cvp = 0.0;
+  double G = 0.0, GRg = 0.0, C = 0.0, mu = 0.0, cp = 0.0, cv = 0.0, kappa = 0.0;
+  double c2 = 0.0, al = 0.0, be = 0.0;
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
     const DevChem& q = ch[c];
-    double ir, v;
+    double v;
     if (q.kind == GALES_CH_CUSTOM) {
-      ir = q.inv_rho;
+      CP = fma(YP[c], q.inv_rho, CP);
+      cvp = fma(YP[c], fma(-TP, q.cv_shift, q.cp), cvp);
+      C = fma(Y[c], q.inv_rho, C);
       v = fma(-T, q.cv_shift, q.cp);
-      c2 = fma(Y[c], q.beta == 0.0 ? 1.e-40 * ir * ir : q.beta_over_rho, c2);
+      c2 = fma(Y[c], q.beta == 0.0 ? 1.e-40 * q.inv_rho * q.inv_rho : q.beta_over_rho, c2);
       al = fma(Y[c], q.alpha_over_rho, al);
       be = fma(Y[c], q.beta_over_rho, be);
     } else {
-      ir = q.R * T * ip;
+      GP = fma(YP[c], q.R, GP);
+      cvp = fma(YP[c], q.cv, cvp);
+      G = fma(Y[c], q.R, G);
+      GRg = fma(Y[c], q.R_over_gamma, GRg);
       v = q.cv;
-      c2 = fma(Y[c], q.R_over_gamma * T * ip * ip, c2);
-      al = fma(Y[c] * iT, ir, al);
-      be = fma(Y[c] * ip, ir, be);
     }
-    o.irho_c[c] = ir;
-    irho = fma(Y[c], ir, irho);
     mu = fma(Y[c], q.mu, mu);
     cp = fma(Y[c], q.cp, cp);
     cv = fma(Y[c], v, cv);
@@ -167,31 +175,32 @@ __device__ __forceinline__ void mixture_fast(const DevChem* ch, double p, double
     o.e_c[c] = v * T;
     o.D_c[c] = q.D;
   }
-  const double rho = 1.0 / irho;
+  double rho, irho, ip;
+  if (has_gas) {
+    const double D = fma(T, G, p * C), DP = fma(TP, GP, pP * CP);
+    const double r = 1.0 / (p * D * DP);
+    ip = D * DP * r;
+    rho = p * p * DP * r;
+    rhoP = pP * p * D * r;
+    irho = D * ip;
+    const double ip2 = ip * ip;
+    c2 = fma(GRg * T, ip2, c2);
+    al = fma(G, ip, al);
+    be = fma(G * T, ip2, be);
+  } else {
+    ip = 0.0;
+    const double r = 1.0 / (C * CP);
+    rho = CP * r;
+    rhoP = C * r;
+    irho = C;
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) o.irho_c[c] = ch[c].kind == GALES_CH_CUSTOM ? ch[c].inv_rho : ch[c].R * T * ip;
+  cvP = cvp;
   o.rho = rho; o.irho = irho; o.mu = mu; o.cp = cp; o.cv = cv; o.kappa = kappa;
   o.c = rsqrt(c2) * irho;
   o.alpha = rho * al;
   o.beta = rho * be;
-}
-
-template <int NC>
-__device__ __forceinline__ void mixture_rho_cv_fast(const DevChem* ch, double p, double T, const double* Y,
-                                                    double& rho_out, double& cv_out) {
-  const double ip = 1.0 / p;
-  double irho = 0.0, cv = 0.0;
-#pragma unroll
-  for (int c = 0; c < NC; ++c) {
-    const DevChem& q = ch[c];
-    if (q.kind == GALES_CH_CUSTOM) {
-      irho = fma(Y[c], q.inv_rho, irho);
-      cv = fma(Y[c], fma(-T, q.cv_shift, q.cp), cv);
-    } else {
-      irho = fma(Y[c], q.R * T * ip, irho);
-      cv = fma(Y[c], q.cv, cv);
-    }
-  }
-  rho_out = 1.0 / irho;
-  cv_out = cv;
 }
 
 // Only rho and cv (what U(P) needs); same operations as mixture().
@@ -316,10 +325,10 @@ __device__ __forceinline__ void make_coef(const Props<NC>& pr, double p, const d
   }
 }
 
-// make_coef for the mixed form, from mixture_fast's reciprocals.
+// make_coef for the mixed form, from mixture_pair_fast's reciprocals; vv = |v|^2.
 template <int DIM, int NC>
-__device__ __forceinline__ void make_coef_fast(const Props<NC>& pr, double p, const double* v, double T,
-                                               const double* Y, Coef<DIM, NC>& c) {
+__device__ __forceinline__ void make_coef_fast(const Props<NC>& pr, double p, const double* v, double vv,
+                                               double T, const double* Y, Coef<DIM, NC>& c) {
   c.p = p; c.T_ = T;
 #pragma unroll
   for (int k = 0; k < DIM; ++k) c.v[k] = v[k];
@@ -328,7 +337,7 @@ __device__ __forceinline__ void make_coef_fast(const Props<NC>& pr, double p, co
   const double rho = pr.rho, irho = pr.irho;
   c.rho = rho;
   c.cv = pr.cv;
-  c.E = fma(pr.cv, T, 0.5 * vsq<DIM>(v));
+  c.E = fma(pr.cv, T, 0.5 * vv);
   c.drho_dp = rho * pr.beta;
   c.drho_dT = -rho * pr.alpha;
   c.de_dp = fma(pr.beta, p, -pr.alpha * T) * irho;
@@ -615,17 +624,26 @@ __device__ __forceinline__ int lu_inverse(double (&A)[N][N], double (&X)[N][N]) 
 // tau = DUDY^{-1} diag(td) for the mixed form (fluid_2d.hpp:946-947), from the
 // structure of DUDY = w r0^T + rho M.  The velocity and mass-fraction rows of
 // DUDY^{-1} are (e_j - w_j e_p^T)/rho; the p and T rows come from the 2x2 system
-// [drho_dp drho_dT; de_dp de_dT] per column.  Every other entry is zero.  irho = 1/rho.
+// [drho_dp drho_dT; de_dp de_dT] per column.  Every other entry is zero (tau_nz).
+// irho = 1/rho, idet = 1/(drho_dp de_dT - drho_dT de_dp) (tau_det gives the
+// determinant).  low_mach applies the low-Mach form of the p row (fluid_2d.hpp:949-
+// 958): tau[0][0] <- 1/(1/tau[0][0] + 1/b) with b = rho tau[1][1] tr(G) (rho_trG =
+// rho tr(G)), tau[0][c] <- 0 for c > 0.  Each entry is formed in FP64 and stored in T.
 template <int DIM, int NC>
-__device__ __forceinline__ void tau_closed(const Coef<DIM, NC>& c, double irho, const double* td,
-                                           double (&tau)[Layout<DIM, NC>::ND][Layout<DIM, NC>::ND]) {
+__host__ __device__ constexpr bool tau_nz(int r, int cc) {
+  return r == 0 || r == Layout<DIM, NC>::iT || cc == 0 || cc == r;
+}
+
+template <int DIM, int NC>
+__device__ __forceinline__ double tau_det(const Coef<DIM, NC>& c) {
+  return fma(c.drho_dp, c.de_dT, -c.drho_dT * c.de_dp);
+}
+
+template <int DIM, int NC, typename T>
+__device__ __forceinline__ void tau_closed(const Coef<DIM, NC>& c, double irho, double idet, const double* td,
+                                           bool low_mach, double rho_trG,
+                                           T (&tau)[Layout<DIM, NC>::ND][Layout<DIM, NC>::ND]) {
   using L = Layout<DIM, NC>;
-  constexpr int ND = L::ND;
-#pragma unroll
-  for (int r = 0; r < ND; ++r)
-#pragma unroll
-    for (int cc = 0; cc < ND; ++cc) tau[r][cc] = 0.0;
-  const double idet = 1.0 / fma(c.drho_dp, c.de_dT, -c.drho_dT * c.de_dp);
   const double q = irho * idet;
   // column p: R1 = 1 + (sum_i drho_dY_i Y_i)/rho, R2 = (|v|^2 - E + sum_i dE_dY_i Y_i)/rho
   double sY = 0.0, sE = -c.E;
@@ -638,26 +656,32 @@ __device__ __forceinline__ void tau_closed(const Coef<DIM, NC>& c, double irho, 
   }
   const double R1 = fma(irho, sY, 1.0), R2 = irho * sE;
   const double t0 = td[0] * idet, ti = td[0] * irho;
-  tau[0][0] = fma(R1, c.de_dT, -c.drho_dT * R2) * t0;
-  tau[L::iT][0] = fma(c.drho_dp, R2, -c.de_dp * R1) * t0;
+  double t00 = fma(R1, c.de_dT, -c.drho_dT * R2) * t0;
+  if (low_mach) {
+    // 1/(1/a + 1/b) = a b/(a + b)
+    const double b = rho_trG * (irho * td[1]);
+    t00 = t00 * b / (t00 + b);
+  }
+  tau[0][0] = to_s<T>(t00);
+  tau[L::iT][0] = to_s<T>(fma(c.drho_dp, R2, -c.de_dp * R1) * t0);
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
-    tau[1 + j][0] = -c.v[j] * ti;
-    tau[1 + j][1 + j] = irho * td[1 + j];
+    tau[1 + j][0] = to_s<T>(-c.v[j] * ti);
+    tau[1 + j][1 + j] = to_s<T>(irho * td[1 + j]);
     const double a = q * td[1 + j] * c.v[j];
-    tau[0][1 + j] = c.drho_dT * a;
-    tau[L::iT][1 + j] = -c.drho_dp * a;
+    tau[0][1 + j] = low_mach ? T(0) : to_s<T>(c.drho_dT * a);
+    tau[L::iT][1 + j] = to_s<T>(-c.drho_dp * a);
   }
-  tau[0][L::iT] = -c.drho_dT * q * td[L::iT];
-  tau[L::iT][L::iT] = c.drho_dp * q * td[L::iT];
+  tau[0][L::iT] = low_mach ? T(0) : to_s<T>(-c.drho_dT * q * td[L::iT]);
+  tau[L::iT][L::iT] = to_s<T>(c.drho_dp * q * td[L::iT]);
 #pragma unroll
   for (int i = 0; i < NC - 1; ++i) {
     const int y = L::iY + i;
-    tau[y][0] = -c.Y[i] * ti;
-    tau[y][y] = irho * td[y];
+    tau[y][0] = to_s<T>(-c.Y[i] * ti);
+    tau[y][y] = to_s<T>(irho * td[y]);
     const double a = q * td[y];
-    tau[0][y] = fma(c.drho_dT, c.dE_dY[i], -c.drho_dY[i] * c.de_dT) * a;
-    tau[L::iT][y] = fma(c.de_dp, c.drho_dY[i], -c.drho_dp * c.dE_dY[i]) * a;
+    tau[0][y] = low_mach ? T(0) : to_s<T>(fma(c.drho_dT, c.dE_dY[i], -c.drho_dY[i] * c.de_dT) * a);
+    tau[L::iT][y] = to_s<T>(fma(c.de_dp, c.drho_dY[i], -c.drho_dp * c.dE_dY[i]) * a);
   }
 }
 
@@ -748,22 +772,19 @@ __device__ __forceinline__ double qform_fma(const double (&G)[DIM][DIM], const d
   return r;
 }
 
-// compute_h for the mixed form, with fused operations and one reciprocal per
-// normalisation.  compute_h branches on |s1| > DBL_EPSILON, where s1 (the part of
-// dv v normal to v) is rounding noise for a rank-one velocity field (every node but
-// one at rest); there only the reference's exact operations take the reference's
-// branch.  This routine decides the branch only when |s1| exceeds 1e-10 |dv v| (and
-// 1e3 DBL_EPSILON), far above what rounding can move, and so does the third
-// direction |s0 x s1|; otherwise it returns with decided = false and the caller runs
-// compute_h on the velocity and gradient formed with the reference's operations.
+// compute_h for the mixed form, with fused operations and one reciprocal square root
+// per normalisation (iv = 1/|v| comes from the caller).  compute_h branches on
+// |s1| > DBL_EPSILON, where s1 (the part of dv v normal to v) is rounding noise for a
+// rank-one velocity field (every node but one at rest); there only the reference's
+// exact operations take the reference's branch.  This routine decides the branch only
+// when |s1| exceeds 1e-10 |dv v| (and 1e3 DBL_EPSILON), far above what rounding can
+// move, and so does the third direction |s0 x s1|; otherwise it returns with
+// decided = false and the caller runs compute_h on the velocity and gradient formed
+// with the reference's operations.  The tests compare squared norms.
 template <int DIM>
-__device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], const double* v,
+__device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], const double* v, double iv,
                                                  const double (&dv)[DIM][DIM], bool& decided) {
   decided = false;
-  double vv = v[0] * v[0];
-#pragma unroll
-  for (int i = 1; i < DIM; ++i) vv = fma(v[i], v[i], vv);
-  const double iv = 1.0 / sqrt(vv);
   double s0[DIM], acc[DIM], s1[DIM];
 #pragma unroll
   for (int i = 0; i < DIM; ++i) s0[i] = v[i] * iv;
@@ -783,9 +804,9 @@ __device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], co
     s1[i] = fma(-ip, s0[i], acc[i]);
     n1 = fma(s1[i], s1[i], n1);
   }
-  n1 = sqrt(n1);
-  if (!(n1 > fmax(1.0e-10 * sqrt(aa), 1.0e3 * kEps))) return 0.0;
-  const double i1 = 1.0 / n1;
+  constexpr double kMin2 = 1.0e6 * kEps * kEps;  // (1e3 DBL_EPSILON)^2
+  if (!(n1 > fmax(1.0e-20 * aa, kMin2))) return 0.0;
+  const double i1 = rsqrt(n1);
 #pragma unroll
   for (int i = 0; i < DIM; ++i) s1[i] *= i1;
   double a[3];
@@ -797,9 +818,9 @@ __device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], co
     s2[0] = fma(s0[1], s1[2], -s0[2] * s1[1]);
     s2[1] = fma(s1[0], s0[2], -s1[2] * s0[0]);
     s2[2] = fma(s0[0], s1[1], -s0[1] * s1[0]);
-    const double n2 = sqrt(fma(s2[0], s2[0], fma(s2[1], s2[1], s2[2] * s2[2])));
-    if (!(n2 > 1.0e3 * kEps)) return 0.0;
-    const double i2 = 1.0 / n2;
+    const double n2 = fma(s2[0], s2[0], fma(s2[1], s2[1], s2[2] * s2[2]));
+    if (!(n2 > kMin2)) return 0.0;
+    const double i2 = rsqrt(n2);
 #pragma unroll
     for (int i = 0; i < 3; ++i) s2[i] *= i2;
     a[2] = qform_fma<DIM>(G, s2);
@@ -807,8 +828,9 @@ __device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], co
   decided = true;
   double h;
   if (DIM == 3 && a[0] != 0.0 && a[1] != 0.0 && a[2] != 0.0) {
-    // 1/a0 + 1/a1 + 1/a2 with one division
-    h = fma(a[0], a[1] + a[2], a[1] * a[2]) / (a[0] * a[1] * a[2]);
+    // 2 sqrt|1/a0 + 1/a1 + 1/a2| = 2 sqrt|num/den| = 2 |num| / sqrt|num den|
+    const double num = fma(a[0], a[1] + a[2], a[1] * a[2]), den = a[0] * a[1] * a[2];
+    return num == 0.0 ? 0.0 : 2.0 * fabs(num) * rsqrt(fabs(num * den));
   } else {
     h = 0.0;
 #pragma unroll
