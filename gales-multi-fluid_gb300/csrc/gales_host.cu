@@ -146,10 +146,12 @@ void parallel_for(int64_t n, F f) {
 // Each point-record chunk buffer holds this many bytes; two of them stay resident
 // in L2 (about a quarter of the 129 MB) while the CSR values stream through it.
 constexpr int kVjpAux = 3 * GALES_MAX_COMP + GALES_MAX_ND;
-// Chunks of the interior pipeline: whole waves of the point kernel (every SM holding
-// as many of its CTAs as fit), kWaves waves per chunk.
-constexpr int kWaves = 1;
+// Chunks of the interior pipeline: one wave of the point kernel that leaves one CTA
+// slot per SM to the matrix stage running beside it on the other stream (with four
+// point CTAs resident per SM the chunk holds three per SM), so that the FP64-bound
+// point stage and the issue-bound matrix stage share every SM.
 constexpr int kRing = 3;    // point-record buffers in flight between the two stages
+inline int point_ctas_per_chunk_sm(int occupancy) { return occupancy >= 3 ? occupancy - 1 : occupancy; }
 
 GeometryOps geometry_ops(int dim, int nen) {
   if (dim == 2 && nen == 3) return geometry_ops_tri3();
@@ -750,8 +752,8 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
     for (int f = 0; f < 2; ++f) {
       const size_t rb = h->ops[f].rec_bytes(h->nc);
       if (rb == 0) continue;
-      const long long wave = (long long)sms * h->ops[f].point_occupancy(h->nc) * 128 / h->ei.nq;
-      h->chunk_elems[f] = std::max<long long>(1, std::min<long long>(kWaves * wave, std::max<int64_t>(h->n_el, 1)));
+      const long long wave = (long long)sms * point_ctas_per_chunk_sm(h->ops[f].point_occupancy(h->nc)) * 128 / h->ei.nq;
+      h->chunk_elems[f] = std::max<long long>(1, std::min<long long>(wave, std::max<int64_t>(h->n_el, 1)));
       bytes = std::max(bytes, rb * (size_t)h->chunk_elems[f]);
     }
     for (int i = 0; i < kRing; ++i)

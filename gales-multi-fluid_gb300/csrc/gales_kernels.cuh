@@ -459,19 +459,52 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
   // velocity gradient in FP64 (input of compute_h; fused in the mixed form, whose
   // compute_h falls back to the reference's operations where they matter)
   double dv[DIM][DIM];
+  constexpr bool kShareDv = FORM == GALES_FORM_MIXED && NEN == DIM + 1 && NQ >= DIM && NQ <= 32 && (32 % NQ) == 0;
+  if constexpr (kShareDv) {
+    // A simplex's velocity gradient is the same at its NQ points, whose lanes are
+    // consecutive in the warp (NQ divides 32): lane iq forms row a = min(iq, DIM - 1)
+    // of dv (the element's shape gradients are the same in every lane; the lane picks
+    // its velocity component from its registers) and the lanes of the element exchange
+    // the rows.  Same operations as the per-point form below.
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned int base = lane & ~(unsigned int)(NQ - 1);
+    const unsigned int gmask = NQ == 32 ? 0xffffffffu : (((1u << NQ) - 1u) << base);
+    const int am = iq < DIM ? iq : DIM - 1;
+    double va[NEN];
 #pragma unroll
-  for (int a = 0; a < DIM; ++a)
+    for (int i = 0; i < NEN; ++i) {
+      double x = Ie[i][1];
+#pragma unroll
+      for (int a = 1; a < DIM; ++a) x = (am == a) ? Ie[i][1 + a] : x;
+      va[i] = x;
+    }
+    double row[DIM];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-      if constexpr (FORM == GALES_FORM_FP64) {
-        dv[a][d] = dI[d][1 + a];
-      } else {
-        double b = q.ds[d][0] * Ie[0][1 + a];
+      double b = q.ds[d][0] * va[0];
 #pragma unroll
-        for (int i = 1; i < NEN; ++i) b = fma(q.ds[d][i], Ie[i][1 + a], b);
-        dv[a][d] = b;
-      }
+      for (int i = 1; i < NEN; ++i) b = fma(q.ds[d][i], va[i], b);
+      row[d] = b;
     }
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) dv[a][d] = __shfl_sync(gmask, row[d], (int)(base + (a < NQ ? a : NQ - 1)));
+  } else {
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        if constexpr (FORM == GALES_FORM_FP64) {
+          dv[a][d] = dI[d][1 + a];
+        } else {
+          double b = q.ds[d][0] * Ie[0][1 + a];
+#pragma unroll
+          for (int i = 1; i < NEN; ++i) b = fma(q.ds[d][i], Ie[i][1 + a], b);
+          dv[a][d] = b;
+        }
+      }
+  }
   // previous-level conservative vector U_P (props at P with shear rate 0) and the
   // current iterate's properties and U
   double p, v[DIM], T, Y[NC];
@@ -1300,7 +1333,7 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
 #pragma unroll
         for (int w = 1; w < WPE; ++w) tr += E.wsum[w];
       }
-      avg = (1.0 + tr) / N;
+      avg = (1.0 + tr) * (1.0 / N);
     }
     if (active) {
       double* srow = E.u.stage + row * NS + a0 * ND;
@@ -1323,14 +1356,14 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
     return;
   }
   if (local) {  // element-level output of execute_i (fluid_2d.hpp:200-201): m = m_, r = -r_
-    if (active && grp == 0) k.local_r[g * N + row] = -widen(racc);
+    if (active && grp == 0) k.local_r[g * N + row] = widen(-racc);
     if (WANT_M && k.local_m)
       for (int t = gl; t < NT; t += ET) k.local_m[g * NT + t] = E.u.stage[(t / N) * NS + t % N];
     return;
   }
   const int mode = k.scatter_mode;
   if (active && grp == 0) {
-    const double rv = blk ? avg * 0.0 : -widen(racc);
+    const double rv = blk ? avg * 0.0 : widen(-racc);
     add_to(k.rhs + (long long)E.nodes[b] * ND + r, rv, mode);
   }
   if constexpr (WANT_M) {

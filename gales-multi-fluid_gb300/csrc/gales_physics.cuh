@@ -772,20 +772,22 @@ __device__ __forceinline__ double qform_fma(const double (&G)[DIM][DIM], const d
   return r;
 }
 
-// compute_h for the mixed form, with fused operations and one reciprocal square root
-// per normalisation (iv = 1/|v| comes from the caller).  compute_h branches on
-// |s1| > DBL_EPSILON, where s1 (the part of dv v normal to v) is rounding noise for a
-// rank-one velocity field (every node but one at rest); there only the reference's
-// exact operations take the reference's branch.  This routine decides the branch only
-// when |s1| exceeds 1e-10 |dv v| (and 1e3 DBL_EPSILON), far above what rounding can
-// move, and so does the third direction |s0 x s1|; otherwise it returns with
-// decided = false and the caller runs compute_h on the velocity and gradient formed
-// with the reference's operations.  The tests compare squared norms.
+// compute_h for the mixed form, with fused operations and no normalisation but of v
+// (iv = 1/|v| comes from the caller).  compute_h branches on |s1| > DBL_EPSILON, where
+// s1 (the part of dv v normal to v) is rounding noise for a rank-one velocity field
+// (every node but one at rest); there only the reference's exact operations take the
+// reference's branch.  This routine decides the branch only when |s1| exceeds 1e-10
+// |dv v| (and 1e3 DBL_EPSILON), far above what rounding can move, and so does the
+// third direction |s0 x s1/|s1||; otherwise it returns with decided = false and the
+// caller runs compute_h on the velocity and gradient formed with the reference's
+// operations.  With w1 = s1 unnormalised and w2 = s0 x w1, alpha_1 = w1^T G w1/|w1|^2
+// and alpha_2 = w2^T G w2/|w2|^2, so h = 1/alpha_0 + |w1|^2/A1 + |w2|^2/A2 takes one
+// reciprocal square root at the end.
 template <int DIM>
 __device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], const double* v, double iv,
                                                  const double (&dv)[DIM][DIM], bool& decided) {
   decided = false;
-  double s0[DIM], acc[DIM], s1[DIM];
+  double s0[DIM], acc[DIM], w1[DIM];
 #pragma unroll
   for (int i = 0; i < DIM; ++i) s0[i] = v[i] * iv;
   double aa = 0.0, ip = 0.0;
@@ -801,42 +803,32 @@ __device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], co
   double n1 = 0.0;
 #pragma unroll
   for (int i = 0; i < DIM; ++i) {
-    s1[i] = fma(-ip, s0[i], acc[i]);
-    n1 = fma(s1[i], s1[i], n1);
+    w1[i] = fma(-ip, s0[i], acc[i]);
+    n1 = fma(w1[i], w1[i], n1);
   }
   constexpr double kMin2 = 1.0e6 * kEps * kEps;  // (1e3 DBL_EPSILON)^2
   if (!(n1 > fmax(1.0e-20 * aa, kMin2))) return 0.0;
-  const double i1 = rsqrt(n1);
-#pragma unroll
-  for (int i = 0; i < DIM; ++i) s1[i] *= i1;
-  double a[3];
-  a[0] = qform_fma<DIM>(G, s0);
-  a[1] = qform_fma<DIM>(G, s1);
-  a[2] = 0.0;
+  const double A0 = qform_fma<DIM>(G, s0), A1 = qform_fma<DIM>(G, w1);
+  double A2 = 0.0, n2 = 0.0;
   if constexpr (DIM == 3) {
-    double s2[3];
-    s2[0] = fma(s0[1], s1[2], -s0[2] * s1[1]);
-    s2[1] = fma(s1[0], s0[2], -s1[2] * s0[0]);
-    s2[2] = fma(s0[0], s1[1], -s0[1] * s1[0]);
-    const double n2 = fma(s2[0], s2[0], fma(s2[1], s2[1], s2[2] * s2[2]));
-    if (!(n2 > kMin2)) return 0.0;
-    const double i2 = rsqrt(n2);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) s2[i] *= i2;
-    a[2] = qform_fma<DIM>(G, s2);
+    double w2[3];
+    w2[0] = fma(s0[1], w1[2], -s0[2] * w1[1]);
+    w2[1] = fma(w1[0], s0[2], -w1[2] * s0[0]);
+    w2[2] = fma(s0[0], w1[1], -s0[1] * w1[0]);
+    n2 = fma(w2[0], w2[0], fma(w2[1], w2[1], w2[2] * w2[2]));
+    if (!(n2 > kMin2 * n1)) return 0.0;
+    A2 = qform_fma<DIM>(G, w2);
   }
   decided = true;
-  double h;
-  if (DIM == 3 && a[0] != 0.0 && a[1] != 0.0 && a[2] != 0.0) {
-    // 2 sqrt|1/a0 + 1/a1 + 1/a2| = 2 sqrt|num/den| = 2 |num| / sqrt|num den|
-    const double num = fma(a[0], a[1] + a[2], a[1] * a[2]), den = a[0] * a[1] * a[2];
+  if (DIM == 3 && A0 != 0.0 && A1 != 0.0 && A2 != 0.0) {
+    // 2 sqrt|num/den| = 2 |num| / sqrt|num den|
+    const double num = fma(A1, A2, A0 * fma(n1, A2, n2 * A1)), den = A0 * A1 * A2;
     return num == 0.0 ? 0.0 : 2.0 * fabs(num) * rsqrt(fabs(num * den));
-  } else {
-    h = 0.0;
-#pragma unroll
-    for (int i = 0; i < DIM; ++i)
-      if (a[i] != 0.0) h += 1.0 / a[i];
   }
+  double h = 0.0;
+  if (A0 != 0.0) h += 1.0 / A0;
+  if (A1 != 0.0) h += n1 / A1;
+  if (DIM == 3 && A2 != 0.0) h += n2 / A2;
   return 2 * sqrt(fabs(h));
 }
 
