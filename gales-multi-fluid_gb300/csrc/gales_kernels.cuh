@@ -290,6 +290,7 @@ __device__ __forceinline__ void geometry(const double (&X)[NEN][DIM], const doub
 template <int DIM, int NEN, int NC, typename S>
 struct alignas(16) QP {
   using L = Layout<DIM, NC>;
+  using Scalar = S;
   static constexpr int ND = L::ND;
   S sh[NEN], ds[DIM][NEN], JxW;
   S p, v[DIM], Y[NC], rho, E, drho_dp, drho_dT, de_dp, de_dT, mu, lambda, kappa;
@@ -303,6 +304,40 @@ struct alignas(16) QP {
   S rf[DIM][ND];    // coefficient of dN_b/dx_k:  F_dif,k - F_adv,k + shock dI/dx_k
   S res[ND];        // least-squares residual Res (fluid_2d.hpp:282)
 };
+
+// Lane layout of the matrix stage (see matrix_kernel); the point stage lays its
+// records out in the matrix CTAs' blocks.
+template <int DIM, int NEN, int NC>
+struct MatShape {
+  static constexpr int ND = Layout<DIM, NC>::ND;
+  static constexpr int N = NEN * ND;                  // rows (and columns) of the block
+  static constexpr int AG = NEN >= 8 ? 2 : 1;          // trial-node groups per row
+  static constexpr int NA = NEN / AG;                  // trial nodes per lane
+  static constexpr int LANES = N * AG;
+  static constexpr int WPE = (LANES + 31) / 32;        // warps per element
+  static constexpr int EPC = WPE == 1 ? 4 : (WPE == 2 ? 2 : 1);  // elements per CTA
+  static constexpr int ET = WPE * 32;                  // threads per element
+  static constexpr int CTA = EPC * ET;
+  static constexpr int NS = N + 1;                     // stage row stride (doubles)
+  static constexpr bool AFFINE = NEN == DIM + 1;
+};
+
+// Point records in a chunk buffer are stored word-major within blocks of BP points,
+// BP = (elements per matrix CTA) x NQ, the points one matrix CTA reads: word f of
+// point p of block b is at [b][f][p].  A warp of the point stage then stores each word
+// for its 32 consecutive points as runs of BP contiguous words (instead of one word
+// per record, 760 bytes apart), and a matrix CTA reads its block as one contiguous
+// range.  RecOut addresses one point's words.
+template <typename QPT, int BP>
+struct RecOut {
+  using S = typename QPT::Scalar;
+  static constexpr int RW = (int)(sizeof(QPT) / sizeof(S));  // words per record
+  S* __restrict__ blk;
+  int p;
+  __device__ __forceinline__ S& at(size_t off) const { return blk[(off / sizeof(S)) * BP + p]; }
+};
+#define GALES_REC(m) out.at(offsetof(QPT, m))
+#define GALES_RECA(m, i) out.at(offsetof(QPT, m) + (size_t)(i) * sizeof(S))
 
 // Element geometry at the interior quadrature points, computed once at handle
 // creation as the reference does at mesh load (mesh.hpp:468-495 builds a quad
@@ -383,9 +418,10 @@ __device__ __noinline__ double compute_h_reference(const double* __restrict__ I,
 //   GALES_FORM_MIXED: FP64 for the mixture EOS and its derivatives, U - U_P, the
 //                     element size h and tau with the closed-form DUDY inverse; the
 //                     fluxes, least-squares residual and dc viscosity in FP32.
-template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
-__device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, NC, S>& out) {
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, int BP>
+__device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<QP<DIM, NEN, NC, S>, BP>& out) {
   using L = Layout<DIM, NC>;
+  using QPT = QP<DIM, NEN, NC, S>;
   constexpr int ND = L::ND;
   constexpr int NG = geo_per_element<DIM, NEN>(NQ);
   using R = typename std::conditional<FORM == GALES_FORM_FP64, double, float>::type;
@@ -561,7 +597,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
       SvR[j] = Sv[j];
-      out.rv[j] = (U[j] - UP[j]) / dt - Sv[j];
+      GALES_RECA(rv, j) = (U[j] - UP[j]) / dt - Sv[j];
     }
   } else {
     const float rf = narrow_rn(pr.rho);
@@ -575,7 +611,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
     SvR[L::iT] = rf * gv;
     const float idt = narrow_rn(k.inv_dt);
 #pragma unroll
-    for (int j = 0; j < ND; ++j) out.rv[j] = fmaf(narrow_rn(U[j] - UP[j]), idt, -SvR[j]);
+    for (int j = 0; j < ND; ++j) GALES_RECA(rv, j) = fmaf(narrow_rn(U[j] - UP[j]), idt, -SvR[j]);
   }
   R Ur[ND];  // U in the form's type (discontinuity capturing)
 #pragma unroll
@@ -749,11 +785,11 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
 #pragma unroll
       for (int cc = 0; cc < ND; ++cc) {
         if (FORM == GALES_FORM_MIXED && !tau_nz<DIM, NC>(r, cc)) {
-          out.tau[r][cc] = S(0);
+          GALES_RECA(tau, (r) * ND + (cc)) = S(0);
           continue;
         }
         const R t = tau[r][cc];
-        out.tau[r][cc] = S(t);
+        GALES_RECA(tau, (r) * ND + (cc)) = S(t);
         if (r < 1 || r >= L::iT) zz[cc] = madd(r0r, t, zz[cc]);
         yy[cc] = madd(mEr, t, yy[cc]);
         if (r >= 1 && r < L::iT) gg[cc] = madd(gr, t, gg[cc]);
@@ -761,10 +797,10 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
     }
 #pragma unroll
     for (int cc = 0; cc < ND; ++cc) {
-      out.z[cc] = S(zz[cc]);
-      out.y[cc] = S(yy[cc]);
-      out.tg[cc] = S(gg[cc]);
-      out.w[cc] = S(cc == 0 ? R(1) : (cc < L::iT ? cr.v[cc - 1] : (cc == L::iT ? cr.E : cr.Y[cc - L::iY])));
+      GALES_RECA(z, cc) = S(zz[cc]);
+      GALES_RECA(y, cc) = S(yy[cc]);
+      GALES_RECA(tg, cc) = S(gg[cc]);
+      GALES_RECA(w, cc) = S(cc == 0 ? R(1) : (cc < L::iT ? cr.v[cc - 1] : (cc == L::iT ? cr.E : cr.Y[cc - L::iY])));
     }
   }
   // fluxes, least-squares residual and dc in the form's type R
@@ -861,33 +897,33 @@ __device__ void point_phase(const KParams& k, long long e, int iq, QP<DIM, NEN, 
 #pragma unroll
     for (int i = 0; i < NC - 1; ++i) fa[L::iY + i] = rhoR * vk * cr.Y[i];
 #pragma unroll
-    for (int j = 0; j < ND; ++j) out.rf[d][j] = S(fd[j] - fa[j] + nu * dU[d][j]);
+    for (int j = 0; j < ND; ++j) GALES_RECA(rf, (d) * ND + (j)) = S(fd[j] - fa[j] + nu * dU[d][j]);
   }
   // write the record
 #pragma unroll
   for (int i = 0; i < NEN; ++i) {
-    out.sh[i] = to_s<S>(sh[i]);
+    GALES_RECA(sh, i) = to_s<S>(sh[i]);
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) out.ds[d][i] = to_s<S>(q.ds[d][i]);
+    for (int d = 0; d < DIM; ++d) GALES_RECA(ds, (d) * NEN + (i)) = to_s<S>(q.ds[d][i]);
   }
-  out.JxW = to_s<S>(JxW);
-  out.p = to_s<S>(p);
+  GALES_REC(JxW) = to_s<S>(JxW);
+  GALES_REC(p) = to_s<S>(p);
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) out.v[d] = to_s<S>(v[d]);
+  for (int d = 0; d < DIM; ++d) GALES_RECA(v, d) = to_s<S>(v[d]);
 #pragma unroll
-  for (int i = 0; i < NC; ++i) out.Y[i] = to_s<S>(Y[i]);
-  out.rho = to_s<S>(c.rho); out.E = to_s<S>(c.E);
-  out.drho_dp = to_s<S>(c.drho_dp); out.drho_dT = to_s<S>(c.drho_dT);
-  out.de_dp = to_s<S>(c.de_dp); out.de_dT = to_s<S>(c.de_dT);
-  out.mu = to_s<S>(c.mu); out.lambda = to_s<S>(c.lambda); out.kappa = to_s<S>(c.kappa);
+  for (int i = 0; i < NC; ++i) GALES_RECA(Y, i) = to_s<S>(Y[i]);
+  GALES_REC(rho) = to_s<S>(c.rho); GALES_REC(E) = to_s<S>(c.E);
+  GALES_REC(drho_dp) = to_s<S>(c.drho_dp); GALES_REC(drho_dT) = to_s<S>(c.drho_dT);
+  GALES_REC(de_dp) = to_s<S>(c.de_dp); GALES_REC(de_dT) = to_s<S>(c.de_dT);
+  GALES_REC(mu) = to_s<S>(c.mu); GALES_REC(lambda) = to_s<S>(c.lambda); GALES_REC(kappa) = to_s<S>(c.kappa);
 #pragma unroll
   for (int i = 0; i < L::NYA; ++i) {
-    out.drho_dY[i] = to_s<S>(c.drho_dY[i]); out.dE_dY[i] = to_s<S>(c.dE_dY[i]);
-    out.rhoD[i] = to_s<S>(c.rhoD[i]); out.rhoDH[i] = to_s<S>(c.rhoDH[i]);
+    GALES_RECA(drho_dY, i) = to_s<S>(c.drho_dY[i]); GALES_RECA(dE_dY, i) = to_s<S>(c.dE_dY[i]);
+    GALES_RECA(rhoD, i) = to_s<S>(c.rhoD[i]); GALES_RECA(rhoDH, i) = to_s<S>(c.rhoDH[i]);
   }
-  out.nu = S(nu);
+  GALES_REC(nu) = S(nu);
 #pragma unroll
-  for (int j = 0; j < ND; ++j) out.res[j] = S(Res[j]);
+  for (int j = 0; j < ND; ++j) GALES_RECA(res, j) = S(Res[j]);
   if (!isfinite(JxW) || !isfinite(pr.rho) || !isfinite(nu)) flag_error(k, GALES_ERR_NONFINITE, e);
 }
 
@@ -960,7 +996,11 @@ __global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1) point_k
   if (li >= n) return;
   const long long g = first + li;
   const long long e = k.el_list ? (long long)k.el_list[g] : g;
-  point_phase<DIM, NEN, NC, NQ, FORM, S>(k, e, iq, out[li * NQ + iq]);
+  using QPT = QP<DIM, NEN, NC, S>;
+  constexpr int BP = MatShape<DIM, NEN, NC>::EPC * NQ;
+  constexpr int RW = RecOut<QPT, BP>::RW;
+  const RecOut<QPT, BP> o{reinterpret_cast<S*>(out) + (t / BP) * (long long)(RW * BP), (int)(t % BP)};
+  point_phase<DIM, NEN, NC, NQ, FORM, S, BP>(k, e, iq, o);
 }
 
 // Interior pass, stage 2: element matrices.  Lane (b, r, g) owns row (b, r) of the
@@ -988,20 +1028,6 @@ __global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1) point_k
 // applied in closed form from a few point scalars (mu, lambda, mu v, lambda v, kappa,
 // rho D_i, rho D_i H_i) and nu DUDY: per point for non-affine elements, once from
 // JxW-weighted sums for simplices (their shape gradients do not depend on the point).
-template <int DIM, int NEN, int NC>
-struct MatShape {
-  static constexpr int ND = Layout<DIM, NC>::ND;
-  static constexpr int N = NEN * ND;                  // rows (and columns) of the block
-  static constexpr int AG = NEN >= 8 ? 2 : 1;          // trial-node groups per row
-  static constexpr int NA = NEN / AG;                  // trial nodes per lane
-  static constexpr int LANES = N * AG;
-  static constexpr int WPE = (LANES + 31) / 32;        // warps per element
-  static constexpr int EPC = WPE == 1 ? 4 : (WPE == 2 ? 2 : 1);  // elements per CTA
-  static constexpr int ET = WPE * 32;                  // threads per element
-  static constexpr int CTA = EPC * ET;
-  static constexpr int NS = N + 1;                     // stage row stride (doubles)
-  static constexpr bool AFFINE = NEN == DIM + 1;
-};
 
 // Per-point vectors t_b = sum_k dN_b/dx_k tau[v_k] shared by the lanes of an element
 // (w, z, y and t_g come with the point record).
@@ -1102,15 +1128,29 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
   const int gl = tid % ET;      // thread index within the element
   ES& E = reinterpret_cast<ES*>(smem_raw)[ec];
   const long long li = (long long)blockIdx.x * EPC + ec;
+  {
+    // the CTA's block of point records ([word][point], see RecOut) into the elements'
+    // records in shared memory, 16-byte loads over the contiguous block
+    using QPT = QP<DIM, NEN, NC, S>;
+    constexpr int BP = EPC * NQ, RW = (int)(sizeof(QPT) / sizeof(S)), V = (int)(16 / sizeof(S));
+    constexpr int NV = RW * BP / V;
+    static_assert((RW * BP) % V == 0, "record block is a whole number of 16-byte words");
+    const int4* src = reinterpret_cast<const int4*>(reinterpret_cast<const S*>(in) + (long long)blockIdx.x * RW * BP);
+    ES* Es = reinterpret_cast<ES*>(smem_raw);
+    for (int i = tid; i < NV; i += M::CTA) {
+      const int4 x = src[i];
+      const S* xs = reinterpret_cast<const S*>(&x);
+#pragma unroll
+      for (int u = 0; u < V; ++u) {
+        const int w = i * V + u, f = w / BP, pp = w - f * BP;
+        reinterpret_cast<S*>(&Es[pp / NQ].u.in.qp[pp % NQ])[f] = xs[u];
+      }
+    }
+  }
+  __syncthreads();
   if (li >= n) return;          // whole element groups exit together
   const long long g = first + li;
   const long long e = k.el_list ? (long long)k.el_list[g] : g;
-  {
-    constexpr int W4 = sizeof(QP<DIM, NEN, NC, S>) * NQ / 16;
-    const int4* src = reinterpret_cast<const int4*>(in + li * NQ);
-    int4* dst = reinterpret_cast<int4*>(E.u.in.qp);
-    for (int i = gl; i < W4; i += ET) dst[i] = src[i];
-  }
   if (gl < NEN) {
     const int nd_ = __ldg(k.conn + e * NEN + gl);
     E.nodes[gl] = nd_;
