@@ -42,6 +42,11 @@ for p in (ROOT, ROOT / "oracle"):
 
 METRIC = "residual+Jacobian elements/s, mixed vs FP64 on 1 GB300 at <=1e-6 rel err; HBM %"
 BYTES_PER_ELEM_TET = 4 * 4 + 8 * 3 * 4 + 2 * 8 * 4 * 7 + 16 * (4 * 7) ** 2 + 16 * 4 * 7  # 13,552
+# DRAM bytes per element of one mixed tet assembly: dram__bytes_read.sum +
+# dram__bytes_write.sum summed by ncu over every kernel of an assembly (interior chunks,
+# zero fill, boundary) on the 163,618-tet mesh of the 30^3 lattice, whose CSR bytes per
+# element (1,002) match the 1.0M-tet mesh's (982); scaled by the element count.
+TRAFFIC_BYTES_PER_ELEM_TET = 5533
 LATTICE_N = 54
 
 
@@ -477,7 +482,8 @@ def main():
         "mixed_over_fp64": ms64 / ms_mx,
         "mixed_rel_err_vs_fp64": {"matrix": err_A, "rhs": err_b},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if hbm else None, "traffic": None,
+                     "frac": (achieved / hbm) if hbm else None, "traffic": TRAFFIC_BYTES_PER_ELEM_TET * ne,
+                     "traffic_source": "ncu DRAM bytes per element of a 163,618-tet assembly x elements",
                      "kernel": "interior_kernel (mixed form)", "kernel_ms": k_mx,
                      "bytes_per_element": BYTES_PER_ELEM_TET, "peak_source": "measured (MEASURED_PEAKS.json)"},
         "e2e": {"value": whole_job_rate(ne, e2e_s * 1e3, world), "unit": "elements/s",

@@ -1054,10 +1054,9 @@ __global__ void __launch_bounds__(256) norm_final_kernel(double* part) {
   if (threadIdx.x == 0) part[kNormBlocks] = sqrt(sh[0]);
 }
 
-// Zero fill of the CSR values and the rhs before the scatter adds into them.  A plain
-// kernel rather than cudaMemsetAsync: captured into a CUDA graph, the memset of the
-// CSR values ran far below the copy bandwidth on GB300 (a graph-replayed hex assembly
-// took 15% longer than the same assembly issued on streams).  16-byte stores on the
+// Zero fill of the CSR values and the rhs before the scatter adds into them, as a
+// kernel of the library (one counted launch each, visible with the other kernels in a
+// profile; it runs at copy bandwidth like cudaMemsetAsync).  16-byte stores on the
 // 16-byte-aligned body, scalar stores for an unaligned head and an odd tail.
 __global__ void __launch_bounds__(256) zero_kernel(double* __restrict__ p, long long n) {
   const long long head = (reinterpret_cast<uintptr_t>(p) & 15u) != 0 ? 1 : 0;
