@@ -931,6 +931,8 @@ KParams base_params(gales_asm* h, double dt) {
     d.inv_R = q.kind == GALES_CH_IDEAL_GAS ? 1.0 / q.R : 0.0;
     d.R_over_gamma = q.kind == GALES_CH_IDEAL_GAS ? q.R / q.gamma : 0.0;
     d.inv_D = 1.0 / q.chemical_diffusivity;
+    // 1/(rho^2 s^2) with s = 1/sqrt(rho beta), or 1e20 when beta = 0 (chemicals.hpp:43-47)
+    d.c2_coef = q.kind == GALES_CH_CUSTOM ? (q.beta == 0.0 ? 1.e-40 * d.inv_rho * d.inv_rho : q.beta / q.rho) : 0.0;
     if (q.kind == GALES_CH_IDEAL_GAS) k.has_gas = 1;
   }
   k.dt = dt;
@@ -939,6 +941,10 @@ KParams base_params(gales_asm* h, double dt) {
   k.dc_scale = h->setup.dc_scale_fact;
   for (int d = 0; d < 3; ++d) k.gravity[d] = h->setup.gravity[d];
   for (int i = 0; i < GALES_MAX_ND; ++i) k.u_ref_inv[i] = h->u_ref_inv[i];
+  for (int d = 0; d < 3; ++d) k.gravity_f[d] = (float)k.gravity[d];
+  for (int i = 0; i < GALES_MAX_ND; ++i) k.u_ref_inv_f[i] = (float)k.u_ref_inv[i];
+  k.inv_dt_f = (float)k.inv_dt;
+  k.dc_scale_f = (float)k.dc_scale;
   memcpy(k.gp, h->ei.gp, sizeof(k.gp));
   memcpy(k.sgp, h->ei.sgp, sizeof(k.sgp));
   k.W_in = h->ei.W_in;

@@ -41,6 +41,8 @@ struct KParams {
   int32_t n_sides, n_side_nodes, n_side_q;
   uint32_t dirichlet_mask[GALES_MAX_FLAGS];
   double sgp[6][4][3];
+  // binary32 copies (round to nearest) of parameters the mixed form uses in FP32
+  float gravity_f[3], u_ref_inv_f[GALES_MAX_ND], inv_dt_f, dc_scale_f;
   // mesh
   const double* coords;
   const int32_t* conn;
@@ -463,7 +465,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
 #pragma unroll
   for (int j = 0; j < ND; ++j) {
     if constexpr (FORM == GALES_FORM_FP64) dd[j] = (Iq[j] - Pq[j]) / k.dt;
-    else dd[j] = narrow_rn(Iq[j] - Pq[j]) * narrow_rn(k.inv_dt);
+    else dd[j] = narrow_rn(Iq[j] - Pq[j]) * k.inv_dt_f;
   }
   // gradients: FP64 in the FP64 form; FP32 of nodal differences in the mixed form
   // (sum_i dN_i/dx = 0, so sum_i dN_i (I_i - I_0) is the same gradient)
@@ -604,12 +606,12 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
     float gv = 0.f;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-      const float gd = narrow_rn(k.gravity[d]);
+      const float gd = k.gravity_f[d];
       SvR[1 + d] = rf * gd;
       gv = fmaf(gd, narrow_rn(v[d]), gv);
     }
     SvR[L::iT] = rf * gv;
-    const float idt = narrow_rn(k.inv_dt);
+    const float idt = k.inv_dt_f;
 #pragma unroll
     for (int j = 0; j < ND; ++j) GALES_RECA(rv, j) = fmaf(narrow_rn(U[j] - UP[j]), idt, -SvR[j]);
   }
@@ -772,7 +774,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
     // matrix stage multiplies with), and w
     R zz[ND], yy[ND], gg[ND], gR[DIM];
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) gR[d] = to_s<R>(k.gravity[d]);
+    for (int d = 0; d < DIM; ++d) gR[d] = FORM == GALES_FORM_FP64 ? R(k.gravity[d]) : R(k.gravity_f[d]);
 #pragma unroll
     for (int cc = 0; cc < ND; ++cc) zz[cc] = yy[cc] = gg[cc] = R(0);
 #pragma unroll
@@ -846,7 +848,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
         R Zn = R(0), Un = R(0), use1 = R(0);
 #pragma unroll
         for (int j = 0; j < ND; ++j) {
-          const R ui = to_s<R>(k.u_ref_inv[j]);
+          const R ui = FORM == GALES_FORM_FP64 ? R(k.u_ref_inv[j]) : R(k.u_ref_inv_f[j]);
           const R z = ui * (AdI[j] - SvR[j]);
           const R u = ui * Ur[j];
           Zn += z * z;
@@ -861,7 +863,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
             R n2 = R(0);
 #pragma unroll
             for (int j = 0; j < ND; ++j) {
-              const R u = to_s<R>(k.u_ref_inv[j]) * dU[d][j];
+              const R u = (FORM == GALES_FORM_FP64 ? R(k.u_ref_inv[j]) : R(k.u_ref_inv_f[j])) * dU[d][j];
               n2 += u * u;
             }
             const R n = sqrt(n2);
@@ -871,7 +873,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
         if (a == 1.0) nu = Zn * h * (R(1) / sqrt(use1));
         else if (a == 2.0) nu = Zn * h * h / Un;
         else if (a == 1.5) nu = Zn * h * ((R(1) / sqrt(use1)) + h / Un) / R(2);
-        nu = to_s<R>(k.dc_scale) * nu;
+        nu = (FORM == GALES_FORM_FP64 ? R(k.dc_scale) : R(k.dc_scale_f)) * nu;
       }
     }
   }
@@ -924,7 +926,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
   GALES_REC(nu) = S(nu);
 #pragma unroll
   for (int j = 0; j < ND; ++j) GALES_RECA(res, j) = S(Res[j]);
-  if (!isfinite(JxW) || !isfinite(pr.rho) || !isfinite(nu)) flag_error(k, GALES_ERR_NONFINITE, e);
+  if (!finite_bits(JxW) || !finite_bits(pr.rho) || !isfinite(nu)) flag_error(k, GALES_ERR_NONFINITE, e);
 }
 
 // Viscous/diffusive tangent contracted with the test-function gradient gb:
@@ -990,16 +992,19 @@ __device__ __forceinline__ double widen(double d) { return d; }
 template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
 __global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1) point_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ out,
                                                      long long first, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long li = t / NQ;
-  const int iq = (int)(t % NQ);
+  // chunk-local indices fit 32 bits (a chunk is one wave of CTAs); 64-bit shifts and
+  // divisions would issue on the FP64 pipe
+  const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int li = t / NQ;
+  const int iq = t - li * NQ;
   if (li >= n) return;
   const long long g = first + li;
   const long long e = k.el_list ? (long long)k.el_list[g] : g;
   using QPT = QP<DIM, NEN, NC, S>;
   constexpr int BP = MatShape<DIM, NEN, NC>::EPC * NQ;
   constexpr int RW = RecOut<QPT, BP>::RW;
-  const RecOut<QPT, BP> o{reinterpret_cast<S*>(out) + (t / BP) * (long long)(RW * BP), (int)(t % BP)};
+  const int blk = t / BP;
+  const RecOut<QPT, BP> o{reinterpret_cast<S*>(out) + (size_t)blk * (size_t)(RW * BP), t - blk * BP};
   point_phase<DIM, NEN, NC, NQ, FORM, S, BP>(k, e, iq, o);
 }
 

@@ -35,6 +35,7 @@ struct DevChem {
   double rho, mu, cp, cv, kappa, alpha, beta, R, gamma, D;
   // reciprocals and ratios for the mixed form's EOS (filled on the host)
   double inv_rho, beta_over_rho, alpha_over_rho, cv_shift, inv_R, R_over_gamma, inv_D;
+  double c2_coef;  // custom chemical: its 1/(rho_c^2 s_c^2) per unit Y_c
 };
 
 // The hardware conversions between binary64 and binary32 issue on the FP64 pipe,
@@ -64,6 +65,11 @@ __device__ __forceinline__ float narrow_rn(double d) {
     bits = sign | (e >= 255 ? 0x7f800000u : 0u);
   }
   return __uint_as_float(bits);
+}
+
+// isfinite on the high word (integer pipe): the exponent field is not all ones
+__device__ __forceinline__ bool finite_bits(double d) {
+  return ((unsigned int)__double2hiint(d) & 0x7ff00000u) != 0x7ff00000u;
 }
 
 template <typename S>
@@ -158,7 +164,7 @@ __device__ __forceinline__ void mixture_pair_fast(const DevChem* ch, bool has_ga
       cvp = fma(YP[c], fma(-TP, q.cv_shift, q.cp), cvp);
       C = fma(Y[c], q.inv_rho, C);
       v = fma(-T, q.cv_shift, q.cp);
-      c2 = fma(Y[c], q.beta == 0.0 ? 1.e-40 * q.inv_rho * q.inv_rho : q.beta_over_rho, c2);
+      c2 = fma(Y[c], q.c2_coef, c2);
       al = fma(Y[c], q.alpha_over_rho, al);
       be = fma(Y[c], q.beta_over_rho, be);
     } else {

@@ -23,7 +23,8 @@ R_U = 8.314462
 class DevChem(C.Structure):
     _fields_ = [("kind", C.c_int32), ("pad", C.c_int32)] + [
         (n, C.c_double) for n in ("rho", "mu", "cp", "cv", "kappa", "alpha", "beta", "R", "gamma", "D", "inv_rho",
-                                  "beta_over_rho", "alpha_over_rho", "cv_shift", "inv_R", "R_over_gamma", "inv_D")]
+                                  "beta_over_rho", "alpha_over_rho", "cv_shift", "inv_R", "R_over_gamma", "inv_D",
+                                  "c2_coef")]
 
 
 @pytest.fixture(scope="module")
