@@ -984,6 +984,22 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
   const long long chunk = h->chunk_elems[form];
   const long long nchunks = (n + chunk - 1) / chunk;
   if (nchunks == 0) return 0;
+  if (concurrent && form == GALES_FORM_MIXED) {
+    // one launch per chunk on the caller's stream: chunk c's point stage (buffer c % 3)
+    // beside chunk c-1's matrix stage (buffer (c-1) % 3), each launch programmatically
+    // dependent on the one before (the first follows the zero fill normally)
+    static_assert(kRing == 3, "the fused interior pass uses three record buffers");
+    for (long long c = 0; c <= nchunks; ++c) {
+      const long long pf = c * chunk, pn = c < nchunks ? std::min(chunk, n - pf) : 0;
+      const long long mf = (c - 1) * chunk, mn = c >= 1 ? std::min(chunk, n - mf) : 0;
+      void* pb = h->qpbuf[c % 3].p;
+      const void* mb = h->qpbuf[(c + 2) % 3].p;
+      LaunchResult r = ops.interior(k, h->nc, want_m, pb, pf, pn, mb, c >= 1 ? mf : 0, mn, c >= 1, st);
+      if (r.err != cudaSuccess) return cuda_fail(h, r.err, "interior kernel");
+      h->launches += r.launches;
+    }
+    return 0;
+  }
   if (concurrent) {
     CK(h, cudaEventRecord(h->ev_fork, st), "event");
     for (int i = 0; i < 2; ++i) CK(h, cudaStreamWaitEvent(h->ist[i], h->ev_fork, 0), "stream wait");

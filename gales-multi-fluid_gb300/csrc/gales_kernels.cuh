@@ -990,11 +990,11 @@ __device__ __forceinline__ double widen(double d) { return d; }
 // held to 128 registers (4 CTAs per SM): more warps hide the FP64 latency better
 // than the spilled values cost.
 template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
-__global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1) point_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ out,
-                                                     long long first, long long n) {
+__device__ __forceinline__ void point_block(const KParams& k, QP<DIM, NEN, NC, S>* __restrict__ out, long long first,
+                                            long long n, int bid) {
   // chunk-local indices fit 32 bits (a chunk is one wave of CTAs); 64-bit shifts and
-  // divisions would issue on the FP64 pipe
-  const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  // divisions would issue on the FP64 pipe.  CTAs of 128 threads.
+  const int t = bid * 128 + (int)threadIdx.x;
   const int li = t / NQ;
   const int iq = t - li * NQ;
   if (li >= n) return;
@@ -1006,6 +1006,12 @@ __global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1) point_k
   const int blk = t / BP;
   const RecOut<QPT, BP> o{reinterpret_cast<S*>(out) + (size_t)blk * (size_t)(RW * BP), t - blk * BP};
   point_phase<DIM, NEN, NC, NQ, FORM, S, BP>(k, e, iq, o);
+}
+
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
+__global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1) point_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ out,
+                                                     long long first, long long n) {
+  point_block<DIM, NEN, NC, NQ, FORM, S>(k, out, first, n, (int)blockIdx.x);
 }
 
 // Interior pass, stage 2: element matrices.  Lane (b, r, g) owns row (b, r) of the
@@ -1119,8 +1125,8 @@ __device__ __forceinline__ void add_viscous_row(S (&acc)[Layout<DIM, NC>::ND], i
 }
 
 template <int DIM, int NEN, int NC, int NQ, typename S, bool WANT_M>
-__global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
-    matrix_kernel(const KParams k, const QP<DIM, NEN, NC, S>* __restrict__ in, long long first, long long n) {
+__device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN, NC, S>* __restrict__ in,
+                                             long long first, long long n, int bid) {
   using L = Layout<DIM, NC>;
   using M = MatShape<DIM, NEN, NC>;
   using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
@@ -1132,7 +1138,7 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
   const int ec = tid / ET;      // element slot in the CTA
   const int gl = tid % ET;      // thread index within the element
   ES& E = reinterpret_cast<ES*>(smem_raw)[ec];
-  const long long li = (long long)blockIdx.x * EPC + ec;
+  const long long li = (long long)bid * EPC + ec;
   {
     // the CTA's block of point records ([word][point], see RecOut) into the elements'
     // records in shared memory, 16-byte loads over the contiguous block
@@ -1140,7 +1146,7 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
     constexpr int BP = EPC * NQ, RW = (int)(sizeof(QPT) / sizeof(S)), V = (int)(16 / sizeof(S));
     constexpr int NV = RW * BP / V;
     static_assert((RW * BP) % V == 0, "record block is a whole number of 16-byte words");
-    const int4* src = reinterpret_cast<const int4*>(reinterpret_cast<const S*>(in) + (long long)blockIdx.x * RW * BP);
+    const int4* src = reinterpret_cast<const int4*>(reinterpret_cast<const S*>(in) + (long long)bid * RW * BP);
     ES* Es = reinterpret_cast<ES*>(smem_raw);
     for (int i = tid; i < NV; i += M::CTA) {
       const int4 x = src[i];
@@ -1433,6 +1439,51 @@ __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
       }
     }
   }
+}
+
+template <int DIM, int NEN, int NC, int NQ, typename S, bool WANT_M>
+__global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
+    matrix_kernel(const KParams k, const QP<DIM, NEN, NC, S>* __restrict__ in, long long first, long long n) {
+  matrix_block<DIM, NEN, NC, NQ, S, WANT_M>(k, in, first, n, (int)blockIdx.x);
+}
+
+// Programmatic dependent launch (sm_90+): a launch made with programmatic stream
+// serialisation may start once every CTA of the previous launch in the stream has
+// signalled (launch_dependents) or exited; wait blocks until that previous launch has
+// completed and its writes are visible.  Without the launch attribute wait returns at
+// once.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Both interior stages in one launch (the mixed form with the atomic scatter): CTAs
+// [0, pt_ctas) run the point stage of chunk c into buffer c % 3, the others the matrix
+// stage of chunk c - 1 from buffer (c - 1) % 3.  CTAs are dispatched in index order, so
+// the long FP64-bound point CTAs take their slots first and the short matrix CTAs run
+// in the slot beside them on each SM and then in the slots they free.  Launches follow
+// each other with programmatic dependence: the next launch's CTAs fill the slots this
+// launch's tail frees.  Its matrix CTAs wait for this launch to complete (they read
+// the records its point CTAs wrote); its point CTAs write buffer (c + 1) % 3, last read
+// by the matrix CTAs of launch c - 1, which has completed by then because every matrix
+// CTA of launch c signals only after its own wait.  One stream, one launch per chunk:
+// the same schedule inside a CUDA graph (whose replay of a two-stream pipeline
+// overlapped the stages less).  Every matrix CTA shape is at most 128 threads; threads
+// beyond it leave at once.
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, bool WANT_M>
+__global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1)
+    interior_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ pt_out, long long pt_first, long long pt_n,
+                    int pt_ctas, const QP<DIM, NEN, NC, S>* __restrict__ mx_in, long long mx_first, long long mx_n) {
+  static_assert(MatShape<DIM, NEN, NC>::CTA <= 128, "matrix CTA fits the 128-thread launch");
+  if ((int)blockIdx.x < pt_ctas) {
+    griddep_launch_dependents();
+    point_block<DIM, NEN, NC, NQ, FORM, S>(k, pt_out, pt_first, pt_n, (int)blockIdx.x);
+    return;
+  }
+  if ((int)threadIdx.x >= MatShape<DIM, NEN, NC>::CTA) return;
+  griddep_wait();
+  griddep_launch_dependents();
+  matrix_block<DIM, NEN, NC, NQ, S, WANT_M>(k, mx_in, mx_first, mx_n, (int)blockIdx.x - pt_ctas);
 }
 
 // ---------------------------------------------------------------------------

@@ -44,8 +44,41 @@ struct InteriorInst {
     cudaError_t e = cudaFuncSetAttribute(matrix_kernel<DIM, NEN, NC, NQ, S, true>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(matrix_kernel<DIM, NEN, NC, NQ, S, false>,
+    e = cudaFuncSetAttribute(matrix_kernel<DIM, NEN, NC, NQ, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(interior_kernel<DIM, NEN, NC, NQ, FORM, S, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(interior_kernel<DIM, NEN, NC, NQ, FORM, S, false>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  }
+  // point stage of pt_n elements into pt_buf and matrix stage of mx_n elements from
+  // mx_buf in one launch (either count may be zero); pdl: programmatic dependence on
+  // the previous launch in the stream (see interior_kernel)
+  static LaunchResult interior(const KParams& k, bool want_m, void* pt_buf, long long pt_first, long long pt_n,
+                               const void* mx_buf, long long mx_first, long long mx_n, bool pdl, cudaStream_t st) {
+    const long long pt_ctas = (pt_n * NQ + 127) / 128, mx_ctas = (mx_n + M::EPC - 1) / M::EPC;
+    if (pt_ctas + mx_ctas == 0) return {cudaSuccess, 0};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(pt_ctas + mx_ctas));
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = sizeof(ES) * M::EPC;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    Rec* po = reinterpret_cast<Rec*>(pt_buf);
+    const Rec* mi = reinterpret_cast<const Rec*>(mx_buf);
+    const int pc = (int)pt_ctas;
+    cudaError_t e = want_m
+        ? cudaLaunchKernelEx(&cfg, interior_kernel<DIM, NEN, NC, NQ, FORM, S, true>, k, po, pt_first, pt_n, pc, mi,
+                             mx_first, mx_n)
+        : cudaLaunchKernelEx(&cfg, interior_kernel<DIM, NEN, NC, NQ, FORM, S, false>, k, po, pt_first, pt_n, pc, mi,
+                             mx_first, mx_n);
+    return {e != cudaSuccess ? e : cudaGetLastError(), 1};
   }
   static LaunchResult matrix(const KParams& k, bool want_m, const void* buf, long long first, long long n,
                              cudaStream_t st) {
@@ -89,6 +122,8 @@ struct InteriorOps {
   LaunchResult (*point)(const KParams&, int nc, void* buf, long long first, long long n, cudaStream_t);
   LaunchResult (*matrix)(const KParams&, int nc, bool want_m, const void* buf, long long first, long long n,
                          cudaStream_t);
+  LaunchResult (*interior)(const KParams&, int nc, bool want_m, void* pt_buf, long long pt_first, long long pt_n,
+                           const void* mx_buf, long long mx_first, long long mx_n, bool pdl, cudaStream_t);
 };
 
 #define GALES_NC_SWITCH(expr_nc, CALL) \
@@ -133,7 +168,17 @@ struct InteriorDispatch {
 #undef GALES_C
     return {cudaErrorInvalidValue, 0};
   }
-  static InteriorOps ops() { return {&prepare, &point_occupancy, &rec_bytes, &point, &matrix}; }
+  static LaunchResult interior(const KParams& k, int nc, bool want_m, void* pt_buf, long long pt_first,
+                               long long pt_n, const void* mx_buf, long long mx_first, long long mx_n, bool pdl,
+                               cudaStream_t st) {
+#define GALES_C(NC)                                                                                              \
+  return InteriorInst<DIM, NEN, NC, NQ, FORM>::interior(k, want_m, pt_buf, pt_first, pt_n, mx_buf, mx_first, mx_n, \
+                                                        pdl, st)
+    GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+    return {cudaErrorInvalidValue, 0};
+  }
+  static InteriorOps ops() { return {&prepare, &point_occupancy, &rec_bytes, &point, &matrix, &interior}; }
 };
 
 // Boundary pass of one element type; S is the matrix arithmetic type of the form.
