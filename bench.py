@@ -43,10 +43,10 @@ for p in (ROOT, ROOT / "oracle"):
 METRIC = "residual+Jacobian elements/s, mixed vs FP64 on 1 GB300 at <=1e-6 rel err; HBM %"
 BYTES_PER_ELEM_TET = 4 * 4 + 8 * 3 * 4 + 2 * 8 * 4 * 7 + 16 * (4 * 7) ** 2 + 16 * 4 * 7  # 13,552
 # DRAM bytes per element of one mixed tet assembly: dram__bytes_read.sum +
-# dram__bytes_write.sum summed by ncu over every kernel of an assembly (interior chunks,
-# zero fill, boundary) on the 163,618-tet mesh of the 30^3 lattice, whose CSR bytes per
-# element (1,002) match the 1.0M-tet mesh's (982); scaled by the element count.
-TRAFFIC_BYTES_PER_ELEM_TET = 5533
+# dram__bytes_write.sum summed by ncu over every kernel of an assembly (interior
+# launches, zero fill, boundary) on the 163,618-tet mesh of the 30^3 lattice, whose CSR
+# bytes per element (1,002) match the 1.0M-tet mesh's (982); scaled by the element count.
+TRAFFIC_BYTES_PER_ELEM_TET = 6727
 LATTICE_N = 54
 
 
