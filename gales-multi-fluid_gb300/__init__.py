@@ -492,7 +492,10 @@ class ResidualCheck:
         return n <= max(1.e-8 * self.res0, 1.e-5), rel
 
 
+from .meshio import read_mesh, write_mesh  # noqa: E402  (uses Mesh and GalesError above)
+
 __all__ = [
+    "read_mesh", "write_mesh",
     "abi", "GalesError", "custom_chemical", "ideal_gas", "ideal_gas_named", "ideal_gas_params", "Material",
     "Setup", "p0_policy", "Mesh", "nb_dofs", "LinearSystem", "FluidAssembly", "ResidualCheck",
     "FORM_FP64", "FORM_MIXED", "TAU_NONE", "TAU_2001", "TAU_2019", "TAU_2007", "TAU_2014",

@@ -249,6 +249,25 @@ double gales_asm_last_phase_ms(gales_asm* h, int32_t phase);
 /* Number of kernel launches made by the library since the handle was created. */
 int64_t gales_asm_launch_count(gales_asm* h);
 
+/* GALES mesh files, replacing the reader of Mesh::mesh_reader (src/fem/mesh/mesh.hpp:
+ * 147-456: read_header, read_elements, read_sides, read_nodes, el_side_info).  Text
+ * lines "MESH! 2D|3D", "nodes N", "elements N", "sides N", one bounds line per
+ * dimension, then N "Node gid x y [z] flag", N "Element gid pid nnodes n... flag" and
+ * N "Side gid pid nsn n... flag" lines; tokens separated by spaces or commas.
+ * pid >= 0 reads the elements and sides of that partition (as one MPI rank of the
+ * reference does), pid < 0 all of them.  The nodes are the sorted distinct gids the
+ * read elements use (local id = position).  A boundary element's local side gets the
+ * flag of the Side line with the same nodes when all its nodes are boundary nodes;
+ * sides with flag > 0 become gales_mesh_desc boundary sides.  Host-only, no GPU use.
+ * On failure err (err_len bytes, may be NULL) holds the reason and the line. */
+typedef struct gales_mesh_file gales_mesh_file;
+int gales_mesh_read(const char* path, int32_t pid, gales_mesh_file** out, char* err, int32_t err_len);
+/* Fills desc with pointers into the mesh file's arrays (valid until it is freed);
+ * node_gid[n_nodes] and el_gid[n_elements] give the file's gids (either may be NULL). */
+int gales_mesh_file_desc(const gales_mesh_file* m, gales_mesh_desc* desc, const int64_t** node_gid,
+                         const int64_t** el_gid);
+void gales_mesh_file_free(gales_mesh_file* m);
+
 #ifdef __cplusplus
 }
 #endif
