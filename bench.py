@@ -303,6 +303,34 @@ def run_hex(args):
     print(json.dumps(line), flush=True)
 
 
+def adaptive_dt_block(gm, fa, mesh, mat, setup, I, dt, torch, dev, with_cpu):
+    """Adaptive time step (f_mc + set_dt) on the benchmark mesh: device state, per-call
+    wall time including the 8-byte read-back of the minimum; the oracle on the first
+    50,000 elements (one thread) beside it."""
+    Id = torch.tensor(I, device=dev)
+    d_el = torch.zeros(mesh.n_elements, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        dt_new = fa.adaptive_dt(Id, dt, 0.5, 1e-6, 1.0, dt_el=d_el)
+    torch.cuda.synchronize(dev)
+    k = 10
+    t0 = time.perf_counter()
+    for _ in range(k):
+        dt_new = fa.adaptive_dt(Id, dt, 0.5, 1e-6, 1.0, dt_el=d_el)
+    ms = (time.perf_counter() - t0) / k * 1e3
+    out = {"workload": "f_mc over the benchmark mesh, CFL 0.5, device state", "ms": ms,
+           "elements_per_s": mesh.n_elements / (ms * 1e-3), "dt_new": dt_new}
+    if with_cpu:
+        import oracle
+        n = min(mesh.n_elements, 50000)
+        sub = gm.Mesh(mesh.coords, mesh.conn[:n], mesh.node_flag, mesh.el_on_boundary[:n],
+                      mesh.bd_sides[mesh.bd_sides[:, 0] < n], name="sample")
+        t0 = time.perf_counter()
+        oracle.adaptive_dt(sub, mat, setup, I, dt, 0.5)
+        out["cpu_oracle_elements_per_s"] = n / (time.perf_counter() - t0)
+        out["cpu_oracle_cores"] = 1
+    return out
+
+
 def vjp_block(gm, syn, torch, dev, n=32):
     """Adjoint workload: ~200k tets, 3 components.  Exact and frozen VJP against the
     forward residual (FP64 and mixed), and the memory a stored-point design would need."""
@@ -494,6 +522,8 @@ def main():
     if rank == 0 and not args.no_vjp:
         syn = importlib.import_module("gales-multi-fluid_gb300.synthetic")
         line["vjp"] = vjp_block(gm, syn, torch, dev)
+    if rank == 0:
+        line["adaptive_dt"] = adaptive_dt_block(gm, fa, mesh, mat, setup, I, dt, torch, dev, not args.no_cpu)
     if rank == 0 and not args.no_cpu:
         rate, cores, n = cpu_oracle_rate(mesh, mat, setup, I, P, dt, None, None, None, 0)
         line["cpu_baseline"] = {"value": rate, "unit": "elements/s", "cores": cores, "kind": "port",

@@ -454,6 +454,17 @@ class FluidAssembly:
         self._check(self._L.gales_asm_norm2(self._h, _addr(rhs), C.byref(out), None))
         return out.value
 
+    def adaptive_dt(self, I, dt: float, cfl: float, dt_min: float, dt_max: float, dt_el=None,
+                    stream: int = 0) -> float:
+        """adaptive_time_criteria::f_mc + set_dt (adaptive_time_step.hpp:183-260, 380-393):
+        the next time step from state I; dt_el (n_elements, host or device) optionally
+        receives every element's smallest Gauss-point value."""
+        out = C.c_double()
+        self._check(self._L.gales_asm_adaptive_dt(self._h, _addr(I), float(dt), float(cfl), float(dt_min),
+                                                  float(dt_max), _addr(dt_el) if dt_el is not None else None,
+                                                  C.byref(out), stream or None))
+        return out.value
+
     def element_blocks(self, I, P, dt: float, elements, which: int = 0, form: int = FORM_FP64,
                        want_matrix: bool = True):
         """Batched fluid::execute_i (which=0) / execute_b (which=1): local (m, r) per element."""
@@ -494,8 +505,13 @@ class ResidualCheck:
 
 from .meshio import read_mesh, write_mesh  # noqa: E402  (uses Mesh and GalesError above)
 
+def dt_update(dt_elem_min: float, dt: float, dt_min: float, dt_max: float) -> float:
+    """set_dt (adaptive_time_step.hpp:380-393) through the library (host arithmetic)."""
+    return abi.lib().gales_dt_update(float(dt_elem_min), float(dt), float(dt_min), float(dt_max))
+
+
 __all__ = [
-    "read_mesh", "write_mesh",
+    "read_mesh", "write_mesh", "dt_update",
     "abi", "GalesError", "custom_chemical", "ideal_gas", "ideal_gas_named", "ideal_gas_params", "Material",
     "Setup", "p0_policy", "Mesh", "nb_dofs", "LinearSystem", "FluidAssembly", "ResidualCheck",
     "FORM_FP64", "FORM_MIXED", "TAU_NONE", "TAU_2001", "TAU_2019", "TAU_2007", "TAU_2014",

@@ -15,4 +15,8 @@ GeometryOps geometry_ops_hex8() { return GeometryDispatch<3, 8, 8>::ops(); }
 
 BoundaryInfo boundary_info_hex8(int nc) { return BoundaryInfoDispatch<3, 8, 6, 4>::info(nc); }
 
+LaunchResult adaptive_dt_hex8(const KParams& k, int nc, double cfl, double* dt_el, long long n, cudaStream_t st) {
+  return adaptive_dt_dispatch<3, 8, 8>(k, nc, cfl, dt_el, n, st);
+}
+
 }  // namespace gales

@@ -1038,6 +1038,14 @@ LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, int form, long lo
   return boundary_hex8(k, h->nc, form, n, st);
 }
 
+LaunchResult dispatch_adaptive_dt(gales_asm* h, const KParams& k, double cfl, double* dt_el, long long n,
+                                  cudaStream_t st) {
+  if (h->dim == 2 && h->nen == 3) return adaptive_dt_tri3(k, h->nc, cfl, dt_el, n, st);
+  if (h->dim == 2 && h->nen == 4) return adaptive_dt_quad4(k, h->nc, cfl, dt_el, n, st);
+  if (h->dim == 3 && h->nen == 4) return adaptive_dt_tet4(k, h->nc, cfl, dt_el, n, st);
+  return adaptive_dt_hex8(k, h->nc, cfl, dt_el, n, st);
+}
+
 LaunchResult dispatch_vjp(gales_asm* h, const KParams& k, bool boundary, long long n, cudaStream_t st) {
   if (h->dim == 2 && h->nen == 3) return boundary ? vjp_boundary_tri3(k, h->nc, n, st) : vjp_interior_tri3(k, h->nc, n, st);
   if (h->dim == 2 && h->nen == 4)
@@ -1097,6 +1105,52 @@ cudaError_t launch_zero(double* p, long long n, int sms, cudaStream_t st) {
   const int blocks = (int)std::max<long long>(1, std::min<long long>(want, 4LL * std::max(sms, 1)));
   zero_kernel<<<blocks, 256, 0, st>>>(p, n);
   return cudaGetLastError();
+}
+
+// First smallest value of x[0..n) (min_element), in two launches: per-block minima,
+// then the minimum of those (partials kept in index order).
+constexpr int kMinBlocks = 256;
+__global__ void __launch_bounds__(256) min_partial_kernel(const double* __restrict__ x, long long n,
+                                                          double* __restrict__ part) {
+  __shared__ double sh[256];
+  __shared__ int has[256];
+  double m = 0.0;
+  int any = 0;
+  for (long long i = (long long)blockIdx.x * 256 + threadIdx.x; i < n; i += (long long)gridDim.x * 256) {
+    const double v = x[i];
+    if (!any || v < m) m = v;
+    any = 1;
+  }
+  sh[threadIdx.x] = m;
+  has[threadIdx.x] = any;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o && has[threadIdx.x + o] && (!has[threadIdx.x] || sh[threadIdx.x + o] < sh[threadIdx.x])) {
+      sh[threadIdx.x] = sh[threadIdx.x + o];
+      has[threadIdx.x] = 1;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = sh[0];
+    part[kMinBlocks + blockIdx.x] = has[0] ? 1.0 : 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(256) min_final_kernel(double* part) {
+  __shared__ double sh[256];
+  __shared__ int has[256];
+  sh[threadIdx.x] = part[threadIdx.x];
+  has[threadIdx.x] = part[kMinBlocks + threadIdx.x] != 0.0;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o && has[threadIdx.x + o] && (!has[threadIdx.x] || sh[threadIdx.x + o] < sh[threadIdx.x])) {
+      sh[threadIdx.x] = sh[threadIdx.x + o];
+      has[threadIdx.x] = 1;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[2 * kMinBlocks] = sh[0];
 }
 
 cudaError_t launch_norm2(const double* x, long long n, double* part, cudaStream_t st) {
@@ -1472,6 +1526,51 @@ int gales_asm_norm2(gales_asm* h, const double* rhs, double* out, void* stream) 
   CK(h, cudaStreamSynchronize(st), "synchronize");
   r = *h->h_aux;
   *out = r;
+  return 0;
+}
+
+double gales_dt_update(double dt_elem_min, double dt, double dt_min, double dt_max) {
+  // set_dt (adaptive_time_step.hpp:380-393): growth bounded by 1% of dt, then clamped
+  double d = (dt_elem_min > (1.01 * dt)) ? 1.01 * dt : dt_elem_min;
+  d = std::max(std::min(d, dt_max), dt_min);
+  return d;
+}
+
+int gales_asm_adaptive_dt(gales_asm* h, const double* I, double dt, double cfl, double dt_min, double dt_max,
+                          double* dt_el, double* dt_new, void* stream) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (!I || !dt_new) return fail(h, GALES_ERR_BAD_INPUT, "null state or result pointer");
+  if (!(dt > 0.0) || !(cfl > 0.0)) return fail(h, GALES_ERR_BAD_INPUT, "dt and CFL must be positive");
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const double* dI = I;
+  if (!is_device_ptr(I)) {
+    CK(h, h->s_I.alloc(h->n_rows), "staging I");
+    CK(h, cudaMemcpyAsync(h->s_I.p, I, (size_t)h->n_rows * sizeof(double), cudaMemcpyHostToDevice, st), "copy I");
+    dI = h->s_I.p;
+  }
+  const bool dev_el = dt_el && is_device_ptr(dt_el);
+  double* del = dt_el;
+  if (!dev_el) {
+    CK(h, h->s_aux.alloc(std::max<int64_t>(h->n_el, 1)), "per-element dt");
+    del = h->s_aux.p;
+  }
+  KParams k = base_params(h, dt);
+  k.I = dI;
+  LaunchResult r = dispatch_adaptive_dt(h, k, cfl, del, h->n_el, st);
+  if (r.err != cudaSuccess) return cuda_fail(h, r.err, "adaptive dt kernel");
+  h->launches += r.launches;
+  CK(h, h->s_th.alloc(std::max(2 * kMinBlocks + 1, 3 * GALES_MAX_COMP)), "min scratch");
+  min_partial_kernel<<<kMinBlocks, 256, 0, st>>>(del, h->n_el, h->s_th.p);
+  min_final_kernel<<<1, 256, 0, st>>>(h->s_th.p);
+  CK(h, cudaGetLastError(), "min kernels");
+  h->launches += 2;
+  CK(h, cudaMemcpyAsync(h->h_aux, h->s_th.p + 2 * kMinBlocks, sizeof(double), cudaMemcpyDeviceToHost, st),
+     "copy min");
+  if (dt_el && !dev_el)
+    CK(h, cudaMemcpyAsync(dt_el, del, (size_t)h->n_el * sizeof(double), cudaMemcpyDeviceToHost, st), "copy dt");
+  CK(h, cudaStreamSynchronize(st), "synchronize");
+  *dt_new = gales_dt_update(*h->h_aux, dt, dt_min, dt_max);
   return 0;
 }
 

@@ -1487,6 +1487,82 @@ __global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1)
 }
 
 // ---------------------------------------------------------------------------
+// Adaptive time step of the multicomponent solver, adaptive_time_criteria::f_mc
+// (adaptive_time_step.hpp:183-260): one thread per element, FP64 with the reference's
+// operations in order (this is instantiated in the FP64 units, without contraction).
+// At each Gauss point: interpolate I and its gradient, the mixture at shear rate 0,
+// |v| (uBLAS norm_2); 1.2 dt where |v| < DBL_EPSILON, else with h = compute_h(v, dv)
+// (compute_del_v, 356-374) and v_tau = |v| (or, for Mach > 0.3,
+// sqrt(|v|^2 + 1.5 c^2 + c sqrt(16|v|^2 + c^2)) in 2D, sqrt(|v|^2 + 2 c^2 +
+// c sqrt(4|v|^2 + c^2)) in 3D), use = 2 max(2 mu/rho, kappa/(rho cv))/h^2 + v_tau/h and
+// CFL/use.  dt_el[e] = the first smallest of the element's values (min_element).
+template <int DIM, int NEN, int NC, int NQ>
+__global__ void __launch_bounds__(128) adaptive_dt_kernel(const KParams k, double cfl, double* __restrict__ dt_el,
+                                                          long long n) {
+  using L = Layout<DIM, NC>;
+  constexpr int ND = L::ND;
+  constexpr int NG = geo_per_element<DIM, NEN>(NQ);
+  const long long e = (long long)blockIdx.x * 128 + threadIdx.x;
+  if (e >= n) return;
+  int nodes[NEN];
+#pragma unroll
+  for (int a = 0; a < NEN; ++a) nodes[a] = __ldg(k.conn + e * NEN + a);
+  double Ie[NEN][ND];
+#pragma unroll
+  for (int i = 0; i < NEN; ++i)
+#pragma unroll
+    for (int j = 0; j < ND; ++j) Ie[i][j] = __ldg(k.I + (long long)nodes[i] * ND + j);
+  double best = 0.0;
+  for (int iq = 0; iq < NQ; ++iq) {
+    const ElemGeo<DIM, NEN>& q = reinterpret_cast<const ElemGeo<DIM, NEN>*>(k.geo)[e * NG + (NG == 1 ? 0 : iq)];
+    double Iq[ND], dI[DIM][ND];
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      double a = 0.0;
+#pragma unroll
+      for (int i = 0; i < NEN; ++i) a += k.sh_tab[iq][i] * Ie[i][j];
+      Iq[j] = a;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        double b = 0.0;
+#pragma unroll
+        for (int i = 0; i < NEN; ++i) b += q.ds[d][i] * Ie[i][j];
+        dI[d][j] = b;
+      }
+    }
+    double p, v[DIM], T, Y[NC];
+    assign<DIM, NC>(Iq, p, v, T, Y);
+    Props<NC> pr;
+    mixture<NC>(k.ch, p, T, Y, pr);
+    const double v_nrm = sqrt(vsq<DIM>(v));
+    double dtg;
+    if (v_nrm < kEps) {
+      dtg = 1.2 * k.dt;
+    } else {
+      double dv[DIM][DIM];
+#pragma unroll
+      for (int a = 0; a < DIM; ++a)
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) dv[a][d] = dI[d][1 + a];
+      const double h = compute_h<DIM>(q.G, v, dv);
+      const double c = pr.c;
+      double v_tau = v_nrm;
+      const double mach = v_nrm / c;
+      if (mach > 0.3) {
+        if (DIM == 2) v_tau = sqrt(v_nrm * v_nrm + 1.5 * c * c + c * sqrt(16.0 * v_nrm * v_nrm + c * c));
+        else v_tau = sqrt(v_nrm * v_nrm + 2.0 * c * c + c * sqrt(4.0 * v_nrm * v_nrm + c * c));
+      }
+      const double m1 = 2.0 * pr.mu / pr.rho, m2 = pr.kappa / (pr.rho * pr.cv);
+      const double mx = (m1 < m2) ? m2 : m1;  // std::max
+      const double use = 2.0 * mx / (h * h) + v_tau / h;
+      dtg = cfl / use;
+    }
+    if (iq == 0 || dtg < best) best = dtg;
+  }
+  dt_el[e] = best;
+}
+
+// ---------------------------------------------------------------------------
 // Boundary pass helpers (fluid_2d.hpp:610-868): boundary-modified A_k and K_kl.
 
 // Entry of the boundary-modified K_kl (fluid_2d.hpp:819-867).

@@ -197,6 +197,19 @@ LaunchResult boundary_dispatch(const KParams& k, int nc, long long n, cudaStream
   return {cudaErrorInvalidValue, 0};
 }
 
+// Adaptive time step (f_mc) per element of one element type.
+template <int DIM, int NEN, int NQ>
+LaunchResult adaptive_dt_dispatch(const KParams& k, int nc, double cfl, double* dt_el, long long n, cudaStream_t st) {
+  if (n <= 0) return {cudaSuccess, 0};
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+#define GALES_C(NC)                                                                       \
+  adaptive_dt_kernel<DIM, NEN, NC, NQ><<<blocks, 128, 0, st>>>(k, cfl, dt_el, n); \
+  return {cudaGetLastError(), 1}
+  GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+  return {cudaErrorInvalidValue, 0};
+}
+
 // Boundary side-point geometry (handle creation) and record sizes.
 struct BoundaryInfo {
   size_t bgeo_bytes;
@@ -252,18 +265,21 @@ LaunchResult boundary_tri3(const KParams&, int nc, int form, long long n, cudaSt
 LaunchResult boundary_tri3_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_tri3();
 BoundaryInfo boundary_info_tri3(int nc);
+LaunchResult adaptive_dt_tri3(const KParams&, int nc, double cfl, double* dt_el, long long n, cudaStream_t);
 InteriorOps interior_ops_quad4_fp64();
 InteriorOps interior_ops_quad4_mixed();
 LaunchResult boundary_quad4(const KParams&, int nc, int form, long long n, cudaStream_t);
 LaunchResult boundary_quad4_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_quad4();
 BoundaryInfo boundary_info_quad4(int nc);
+LaunchResult adaptive_dt_quad4(const KParams&, int nc, double cfl, double* dt_el, long long n, cudaStream_t);
 InteriorOps interior_ops_tet4_fp64();
 InteriorOps interior_ops_tet4_mixed();
 LaunchResult boundary_tet4(const KParams&, int nc, int form, long long n, cudaStream_t);
 LaunchResult boundary_tet4_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_tet4();
 BoundaryInfo boundary_info_tet4(int nc);
+LaunchResult adaptive_dt_tet4(const KParams&, int nc, double cfl, double* dt_el, long long n, cudaStream_t);
 InteriorOps interior_ops_hex8_fp64();
 InteriorOps interior_ops_hex8_mixed();
 LaunchResult boundary_hex8(const KParams&, int nc, int form, long long n, cudaStream_t);
@@ -279,5 +295,6 @@ LaunchResult vjp_boundary_hex8(const KParams&, int nc, long long n, cudaStream_t
 LaunchResult boundary_hex8_mixed(const KParams&, int nc, long long n, cudaStream_t);
 GeometryOps geometry_ops_hex8();
 BoundaryInfo boundary_info_hex8(int nc);
+LaunchResult adaptive_dt_hex8(const KParams&, int nc, double cfl, double* dt_el, long long n, cudaStream_t);
 
 }  // namespace gales

@@ -15,4 +15,8 @@ GeometryOps geometry_ops_quad4() { return GeometryDispatch<2, 4, 4>::ops(); }
 
 BoundaryInfo boundary_info_quad4(int nc) { return BoundaryInfoDispatch<2, 4, 4, 2>::info(nc); }
 
+LaunchResult adaptive_dt_quad4(const KParams& k, int nc, double cfl, double* dt_el, long long n, cudaStream_t st) {
+  return adaptive_dt_dispatch<2, 4, 4>(k, nc, cfl, dt_el, n, st);
+}
+
 }  // namespace gales

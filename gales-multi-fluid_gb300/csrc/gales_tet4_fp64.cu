@@ -15,4 +15,8 @@ GeometryOps geometry_ops_tet4() { return GeometryDispatch<3, 4, 4>::ops(); }
 
 BoundaryInfo boundary_info_tet4(int nc) { return BoundaryInfoDispatch<3, 4, 4, 3>::info(nc); }
 
+LaunchResult adaptive_dt_tet4(const KParams& k, int nc, double cfl, double* dt_el, long long n, cudaStream_t st) {
+  return adaptive_dt_dispatch<3, 4, 4>(k, nc, cfl, dt_el, n, st);
+}
+
 }  // namespace gales

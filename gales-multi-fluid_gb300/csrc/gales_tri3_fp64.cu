@@ -15,4 +15,8 @@ GeometryOps geometry_ops_tri3() { return GeometryDispatch<2, 3, 3>::ops(); }
 
 BoundaryInfo boundary_info_tri3(int nc) { return BoundaryInfoDispatch<2, 3, 3, 2>::info(nc); }
 
+LaunchResult adaptive_dt_tri3(const KParams& k, int nc, double cfl, double* dt_el, long long n, cudaStream_t st) {
+  return adaptive_dt_dispatch<2, 3, 3>(k, nc, cfl, dt_el, n, st);
+}
+
 }  // namespace gales

@@ -236,6 +236,19 @@ int gales_asm_element_blocks(gales_asm* h, const double* I, const double* P, dou
 /* ||b||_2 of a rhs vector (residual_check.hpp:48-51). */
 int gales_asm_norm2(gales_asm* h, const double* rhs, double* out, void* stream);
 
+/* Adaptive time step of the multicomponent solver (adaptive_time_criteria::f_mc,
+ * adaptive_time_step.hpp:183-260, called from main.cpp:258-261 after a time step): for
+ * every element the smallest over its Gauss points of CFL/use, with
+ * use = 2 max(2 mu/rho, kappa/(rho cv))/h^2 + v_tau/h from the state I (FP64, the
+ * reference's operations), or 1.2 dt where |v| < DBL_EPSILON.  dt_el (n_elements,
+ * host or device, may be NULL) receives those values; *dt_new the next step by
+ * set_dt (380-393; gales_dt_update).  The call synchronises its stream. */
+int gales_asm_adaptive_dt(gales_asm* h, const double* I, double dt, double cfl, double dt_min, double dt_max,
+                          double* dt_el, double* dt_new, void* stream);
+/* set_dt (adaptive_time_step.hpp:380-393) on the smallest element value: at most
+ * 1.01 dt, then clamped to [dt_min, dt_max].  Host arithmetic only. */
+double gales_dt_update(double dt_elem_min, double dt, double dt_min, double dt_max);
+
 /* Status of the last call: error bits and the first offending element (-1 if none). */
 int gales_asm_status(gales_asm* h, int64_t* first_bad_element);
 const char* gales_asm_last_error(gales_asm* h);

@@ -1378,6 +1378,65 @@ int gor_element(const gales_mesh_desc* mesh, const gales_material_desc* mat,
   return element_boundary(cx, X, Ie, flags, m, r, m != nullptr);
 }
 
+/* adaptive_time_criteria::f_mc (adaptive_time_step.hpp:183-260): per element, the first
+ * smallest over its Gauss points of CFL/use, use = 2 max(2 mu/rho, kappa/(rho cv))/h^2
+ * + v_tau/h with v_tau = |v|, or for Mach > 0.3 the acoustic form of 230-234; 1.2 dt
+ * where |v| < DBL_EPSILON.  compute_del_v (356-374): del_v(i, j) = dI_j[1+i]. */
+int gor_adaptive_dt(const gales_mesh_desc* mesh, const gales_material_desc* mat, const gales_setup_desc* setup,
+                    const double* I, double dt, double cfl, double* dt_el) {
+  Ctx cx;
+  if (!init_ctx(cx, mesh, mat, setup, dt)) return GALES_ERR_UNSUPPORTED;
+  const int dim = cx.dim, nd = cx.nd, nen = cx.nen;
+  for (int64_t e = 0; e < mesh->n_elements; ++e) {
+    double X[8][3];
+    double Ie[8 * MD], Pe[8 * MD];
+    gather(cx, *mesh, e, I, I, X, Ie, Pe);
+    std::vector<double> dt_gp;
+    for (int iq = 0; iq < cx.et.nq; ++iq) {
+      Quad q;
+      make_quad(cx.et, X, cx.et.gp[iq], true, q);
+      double Iq[MD], dI[3][MD];
+      for (int j = 0; j < nd; ++j) {
+        double a = 0.0;
+        for (int i = 0; i < nen; ++i) a += q.sh[i] * Ie[nd * i + j];
+        Iq[j] = a;
+      }
+      for (int k = 0; k < dim; ++k)
+        for (int j = 0; j < nd; ++j) {
+          double a = 0.0;
+          for (int i = 0; i < nen; ++i) a += q.ds[k][i] * Ie[nd * i + j];
+          dI[k][j] = a;
+        }
+      double p, vel[3] = {0, 0, 0}, T, Y[GALES_MAX_COMP];
+      assign(cx, Iq, p, vel, T, Y);
+      Props pr;
+      properties(*mat, p, T, Y, pr);
+      double v_nrm = 0.0;
+      for (int k = 0; k < dim; ++k) v_nrm += vel[k] * vel[k];
+      v_nrm = sqrt(v_nrm);
+      if (v_nrm < TOL) {
+        dt_gp.push_back(1.2 * dt);
+        continue;
+      }
+      double del_v[3][3];
+      for (int i = 0; i < dim; ++i)
+        for (int j = 0; j < dim; ++j) del_v[i][j] = dI[j][1 + i];
+      const double h = compute_h(q, dim, vel, del_v);
+      const double c = pr.c;
+      double v_tau = v_nrm;
+      const double Mach = v_nrm / c;
+      if (Mach > 0.3) {
+        if (dim == 2) v_tau = sqrt(v_nrm * v_nrm + 1.5 * c * c + c * sqrt(16.0 * v_nrm * v_nrm + c * c));
+        else v_tau = sqrt(v_nrm * v_nrm + 2.0 * c * c + c * sqrt(4.0 * v_nrm * v_nrm + c * c));
+      }
+      const double use = 2.0 * std::max(2.0 * pr.mu / pr.rho, pr.kappa / (pr.rho * pr.cv)) / (h * h) + v_tau / h;
+      dt_gp.push_back(cfl / use);
+    }
+    dt_el[e] = *std::min_element(dt_gp.begin(), dt_gp.end());
+  }
+  return 0;
+}
+
 /* fluid_assembly::execute (fluid_assembly.hpp:39-68).  vals may be NULL (residual only).
  * With colour != NULL, colours run in order and the elements of one colour run on
  * nthreads threads (no two share a node); otherwise elements run serially in order. */

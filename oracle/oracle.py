@@ -47,8 +47,10 @@ def lib() -> C.CDLL:
                                   dp, dp, C.c_double, C.c_int64, C.c_int, dp, dp]
         L.gor_assemble.argtypes = [C.POINTER(abi.MeshDesc), C.POINTER(abi.MaterialDesc), C.POINTER(abi.SetupDesc),
                                    dp, dp, C.c_double, i64p, i32p, dp, dp, C.c_int, i32p, C.c_int32, i64p]
+        L.gor_adaptive_dt.argtypes = [C.POINTER(abi.MeshDesc), C.POINTER(abi.MaterialDesc),
+                                      C.POINTER(abi.SetupDesc), dp, C.c_double, C.c_double, dp]
         for f in ("gor_properties", "gor_inverse", "gor_quad", "gor_gauss", "gor_pattern", "gor_colouring",
-                  "gor_element", "gor_assemble"):
+                  "gor_element", "gor_assemble", "gor_adaptive_dt"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -164,3 +166,21 @@ def assemble(mesh, material, setup, I, P, dt, row_ptr, col, want_matrix=True, nt
                            _i64(row_ptr), _i32(col), _d(vals) if want_matrix else None, _d(rhs), nthreads, colour_p,
                            n_colours, C.byref(fb))
     return vals, rhs, s, fb.value
+
+
+def adaptive_dt(mesh, material, setup, I, dt, cfl):
+    """adaptive_time_criteria::f_mc on the CPU: every element's smallest Gauss-point dt."""
+    I = np.ascontiguousarray(I, dtype=np.float64)
+    out = np.zeros(mesh.n_elements)
+    s = lib().gor_adaptive_dt(C.byref(mesh.desc()), C.byref(material.desc), C.byref(setup.desc), _d(I),
+                              float(dt), float(cfl), _d(out))
+    if s:
+        raise RuntimeError(f"gor_adaptive_dt status {s}")
+    return out
+
+
+def set_dt(dt_el_min, dt, dt_min, dt_max):
+    """set_dt (adaptive_time_step.hpp:380-393)."""
+    d = 1.01 * dt if dt_el_min > 1.01 * dt else dt_el_min
+    return max(min(d, dt_max), dt_min)
+
