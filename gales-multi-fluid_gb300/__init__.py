@@ -465,6 +465,17 @@ class FluidAssembly:
                                                   C.byref(out), stream or None))
         return out.value
 
+    SECONDARY_FIELDS = ("rho", "mu", "cp", "cv", "alpha", "beta", "kappa", "sound_speed")
+
+    def secondary_dofs(self, I, out=None, stream: int = 0):
+        """secondary_dofs::execute (secondary_dofs.hpp:56-101): the mixture at every
+        node, an (8, n_nodes) array (or the given host/device buffer) in the order of
+        SECONDARY_FIELDS."""
+        if out is None:
+            out = np.zeros((8, self.mesh.n_nodes))
+        self._check(self._L.gales_asm_secondary_dofs(self._h, _addr(I), _addr(out), stream or None))
+        return out
+
     def element_blocks(self, I, P, dt: float, elements, which: int = 0, form: int = FORM_FP64,
                        want_matrix: bool = True):
         """Batched fluid::execute_i (which=0) / execute_b (which=1): local (m, r) per element."""

@@ -143,6 +143,8 @@ def lib() -> C.CDLL:
     L.gales_asm_launch_count.restype = C.c_int64
     L.gales_asm_adaptive_dt.argtypes = [vp, vp, C.c_double, C.c_double, C.c_double, C.c_double, vp, _p(C.c_double), vp]
     L.gales_asm_adaptive_dt.restype = C.c_int
+    L.gales_asm_secondary_dofs.argtypes = [vp, vp, vp, vp]
+    L.gales_asm_secondary_dofs.restype = C.c_int
     L.gales_dt_update.argtypes = [C.c_double] * 4
     L.gales_dt_update.restype = C.c_double
     L.gales_mesh_read.argtypes = [C.c_char_p, i32, _p(vp), C.c_char_p, i32]
@@ -163,4 +165,5 @@ EXPORTED = [
     "gales_asm_vjp", "gales_asm_element_blocks", "gales_asm_norm2", "gales_asm_status", "gales_asm_last_error",
     "gales_asm_last_ms", "gales_asm_last_phase_ms", "gales_asm_launch_count",
     "gales_mesh_read", "gales_mesh_file_desc", "gales_mesh_file_free", "gales_asm_adaptive_dt", "gales_dt_update",
+    "gales_asm_secondary_dofs",
 ]

@@ -1574,6 +1574,35 @@ int gales_asm_adaptive_dt(gales_asm* h, const double* I, double dt, double cfl, 
   return 0;
 }
 
+int gales_asm_secondary_dofs(gales_asm* h, const double* I, double* out, void* stream) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (!I || !out) return fail(h, GALES_ERR_BAD_INPUT, "null state or output pointer");
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const double* dI = I;
+  if (!is_device_ptr(I)) {
+    CK(h, h->s_I.alloc(h->n_rows), "staging I");
+    CK(h, cudaMemcpyAsync(h->s_I.p, I, (size_t)h->n_rows * sizeof(double), cudaMemcpyHostToDevice, st), "copy I");
+    dI = h->s_I.p;
+  }
+  const int64_t n = h->n_nodes;
+  const bool dev_out = is_device_ptr(out);
+  double* dout = out;
+  if (!dev_out) {
+    CK(h, h->s_aux.alloc(std::max<int64_t>(8 * n, 1)), "staging output");
+    dout = h->s_aux.p;
+  }
+  KParams k = base_params(h, 1.0);
+  k.I = dI;
+  LaunchResult r = h->dim == 2 ? secondary_dofs_2d(k, h->nc, dout, n, st) : secondary_dofs_3d(k, h->nc, dout, n, st);
+  if (r.err != cudaSuccess) return cuda_fail(h, r.err, "secondary dofs kernel");
+  h->launches += r.launches;
+  if (!dev_out)
+    CK(h, cudaMemcpyAsync(out, dout, (size_t)(8 * n) * sizeof(double), cudaMemcpyDeviceToHost, st), "copy output");
+  CK(h, cudaStreamSynchronize(st), "synchronize");
+  return 0;
+}
+
 int gales_asm_status(gales_asm* h, int64_t* first_bad_element) {
   if (!h) return GALES_ERR_BAD_INPUT;
   if (first_bad_element) *first_bad_element = h->first_bad;

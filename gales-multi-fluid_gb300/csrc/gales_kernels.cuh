@@ -1562,6 +1562,27 @@ __global__ void __launch_bounds__(128) adaptive_dt_kernel(const KParams k, doubl
   dt_el[e] = best;
 }
 
+// Secondary variables at the nodes, secondary_dofs::execute (secondary_dofs.hpp:56-101):
+// the mixture properties of every node's state at shear rate 0, written word-major:
+// out[f * n + node] for f = rho, mu, cp, cv, alpha, beta, kappa, sound speed (the
+// order of 146-153).  FP64 with the reference's operations (FP64 units).
+template <int DIM, int NC>
+__global__ void __launch_bounds__(128) secondary_dofs_kernel(const KParams k, double* __restrict__ out, long long n) {
+  using L = Layout<DIM, NC>;
+  const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
+  if (i >= n) return;
+  double w[L::ND];
+#pragma unroll
+  for (int j = 0; j < L::ND; ++j) w[j] = __ldg(k.I + i * L::ND + j);
+  double p, v[DIM], T, Y[NC];
+  assign<DIM, NC>(w, p, v, T, Y);
+  Props<NC> pr;
+  mixture<NC>(k.ch, p, T, Y, pr);
+  const double f[8] = {pr.rho, pr.mu, pr.cp, pr.cv, pr.alpha, pr.beta, pr.kappa, pr.c};
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q * n + i] = f[q];
+}
+
 // ---------------------------------------------------------------------------
 // Boundary pass helpers (fluid_2d.hpp:610-868): boundary-modified A_k and K_kl.
 

@@ -210,6 +210,19 @@ LaunchResult adaptive_dt_dispatch(const KParams& k, int nc, double cfl, double* 
   return {cudaErrorInvalidValue, 0};
 }
 
+// Secondary variables at the nodes (any element type of the dimension).
+template <int DIM>
+LaunchResult secondary_dofs_dispatch(const KParams& k, int nc, double* out, long long n, cudaStream_t st) {
+  if (n <= 0) return {cudaSuccess, 0};
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+#define GALES_C(NC)                                                            \
+  secondary_dofs_kernel<DIM, NC><<<blocks, 128, 0, st>>>(k, out, n); \
+  return {cudaGetLastError(), 1}
+  GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+  return {cudaErrorInvalidValue, 0};
+}
+
 // Boundary side-point geometry (handle creation) and record sizes.
 struct BoundaryInfo {
   size_t bgeo_bytes;
@@ -266,6 +279,7 @@ LaunchResult boundary_tri3_mixed(const KParams&, int nc, long long n, cudaStream
 GeometryOps geometry_ops_tri3();
 BoundaryInfo boundary_info_tri3(int nc);
 LaunchResult adaptive_dt_tri3(const KParams&, int nc, double cfl, double* dt_el, long long n, cudaStream_t);
+LaunchResult secondary_dofs_2d(const KParams&, int nc, double* out, long long n, cudaStream_t);
 InteriorOps interior_ops_quad4_fp64();
 InteriorOps interior_ops_quad4_mixed();
 LaunchResult boundary_quad4(const KParams&, int nc, int form, long long n, cudaStream_t);
@@ -280,6 +294,7 @@ LaunchResult boundary_tet4_mixed(const KParams&, int nc, long long n, cudaStream
 GeometryOps geometry_ops_tet4();
 BoundaryInfo boundary_info_tet4(int nc);
 LaunchResult adaptive_dt_tet4(const KParams&, int nc, double cfl, double* dt_el, long long n, cudaStream_t);
+LaunchResult secondary_dofs_3d(const KParams&, int nc, double* out, long long n, cudaStream_t);
 InteriorOps interior_ops_hex8_fp64();
 InteriorOps interior_ops_hex8_mixed();
 LaunchResult boundary_hex8(const KParams&, int nc, int form, long long n, cudaStream_t);

@@ -19,4 +19,8 @@ LaunchResult adaptive_dt_tet4(const KParams& k, int nc, double cfl, double* dt_e
   return adaptive_dt_dispatch<3, 4, 4>(k, nc, cfl, dt_el, n, st);
 }
 
+LaunchResult secondary_dofs_3d(const KParams& k, int nc, double* out, long long n, cudaStream_t st) {
+  return secondary_dofs_dispatch<3>(k, nc, out, n, st);
+}
+
 }  // namespace gales

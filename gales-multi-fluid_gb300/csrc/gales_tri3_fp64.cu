@@ -19,4 +19,8 @@ LaunchResult adaptive_dt_tri3(const KParams& k, int nc, double cfl, double* dt_e
   return adaptive_dt_dispatch<2, 3, 3>(k, nc, cfl, dt_el, n, st);
 }
 
+LaunchResult secondary_dofs_2d(const KParams& k, int nc, double* out, long long n, cudaStream_t st) {
+  return secondary_dofs_dispatch<2>(k, nc, out, n, st);
+}
+
 }  // namespace gales

@@ -249,6 +249,13 @@ int gales_asm_adaptive_dt(gales_asm* h, const double* I, double dt, double cfl, 
  * 1.01 dt, then clamped to [dt_min, dt_max].  Host arithmetic only. */
 double gales_dt_update(double dt_elem_min, double dt, double dt_min, double dt_max);
 
+/* Secondary variables at the nodes (secondary_dofs::execute, secondary_dofs.hpp:56-101,
+ * the mixture of every node's state at shear rate 0): out[f * n_nodes + node] for
+ * f = 0..7 = rho, mu, cp, cv, alpha, beta, kappa, sound speed (host or device, 8 n_nodes
+ * doubles).  The magma volume and mass fractions (pp_vf_g) need the magma mixtures and
+ * are not provided.  The call synchronises its stream. */
+int gales_asm_secondary_dofs(gales_asm* h, const double* I, double* out, void* stream);
+
 /* Status of the last call: error bits and the first offending element (-1 if none). */
 int gales_asm_status(gales_asm* h, int64_t* first_bad_element);
 const char* gales_asm_last_error(gales_asm* h);

@@ -59,3 +59,25 @@ def test_adaptive_dt_device_buffers(cuda_lib):
     ref = oracle.adaptive_dt(mesh, mat, setup, I, dt, 0.5)
     assert np.array_equal(d_el.cpu().numpy(), ref)
     assert dt_new == oracle.set_dt(ref.min(), dt, 1e-6, 10.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind, nc", [("tri", 2), ("tet", 3), ("hex", 4)])
+def test_secondary_dofs_match_oracle_properties(kind, nc, cuda_lib):
+    """secondary_dofs::execute (secondary_dofs.hpp:56-101): the mixture at every node,
+    bit for bit with the oracle's properties (fluid_properties.hpp:199-227)."""
+    mesh, mat, setup, I, P, dt = cases.make(kind, nc)
+    fa = gm.FluidAssembly(mesh, mat, setup)
+    got = fa.secondary_dofs(I)
+    nd, dim = fa.nd, mesh.dim
+    S = I.reshape(-1, nd)
+    keys = ["rho", "mu", "cp", "cv", "alpha", "beta", "kappa", "c"]
+    for node in range(0, mesh.n_nodes, max(1, mesh.n_nodes // 97)):
+        Y = np.zeros(nc)
+        Y[:nc - 1] = S[node, dim + 2:]
+        s = 0.0
+        for i in range(nc - 1):
+            s += Y[i]
+        Y[nc - 1] = 1.0 - s
+        ref = oracle.properties(mat, S[node, 0], S[node, dim + 1], Y)
+        assert np.array_equal(got[:, node], np.array([ref[k] for k in keys])), node
