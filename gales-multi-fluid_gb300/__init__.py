@@ -516,13 +516,49 @@ class ResidualCheck:
 
 from .meshio import read_mesh, write_mesh  # noqa: E402  (uses Mesh and GalesError above)
 
+def pressure_profile(material: "Material", p0: float, h: float, T, T1, Y=None, Y1=None) -> np.ndarray:
+    """Hydrostatic pressure column (pressure_profile.hpp:480-496, RK4 from p0 at the top
+    with step h): T, Y at the n+1 column points and T1, Y1 at the points h/2 below them
+    (Y, Y1: (n+1, nc-1) independent mass fractions).  Returns p at the column points."""
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    T1 = np.ascontiguousarray(T1, dtype=np.float64)
+    n = len(T) - 1
+    nc = material.nb_comp
+    Y = np.ascontiguousarray(np.zeros((n + 1, nc - 1)) if Y is None else Y, dtype=np.float64)
+    Y1 = np.ascontiguousarray(np.zeros((n + 1, nc - 1)) if Y1 is None else Y1, dtype=np.float64)
+    if len(T1) != n + 1 or Y.shape != (n + 1, nc - 1) or Y1.shape != (n + 1, nc - 1):
+        raise ValueError("T, T1: n+1 values; Y, Y1: (n+1, nc-1)")
+    p = np.zeros(n + 1)
+    dp = C.POINTER(C.c_double)
+    rc = abi.lib().gales_pressure_profile(C.byref(material.desc), float(p0), float(h), n, T.ctypes.data_as(dp),
+                                          T1.ctypes.data_as(dp), Y.ctypes.data_as(dp), Y1.ctypes.data_as(dp),
+                                          p.ctypes.data_as(dp))
+    if rc:
+        raise GalesError(rc, "gales_pressure_profile")
+    return p
+
+
+def pressure_interpolate(y_col, p_col, y) -> np.ndarray:
+    """p_interpolation (pressure_profile.hpp:26-41) of a column at the heights y."""
+    y_col = np.ascontiguousarray(y_col, dtype=np.float64)
+    p_col = np.ascontiguousarray(p_col, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    out = np.zeros(len(y))
+    dp = C.POINTER(C.c_double)
+    rc = abi.lib().gales_pressure_interpolate(y_col.ctypes.data_as(dp), p_col.ctypes.data_as(dp), len(y_col),
+                                              y.ctypes.data_as(dp), len(y), out.ctypes.data_as(dp))
+    if rc:
+        raise GalesError(rc, "gales_pressure_interpolate: a height outside the column")
+    return out
+
+
 def dt_update(dt_elem_min: float, dt: float, dt_min: float, dt_max: float) -> float:
     """set_dt (adaptive_time_step.hpp:380-393) through the library (host arithmetic)."""
     return abi.lib().gales_dt_update(float(dt_elem_min), float(dt), float(dt_min), float(dt_max))
 
 
 __all__ = [
-    "read_mesh", "write_mesh", "dt_update",
+    "read_mesh", "write_mesh", "dt_update", "pressure_profile", "pressure_interpolate",
     "abi", "GalesError", "custom_chemical", "ideal_gas", "ideal_gas_named", "ideal_gas_params", "Material",
     "Setup", "p0_policy", "Mesh", "nb_dofs", "LinearSystem", "FluidAssembly", "ResidualCheck",
     "FORM_FP64", "FORM_MIXED", "TAU_NONE", "TAU_2001", "TAU_2019", "TAU_2007", "TAU_2014",

@@ -145,6 +145,10 @@ def lib() -> C.CDLL:
     L.gales_asm_adaptive_dt.restype = C.c_int
     L.gales_asm_secondary_dofs.argtypes = [vp, vp, vp, vp]
     L.gales_asm_secondary_dofs.restype = C.c_int
+    L.gales_pressure_profile.argtypes = [_p(MaterialDesc), C.c_double, C.c_double, i32, dp, dp, dp, dp, dp]
+    L.gales_pressure_profile.restype = C.c_int
+    L.gales_pressure_interpolate.argtypes = [dp, dp, i32, dp, i64, dp]
+    L.gales_pressure_interpolate.restype = C.c_int
     L.gales_dt_update.argtypes = [C.c_double] * 4
     L.gales_dt_update.restype = C.c_double
     L.gales_mesh_read.argtypes = [C.c_char_p, i32, _p(vp), C.c_char_p, i32]
@@ -165,5 +169,5 @@ EXPORTED = [
     "gales_asm_vjp", "gales_asm_element_blocks", "gales_asm_norm2", "gales_asm_status", "gales_asm_last_error",
     "gales_asm_last_ms", "gales_asm_last_phase_ms", "gales_asm_launch_count",
     "gales_mesh_read", "gales_mesh_file_desc", "gales_mesh_file_free", "gales_asm_adaptive_dt", "gales_dt_update",
-    "gales_asm_secondary_dofs",
+    "gales_asm_secondary_dofs", "gales_pressure_profile", "gales_pressure_interpolate",
 ]

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <atomic>
 #include <cfloat>
 #include <climits>
@@ -914,25 +915,28 @@ int gales_asm_set_scatter(gales_asm* h, int32_t mode) {
 
 namespace {
 
+void fill_chem(const gales_chemical_desc& q, DevChem& d) {
+  d.kind = q.kind;
+  d.rho = q.rho; d.mu = q.mu; d.cp = q.cp; d.cv = q.cv; d.kappa = q.kappa;
+  d.alpha = q.alpha; d.beta = q.beta; d.R = q.R; d.gamma = q.gamma; d.D = q.chemical_diffusivity;
+  // ratios used by the mixed form's EOS
+  d.inv_rho = q.kind == GALES_CH_CUSTOM ? 1.0 / q.rho : 0.0;
+  d.beta_over_rho = q.kind == GALES_CH_CUSTOM ? q.beta / q.rho : 0.0;
+  d.alpha_over_rho = q.kind == GALES_CH_CUSTOM ? q.alpha / q.rho : 0.0;
+  d.cv_shift = (q.kind == GALES_CH_CUSTOM && q.beta != 0.0) ? q.alpha * q.alpha / (q.rho * q.beta) : 0.0;
+  d.inv_R = q.kind == GALES_CH_IDEAL_GAS ? 1.0 / q.R : 0.0;
+  d.R_over_gamma = q.kind == GALES_CH_IDEAL_GAS ? q.R / q.gamma : 0.0;
+  d.inv_D = 1.0 / q.chemical_diffusivity;
+  // 1/(rho^2 s^2) with s = 1/sqrt(rho beta), or 1e20 when beta = 0 (chemicals.hpp:43-47)
+  d.c2_coef = q.kind == GALES_CH_CUSTOM ? (q.beta == 0.0 ? 1.e-40 * d.inv_rho * d.inv_rho : q.beta / q.rho) : 0.0;
+}
+
 KParams base_params(gales_asm* h, double dt) {
   KParams k;
   memset(&k, 0, sizeof(k));
   for (int c = 0; c < h->nc; ++c) {
     const gales_chemical_desc& q = h->mat.comp[c];
-    DevChem& d = k.ch[c];
-    d.kind = q.kind;
-    d.rho = q.rho; d.mu = q.mu; d.cp = q.cp; d.cv = q.cv; d.kappa = q.kappa;
-    d.alpha = q.alpha; d.beta = q.beta; d.R = q.R; d.gamma = q.gamma; d.D = q.chemical_diffusivity;
-    // ratios used by the mixed form's EOS
-    d.inv_rho = q.kind == GALES_CH_CUSTOM ? 1.0 / q.rho : 0.0;
-    d.beta_over_rho = q.kind == GALES_CH_CUSTOM ? q.beta / q.rho : 0.0;
-    d.alpha_over_rho = q.kind == GALES_CH_CUSTOM ? q.alpha / q.rho : 0.0;
-    d.cv_shift = (q.kind == GALES_CH_CUSTOM && q.beta != 0.0) ? q.alpha * q.alpha / (q.rho * q.beta) : 0.0;
-    d.inv_R = q.kind == GALES_CH_IDEAL_GAS ? 1.0 / q.R : 0.0;
-    d.R_over_gamma = q.kind == GALES_CH_IDEAL_GAS ? q.R / q.gamma : 0.0;
-    d.inv_D = 1.0 / q.chemical_diffusivity;
-    // 1/(rho^2 s^2) with s = 1/sqrt(rho beta), or 1e20 when beta = 0 (chemicals.hpp:43-47)
-    d.c2_coef = q.kind == GALES_CH_CUSTOM ? (q.beta == 0.0 ? 1.e-40 * d.inv_rho * d.inv_rho : q.beta / q.rho) : 0.0;
+    fill_chem(q, k.ch[c]);
     if (q.kind == GALES_CH_IDEAL_GAS) k.has_gas = 1;
   }
   k.dt = dt;
@@ -1600,6 +1604,65 @@ int gales_asm_secondary_dofs(gales_asm* h, const double* I, double* out, void* s
   if (!dev_out)
     CK(h, cudaMemcpyAsync(out, dout, (size_t)(8 * n) * sizeof(double), cudaMemcpyDeviceToHost, st), "copy output");
   CK(h, cudaStreamSynchronize(st), "synchronize");
+  return 0;
+}
+
+int gales_pressure_profile(const gales_material_desc* mat, double p0, double h, int32_t n_steps, const double* T,
+                           const double* T1, const double* Y, const double* Y1, double* p_out) {
+  if (!mat || !T || !T1 || !p_out || n_steps < 0) return GALES_ERR_BAD_INPUT;
+  const int nc = mat->nb_comp;
+  if (nc < 1 || nc > GALES_MAX_COMP) return GALES_ERR_BAD_INPUT;
+  if (nc > 1 && (!Y || !Y1)) return GALES_ERR_BAD_INPUT;
+  DevChem ch[GALES_MAX_COMP];
+  for (int c = 0; c < nc; ++c) fill_chem(mat->comp[c], ch[c]);
+  auto full_Y = [&](const double* y, double* out) {  // A[i][nc-1] = 1 - accumulate(A[i][0..nc-2])
+    double s = 0.0;
+    for (int c = 0; c < nc - 1; ++c) {
+      out[c] = y[c];
+      s = s + y[c];
+    }
+    out[nc - 1] = 1.0 - s;
+  };
+  auto rho = [&](double p, double t, const double* y) {
+    switch (nc) {
+#define GALES_RHO(N)                        \
+  case N: {                                 \
+    Props<N> pr;                            \
+    mixture<N>(ch, p, t, y, pr);            \
+    return pr.rho;                          \
+  }
+      GALES_RHO(1) GALES_RHO(2) GALES_RHO(3) GALES_RHO(4) GALES_RHO(5) GALES_RHO(6) GALES_RHO(7) GALES_RHO(8)
+#undef GALES_RHO
+      default: return 0.0;
+    }
+  };
+  double Ya[GALES_MAX_COMP], Yb[GALES_MAX_COMP], Yc[GALES_MAX_COMP];
+  p_out[0] = p0;
+  for (int32_t i = 0; i < n_steps; ++i) {
+    full_Y(Y + (size_t)i * (nc - 1), Ya);
+    full_Y(Y1 + (size_t)i * (nc - 1), Yb);
+    full_Y(Y + (size_t)(i + 1) * (nc - 1), Yc);
+    const double m1 = 9.81 * rho(p_out[i], T[i], Ya);
+    const double m2 = 9.81 * rho(p_out[i] + 0.5 * h * m1, T1[i], Yb);
+    const double m3 = 9.81 * rho(p_out[i] + 0.5 * h * m2, T1[i], Yb);
+    const double m4 = 9.81 * rho(p_out[i] + h * m3, T[i + 1], Yc);
+    p_out[i + 1] = p_out[i] + h / 6. * (m1 + 2.0 * (m2 + m3) + m4);
+  }
+  return 0;
+}
+
+int gales_pressure_interpolate(const double* y_col, const double* p_col, int32_t n_col, const double* y, int64_t n,
+                               double* p_out) {
+  if (!y_col || !p_col || !y || !p_out || n_col < 2 || n < 0) return GALES_ERR_BAD_INPUT;
+  const bool ascending = y_col[0] < y_col[n_col - 1];
+  for (int64_t k = 0; k < n; ++k) {
+    size_t i = ascending ? (size_t)(std::lower_bound(y_col, y_col + n_col, y[k]) - y_col)
+                         : (size_t)(std::lower_bound(y_col, y_col + n_col, y[k], std::greater<double>()) - y_col);
+    if (i > 0) i--;
+    if (i >= (size_t)n_col - 1) return GALES_ERR_BAD_INPUT;  // outside the column (the reference's Error)
+    const double f = (y[k] - y_col[i]) / (y_col[i + 1] - y_col[i]);
+    p_out[k] = f * p_col[i + 1] + (1.0 - f) * p_col[i];
+  }
   return 0;
 }
 

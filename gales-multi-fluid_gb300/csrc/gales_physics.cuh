@@ -97,8 +97,8 @@ struct Props {
 };
 
 template <int NC>
-__device__ __forceinline__ void mixture(const DevChem* ch, double p, double T, const double* Y,
-                                        Props<NC>& o) {
+__host__ __device__ __forceinline__ void mixture(const DevChem* ch, double p, double T, const double* Y,
+                                                 Props<NC>& o) {
   double rho = 0.0, mu = 0.0, cp = 0.0, cv = 0.0, kappa = 0.0, c2 = 0.0;
   double calpha[NC], cbeta[NC];
 #pragma unroll

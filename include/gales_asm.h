@@ -256,6 +256,22 @@ double gales_dt_update(double dt_elem_min, double dt, double dt_min, double dt_m
  * are not provided.  The call synchronises its stream. */
 int gales_asm_secondary_dofs(gales_asm* h, const double* I, double* out, void* stream);
 
+/* Hydrostatic pressure column of the multicomponent solver (pressure_profile_mc,
+ * pressure_profile.hpp:326-516, Runge_Kutta 480-496), host arithmetic: from p_out[0] = p0
+ * at the top, p_out[i+1] = p_out[i] + h/6 (m1 + 2 (m2 + m3) + m4) with m = 9.81 rho(p, T,
+ * Y) at the start (T[i], Y[i]), twice at the midpoint (T1[i], Y1[i]) and at the end
+ * (T[i+1], Y[i+1]).  T and Y sample the case's initial_T / initial_Y at the column points
+ * y_i = max - h i, T1 and Y1 at y_i - h/2 (n_steps + 1 entries each; Y holds the nc - 1
+ * independent fractions per point, the last is 1 - their sum as the reference forms it).
+ * p_out has n_steps + 1 entries. */
+int gales_pressure_profile(const gales_material_desc* mat, double p0, double h, int32_t n_steps, const double* T,
+                           const double* T1, const double* Y, const double* Y1, double* p_out);
+/* p_interpolation (pressure_profile.hpp:26-41): linear interpolation of the column
+ * (y_col, p_col) at the heights y[0..n); GALES_ERR_BAD_INPUT when a height falls
+ * outside the column (where the reference stops with an error). */
+int gales_pressure_interpolate(const double* y_col, const double* p_col, int32_t n_col, const double* y, int64_t n,
+                               double* p_out);
+
 /* Status of the last call: error bits and the first offending element (-1 if none). */
 int gales_asm_status(gales_asm* h, int64_t* first_bad_element);
 const char* gales_asm_last_error(gales_asm* h);

@@ -184,3 +184,48 @@ def set_dt(dt_el_min, dt, dt_min, dt_max):
     d = 1.01 * dt if dt_el_min > 1.01 * dt else dt_el_min
     return max(min(d, dt_max), dt_min)
 
+
+
+def pressure_profile(material, p0, h, T, T1, Y, Y1):
+    """pressure_profile_mc::Runge_Kutta (pressure_profile.hpp:480-496), with the last
+    mass fraction formed as 1 - accumulate(...) (pressure_profile.hpp:378-388)."""
+    nc = material.nb_comp
+    n = len(T) - 1
+
+    def full(y):
+        s = 0.0
+        for c in range(nc - 1):
+            s = s + float(y[c])
+        return [float(x) for x in y[:nc - 1]] + [1.0 - s]
+
+    def rho(p, t, y):
+        return properties(material, p, t, np.asarray(full(y)))["rho"]
+
+    p = [float(p0)]
+    for i in range(n):
+        m1 = 9.81 * rho(p[i], T[i], Y[i])
+        m2 = 9.81 * rho(p[i] + 0.5 * h * m1, T1[i], Y1[i])
+        m3 = 9.81 * rho(p[i] + 0.5 * h * m2, T1[i], Y1[i])
+        m4 = 9.81 * rho(p[i] + h * m3, T[i + 1], Y[i + 1])
+        p.append(p[i] + h / 6. * (m1 + 2.0 * (m2 + m3) + m4))
+    return np.array(p)
+
+
+def pressure_interpolate(y_col, p_col, y):
+    """p_interpolation (pressure_profile.hpp:26-41)."""
+    import bisect
+    y_col = [float(v) for v in y_col]
+    out = []
+    for yy in y:
+        if y_col[0] < y_col[-1]:
+            i = bisect.bisect_left(y_col, yy)
+        else:
+            neg = [-v for v in y_col]
+            i = bisect.bisect_left(neg, -yy)
+        if i > 0:
+            i -= 1
+        if i >= len(y_col) - 1:
+            raise IndexError("index i goes out of the vector scope")
+        f = (yy - y_col[i]) / (y_col[i + 1] - y_col[i])
+        out.append(f * p_col[i + 1] + (1.0 - f) * p_col[i])
+    return np.array(out)
