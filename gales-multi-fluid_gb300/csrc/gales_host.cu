@@ -152,6 +152,7 @@ constexpr int kVjpAux = 3 * GALES_MAX_COMP + GALES_MAX_ND;
 // point CTAs resident per SM the chunk holds three per SM), so that the FP64-bound
 // point stage and the issue-bound matrix stage share every SM.
 constexpr int kRing = 3;    // point-record buffers in flight between the two stages
+constexpr int kCopyEvents = 24;  // row copies per host-buffer assembly (at most)
 inline int point_ctas_per_chunk_sm(int occupancy) { return occupancy >= 3 ? occupancy - 1 : occupancy; }
 
 GeometryOps geometry_ops(int dim, int nen) {
@@ -216,6 +217,12 @@ struct gales_asm {
   int32_t n_colours = 0;
   std::vector<int32_t> colour_order;  // elements sorted by colour
   std::vector<int32_t> sweep;         // elements along a Morton curve of their centroids
+  // host-buffer calls: elements grouped by the bucket of their lowest node (Morton order
+  // inside a bucket), so that finished CSR rows form a growing prefix that is copied to
+  // the host while later chunks run
+  std::vector<int32_t> sweep_rows;
+  std::vector<int64_t> bucket_end;    // end (exclusive) of each bucket in sweep_rows
+  int64_t bucket_nodes = 1;
   std::vector<int64_t> colour_off;
   std::vector<int32_t> bd_list;
   std::vector<int8_t> bd_sides;
@@ -224,7 +231,7 @@ struct gales_asm {
   std::vector<int32_t> bpt_off, bpt_el, bpt_ip;
   // device
   DevBuf<double> d_coords;
-  DevBuf<int32_t> d_conn, d_node_flag, d_colour_order, d_bd_list, d_sweep;
+  DevBuf<int32_t> d_conn, d_node_flag, d_colour_order, d_bd_list, d_sweep, d_sweep_rows;
   DevBuf<int64_t> d_node_rp;
   DevBuf<uint16_t> d_slot;
   DevBuf<int8_t> d_bd_sides;
@@ -252,6 +259,9 @@ struct gales_asm {
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
   cudaEvent_t ev_pt[kRing] = {}, ev_mx[kRing] = {};   // chunk in a buffer written / consumed
   cudaStream_t bst = nullptr;                  // boundary pass, concurrent with the interior
+  cudaStream_t cst = nullptr;                  // device-to-host copies of finished CSR rows
+  cudaEvent_t ev_copy[kCopyEvents] = {};
+  cudaEvent_t ev_cjoin = nullptr;
   cudaEvent_t ev_bfork = nullptr, ev_bjoin = nullptr;
   int status = 0;
   int64_t first_bad = -1;
@@ -288,6 +298,18 @@ bool is_device_ptr(const void* p) {
     return false;
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Page-locked host memory (cudaHostAlloc or registered): copies into it run
+// asynchronously, so they may overlap the assembly.
+bool is_pinned_host_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
 }
 
 // Reference fluid properties at the dc_2006 reference state (fluid_2d.hpp:123-135):
@@ -514,6 +536,25 @@ void build_sweep(gales_asm* h, const double* coords) {
   std::sort(key.begin(), key.end());
   h->sweep.resize(h->n_el);
   for (int64_t e = 0; e < h->n_el; ++e) h->sweep[e] = key[e].second;
+  // bucket of the lowest node of every element; stable sort of the Morton order by it
+  h->bucket_nodes = std::max<int64_t>(1, (h->n_nodes + 127) / 128);
+  const int64_t nb = (h->n_nodes + h->bucket_nodes - 1) / h->bucket_nodes;
+  std::vector<int64_t> count(nb + 1, 0);
+  std::vector<int32_t> bucket(h->n_el);
+  for (int64_t e = 0; e < h->n_el; ++e) {
+    int32_t lo_node = h->conn[e * nen];
+    for (int n = 1; n < nen; ++n) lo_node = std::min(lo_node, h->conn[e * nen + n]);
+    bucket[e] = (int32_t)(lo_node / h->bucket_nodes);
+    ++count[bucket[e] + 1];
+  }
+  for (int64_t b = 0; b < nb; ++b) count[b + 1] += count[b];
+  h->bucket_end.assign(count.begin() + 1, count.end());
+  h->sweep_rows.resize(h->n_el);
+  std::vector<int64_t> pos(count.begin(), count.end() - 1);
+  for (int64_t i = 0; i < h->n_el; ++i) {
+    const int32_t e = h->sweep[i];
+    h->sweep_rows[pos[bucket[e]]++] = e;
+  }
 }
 
 int validate(gales_asm* h, const gales_mesh_desc* m, const gales_material_desc* mat,
@@ -713,6 +754,7 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   UP(h->d_slot, slot.data(), slot.size(), "slot");
   UP(h->d_colour_order, h->colour_order.data(), h->colour_order.size(), "colour_order");
   UP(h->d_sweep, h->sweep.data(), h->sweep.size(), "sweep");
+  UP(h->d_sweep_rows, h->sweep_rows.data(), h->sweep_rows.size(), "row-order sweep");
   UP(h->d_bd_list, h->bd_list.data(), h->bd_list.size(), "bd_list");
   UP(h->d_bd_sides, h->bd_sides.data(), h->bd_sides.size(), "bd_sides");
   UP(h->d_bpt_off, h->bpt_off.data(), h->bpt_off.size(), "bpt_off");
@@ -738,6 +780,10 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   if ((ce = cudaEventCreateWithFlags(&h->ev_bfork, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreateWithFlags(&h->ev_bjoin, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaStreamCreateWithFlags(&h->bst, cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
+  if ((ce = cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
+  for (int i = 0; i < kCopyEvents; ++i)
+    if ((ce = cudaEventCreateWithFlags(&h->ev_copy[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
+  if ((ce = cudaEventCreateWithFlags(&h->ev_cjoin, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   for (int i = 0; i < 2; ++i) {
     if ((ce = cudaEventCreateWithFlags(&h->ev_join[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
     // ist[0] runs the point stage, ist[1] the matrix stage
@@ -826,6 +872,7 @@ void gales_asm_destroy(gales_asm* h) {
   cudaSetDevice(h->device);
   h->d_coords.release(); h->d_conn.release(); h->d_node_flag.release();
   h->d_colour_order.release(); h->d_bd_list.release(); h->d_node_rp.release(); h->d_sweep.release();
+  h->d_sweep_rows.release();
   h->d_slot.release(); h->d_bd_sides.release(); h->d_side_bc.release();
   h->d_bpt_off.release(); h->d_bpt_el.release(); h->d_bpt_ip.release(); h->d_bgeo.release(); h->d_bpt_rec.release();
   h->d_status.release(); h->d_first_bad.release(); h->d_geo.release();
@@ -844,6 +891,10 @@ void gales_asm_destroy(gales_asm* h) {
   if (h->ev_bfork) cudaEventDestroy(h->ev_bfork);
   if (h->ev_bjoin) cudaEventDestroy(h->ev_bjoin);
   if (h->bst) cudaStreamDestroy(h->bst);
+  if (h->cst) cudaStreamDestroy(h->cst);
+  for (int i = 0; i < kCopyEvents; ++i)
+    if (h->ev_copy[i]) cudaEventDestroy(h->ev_copy[i]);
+  if (h->ev_cjoin) cudaEventDestroy(h->ev_cjoin);
   for (int i = 0; i < kRing; ++i) {
     h->qpbuf[i].release();
     if (h->ev_pt[i]) cudaEventDestroy(h->ev_pt[i]);
@@ -974,6 +1025,39 @@ KParams base_params(gales_asm* h, double dt) {
   return k;
 }
 
+// Device-to-host copy of the CSR values of a host-buffer call while the interior pass
+// runs: with the elements in row order (sweep_rows), the node rows [0, K) are final
+// once every element whose lowest node is below K has been assembled (an element adds
+// only into the rows of its own nodes), i.e. once the buckets of those nodes are done;
+// the boundary pass (another stream) must have finished too.  After a launch that
+// finishes a large enough prefix, an event on the assembly stream releases the copy of
+// the new rows on the copy stream.
+struct RowCopy {
+  double* host_vals;
+  const double* dev_vals;
+  int64_t copied_nodes = 0;   // node rows already sent
+  size_t bucket = 0;          // first unfinished bucket
+  int events = 0;             // copy events used
+};
+
+int copy_finished_rows(gales_asm* h, RowCopy& rc, int64_t elements_done, bool last, cudaStream_t st) {
+  while (rc.bucket < h->bucket_end.size() && h->bucket_end[rc.bucket] <= elements_done) ++rc.bucket;
+  const int64_t k = last ? h->n_nodes : std::min<int64_t>(h->n_nodes, (int64_t)rc.bucket * h->bucket_nodes);
+  const int64_t piece = std::max<int64_t>(1, h->n_nodes / (kCopyEvents - 2));
+  if (k <= rc.copied_nodes || (!last && k - rc.copied_nodes < piece)) return 0;
+  if (rc.events >= kCopyEvents) return 0;
+  cudaEvent_t ev = h->ev_copy[rc.events++];
+  CK(h, cudaEventRecord(ev, st), "event");
+  CK(h, cudaStreamWaitEvent(h->cst, ev, 0), "stream wait");
+  const int64_t nd2 = (int64_t)h->nd * h->nd;
+  const int64_t a = h->node_rp[rc.copied_nodes] * nd2, b = h->node_rp[k] * nd2;
+  CK(h, cudaMemcpyAsync(rc.host_vals + a, rc.dev_vals + a, (size_t)(b - a) * sizeof(double), cudaMemcpyDeviceToHost,
+                        h->cst),
+     "copy rows");
+  rc.copied_nodes = k;
+  return 0;
+}
+
 // Interior pass over n listed elements (k.el_list, or elements 0..n-1): point stage then
 // matrix stage per chunk.  Concurrent (atomic scatter): the point stage runs on ist[0]
 // and the matrix stage on ist[1], chunk c's matrix waiting on its
@@ -981,7 +1065,7 @@ KParams base_params(gales_asm* h, double dt) {
 // been consumed (ev_mx).  Otherwise (plain read-modify-write of coloured batches)
 // both stages run on the caller's stream.
 int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long long n, cudaStream_t st,
-                 bool concurrent) {
+                 bool concurrent, RowCopy* rc = nullptr) {
   const InteriorOps& ops = h->ops[form];
   const size_t rb = ops.rec_bytes(h->nc);
   if (rb == 0) return fail(h, GALES_ERR_UNSUPPORTED, "no interior kernel for this element/component count");
@@ -1001,6 +1085,10 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
       LaunchResult r = ops.interior(k, h->nc, want_m, pb, pf, pn, mb, c >= 1 ? mf : 0, mn, c >= 1, st);
       if (r.err != cudaSuccess) return cuda_fail(h, r.err, "interior kernel");
       h->launches += r.launches;
+      if (rc && c >= 1) {
+        const int e = copy_finished_rows(h, *rc, mf + mn, c == nchunks, st);
+        if (e) return e;
+      }
     }
     return 0;
   }
@@ -1167,7 +1255,7 @@ cudaError_t launch_norm2(const double* x, long long n, double* part, cudaStream_
 // With enqueue_only the call records no timing events and leaves the status word
 // alone (it accumulates until gales_asm_sync), so it may be captured into a graph.
 int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, int form, double* dvals,
-                 double* drhs, cudaStream_t st, bool enqueue_only = false) {
+                 double* drhs, cudaStream_t st, bool enqueue_only = false, RowCopy* rc = nullptr) {
   KParams k = base_params(h, dt);
   k.I = dI;
   k.P = dP;
@@ -1207,7 +1295,10 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
     LaunchResult r = dispatch_boundary(h, kb, form, kb.n_list, h->bst);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
     h->launches += r.launches;
+    CK(h, cudaEventRecord(h->ev_bjoin, h->bst), "event");
   }
+  // finished rows may be copied only once the boundary pass has added into them
+  if (rc && bd_concurrent) CK(h, cudaStreamWaitEvent(h->cst, h->ev_bjoin, 0), "stream wait");
   if (h->scatter_mode == GALES_SCATTER_COLOURED) {
     for (int c = 0; c < h->n_colours; ++c) {
       KParams kc = k;
@@ -1217,14 +1308,13 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
       if (rc) return rc;
     }
   } else {
-    k.el_list = h->d_sweep.p;
+    k.el_list = rc ? h->d_sweep_rows.p : h->d_sweep.p;
     k.n_list = h->n_el;
-    int rc = run_interior(h, k, form, want_m, h->n_el, st, true);
-    if (rc) return rc;
+    int e = run_interior(h, k, form, want_m, h->n_el, st, true, rc);
+    if (e) return e;
   }
   if (timed) CK(h, cudaEventRecord(h->evp[2], st), "event");
   if (bd_concurrent) {
-    CK(h, cudaEventRecord(h->ev_bjoin, h->bst), "event");
     CK(h, cudaStreamWaitEvent(st, h->ev_bjoin, 0), "stream wait");
   } else if (has_bd) {
     LaunchResult r = dispatch_boundary(h, kb, form, kb.n_list, st);
@@ -1286,9 +1376,29 @@ int assemble_impl(gales_asm* h, const double* I, const double* P, double dt, int
     CK(h, h->s_rhs.alloc(h->n_rows), "staging rhs");
     drhs = h->s_rhs.p;
   }
-  int rc = run_assembly(h, dI, dP, dt, form, dvals, drhs, st);
+  // host CSR values: copied row prefix by row prefix while the single-launch interior
+  // pass runs (mixed form, atomic scatter), else after the assembly
+  const bool pipelined =
+      hV && form == GALES_FORM_MIXED && h->scatter_mode == GALES_SCATTER_ATOMIC && is_pinned_host_ptr(vals);
+  RowCopy copy{vals, dvals};
+  int rc = run_assembly(h, dI, dP, dt, form, dvals, drhs, st, false, pipelined ? &copy : nullptr);
   if (rc) return rc;
-  if (hV) CK(h, cudaMemcpyAsync(vals, dvals, (size_t)h->nnz * sizeof(double), cudaMemcpyDeviceToHost, st), "copy vals");
+  if (pipelined) {
+    if (copy.copied_nodes < h->n_nodes) {  // rows not sent during the pass (for instance no chunk)
+      CK(h, cudaStreamWaitEvent(h->cst, h->ev_bjoin, 0), "stream wait");
+      copy.events = 0;
+      CK(h, cudaEventRecord(h->ev_copy[0], st), "event");
+      CK(h, cudaStreamWaitEvent(h->cst, h->ev_copy[0], 0), "stream wait");
+      const int64_t a = h->node_rp[copy.copied_nodes] * (int64_t)h->nd * h->nd;
+      CK(h, cudaMemcpyAsync(vals + a, dvals + a, (size_t)(h->nnz - a) * sizeof(double), cudaMemcpyDeviceToHost,
+                            h->cst),
+         "copy rows");
+    }
+    CK(h, cudaEventRecord(h->ev_cjoin, h->cst), "event");
+    CK(h, cudaStreamWaitEvent(st, h->ev_cjoin, 0), "stream wait");
+  } else if (hV) {
+    CK(h, cudaMemcpyAsync(vals, dvals, (size_t)h->nnz * sizeof(double), cudaMemcpyDeviceToHost, st), "copy vals");
+  }
   if (hR) CK(h, cudaMemcpyAsync(rhs, drhs, sb, cudaMemcpyDeviceToHost, st), "copy rhs");
   CK(h, cudaEventRecord(h->ev1, st), "event");
   rc = finish(h, st);
