@@ -1852,9 +1852,11 @@ extern "C" int gales_asm_assemble_noalloc(gales_asm* h, const double* I, const d
   const InteriorOps& ops = h->ops[form];
   const size_t rb = ops.rec_bytes(h->nc);
   if (rb == 0) return fail(h, GALES_ERR_UNSUPPORTED, "no interior kernel for this element/component count");
-  if (rb > GALES_NOALLOC_SCRATCH_BYTES)
+  // point records are written in blocks of a matrix CTA's elements (at most 4), so a
+  // chunk is a multiple of 4 elements and its blocks never pass the chunk's bytes
+  if (4 * rb > GALES_NOALLOC_SCRATCH_BYTES)
     return fail(h, GALES_ERR_UNSUPPORTED,
-                "one element's point records (" + std::to_string(rb) + " bytes) exceed the " +
+                "four elements' point records (" + std::to_string(4 * rb) + " bytes) exceed the " +
                     std::to_string((long long)GALES_NOALLOC_SCRATCH_BYTES) + "-byte no-allocation scratch");
   void* scratch = nullptr;
   int rc = noalloc_scratch(h, &scratch);
@@ -1875,7 +1877,7 @@ extern "C" int gales_asm_assemble_noalloc(gales_asm* h, const double* I, const d
   CK(h, cudaMemsetAsync(rhs, 0, (size_t)h->n_rows * sizeof(double), st), "memset rhs");
   // The point records of a chunk are written in full by the point kernel before the
   // matrix kernel reads them, so nothing in the scratch has to start at zero.
-  const long long chunk = (long long)(GALES_NOALLOC_SCRATCH_BYTES / rb);
+  const long long chunk = (long long)(GALES_NOALLOC_SCRATCH_BYTES / rb) / 4 * 4;
   for (long long first = 0; first < h->n_el; first += chunk) {
     const long long cnt = std::min(chunk, h->n_el - first);
     LaunchResult r = ops.point(k, h->nc, scratch, first, cnt, st);

@@ -193,8 +193,10 @@ int gales_asm_assemble(gales_asm* h, const double* I, const double* P, double dt
  * GALES_ERR_BAD_INPUT since staging them would allocate), the work runs on the
  * caller's stream only, and the per-point records live in one library-wide
  * device array of GALES_NOALLOC_SCRATCH_BYTES, which every GPU that loads the
- * library keeps until exit.  An element whose point records exceed that size is
- * rejected with GALES_ERR_UNSUPPORTED; larger meshes are processed in chunks.
+ * library keeps until exit.  Point records are laid out in blocks of up to four
+ * elements: when four elements' records exceed that size the call is rejected with
+ * GALES_ERR_UNSUPPORTED; larger meshes are processed in chunks of a multiple of four
+ * elements.
  * The first call on a device looks up the array's device address (once per
  * device); make that first call before any stream capture.  All calls, from every
  * handle, share the one array and it keeps the last call's contents: calls that

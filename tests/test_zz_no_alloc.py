@@ -35,6 +35,28 @@ def test_noalloc_matches_assemble_twice(kind, nc, form, cuda_lib, gm):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("form", [0, 1])
+def test_noalloc_many_scratch_chunks(form, cuda_lib, gm):
+    """A mesh far larger than one scratch chunk: the chunks (multiples of a matrix CTA's
+    elements) keep every block of point records inside the scratch."""
+    import torch
+    syn = cases.syn
+    mesh = syn.box_tet_delaunay(22, seed=3)
+    mat, setup = syn.material_for(3, 0), syn.setup_for(3, 3)
+    I, P = syn.state_for(mesh, 3, 0)
+    fa = gm.FluidAssembly(mesh, mat, setup)
+    Id, Pd = torch.from_numpy(I).cuda(), torch.from_numpy(P).cuda()
+    ref = fa.linear_system(device="cuda")
+    fa.execute(Id, Pd, 1e-3, ref, form=form)
+    lp = fa.linear_system(device="cuda")
+    fa.execute_noalloc(Id, Pd, 1e-3, lp, form=form)
+    torch.cuda.synchronize()
+    tol = 1e-12 if form == 0 else 1e-6
+    assert rel(lp.vals.cpu().numpy(), ref.vals.cpu().numpy()) <= tol
+    assert rel(lp.rhs.cpu().numpy(), ref.rhs.cpu().numpy()) <= tol
+
+
+@pytest.mark.gpu
 def test_noalloc_rejects_host_buffers(cuda_lib, gm):
     mesh, mat, setup, I, P, dt = cases.make("tri", 2)
     fa = gm.FluidAssembly(mesh, mat, setup)
