@@ -480,6 +480,42 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
         for (int i = 0; i < NEN; ++i) b += q.ds[d][i] * Ie[i][j];
         dI[d][j] = b;
       }
+  } else if constexpr (NEN == DIM + 1 && NQ >= 2 && NQ <= 32 && (32 % NQ) == 0) {
+    // A simplex's gradient is the same at its NQ points, whose lanes are consecutive in
+    // the warp: lane iq forms the columns j = iq, iq + NQ, ... of dI (its FP64 nodal
+    // differences picked from its registers) and the lanes of the element exchange
+    // them.  Same operations as the per-point form below.
+    constexpr int NSL = (ND + NQ - 1) / NQ;
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned int base = lane & ~(unsigned int)(NQ - 1);
+    const unsigned int gmask = NQ == 32 ? 0xffffffffu : (((1u << NQ) - 1u) << base);
+    float colv[NSL][DIM];
+#pragma unroll
+    for (int sl = 0; sl < NSL; ++sl) {
+      const int jj = iq + NQ * sl;
+      const int jc = jj < ND ? jj : ND - 1;
+      float c[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) c[d] = 0.f;
+#pragma unroll
+      for (int i = 1; i < NEN; ++i) {
+        double a = Ie[i][0], b0 = Ie[0][0];
+#pragma unroll
+        for (int j = 1; j < ND; ++j) {
+          a = (jc == j) ? Ie[i][j] : a;
+          b0 = (jc == j) ? Ie[0][j] : b0;
+        }
+        const float dif = narrow_rn(a - b0);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) c[d] = fmaf(narrow_rn(q.ds[d][i]), dif, c[d]);
+      }
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) colv[sl][d] = c[d];
+    }
+#pragma unroll
+    for (int j = 0; j < ND; ++j)
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) dI[d][j] = __shfl_sync(gmask, colv[j / NQ][d], (int)(base + j % NQ));
   } else {
 #pragma unroll
     for (int d = 0; d < DIM; ++d)
@@ -963,7 +999,20 @@ __device__ __forceinline__ S kd_entry(const C& c, const S* gb, S gbv, int l, int
 // Exact widening of binary32 to binary64 with 32-bit integer operations only (see
 // narrow_rn): exponent rebias 127 -> 1023, the 23-bit significand split over the two
 // words; subnormals normalised, infinities and NaN keep their payload.
+__device__ __forceinline__ double widen_special(float f);
 __device__ __forceinline__ double widen(float f) {
+  // normal numbers and zeros: the exponent field shifted into place and rebiased by
+  // (1023 - 127) << 20, the significand split over the two words
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int a = u & 0x7fffffffu;
+  if (a - 0x00800000u < 0x7f000000u || a == 0u) {
+    const unsigned int hi = (a == 0u ? 0u : (a >> 3) + 0x38000000u) | (u & 0x80000000u);
+    return __hiloint2double((int)hi, (int)(u << 29));
+  }
+  return widen_special(f);
+}
+// subnormals, infinities and NaN
+__device__ __forceinline__ double widen_special(float f) {
   const unsigned int u = __float_as_uint(f);
   const unsigned int sign = u & 0x80000000u;
   const unsigned int ex = (u >> 23) & 0xffu;

@@ -53,10 +53,11 @@ def _extract(path, signature):
 def conv(tmp_path_factory):
     narrow = _extract(CSRC / "gales_physics.cuh", "__device__ __forceinline__ float narrow_rn(double d)")
     widen = _extract(CSRC / "gales_kernels.cuh", "__device__ __forceinline__ double widen(float f)")
-    src = SHIM + narrow + "\n" + widen + r"""
+    special = _extract(CSRC / "gales_kernels.cuh", "__device__ __forceinline__ double widen_special(float f) {")
+    src = (SHIM + narrow + "\ninline double widen_special(float f);\n" + widen + "\n" + special + r"""
 extern "C" void narrow_many(const double* x, float* y, long n) { for (long i = 0; i < n; ++i) y[i] = narrow_rn(x[i]); }
 extern "C" void widen_many(const float* x, double* y, long n) { for (long i = 0; i < n; ++i) y[i] = widen(x[i]); }
-"""
+""")
     d = tmp_path_factory.mktemp("conv")
     (d / "conv.cpp").write_text(src)
     so = d / "conv.so"
