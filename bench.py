@@ -46,7 +46,7 @@ BYTES_PER_ELEM_TET = 4 * 4 + 8 * 3 * 4 + 2 * 8 * 4 * 7 + 16 * (4 * 7) ** 2 + 16 
 # dram__bytes_write.sum summed by ncu over every kernel of an assembly (interior
 # launches, zero fill, boundary) on the 163,618-tet mesh of the 30^3 lattice, whose CSR
 # bytes per element (1,002) match the 1.0M-tet mesh's (982); scaled by the element count.
-TRAFFIC_BYTES_PER_ELEM_TET = 6727
+TRAFFIC_BYTES_PER_ELEM_TET = 6877
 LATTICE_N = 54
 
 
