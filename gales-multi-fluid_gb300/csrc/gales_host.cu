@@ -144,13 +144,13 @@ void parallel_for(int64_t n, F f) {
   for (auto& x : th) x.join();
 }
 
-// Each point-record chunk buffer holds this many bytes; two of them stay resident
-// in L2 (about a quarter of the 129 MB) while the CSR values stream through it.
+// Scratch of the exact VJP: the theta and u_ref_inv cotangents.
 constexpr int kVjpAux = 3 * GALES_MAX_COMP + GALES_MAX_ND;
-// Chunks of the interior pipeline: one wave of the point kernel that leaves one CTA
-// slot per SM to the matrix stage running beside it on the other stream (with four
-// point CTAs resident per SM the chunk holds three per SM), so that the FP64-bound
-// point stage and the issue-bound matrix stage share every SM.
+// Chunks of the interior pass: one wave of the point stage that leaves one CTA slot per
+// SM to the matrix stage running beside it (with four point CTAs resident per SM the
+// chunk holds three per SM), so that the FP64-bound point stage and the issue-bound
+// matrix stage share every SM.  A chunk's point records (about 44 MB for tets) stay in
+// L2 until the matrix stage reads them.
 constexpr int kRing = 3;    // point-record buffers in flight between the two stages
 constexpr int kCopyEvents = 24;  // row copies per host-buffer assembly (at most)
 inline int point_ctas_per_chunk_sm(int occupancy) { return occupancy >= 3 ? occupancy - 1 : occupancy; }
@@ -249,7 +249,8 @@ struct gales_asm {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t evp[4] = {nullptr, nullptr, nullptr, nullptr};  // clear | interior | boundary | end
   int32_t scatter_mode = GALES_SCATTER_ATOMIC;
-  // interior pipeline: point-record chunk buffers (scratch) and two internal streams
+  // interior pass: point-record chunk buffers (scratch) and, for the FP64 form, two
+  // internal streams
   InteriorOps ops[2];
   DevBuf<unsigned char> qpbuf[kRing];
   long long chunk_elems[2] = {1, 1};   // elements per chunk, per form
@@ -1059,11 +1060,14 @@ int copy_finished_rows(gales_asm* h, RowCopy& rc, int64_t elements_done, bool la
 }
 
 // Interior pass over n listed elements (k.el_list, or elements 0..n-1): point stage then
-// matrix stage per chunk.  Concurrent (atomic scatter): the point stage runs on ist[0]
-// and the matrix stage on ist[1], chunk c's matrix waiting on its
+// matrix stage per chunk.  Mixed form with the atomic scatter: one interior_kernel
+// launch per chunk on the caller's stream (point stage of chunk c beside the matrix
+// stage of chunk c-1, programmatically dependent launches), with the optional
+// device-to-host copy of finished rows (rc).  FP64 form with the atomic scatter: the
+// point stage on ist[0] and the matrix stage on ist[1], chunk c's matrix waiting on its
 // records (ev_pt) and chunk c+kRing's point stage waiting until chunk c's buffer has
-// been consumed (ev_mx).  Otherwise (plain read-modify-write of coloured batches)
-// both stages run on the caller's stream.
+// been consumed (ev_mx).  Otherwise (plain read-modify-write of coloured batches, or
+// element-level output) both stages run on the caller's stream.
 int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long long n, cudaStream_t st,
                  bool concurrent, RowCopy* rc = nullptr) {
   const InteriorOps& ops = h->ops[form];
