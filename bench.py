@@ -166,6 +166,10 @@ def cpu_oracle_rate(mesh, mat, setup, I, P, dt, row_ptr, col, colour, n_colours,
 
 
 BYTES_PER_ELEM_HEX = 4 * 8 + 8 * 3 * 8 + 2 * 8 * 8 * 8 + 16 * (8 * 8) ** 2 + 16 * 8 * 8  # 67,808
+# DRAM bytes per element of one mixed hex assembly, summed by ncu over every kernel of
+# an assembly on the 64,000-hex mesh of a 40^3 grid (CSR bytes per element 14,172, 1.9%
+# above the 160x160x156 mesh's 13,911); scaled by the element count.
+TRAFFIC_BYTES_PER_ELEM_HEX = 64105
 
 
 def top_gas_flux_lambda(mesh, mat, I, nd):
@@ -290,7 +294,9 @@ def run_hex(args):
         "fp64": {"value": ne / (ms64 * 1e-3), "unit": "elements/s", "ms_per_step": ms64, "interior_kernel_ms": k64},
         "mixed_over_fp64": ms64 / ms_graph,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-                     "frac": ach / hbm if hbm else None, "traffic": None, "kernel": "interior_kernel (mixed form)",
+                     "frac": ach / hbm if hbm else None, "traffic": TRAFFIC_BYTES_PER_ELEM_HEX * ne,
+                     "traffic_source": "ncu DRAM bytes per element of a 64,000-hex assembly x elements",
+                     "kernel": "interior_kernel (mixed form)",
                      "kernel_ms": k_mx, "bytes_per_element": BYTES_PER_ELEM_HEX,
                      "peak_source": "measured (MEASURED_PEAKS.json)"},
         "objective_vjp": {"J": Jval, "ms": vjp_ms,
