@@ -337,6 +337,49 @@ def adaptive_dt_block(gm, fa, mesh, mat, setup, I, dt, torch, dev, with_cpu):
     return out
 
 
+def linear_solve_block(gm, fa, lp, torch, dev, tstream):
+    """The linear solve after the assembly (belos_linear_solver::execute with the shipped
+    setup.txt settings: flexible GMRES(200), 5 restarts, ILU(1), 1e-9) on the mixed-form
+    system the timed steps left in device memory: wall time of the call (factorisation
+    included), its factorisation alone and one preconditioner application."""
+    stream = tstream.cuda_stream
+    try:
+        t0 = time.perf_counter()
+        sol = fa.linear_solver()
+        create_s = time.perf_counter() - t0
+        x = torch.zeros(fa.n_rows, dtype=torch.float64, device=dev)
+        runs = []
+        for _ in range(2):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            sol.solve(lp.vals, lp.rhs, x, stream=stream)
+            runs.append(time.perf_counter() - t0)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        sol.factorize(lp.vals, stream=stream)
+        torch.cuda.synchronize(dev)
+        factor_ms = (time.perf_counter() - t0) * 1e3
+        v = torch.ones(fa.n_rows, dtype=torch.float64, device=dev)
+        z = torch.zeros_like(v)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sol.apply(v, z, stream=stream)
+        e0.record(tstream)
+        for _ in range(5):
+            sol.apply(v, z, stream=stream)
+        e1.record(tstream)
+        torch.cuda.synchronize(dev)
+        lf, lb = sol.levels()
+        ms = min(runs) * 1e3
+        return {"what": "FGMRES(200) + ILU(1), rel. residual 1e-9, x0 = 0, device CSR of the mixed assembly",
+                "rows": fa.n_rows, "ms": ms, "iterations": sol.num_it, "rel_res": sol.RRE,
+                "converged": sol.converged, "factor_ms": factor_ms,
+                "apply_ms": e0.elapsed_time(e1) / 5, "levels_fwd_bwd": [lf, lb],
+                "ms_per_iteration": (ms - factor_ms) / max(1, sol.num_it), "create_s": create_s}
+    except Exception as e:  # reported, never fatal to the assembly line
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def vjp_block(gm, syn, torch, dev, n=32):
     """Adjoint workload: ~200k tets, 3 components.  Exact and frozen VJP against the
     forward residual (FP64 and mixed), and the memory a stored-point design would need."""
@@ -406,6 +449,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-solve", action="store_true", help="skip the linear solve after the assembly")
     ap.add_argument("--lattice", type=int, default=LATTICE_N, help="lattice points per side (54 -> 1.0M tets)")
     ap.add_argument("--only", default="both", choices=["both", "mixed", "fp64"],
                     help="profiling aid: run only one form (no e2e, no CPU leg)")
@@ -530,6 +574,8 @@ def main():
         line["vjp"] = vjp_block(gm, syn, torch, dev)
     if rank == 0:
         line["adaptive_dt"] = adaptive_dt_block(gm, fa, mesh, mat, setup, I, dt, torch, dev, not args.no_cpu)
+    if rank == 0 and not args.no_solve:
+        line["linear_solve"] = linear_solve_block(gm, fa, lp, torch, dev, stream)
     if rank == 0 and not args.no_cpu:
         rate, cores, n = cpu_oracle_rate(mesh, mat, setup, I, P, dt, None, None, None, 0)
         line["cpu_baseline"] = {"value": rate, "unit": "elements/s", "cores": cores, "kind": "port",

@@ -499,14 +499,156 @@ class FluidAssembly:
         return self._L.gales_asm_launch_count(self._h)
 
 
+    def linear_solver(self, params: Optional["SolverParams"] = None) -> "LinearSolver":
+        """belos_linear_solver for this handle's systems, on the GPU."""
+        return LinearSolver(self, params)
+
+
+PRECOND_NONE, PRECOND_ILU = 0, 1
+
+
+@dataclass
+class SolverParams:
+    """The ls_* keys of setup.txt read by belos_linear_solver
+    (belos_linear_solver_factory.hpp:77-86); defaults are the shipped P0 case's."""
+    rel_res_tol: float = 1e-9
+    maxsubspace: int = 200
+    maxrestarts: int = 5
+    maxiters: int = -1
+    fill: int = 1
+    precond: int = PRECOND_ILU
+
+    def desc(self) -> abi.SolverParams:
+        return abi.SolverParams(float(self.rel_res_tol), int(self.maxsubspace), int(self.maxrestarts),
+                                int(self.maxiters), int(self.fill), int(self.precond))
+
+
+class LinearSolver:
+    """belos_linear_solver (belos_linear_solver_factory.hpp:69-274) on the GPU: flexible
+    GMRES with a right ILU(fill) preconditioner on the assembled CSR values, which may
+    stay in device memory.  solve() returns the execute() seconds and sets
+    num_it / ARE / RRE like the reference's accessors."""
+
+    def __init__(self, fa: "FluidAssembly", params: Optional[SolverParams] = None):
+        self.params = params or SolverParams()
+        self._L = fa._L
+        self._fa = fa  # keeps the assembly handle alive
+        h = C.c_void_p()
+        rc = self._L.gales_solver_create(fa._h, C.byref(self.params.desc()), C.byref(h))
+        if rc != 0:
+            raise GalesError(rc, "gales_solver_create failed")
+        self._h = h
+        self.nd, self.n_rows = fa.nd, fa.n_rows
+        self.result = abi.SolverResult()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gales_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise GalesError(rc, self._L.gales_solver_last_error(self._h).decode())
+
+    def solve(self, vals, rhs, x, stream: int = 0) -> float:
+        """execute(): A x = rhs for the CSR values vals (host or device buffers)."""
+        self._check(self._L.gales_solver_solve(self._h, _addr(vals), _addr(rhs), _addr(x), C.byref(self.result),
+                                               stream or None))
+        return self.result.seconds
+
+    @property
+    def num_it(self) -> int:
+        return int(self.result.iterations)
+
+    @property
+    def ARE(self) -> float:
+        return float(self.result.abs_res)
+
+    @property
+    def RRE(self) -> float:
+        return float(self.result.rel_res)
+
+    @property
+    def converged(self) -> bool:
+        return bool(self.result.converged)
+
+    def factorize(self, vals, stream: int = 0):
+        self._check(self._L.gales_solver_factorize(self._h, _addr(vals), stream or None))
+
+    def apply(self, v, z, stream: int = 0):
+        """z = M^-1 v with the current factor (device buffers)."""
+        self._check(self._L.gales_solver_apply(self._h, _addr(v), _addr(z), stream or None))
+
+    def factor(self):
+        """The factor as node blocks: (row_ptr, col, blocks[nnz_blocks, nd, nd])."""
+        nb, nnz = C.c_int64(), C.c_int64()
+        rp, cl = C.POINTER(C.c_int64)(), C.POINTER(C.c_int32)()
+        self._check(self._L.gales_solver_factor(self._h, C.byref(nb), C.byref(nnz), C.byref(rp), C.byref(cl), None))
+        vals = np.zeros((nnz.value, self.nd, self.nd))
+        self._check(self._L.gales_solver_factor(self._h, None, None, None, None, _addr(vals)))
+        return (np.ctypeslib.as_array(rp, shape=(nb.value + 1,)).copy(),
+                np.ctypeslib.as_array(cl, shape=(nnz.value,)).copy(), vals)
+
+    def levels(self):
+        f, b = C.c_int32(), C.c_int32()
+        self._check(self._L.gales_solver_levels(self._h, C.byref(f), C.byref(b)))
+        return f.value, b.value
+
+    def correct(self, I, dx, trim=(-1, -1), lo: float = 0.0, hi: float = 1.0, stream: int = 0):
+        """fluid_updater::corrector + model::dof_trimmer on the device: I += dx, then the
+        dofs with index in [trim[0], trim[1]) clamped into [lo, hi]."""
+        self._check(self._L.gales_solver_correct(self._h, _addr(I), _addr(dx), int(trim[0]), int(trim[1]),
+                                                 float(lo), float(hi), stream or None))
+
+    def launch_count(self) -> int:
+        return self._L.gales_solver_launches(self._h)
+
+
+def iluk_pattern(row_ptr, col, fill: int = 1):
+    """Host-side node-level ILU(fill) pattern (no GPU): (f_row_ptr, f_col, level_fwd,
+    level_bwd, (n_levels_fwd, n_levels_bwd))."""
+    L = abi.lib()
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    n = len(row_ptr) - 1
+    nnz = C.c_int64()
+    i64p, i32p = C.POINTER(C.c_int64), C.POINTER(C.c_int32)
+    rc = L.gales_iluk_pattern(n, row_ptr.ctypes.data_as(i64p), col.ctypes.data_as(i32p), int(fill), C.byref(nnz),
+                              None, None, None, None, None)
+    if rc:
+        raise GalesError(rc, "gales_iluk_pattern failed")
+    f_rp = np.zeros(n + 1, dtype=np.int64)
+    f_col = np.zeros(nnz.value, dtype=np.int32)
+    lf = np.zeros(n, dtype=np.int32)
+    lb = np.zeros(n, dtype=np.int32)
+    nl = np.zeros(2, dtype=np.int32)
+    rc = L.gales_iluk_pattern(n, row_ptr.ctypes.data_as(i64p), col.ctypes.data_as(i32p), int(fill), C.byref(nnz),
+                              f_rp.ctypes.data_as(i64p), f_col.ctypes.data_as(i32p), lf.ctypes.data_as(i32p),
+                              lb.ctypes.data_as(i32p), nl.ctypes.data_as(i32p))
+    if rc:
+        raise GalesError(rc, "gales_iluk_pattern failed")
+    return f_rp, f_col, lf, lb, (int(nl[0]), int(nl[1]))
+
+
 class ResidualCheck:
     """residual_check (residual_check.hpp:42-80): ||b||_2 against iteration 0."""
 
     def __init__(self):
         self.res0 = 0.0
 
-    def execute(self, b, it_count: int):
-        n = float(np.linalg.norm(np.asarray(b if isinstance(b, np.ndarray) else b.detach().cpu().numpy())))
+    def execute(self, b, it_count: int, norm: Optional[float] = None):
+        """b is the rhs (host array) or None with norm = ||b||_2 computed elsewhere
+        (FluidAssembly.norm2 on the device)."""
+        if norm is not None:
+            n = float(norm)
+        else:
+            n = float(np.linalg.norm(np.asarray(b if isinstance(b, np.ndarray) else b.detach().cpu().numpy())))
         if it_count == 0:
             self.res0 = n
             return False, n

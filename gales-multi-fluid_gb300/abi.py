@@ -85,6 +85,18 @@ class SetupDesc(C.Structure):
     ]
 
 
+class SolverParams(C.Structure):
+    """gales_solver_params (include/gales_asm.h)."""
+    _fields_ = [("rel_res_tol", C.c_double), ("maxsubspace", C.c_int32), ("maxrestarts", C.c_int32),
+                ("maxiters", C.c_int64), ("fill", C.c_int32), ("precond", C.c_int32)]
+
+
+class SolverResult(C.Structure):
+    """gales_solver_result (include/gales_asm.h)."""
+    _fields_ = [("iterations", C.c_int64), ("abs_res", C.c_double), ("rel_res", C.c_double),
+                ("seconds", C.c_double), ("converged", C.c_int32), ("cycles", C.c_int32)]
+
+
 _lib = None
 
 
@@ -157,6 +169,32 @@ def lib() -> C.CDLL:
     L.gales_mesh_file_desc.restype = C.c_int
     L.gales_mesh_file_free.argtypes = [vp]
     L.gales_mesh_file_free.restype = None
+    sp_ = _p(SolverParams)
+    L.gales_solver_default.argtypes = [sp_]
+    L.gales_solver_default.restype = None
+    L.gales_solver_create.argtypes = [vp, sp_, _p(vp)]
+    L.gales_solver_create.restype = C.c_int
+    L.gales_solver_solve.argtypes = [vp, vp, vp, vp, _p(SolverResult), vp]
+    L.gales_solver_solve.restype = C.c_int
+    L.gales_solver_factorize.argtypes = [vp, vp, vp]
+    L.gales_solver_factorize.restype = C.c_int
+    L.gales_solver_apply.argtypes = [vp, vp, vp, vp]
+    L.gales_solver_apply.restype = C.c_int
+    L.gales_solver_factor.argtypes = [vp, _p(i64), _p(i64), _p(_p(C.c_int64)), _p(_p(C.c_int32)), vp]
+    L.gales_solver_factor.restype = C.c_int
+    L.gales_solver_levels.argtypes = [vp, _p(i32), _p(i32)]
+    L.gales_solver_levels.restype = C.c_int
+    L.gales_solver_correct.argtypes = [vp, vp, vp, i32, i32, C.c_double, C.c_double, vp]
+    L.gales_solver_correct.restype = C.c_int
+    L.gales_solver_launches.argtypes = [vp]
+    L.gales_solver_launches.restype = C.c_int64
+    L.gales_solver_last_error.argtypes = [vp]
+    L.gales_solver_last_error.restype = C.c_char_p
+    L.gales_solver_destroy.argtypes = [vp]
+    L.gales_solver_destroy.restype = None
+    L.gales_iluk_pattern.argtypes = [i64, _p(C.c_int64), _p(C.c_int32), i32, _p(i64), _p(C.c_int64),
+                                     _p(C.c_int32), _p(C.c_int32), _p(C.c_int32), _p(C.c_int32)]
+    L.gales_iluk_pattern.restype = C.c_int
     _lib = L
     return L
 
@@ -170,4 +208,7 @@ EXPORTED = [
     "gales_asm_last_ms", "gales_asm_last_phase_ms", "gales_asm_launch_count",
     "gales_mesh_read", "gales_mesh_file_desc", "gales_mesh_file_free", "gales_asm_adaptive_dt", "gales_dt_update",
     "gales_asm_secondary_dofs", "gales_pressure_profile", "gales_pressure_interpolate",
+    "gales_solver_default", "gales_solver_create", "gales_solver_solve", "gales_solver_factorize",
+    "gales_solver_apply", "gales_solver_factor", "gales_solver_levels", "gales_solver_correct",
+    "gales_solver_launches", "gales_solver_last_error", "gales_solver_destroy", "gales_iluk_pattern",
 ]

@@ -7,9 +7,11 @@ b (fluid_assembly::execute), checks ||b|| against iteration 0
 A dI = b and corrects I += dI (fluid_updater.hpp:23-26), then clamps the mass
 fractions into [0, 1] (model.hpp:176-184, dof_trimmer).
 
-The assembly runs on the GPU through the library; the linear solve stands in for
-the reference's Belos GMRES with restarted GMRES on the assembled CSR matrix,
-preconditioned by an incomplete LU factorisation (scipy, on the host).
+time_step runs the assembly on the GPU and a host linear solve (scipy GMRES with an
+incomplete LU); time_step_device keeps the whole loop on the GPU: the assembly, the
+residual norm, the library's flexible GMRES with ILU(k) on the device CSR values (the
+reference's Belos/Ifpack solve) and the corrector with the dof trimmer, so that only
+scalars cross to the host.
 
 The tangent and the residual may come from different forms.  Newton tolerates an
 approximate tangent but not an approximate residual: with the mixed form's FP32
@@ -63,3 +65,43 @@ def time_step(fa, I_prev: np.ndarray, dt: float, form: int, max_it: int = 20, tr
             S = I.reshape(-1, nd)
             np.clip(S[:, dim + 2:], 0.0, 1.0, out=S[:, dim + 2:])
     return {"converged": False, "iterations": max_it, "history": history, "state": I}
+
+
+def time_step_device(fa, solver, I_prev, dt: float, form: int, max_it: int = 3, trim=None, residual_form=None,
+                     lp=None) -> dict:
+    """One time step of main.cpp:216-245 on the GPU from the converged device state
+    I_prev (a float64 cuda tensor): predictor P = I; per iteration the assembly, the
+    residual check on ||b|| (FluidAssembly.norm2), the solve (LinearSolver) and the
+    corrector I += dx followed by dof_trimmer on the dof range `trim` (default: dof
+    dim + 2, the first mass fraction, to [0, 1], as main.cpp:235 trims dof 4 of the 2D
+    cases).  max_it is setup.txt's n_max_it.  Returns the iteration at which the check
+    passed, the relative residuals, the solver's iteration counts and the state."""
+    import importlib
+    import torch
+    gm = importlib.import_module("gales-multi-fluid_gb300")
+    dev = I_prev.device
+    P = I_prev.clone()
+    I = P.clone()
+    if lp is None:
+        lp = fa.device_system(dev)
+    x = torch.zeros(fa.n_rows, dtype=torch.float64, device=dev)
+    rhs = torch.zeros_like(x) if residual_form is not None and residual_form != form else None
+    if trim is None:
+        trim = (fa.dim + 2, fa.dim + 3) if fa.nb_comp > 1 else (-1, -1)
+    check = gm.ResidualCheck()
+    history, lin_its = [], []
+    for it in range(max_it):
+        fa.execute(I, P, dt, lp, form=form)
+        if rhs is not None:
+            fa.residual(I, P, dt, rhs, form=residual_form)
+            lp.rhs.copy_(rhs)
+        converged, res = check.execute(None, it, norm=fa.norm2(lp.rhs))
+        history.append(1.0 if it == 0 else res)
+        if converged:
+            return {"converged": True, "iterations": it, "history": history, "linear_iterations": lin_its,
+                    "state": I}
+        solver.solve(lp.vals, lp.rhs, x)
+        lin_its.append(solver.num_it)
+        solver.correct(I, x, trim)
+    return {"converged": False, "iterations": max_it, "history": history, "linear_iterations": lin_its,
+            "state": I}

@@ -274,6 +274,74 @@ int gales_pressure_profile(const gales_material_desc* mat, double p0, double h, 
 int gales_pressure_interpolate(const double* y_col, const double* p_col, int32_t n_col, const double* y, int64_t n,
                                double* p_out);
 
+/* Linear solve of the assembled system on the GPU, replacing belos_linear_solver
+ * (src/fem/ls/belos_linear_solver_factory.hpp:69-274) as main.cpp:216-245 drives it:
+ * flexible GMRES with a right ILU(fill) preconditioner (Belos "Flexible GMRES", Ifpack
+ * "ILU", setup.txt ls_* keys), x0 = 0, converged when ||b - A x|| <= rel_res_tol ||b||.
+ * The factor is the scalar ILU(fill) of the assembled CSR matrix, stored as node blocks
+ * (the pattern's dense nd x nd blocks make the two identical).  One solver per assembly
+ * handle; it reads the handle's node graph at creation. */
+#define GALES_PRECOND_NONE 0
+#define GALES_PRECOND_ILU 1
+
+typedef struct gales_solver_params {
+  double rel_res_tol;    /* ls_rel_res_tol (belos_linear_solver_factory.hpp:77) */
+  int32_t maxsubspace;   /* ls_maxsubspace: Krylov vectors per cycle ("Num Blocks") */
+  int32_t maxrestarts;   /* ls_maxrestarts */
+  int64_t maxiters;      /* ls_maxiters; -1: rows - 1 (belos_linear_solver_factory.hpp:128) */
+  int32_t fill;          /* ls_fill: ILU level of fill */
+  int32_t precond;       /* GALES_PRECOND_ILU (ls_precond ILU) or GALES_PRECOND_NONE */
+} gales_solver_params;
+
+typedef struct gales_solver_result {
+  int64_t iterations;    /* num_it(): Arnoldi steps over all cycles */
+  double abs_res;        /* ARE(): ||b - A x|| */
+  double rel_res;        /* RRE(): ||b - A x|| / ||b|| */
+  double seconds;        /* wall time of the call (execute()'s return value) */
+  int32_t converged;
+  int32_t cycles;        /* GMRES cycles (1 + restarts) */
+} gales_solver_result;
+
+typedef struct gales_solver gales_solver;
+
+/* The shipped settings (sim/fluid_mc/P0/setup.txt:10-16): 1e-9, 200, 5, -1, fill 1, ILU. */
+void gales_solver_default(gales_solver_params* p);
+/* Symbolic factorisation and level sets on the device's current context; p may be NULL
+ * (defaults).  Allocates the factor and (maxsubspace + 1) + maxsubspace Krylov vectors. */
+int gales_solver_create(gales_asm* h, const gales_solver_params* p, gales_solver** out);
+/* execute(): factorises vals (the handle's CSR values), then solves A x = rhs.  vals,
+ * rhs and x are host or device arrays; the call synchronises its stream.  res may be
+ * NULL.  GALES_ERR_SINGULAR for a zero pivot in the factorisation. */
+int gales_solver_solve(gales_solver* s, const double* vals, const double* rhs, double* x, gales_solver_result* res,
+                       void* stream);
+/* The factorisation alone (synchronises), and z = M^-1 v with the current factor
+ * (device arrays, enqueued on the stream). */
+int gales_solver_factorize(gales_solver* s, const double* vals, void* stream);
+int gales_solver_apply(gales_solver* s, const double* v, double* z, void* stream);
+/* The factor as node blocks: the block pattern (host arrays owned by the solver) and,
+ * when vals is not NULL, nnz_blocks * nd * nd values (block-major, row-major blocks;
+ * unit L strictly below the diagonal, U on and above it).  Synchronises the device. */
+int gales_solver_factor(gales_solver* s, int64_t* n_block_rows, int64_t* nnz_blocks, const int64_t** row_ptr,
+                        const int32_t** col, double* vals);
+/* Number of levels of the forward and backward substitutions (launches per sweep). */
+int gales_solver_levels(gales_solver* s, int32_t* n_levels_fwd, int32_t* n_levels_bwd);
+/* fluid_updater::corrector and model::dof_trimmer (fluid_updater.hpp:23-26,
+ * model.hpp:176-184): I += dx on the device, then every node's dofs with index in
+ * [trim_first, trim_last) clamped to max(lo, min(v, hi)) (main.cpp:235 trims dof 4 to
+ * [0, 1]).  Device arrays, enqueued on the stream. */
+int gales_solver_correct(gales_solver* s, double* I, const double* dx, int32_t trim_first, int32_t trim_last,
+                         double lo, double hi, void* stream);
+int64_t gales_solver_launches(gales_solver* s);
+const char* gales_solver_last_error(gales_solver* s);
+void gales_solver_destroy(gales_solver* s);
+/* Host-only: the node-level ILU(fill) pattern (sorted columns, diagonal included) of a
+ * graph with sorted columns, and each row's forward / backward substitution level.
+ * With f_row_ptr NULL only *nnz is set.  n_levels (may be NULL) receives the two level
+ * counts.  No GPU use. */
+int gales_iluk_pattern(int64_t n, const int64_t* row_ptr, const int32_t* col, int32_t fill, int64_t* nnz,
+                       int64_t* f_row_ptr, int32_t* f_col, int32_t* level_fwd, int32_t* level_bwd,
+                       int32_t* n_levels);
+
 /* Status of the last call: error bits and the first offending element (-1 if none). */
 int gales_asm_status(gales_asm* h, int64_t* first_bad_element);
 const char* gales_asm_last_error(gales_asm* h);

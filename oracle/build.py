@@ -1,4 +1,5 @@
-"""Build recipe of the CPU oracle (test infrastructure; see gales_oracle.cpp).
+"""Build recipe of the CPU oracle (test infrastructure; see gales_oracle.cpp and
+solver_oracle.cpp).
 
 Compiled without floating-point contraction so that x86_64 and aarch64 hosts
 give bit-identical results.  Output: oracle/_build/libgales_oracle.so.
@@ -11,18 +12,18 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-SRC = HERE / "gales_oracle.cpp"
+SRCS = [HERE / "gales_oracle.cpp", HERE / "solver_oracle.cpp"]
 OUT = HERE / "_build" / "libgales_oracle.so"
 
 
 def build(verbose: bool = False) -> Path:
     OUT.parent.mkdir(exist_ok=True)
     hdr = HERE.parent / "include" / "gales_asm.h"
-    if OUT.exists() and OUT.stat().st_mtime > max(SRC.stat().st_mtime, hdr.stat().st_mtime):
+    if OUT.exists() and OUT.stat().st_mtime > max([s.stat().st_mtime for s in SRCS] + [hdr.stat().st_mtime]):
         return OUT
     cxx = shutil.which("g++") or "g++"
     cmd = [cxx, "-std=c++17", "-O3", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-           "-o", str(OUT), str(SRC)]
+           "-o", str(OUT), *[str(s) for s in SRCS]]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if verbose or r.returncode != 0:
         sys.stderr.write(r.stdout + r.stderr)

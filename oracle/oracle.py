@@ -49,6 +49,11 @@ def lib() -> C.CDLL:
                                    dp, dp, C.c_double, i64p, i32p, dp, dp, C.c_int, i32p, C.c_int32, i64p]
         L.gor_adaptive_dt.argtypes = [C.POINTER(abi.MeshDesc), C.POINTER(abi.MaterialDesc),
                                       C.POINTER(abi.SetupDesc), dp, C.c_double, C.c_double, dp]
+        L.gor_iluk.argtypes = [C.c_int64, i64p, i32p, dp, C.c_int32, i64p, i64p, i32p, dp]
+        L.gor_iluk.restype = C.c_int64
+        L.gor_fgmres.argtypes = [C.c_int64, i64p, i32p, dp, dp, C.c_int32, C.c_int32, C.c_double, C.c_int32,
+                                 C.c_int32, C.c_int64, dp, dp]
+        L.gor_fgmres.restype = C.c_int64
         for f in ("gor_properties", "gor_inverse", "gor_quad", "gor_gauss", "gor_pattern", "gor_colouring",
                   "gor_element", "gor_assemble", "gor_adaptive_dt"):
             getattr(L, f).restype = C.c_int
@@ -184,6 +189,39 @@ def set_dt(dt_el_min, dt, dt_min, dt_max):
     d = 1.01 * dt if dt_el_min > 1.01 * dt else dt_el_min
     return max(min(d, dt_max), dt_min)
 
+
+def iluk(row_ptr, col, vals, fill=1):
+    """Ifpack ILU(fill) of a CSR matrix (solver_oracle.cpp): (f_rp, f_col, f_val, bad_row)."""
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    n = len(row_ptr) - 1
+    nnz = C.c_int64()
+    lib().gor_iluk(n, _i64(row_ptr), _i32(col), _d(vals), int(fill), C.byref(nnz), None, None, None)
+    f_rp = np.zeros(n + 1, dtype=np.int64)
+    f_col = np.zeros(nnz.value, dtype=np.int32)
+    f_val = np.zeros(nnz.value)
+    bad = lib().gor_iluk(n, _i64(row_ptr), _i32(col), _d(vals), int(fill), C.byref(nnz), _i64(f_rp), _i32(f_col),
+                         _d(f_val))
+    return f_rp, f_col, f_val, int(bad) - 1
+
+
+def fgmres(row_ptr, col, vals, b, tol=1e-9, maxsubspace=200, maxrestarts=5, maxiters=-1, fill=1, precond=True):
+    """belos_linear_solver::execute with Flexible GMRES and ILU (solver_oracle.cpp).
+    Returns (x, dict(iterations, abs_res, rel_res, converged, cycles))."""
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = len(row_ptr) - 1
+    x = np.zeros(n)
+    out = np.zeros(5)
+    bad = lib().gor_fgmres(n, _i64(row_ptr), _i32(col), _d(vals), _d(b), int(fill), int(bool(precond)), float(tol),
+                           int(maxsubspace), int(maxrestarts), int(maxiters), _d(x), _d(out))
+    if bad:
+        raise ZeroDivisionError(f"zero pivot in row {bad - 1}")
+    return x, dict(iterations=int(out[0]), abs_res=float(out[1]), rel_res=float(out[2]), converged=bool(out[3]),
+                   cycles=int(out[4]))
 
 
 def pressure_profile(material, p0, h, T, T1, Y, Y1):
