@@ -504,7 +504,7 @@ class FluidAssembly:
         return LinearSolver(self, params)
 
 
-PRECOND_NONE, PRECOND_ILU = 0, 1
+PRECOND_NONE, PRECOND_ILU, PRECOND_ILU_FP32 = 0, 1, 2
 
 
 @dataclass

@@ -187,9 +187,9 @@ __device__ __forceinline__ int64_t find_col(const int32_t* __restrict__ c, int64
 
 // Scatter the assembled values into the factor blocks (fill blocks stay zero): warp per
 // node row, lanes over the row's nd x deg*nd values.
-template <int ND>
+template <int ND, typename T>
 __global__ void matrix_to_factor_kernel(const double* __restrict__ vals, const int64_t* __restrict__ node_rp,
-                                        const int64_t* __restrict__ a2f, int64_t n_nodes, double* __restrict__ F) {
+                                        const int64_t* __restrict__ a2f, int64_t n_nodes, T* __restrict__ F) {
   const int64_t i = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (i >= n_nodes) return;
   const int lane = threadIdx.x & 31;
@@ -199,7 +199,7 @@ __global__ void matrix_to_factor_kernel(const double* __restrict__ vals, const i
     for (int64_t e = lane; e < len; e += 32) {
       const int64_t t = t0 + e / ND;
       const int kk = (int)(e % ND);
-      F[a2f[t] * (ND * ND) + k * ND + kk] = vals[base + k * len + e];
+      F[a2f[t] * (ND * ND) + k * ND + kk] = (T)vals[base + k * len + e];
     }
   }
 }
@@ -209,8 +209,8 @@ __global__ void matrix_to_factor_kernel(const double* __restrict__ vals, const i
 // r), then A_IJ -= L_IK U_KJ for the upper blocks J of row K present in row I (lanes
 // over (J, r)).  Then the row-wise Doolittle step of the diagonal block, applied across
 // the whole block row.  Every entry sees the subtractions of the scalar ikj order.
-template <int ND>
-__global__ void ilu_factor_level_kernel(double* __restrict__ F, const int64_t* __restrict__ f_rp,
+template <int ND, typename T>
+__global__ void ilu_factor_level_kernel(T* __restrict__ F, const int64_t* __restrict__ f_rp,
                                         const int32_t* __restrict__ f_col, const int64_t* __restrict__ f_diag,
                                         const int32_t* __restrict__ rows, int64_t count,
                                         unsigned int* __restrict__ status) {
@@ -223,15 +223,15 @@ __global__ void ilu_factor_level_kernel(double* __restrict__ F, const int64_t* _
   for (int64_t p = p0; p < pd; ++p) {
     const int32_t K = f_col[p];
     const int64_t dK = f_diag[K], pK1 = f_rp[K + 1];
-    double* B = F + p * BB;
-    const double* UK = F + dK * BB;
+    T* B = F + p * BB;
+    const T* UK = F + dK * BB;
     if (lane < ND) {
-      double row[ND];
+      T row[ND];
 #pragma unroll
       for (int c = 0; c < ND; ++c) row[c] = B[lane * ND + c];
 #pragma unroll
       for (int c = 0; c < ND; ++c) {
-        double s = row[c];
+        T s = row[c];
 #pragma unroll
         for (int c2 = 0; c2 < c; ++c2) s -= row[c2] * UK[c2 * ND + c];
         row[c] = s / UK[c * ND + c];
@@ -246,55 +246,55 @@ __global__ void ilu_factor_level_kernel(double* __restrict__ F, const int64_t* _
       const int r = (int)(it % ND);
       const int64_t pos = find_col(f_col, p + 1, p1, f_col[q]);
       if (pos < 0) continue;
-      double l[ND];
+      T l[ND];
 #pragma unroll
       for (int m = 0; m < ND; ++m) l[m] = B[r * ND + m];
-      const double* U = F + q * BB;
-      double* T = F + pos * BB + r * ND;
+      const T* U = F + q * BB;
+      T* tgt = F + pos * BB + r * ND;
 #pragma unroll
       for (int c = 0; c < ND; ++c) {
-        double s = T[c];
+        T s = tgt[c];
 #pragma unroll
         for (int m = 0; m < ND; ++m) s -= l[m] * U[m * ND + c];
-        T[c] = s;
+        tgt[c] = s;
       }
     }
     __syncwarp();
   }
   // Diagonal block and the upper blocks: rows r in order, pivots c2 < r in order.
-  double* D = F + pd * BB;
+  T* D = F + pd * BB;
   const int64_t ncols = (p1 - pd) * ND;  // columns of the block row from the diagonal block on
   for (int r = 1; r < ND; ++r) {
     for (int c2 = 0; c2 < r; ++c2) {
-      const double l = D[r * ND + c2] / D[c2 * ND + c2];
+      const T l = D[r * ND + c2] / D[c2 * ND + c2];
       __syncwarp();
       if (lane == 0) D[r * ND + c2] = l;
       for (int64_t e = lane; e < ncols; e += 32) {
         const int64_t b = e / ND;
         const int c = (int)(e % ND);
         if (b == 0 && c <= c2) continue;
-        double* Rb = F + (pd + b) * BB;
+        T* Rb = F + (pd + b) * BB;
         Rb[r * ND + c] -= l * Rb[c2 * ND + c];
       }
       __syncwarp();
     }
   }
-  if (lane < ND && D[lane * ND + lane] == 0.0) atomicOr(status, (unsigned)GALES_ERR_SINGULAR);
+  if (lane < ND && D[lane * ND + lane] == T(0)) atomicOr(status, (unsigned)GALES_ERR_SINGULAR);
 }
 
 // The same factorisation step with the block row I and, for each lower block K, row
 // K's diagonal and upper blocks staged in shared memory (one warp per CTA): the row's
 // column search, its updates and the diagonal step then run on shared memory, and each
 // K costs one coalesced copy.  Same operations in the same order as above.
-template <int ND>
-__global__ void ilu_factor_level_smem_kernel(double* __restrict__ F, const int64_t* __restrict__ f_rp,
+template <int ND, typename T>
+__global__ void ilu_factor_level_smem_kernel(T* __restrict__ F, const int64_t* __restrict__ f_rp,
                                              const int32_t* __restrict__ f_col, const int64_t* __restrict__ f_diag,
                                              const int32_t* __restrict__ rows, int64_t count,
                                              unsigned int* __restrict__ status, int max_row, int max_u) {
   constexpr int BB = ND * ND;
-  extern __shared__ double sm[];
-  double* R = sm;                                  // [max_row][BB] the block row
-  double* UK = R + (size_t)max_row * BB;           // [1 + max_u][BB] row K from its diagonal on
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T* R = reinterpret_cast<T*>(sm_raw);             // [max_row][BB] the block row
+  T* UK = R + (size_t)max_row * BB;                // [1 + max_u][BB] row K from its diagonal on
   int32_t* RC = (int32_t*)(UK + (size_t)(1 + max_u) * BB);  // [max_row] the row's columns
   int32_t* UC = RC + max_row;                      // [max_u] row K's upper columns
   const int64_t w = blockIdx.x;
@@ -313,14 +313,14 @@ __global__ void ilu_factor_level_smem_kernel(double* __restrict__ F, const int64
     for (int64_t e = lane; e < (int64_t)(nu + 1) * BB; e += 32) UK[e] = F[dK * BB + e];
     for (int e = lane; e < nu; e += 32) UC[e] = f_col[dK + 1 + e];
     __syncwarp();
-    double* B = R + (size_t)b * BB;
+    T* B = R + (size_t)b * BB;
     if (lane < ND) {
-      double row[ND];
+      T row[ND];
 #pragma unroll
       for (int c = 0; c < ND; ++c) row[c] = B[lane * ND + c];
 #pragma unroll
       for (int c = 0; c < ND; ++c) {
-        double s = row[c];
+        T s = row[c];
 #pragma unroll
         for (int c2 = 0; c2 < c; ++c2) s -= row[c2] * UK[c2 * ND + c];
         row[c] = s / UK[c * ND + c];
@@ -334,40 +334,40 @@ __global__ void ilu_factor_level_smem_kernel(double* __restrict__ F, const int64
       const int qi = it / ND, r = it - qi * ND;
       const int64_t pos = find_col(RC, b + 1, nb, UC[qi]);
       if (pos < 0) continue;
-      double l[ND];
+      T l[ND];
 #pragma unroll
       for (int m = 0; m < ND; ++m) l[m] = B[r * ND + m];
-      const double* U = UK + (size_t)(1 + qi) * BB;
-      double* T = R + pos * BB + r * ND;
+      const T* U = UK + (size_t)(1 + qi) * BB;
+      T* tgt = R + pos * BB + r * ND;
 #pragma unroll
       for (int c = 0; c < ND; ++c) {
-        double s = T[c];
+        T s = tgt[c];
 #pragma unroll
         for (int m = 0; m < ND; ++m) s -= l[m] * U[m * ND + c];
-        T[c] = s;
+        tgt[c] = s;
       }
     }
     __syncwarp();
   }
-  double* D = R + (size_t)bd * BB;
+  T* D = R + (size_t)bd * BB;
   const int ncols = (nb - bd) * ND;
   for (int r = 1; r < ND; ++r) {
     for (int c2 = 0; c2 < r; ++c2) {
-      const double l = D[r * ND + c2] / D[c2 * ND + c2];
+      const T l = D[r * ND + c2] / D[c2 * ND + c2];
       __syncwarp();
       if (lane == 0) D[r * ND + c2] = l;
       for (int e = lane; e < ncols; e += 32) {
         const int bb = e / ND;
         const int c = e - bb * ND;
         if (bb == 0 && c <= c2) continue;
-        double* Rb = D + (size_t)bb * BB;
+        T* Rb = D + (size_t)bb * BB;
         Rb[r * ND + c] -= l * Rb[c2 * ND + c];
       }
       __syncwarp();
     }
   }
   for (int64_t e = lane; e < (int64_t)nb * BB; e += 32) F[p0 * BB + e] = R[e];
-  if (lane < ND && D[lane * ND + lane] == 0.0) atomicOr(status, (unsigned)GALES_ERR_SINGULAR);
+  if (lane < ND && D[lane * ND + lane] == T(0)) atomicOr(status, (unsigned)GALES_ERR_SINGULAR);
 }
 
 // Block sums of one node row's lower (upper) blocks: lanes form G = 32 / ND groups of
@@ -375,13 +375,13 @@ __global__ void ilu_factor_level_smem_kernel(double* __restrict__ F, const int64
 // up to 8 blocks per lane are loaded first, so that every block's loads are in flight at
 // once (a row's substitution is one dependency level, bound by memory latency).  The
 // group partial sums are added in group order (deterministic).
-template <int ND>
-__device__ __forceinline__ double block_row_sum(const double* __restrict__ F, const int32_t* __restrict__ f_col,
-                                                int64_t pa, int64_t pb, const double* z, double* red) {
+template <int ND, typename T>
+__device__ __forceinline__ T block_row_sum(const T* __restrict__ F, const int32_t* __restrict__ f_col, int64_t pa,
+                                           int64_t pb, const T* z, T* red) {
   constexpr int BB = ND * ND, G = 32 / ND;
   const int lane = threadIdx.x & 31;
   const int g = lane / ND, r = lane - g * ND;
-  double s = 0.0;
+  T s = 0;
   if (g < G) {
     for (int64_t base = pa + g; base < pb; base += 8 * G) {
       int32_t cidx[8];
@@ -393,8 +393,8 @@ __device__ __forceinline__ double block_row_sum(const double* __restrict__ F, co
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         if (cidx[k] < 0) continue;
-        const double* B = F + (base + (int64_t)k * G) * BB + r * ND;
-        const double* zc = z + (int64_t)cidx[k] * ND;
+        const T* B = F + (base + (int64_t)k * G) * BB + r * ND;
+        const T* zc = z + (int64_t)cidx[k] * ND;
 #pragma unroll
         for (int c = 0; c < ND; ++c) s += B[c] * zc[c];
       }
@@ -402,7 +402,7 @@ __device__ __forceinline__ double block_row_sum(const double* __restrict__ F, co
   }
   red[lane] = s;
   __syncwarp();
-  double t = 0.0;
+  T t = 0;
   if (lane < ND)
 #pragma unroll
     for (int q = 0; q < G; ++q) t += red[q * ND + lane];
@@ -410,60 +410,68 @@ __device__ __forceinline__ double block_row_sum(const double* __restrict__ F, co
   return t;
 }
 
-// y_I = L_II^-1 (v_I - sum_K L_IK y_K), L_II unit lower: warp per node row.
-template <int ND>
-__global__ void ilu_lower_level_kernel(const double* __restrict__ F, const int64_t* __restrict__ f_rp,
+// y_I = L_II^-1 (v_I - sum_K L_IK y_K), L_II unit lower: warp per node row.  The
+// working vector zw is the output column itself for an FP64 factor (zw_follows = 1) or
+// a T scratch vector.
+template <int ND, typename T>
+__global__ void ilu_lower_level_kernel(const T* __restrict__ F, const int64_t* __restrict__ f_rp,
                                        const int32_t* __restrict__ f_col, const int64_t* __restrict__ f_diag,
                                        const int32_t* __restrict__ rows, int64_t count, const double* vbase,
-                                       double* zbase, const int* __restrict__ jidx, int64_t ld) {
+                                       T* zwbase, const int* __restrict__ jidx, int64_t ld, int zw_follows) {
   constexpr int BB = ND * ND;
-  __shared__ double red[kWarpsPerBlock][32];
+  __shared__ T red[kWarpsPerBlock][32];
   const int64_t w = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (w >= count) return;
   const int lane = threadIdx.x & 31;
   const int64_t off = jidx ? (int64_t)(*jidx) * ld : 0;
   const double* v = vbase + off;
-  double* z = zbase + off;
+  T* zw = zwbase + (zw_follows ? off : 0);
   const int32_t I = rows[w];
   const int64_t p0 = f_rp[I], pd = f_diag[I];
   const int r = lane < ND ? lane : 0;
-  const double vi = v[(int64_t)I * ND + r];
-  double s = vi - block_row_sum<ND>(F, f_col, p0, pd, z, red[threadIdx.x >> 5]);
-  const double* D = F + pd * BB + r * ND;
+  const T vi = (T)v[(int64_t)I * ND + r];
+  T s = vi - block_row_sum<ND, T>(F, f_col, p0, pd, zw, red[threadIdx.x >> 5]);
+  const T* D = F + pd * BB + r * ND;
 #pragma unroll
   for (int c = 0; c < ND - 1; ++c) {
-    const double zc = __shfl_sync(0xffffffffu, s, c);
+    const T zc = __shfl_sync(0xffffffffu, s, c);
     if (lane > c) s -= D[c] * zc;
   }
-  if (lane < ND) z[(int64_t)I * ND + lane] = s;
+  if (lane < ND) zw[(int64_t)I * ND + lane] = s;
 }
 
-// x_I = U_II^-1 (y_I - sum_J U_IJ x_J), in place on z.
-template <int ND>
-__global__ void ilu_upper_level_kernel(const double* __restrict__ F, const int64_t* __restrict__ f_rp,
+// x_I = U_II^-1 (y_I - sum_J U_IJ x_J), in place on zw; with a scratch zw the row is
+// also written to the FP64 output column.
+template <int ND, typename T>
+__global__ void ilu_upper_level_kernel(const T* __restrict__ F, const int64_t* __restrict__ f_rp,
                                        const int32_t* __restrict__ f_col, const int64_t* __restrict__ f_diag,
-                                       const int32_t* __restrict__ rows, int64_t count, double* zbase,
-                                       const int* __restrict__ jidx, int64_t ld) {
+                                       const int32_t* __restrict__ rows, int64_t count, T* zwbase,
+                                       double* zoutbase, const int* __restrict__ jidx, int64_t ld, int zw_follows) {
   constexpr int BB = ND * ND;
-  __shared__ double red[kWarpsPerBlock][32];
+  __shared__ T red[kWarpsPerBlock][32];
   const int64_t w = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   if (w >= count) return;
   const int lane = threadIdx.x & 31;
-  double* z = zbase + (jidx ? (int64_t)(*jidx) * ld : 0);
+  const int64_t off = jidx ? (int64_t)(*jidx) * ld : 0;
+  T* zw = zwbase + (zw_follows ? off : 0);
+  double* zout = zoutbase + off;
   const int32_t I = rows[w];
   const int64_t p1 = f_rp[I + 1], pd = f_diag[I];
   const int r = lane < ND ? lane : 0;
-  const double yi = z[(int64_t)I * ND + r];
-  double s = yi - block_row_sum<ND>(F, f_col, pd + 1, p1, z, red[threadIdx.x >> 5]);
-  const double* D = F + pd * BB + r * ND;
+  const T yi = zw[(int64_t)I * ND + r];
+  T s = yi - block_row_sum<ND, T>(F, f_col, pd + 1, p1, zw, red[threadIdx.x >> 5]);
+  const T* D = F + pd * BB + r * ND;
 #pragma unroll
   for (int c = ND - 1; c >= 0; --c) {
-    const double mine = s / D[c];  // meaningful on lane c only
-    const double xc = __shfl_sync(0xffffffffu, mine, c);
+    const T mine = s / D[c];  // meaningful on lane c only
+    const T xc = __shfl_sync(0xffffffffu, mine, c);
     if (lane == c) s = xc;
     else if (lane < c) s -= D[c] * xc;
   }
-  if (lane < ND) z[(int64_t)I * ND + lane] = s;
+  if (lane < ND) {
+    zw[(int64_t)I * ND + lane] = s;
+    if (!zw_follows) zout[(int64_t)I * ND + lane] = (double)s;
+  }
 }
 
 // y = A x (or y = b - A x) on the assembly's CSR values: warp per scalar row.
@@ -601,6 +609,7 @@ struct gales_solver {
   Dev<int64_t> d_node_rp, d_f_rp, d_f_diag, d_a2f;
   Dev<int32_t> d_node_col, d_f_col, d_rows_f, d_rows_b;
   Dev<double> d_F, d_V, d_Z, d_w, d_r, d_x, d_part, d_h, d_h2, d_y, d_vals, d_b;
+  Dev<float> d_Ff, d_zf;     // FP32 factor and its substitution vector (GALES_PRECOND_ILU_FP32)
   Dev<int> d_j;
   Dev<unsigned int> d_status;
   double* h_buf = nullptr;   // pinned: Hessenberg column and the least-squares solution
@@ -642,21 +651,31 @@ bool dev_ptr(const void* p) {
 
 inline unsigned grid_for(int64_t warps) { return (unsigned)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock); }
 
-template <int ND>
+template <typename T>
+T* factor_ptr(gales_solver* s);
+template <>
+double* factor_ptr<double>(gales_solver* s) { return s->d_F.p; }
+template <>
+float* factor_ptr<float>(gales_solver* s) { return s->d_Ff.p; }
+
+// Launch wrappers for nd = ND and a factor stored in T (double: the reference's FP64
+// arithmetic; float: FP32 factor and substitutions, scratch vector d_zf).
+template <int ND, typename T>
 struct Kernels {
+  static constexpr bool kF64 = sizeof(T) == sizeof(double);
   static cudaError_t to_factor(gales_solver* s, const double* vals, cudaStream_t st) {
-    matrix_to_factor_kernel<ND><<<grid_for(s->n_nodes), 32 * kWarpsPerBlock, 0, st>>>(
-        vals, s->d_node_rp.p, s->d_a2f.p, s->n_nodes, s->d_F.p);
+    matrix_to_factor_kernel<ND, T><<<grid_for(s->n_nodes), 32 * kWarpsPerBlock, 0, st>>>(
+        vals, s->d_node_rp.p, s->d_a2f.p, s->n_nodes, factor_ptr<T>(s));
     return cudaGetLastError();
   }
   static size_t factor_smem(int max_row, int max_u) {
-    return ((size_t)max_row + 1 + max_u) * ND * ND * sizeof(double) + ((size_t)max_row + max_u) * sizeof(int32_t);
+    return ((size_t)max_row + 1 + max_u) * ND * ND * sizeof(T) + ((size_t)max_row + max_u) * sizeof(int32_t);
   }
   static cudaError_t prepare(gales_solver* s) {
     const size_t bytes = factor_smem(s->max_row, s->max_u);
     s->factor_smem = 0;
     if (bytes > (size_t)s->smem_optin) return cudaSuccess;  // rows too long: the global-memory kernel
-    cudaError_t e = cudaFuncSetAttribute(ilu_factor_level_smem_kernel<ND>,
+    cudaError_t e = cudaFuncSetAttribute(ilu_factor_level_smem_kernel<ND, T>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) s->factor_smem = bytes;
     return e;
@@ -664,25 +683,29 @@ struct Kernels {
   static cudaError_t factor_level(gales_solver* s, int l, cudaStream_t st) {
     const int64_t o = s->lev_off_f[l], c = s->lev_off_f[l + 1] - o;
     if (s->factor_smem)
-      ilu_factor_level_smem_kernel<ND><<<(unsigned)c, 32, s->factor_smem, st>>>(
-          s->d_F.p, s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_f.p + o, c, s->d_status.p, s->max_row,
-          s->max_u);
+      ilu_factor_level_smem_kernel<ND, T><<<(unsigned)c, 32, s->factor_smem, st>>>(
+          factor_ptr<T>(s), s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_f.p + o, c, s->d_status.p,
+          s->max_row, s->max_u);
     else
-      ilu_factor_level_kernel<ND><<<grid_for(c), 32 * kWarpsPerBlock, 0, st>>>(
-          s->d_F.p, s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_f.p + o, c, s->d_status.p);
+      ilu_factor_level_kernel<ND, T><<<grid_for(c), 32 * kWarpsPerBlock, 0, st>>>(
+          factor_ptr<T>(s), s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_f.p + o, c, s->d_status.p);
     return cudaGetLastError();
   }
   static cudaError_t lower_level(gales_solver* s, int l, const double* v, double* z, const int* j, int64_t ld,
                                  cudaStream_t st) {
     const int64_t o = s->lev_off_f[l], c = s->lev_off_f[l + 1] - o;
-    ilu_lower_level_kernel<ND><<<grid_for(c), 32 * kWarpsPerBlock, 0, st>>>(
-        s->d_F.p, s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_f.p + o, c, v, z, j, ld);
+    T* zw = kF64 ? reinterpret_cast<T*>(z) : reinterpret_cast<T*>(s->d_zf.p);
+    ilu_lower_level_kernel<ND, T><<<grid_for(c), 32 * kWarpsPerBlock, 0, st>>>(
+        factor_ptr<T>(s), s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_f.p + o, c, v, zw, j, ld,
+        kF64 ? 1 : 0);
     return cudaGetLastError();
   }
   static cudaError_t upper_level(gales_solver* s, int l, double* z, const int* j, int64_t ld, cudaStream_t st) {
     const int64_t o = s->lev_off_b[l], c = s->lev_off_b[l + 1] - o;
-    ilu_upper_level_kernel<ND><<<grid_for(c), 32 * kWarpsPerBlock, 0, st>>>(
-        s->d_F.p, s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_b.p + o, c, z, j, ld);
+    T* zw = kF64 ? reinterpret_cast<T*>(z) : reinterpret_cast<T*>(s->d_zf.p);
+    ilu_upper_level_kernel<ND, T><<<grid_for(c), 32 * kWarpsPerBlock, 0, st>>>(
+        factor_ptr<T>(s), s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_b.p + o, c, zw, z, j, ld,
+        kF64 ? 1 : 0);
     return cudaGetLastError();
   }
   static cudaError_t spmv(gales_solver* s, const double* vals, const double* x, const double* b, double* y,
@@ -702,25 +725,34 @@ struct Ops {
   cudaError_t (*spmv)(gales_solver*, const double*, const double*, const double*, double*, cudaStream_t);
 };
 
-template <int ND>
+template <int ND, typename T>
 Ops ops_for() {
-  return {Kernels<ND>::prepare, Kernels<ND>::to_factor, Kernels<ND>::factor_level, Kernels<ND>::lower_level, Kernels<ND>::upper_level,
-          Kernels<ND>::spmv};
+  using K = Kernels<ND, T>;
+  return {K::prepare, K::to_factor, K::factor_level, K::lower_level, K::upper_level, K::spmv};
 }
 
-bool ops(int nd, Ops& o) {
+template <typename T>
+bool ops_t(int nd, Ops& o) {
   switch (nd) {
-    case 4: o = ops_for<4>(); return true;
-    case 5: o = ops_for<5>(); return true;
-    case 6: o = ops_for<6>(); return true;
-    case 7: o = ops_for<7>(); return true;
-    case 8: o = ops_for<8>(); return true;
-    case 9: o = ops_for<9>(); return true;
-    case 10: o = ops_for<10>(); return true;
-    case 11: o = ops_for<11>(); return true;
-    case 12: o = ops_for<12>(); return true;
+    case 4: o = ops_for<4, T>(); return true;
+    case 5: o = ops_for<5, T>(); return true;
+    case 6: o = ops_for<6, T>(); return true;
+    case 7: o = ops_for<7, T>(); return true;
+    case 8: o = ops_for<8, T>(); return true;
+    case 9: o = ops_for<9, T>(); return true;
+    case 10: o = ops_for<10, T>(); return true;
+    case 11: o = ops_for<11, T>(); return true;
+    case 12: o = ops_for<12, T>(); return true;
     default: return false;
   }
+}
+
+bool ops(const gales_solver* s, Ops& o) {
+  return s->prm.precond == GALES_PRECOND_ILU_FP32 ? ops_t<float>(s->nd, o) : ops_t<double>(s->nd, o);
+}
+
+inline bool has_ilu(const gales_solver* s) {
+  return s->prm.precond == GALES_PRECOND_ILU || s->prm.precond == GALES_PRECOND_ILU_FP32;
 }
 
 // z = M^-1 v for columns addressed by *j (graph) or plain pointers (j null).
@@ -748,7 +780,10 @@ unsigned stream_grid(int64_t n, int sms) {
 }
 
 int factorize(gales_solver* s, const Ops& o, const double* vals, cudaStream_t st) {
-  SCK(s, cudaMemsetAsync(s->d_F.p, 0, s->d_F.n * sizeof(double), st), "clear factor");
+  if (s->prm.precond == GALES_PRECOND_ILU_FP32)
+    SCK(s, cudaMemsetAsync(s->d_Ff.p, 0, s->d_Ff.n * sizeof(float), st), "clear factor");
+  else
+    SCK(s, cudaMemsetAsync(s->d_F.p, 0, s->d_F.n * sizeof(double), st), "clear factor");
   SCK(s, cudaMemsetAsync(s->d_status.p, 0, sizeof(unsigned int), st), "clear status");
   SCK(s, o.to_factor(s, vals, st), "matrix to factor");
   const int nf = (int)s->lev_off_f.size() - 1;
@@ -821,7 +856,7 @@ int gales_solver_create(gales_asm* h, const gales_solver_params* prm, gales_solv
   gales_solver_default(&p);
   if (prm) p = *prm;
   if (!(p.rel_res_tol >= 0.0) || p.maxsubspace < 1 || p.maxrestarts < 0 || p.fill < 0 ||
-      (p.precond != GALES_PRECOND_ILU && p.precond != GALES_PRECOND_NONE))
+      (p.precond != GALES_PRECOND_ILU && p.precond != GALES_PRECOND_ILU_FP32 && p.precond != GALES_PRECOND_NONE))
     return GALES_ERR_BAD_INPUT;
   int64_t n_nodes = 0, nnz_nodes = 0, n_rows = 0, nnz = 0;
   const int64_t* nrp = nullptr;
@@ -839,7 +874,7 @@ int gales_solver_create(gales_asm* h, const gales_solver_params* prm, gales_solv
   s->nnz = nnz;
   s->m = p.maxsubspace;
   Ops o;
-  if (!ops(s->nd, o)) {
+  if (!ops(s, o)) {
     delete s;
     return GALES_ERR_UNSUPPORTED;
   }
@@ -853,7 +888,7 @@ int gales_solver_create(gales_asm* h, const gales_solver_params* prm, gales_solv
   cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
   s->dot_blocks = std::max(1, 2 * s->sms);
   std::vector<int64_t> a2f;
-  if (p.precond == GALES_PRECOND_ILU) {
+  if (has_ilu(s)) {
     iluk_symbolic(n_nodes, s->node_rp.data(), s->node_col.data(), p.fill, s->f_rp, s->f_col, s->f_diag);
     level_sets(n_nodes, s->f_rp, s->f_col, s->f_diag, true, s->lev_f, s->lev_off_f, s->rows_f);
     level_sets(n_nodes, s->f_rp, s->f_col, s->f_diag, false, s->lev_b, s->lev_off_b, s->rows_b);
@@ -873,7 +908,9 @@ int gales_solver_create(gales_asm* h, const gales_solver_params* prm, gales_solv
   const size_t bb = (size_t)s->nd * s->nd;
   if (s->d_node_rp.upload(s->node_rp) || s->d_node_col.upload(s->node_col) || s->d_f_rp.upload(s->f_rp) ||
       s->d_f_col.upload(s->f_col) || s->d_f_diag.upload(s->f_diag) || s->d_a2f.upload(a2f) ||
-      s->d_rows_f.upload(s->rows_f) || s->d_rows_b.upload(s->rows_b) || s->d_F.alloc(s->f_col.size() * bb) ||
+      s->d_rows_f.upload(s->rows_f) || s->d_rows_b.upload(s->rows_b) || (p.precond == GALES_PRECOND_ILU ? s->d_F.alloc(s->f_col.size() * bb)
+                                       : s->d_Ff.alloc(s->f_col.size() * bb)) ||
+      (p.precond == GALES_PRECOND_ILU_FP32 ? s->d_zf.alloc(n_rows) : cudaSuccess) ||
       s->d_V.alloc((size_t)(s->m + 1) * n_rows) || s->d_Z.alloc((size_t)s->m * n_rows) || s->d_w.alloc(n_rows) ||
       s->d_r.alloc(n_rows) || s->d_x.alloc(n_rows) || s->d_part.alloc((size_t)s->dot_blocks * (s->m + 2)) ||
       s->d_h.alloc(s->m + 2) || s->d_h2.alloc(s->m + 2) || s->d_y.alloc(s->m + 2) || s->d_j.alloc(1) ||
@@ -885,7 +922,7 @@ int gales_solver_create(gales_asm* h, const gales_solver_params* prm, gales_solv
     cudaGetLastError();
     return bail(GALES_ERR_NO_MEMORY);
   }
-  if (p.precond == GALES_PRECOND_ILU) {
+  if (has_ilu(s)) {
     cudaDeviceGetAttribute(&s->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device);
     if (o.prepare(s) != cudaSuccess) {
       cudaGetLastError();
@@ -904,7 +941,7 @@ int gales_solver_create(gales_asm* h, const gales_solver_params* prm, gales_solv
 
 int gales_solver_factorize(gales_solver* s, const double* vals, void* stream) {
   if (!s || !vals) return GALES_ERR_BAD_INPUT;
-  if (s->prm.precond != GALES_PRECOND_ILU) return 0;
+  if (!has_ilu(s)) return 0;
   SCK(s, cudaSetDevice(s->device), "cudaSetDevice");
   cudaStream_t st = (cudaStream_t)stream;
   const double* dv = vals;
@@ -914,7 +951,7 @@ int gales_solver_factorize(gales_solver* s, const double* vals, void* stream) {
     dv = s->d_vals.p;
   }
   Ops o;
-  ops(s->nd, o);
+  ops(s, o);
   return factorize(s, o, dv, st);
 }
 
@@ -922,13 +959,13 @@ int gales_solver_apply(gales_solver* s, const double* v, double* z, void* stream
   if (!s || !v || !z || !dev_ptr(v) || !dev_ptr(z)) return GALES_ERR_BAD_INPUT;
   SCK(s, cudaSetDevice(s->device), "cudaSetDevice");
   cudaStream_t st = (cudaStream_t)stream;
-  if (s->prm.precond != GALES_PRECOND_ILU) {
+  if (!has_ilu(s)) {
     copy_kernel<<<stream_grid(s->n_rows, s->sms), 256, 0, st>>>(v, z, s->n_rows);
     SCK(s, cudaGetLastError(), "copy");
     return 0;
   }
   Ops o;
-  ops(s->nd, o);
+  ops(s, o);
   return apply_prec(s, o, v, z, nullptr, 0, st);
 }
 
@@ -942,8 +979,14 @@ int gales_solver_factor(gales_solver* s, int64_t* n_block_rows, int64_t* nnz_blo
   if (vals && !s->f_col.empty()) {
     SCK(s, cudaSetDevice(s->device), "cudaSetDevice");
     SCK(s, cudaDeviceSynchronize(), "synchronize");
-    SCK(s, cudaMemcpy(vals, s->d_F.p, s->f_col.size() * s->nd * s->nd * sizeof(double), cudaMemcpyDeviceToHost),
-        "copy factor");
+    const size_t cnt = s->f_col.size() * s->nd * s->nd;
+    if (s->prm.precond == GALES_PRECOND_ILU_FP32) {
+      std::vector<float> tmp(cnt);
+      SCK(s, cudaMemcpy(tmp.data(), s->d_Ff.p, cnt * sizeof(float), cudaMemcpyDeviceToHost), "copy factor");
+      for (size_t i = 0; i < cnt; ++i) vals[i] = tmp[i];
+    } else {
+      SCK(s, cudaMemcpy(vals, s->d_F.p, cnt * sizeof(double), cudaMemcpyDeviceToHost), "copy factor");
+    }
   }
   return 0;
 }
@@ -966,7 +1009,7 @@ int gales_solver_solve(gales_solver* s, const double* vals, const double* rhs, d
   const gales_solver_params& p = s->prm;
   const int64_t maxiters = p.maxiters < 0 ? n - 1 : p.maxiters;
   Ops o;
-  ops(s->nd, o);
+  ops(s, o);
   const double* dA = vals;
   if (!dev_ptr(vals)) {
     SCK(s, s->d_vals.alloc(s->nnz), "staging values");
@@ -981,7 +1024,7 @@ int gales_solver_solve(gales_solver* s, const double* vals, const double* rhs, d
   }
   const bool x_dev = dev_ptr(x);
   double* dx = x_dev ? x : s->d_x.p;
-  const bool prec = p.precond == GALES_PRECOND_ILU;
+  const bool prec = has_ilu(s);
   if (prec) {
     const int rc = factorize(s, o, dA, st);
     if (rc) return rc;
@@ -1125,6 +1168,8 @@ void gales_solver_destroy(gales_solver* s) {
   if (s->h_buf) cudaFreeHost(s->h_buf);
   for (auto* b : {&s->d_node_rp, &s->d_f_rp, &s->d_f_diag, &s->d_a2f}) b->release();
   for (auto* b : {&s->d_node_col, &s->d_f_col, &s->d_rows_f, &s->d_rows_b}) b->release();
+  s->d_Ff.release();
+  s->d_zf.release();
   for (auto* b : {&s->d_F, &s->d_V, &s->d_Z, &s->d_w, &s->d_r, &s->d_x, &s->d_part, &s->d_h, &s->d_h2, &s->d_y,
                   &s->d_vals, &s->d_b})
     b->release();

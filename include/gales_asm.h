@@ -282,7 +282,9 @@ int gales_pressure_interpolate(const double* y_col, const double* p_col, int32_t
  * (the pattern's dense nd x nd blocks make the two identical).  One solver per assembly
  * handle; it reads the handle's node graph at creation. */
 #define GALES_PRECOND_NONE 0
-#define GALES_PRECOND_ILU 1
+#define GALES_PRECOND_ILU 1       /* FP64 factor: the scalar ILU(fill) bit for bit */
+#define GALES_PRECOND_ILU_FP32 2  /* the same factorisation and substitutions in FP32 (the
+                                     Krylov vectors, products and residuals stay FP64) */
 
 typedef struct gales_solver_params {
   double rel_res_tol;    /* ls_rel_res_tol (belos_linear_solver_factory.hpp:77) */
@@ -290,7 +292,7 @@ typedef struct gales_solver_params {
   int32_t maxrestarts;   /* ls_maxrestarts */
   int64_t maxiters;      /* ls_maxiters; -1: rows - 1 (belos_linear_solver_factory.hpp:128) */
   int32_t fill;          /* ls_fill: ILU level of fill */
-  int32_t precond;       /* GALES_PRECOND_ILU (ls_precond ILU) or GALES_PRECOND_NONE */
+  int32_t precond;       /* GALES_PRECOND_ILU (ls_precond ILU), _ILU_FP32 or _NONE */
 } gales_solver_params;
 
 typedef struct gales_solver_result {
