@@ -31,6 +31,7 @@ FORM_MIXED = 1
 CH_CUSTOM = 0
 CH_IDEAL_GAS = 1
 TAU_NONE = 0
+MAGMA_LOOKUP_RANGE, MAGMA_VISCOSITY, MAGMA_PAL_ITER = 1, 2, 4  # gales_magma_status bits
 TAU_2001 = 2001
 TAU_2019 = 2019
 TAU_2007 = 2007
@@ -83,6 +84,17 @@ class SetupDesc(C.Structure):
         ("dirichlet_mask", C.c_uint32 * MAX_FLAGS),
         ("side_bc", SideBC * MAX_FLAGS),
     ]
+
+
+class MagmaDesc(C.Structure):
+    """gales_magma_desc (include/gales_asm.h)."""
+    _fields_ = [("oxide_wf", C.c_double * 10), ("melt_kappa", C.c_double),
+                ("h2o_wf", C.c_double), ("h2o_l_cp", C.c_double), ("h2o_l_kappa", C.c_double),
+                ("co2_wf", C.c_double), ("co2_l_cp", C.c_double), ("co2_l_kappa", C.c_double),
+                ("crystal_fraction", C.c_double), ("crystal_rho", C.c_double),
+                ("gas_on_mu", C.c_int32), ("crystal_on_mu", C.c_int32), ("n_p", C.c_int32), ("n_T", C.c_int32),
+                ("p_table", C.POINTER(C.c_double)), ("T_table", C.POINTER(C.c_double)),
+                ("wf_l_h2o", C.POINTER(C.c_double)), ("wf_l_co2", C.POINTER(C.c_double))]
 
 
 class SolverParams(C.Structure):
@@ -195,6 +207,16 @@ def lib() -> C.CDLL:
     L.gales_iluk_pattern.argtypes = [i64, _p(C.c_int64), _p(C.c_int32), i32, _p(i64), _p(C.c_int64),
                                      _p(C.c_int32), _p(C.c_int32), _p(C.c_int32), _p(C.c_int32)]
     L.gales_iluk_pattern.restype = C.c_int
+    L.gales_magma_create.argtypes = [_p(MagmaDesc), i32, _p(vp)]
+    L.gales_magma_create.restype = C.c_int
+    L.gales_magma_properties.argtypes = [vp, vp, vp, vp, vp, i64, vp, vp, vp]
+    L.gales_magma_properties.restype = C.c_int
+    L.gales_magma_status.argtypes = [vp]
+    L.gales_magma_status.restype = C.c_int
+    L.gales_magma_last_error.argtypes = [vp]
+    L.gales_magma_last_error.restype = C.c_char_p
+    L.gales_magma_destroy.argtypes = [vp]
+    L.gales_magma_destroy.restype = None
     _lib = L
     return L
 
@@ -211,4 +233,6 @@ EXPORTED = [
     "gales_solver_default", "gales_solver_create", "gales_solver_solve", "gales_solver_factorize",
     "gales_solver_apply", "gales_solver_factor", "gales_solver_levels", "gales_solver_correct",
     "gales_solver_launches", "gales_solver_last_error", "gales_solver_destroy", "gales_iluk_pattern",
+    "gales_magma_create", "gales_magma_properties", "gales_magma_status", "gales_magma_last_error",
+    "gales_magma_destroy",
 ]

@@ -17,7 +17,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = HERE / "libgales_asm.so"
-SOURCES = (["gales_host.cu", "gales_mesh_io.cu", "gales_solver.cu"] + [f"gales_{t}_{f}.cu" for t in ("hex8", "tet4", "tri3", "quad4") for f in ("fp64", "mixed")]
+SOURCES = (["gales_host.cu", "gales_mesh_io.cu", "gales_solver.cu", "gales_magma.cu"] + [f"gales_{t}_{f}.cu" for t in ("hex8", "tet4", "tri3", "quad4") for f in ("fp64", "mixed")]
            + [f"gales_vjp_{t}.cu" for t in ("hex8", "tet4", "tri3", "quad4")])
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no implicit contraction in the FP64 form's units, which perform the

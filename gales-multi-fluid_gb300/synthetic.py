@@ -18,6 +18,8 @@ numpy.random.default_rng(seed).
 """
 from __future__ import annotations
 
+import importlib
+
 import numpy as np
 
 from . import Material, Mesh, Setup, custom_chemical, ideal_gas, ideal_gas_named, nb_dofs, p0_policy
@@ -329,3 +331,43 @@ def workload(name: str, seed: int = 0):
     setup = setup_for(mesh.dim, nc)
     I, P = state_for(mesh, nc, seed)
     return mesh, mat, setup, I, P, 1e-3
+
+
+# ---------------------------------------------------------------------------
+# Magma mixtures (props.txt mix_of_mix of magma_mix): synthetic compositions and
+# solubility tables in the input/lookuptable format.  The tables stand in for the
+# reference's solwcad-generated files (not shipped with this project): the same
+# pressure grid (60-300 MPa, 0.1 MPa steps), dissolved H2O growing as sqrt(p) and CO2
+# linearly until all of the magma's volatile is dissolved.
+
+TRACHYTE_LIKE = [0.600, 0.005, 0.180, 0.020, 0.030, 0.001, 0.010, 0.030, 0.060, 0.060]
+BASALT_LIKE = [0.490, 0.015, 0.160, 0.020, 0.080, 0.002, 0.080, 0.110, 0.030, 0.013]
+
+
+def magma_tables(h2o_wf: float, co2_wf: float, n_p: int = 2401, p_lo: float = 6.0e7, p_hi: float = 3.0e8,
+                 n_T: int = 0, T_lo: float = 1100.0, T_hi: float = 1500.0):
+    """(p_table, wf_l_h2o, wf_l_co2, T_table or None): dissolved weight fractions on the
+    liquid, [n_T][n_p] when n_T > 0 (solubility falling slightly with T)."""
+    p = np.linspace(p_lo, p_hi, n_p)
+    h2o = np.minimum(h2o_wf, 0.8 * h2o_wf * np.sqrt(p / p_lo))
+    co2 = np.minimum(co2_wf, 0.15 * co2_wf * (p / p_lo))
+    if n_T <= 0:
+        return p, h2o, co2, None
+    T = np.linspace(T_lo, T_hi, n_T)
+    f = 1.0 - 0.1 * (T - T_lo) / (T_hi - T_lo)
+    return p, np.outer(f, h2o), np.outer(f, co2), T
+
+
+def magma_pair(gas_on_mu: str = "Ishii_Zuber", crystal_on_mu: str = "none", crystal_fraction: float = 0.0,
+               n_T: int = 0):
+    """Two magma_mix components like the shipped P0 case's (a K-rich and a trachytic
+    melt with a few wt% volatiles), with synthetic tables."""
+    magma = importlib.import_module("gales-multi-fluid_gb300.magma")
+    out = []
+    for name, ox, h2o, co2 in (("basaltic", BASALT_LIKE, 0.02, 0.01), ("trachytic", TRACHYTE_LIKE, 0.01, 0.001)):
+        m = magma.MagmaMix(name=name, oxide_wf=ox, h2o_wf=h2o, co2_wf=co2, gas_on_mu=gas_on_mu,
+                           crystal_on_mu=crystal_on_mu, crystal_fraction=crystal_fraction,
+                           crystal_rho=2700.0 if crystal_fraction else 0.0)
+        p, a, b, T = magma_tables(h2o, co2, n_T=n_T)
+        out.append(m.with_tables(p, a, b, T))
+    return out

@@ -344,6 +344,59 @@ int gales_iluk_pattern(int64_t n, const int64_t* row_ptr, const int32_t* col, in
                        int64_t* f_row_ptr, int32_t* f_col, int32_t* level_fwd, int32_t* level_bwd,
                        int32_t* n_levels);
 
+/* Magma mixtures (src/fem/physical_props/fluid/mixtures.hpp:114-511): melt, H2O(l),
+ * CO2(l), H2O(g), CO2(g) with the liquid-phase volatile fractions from solubility lookup
+ * tables, Giordano et al. (2008) viscosity (GiordanoEtAlViscosityModel.hpp) and the gas
+ * and crystal corrections of mixtures.hpp:250-341; several magmas form a mixture of
+ * sub-mixtures (fluid_properties.hpp:171-200, props.txt "mix_of_mix" of "magma_mix"). */
+#define GALES_GAS_MU_NONE 0
+#define GALES_GAS_MU_ISHII_ZUBER 1        /* mixtures.hpp:296-299 */
+#define GALES_GAS_MU_PAL_2003 2           /* mixtures.hpp:260-291 (Newton loop bounded to 200 steps) */
+#define GALES_CRYSTAL_MU_NONE 0
+#define GALES_CRYSTAL_MU_EINSTEIN_ROSCOE 1  /* mixtures.hpp:305-308 */
+#define GALES_CRYSTAL_MU_CARICCHI 2         /* mixtures.hpp:314-330 */
+/* magma status bits (gales_magma_status) */
+#define GALES_MAGMA_LOOKUP_RANGE 1   /* a pressure or temperature outside the table (the reference stops) */
+#define GALES_MAGMA_VISCOSITY 2      /* a zero denominator of the viscosity model (the reference stops) */
+#define GALES_MAGMA_PAL_ITER 4       /* Pal 2003's iteration did not stop within 200 steps */
+
+/* One magma_mix block of props.txt (fluid_properties_reader.hpp:293-420; defaults there:
+ * melt_kappa 1.5, h2o_l/co2_l cp 2278, kappa 0.64).  The solubility tables are the files
+ * of input/lookuptable: pressures (equispaced, n_p), optional temperatures (n_T > 0:
+ * bilinear in (T, p), tables [n_T][n_p]; n_T = 0: linear in p, tables [n_p]), and the
+ * weight fractions of H2O and CO2 dissolved in the liquid.  Host arrays, copied at
+ * creation. */
+typedef struct gales_magma_desc {
+  double oxide_wf[10];   /* SiO2 TiO2 Al2O3 Fe2O3 FeO MnO MgO CaO Na2O K2O (normalised) */
+  double melt_kappa;
+  double h2o_wf, h2o_l_cp, h2o_l_kappa;
+  double co2_wf, co2_l_cp, co2_l_kappa;
+  double crystal_fraction, crystal_rho;
+  int32_t gas_on_mu;      /* GALES_GAS_MU_* */
+  int32_t crystal_on_mu;  /* GALES_CRYSTAL_MU_* */
+  int32_t n_p, n_T;
+  const double* p_table;
+  const double* T_table;
+  const double* wf_l_h2o;
+  const double* wf_l_co2;
+} gales_magma_desc;
+
+typedef struct gales_magma gales_magma;
+
+/* Upload nb_comp magma mixtures (1..GALES_MAX_COMP) to the current device. */
+int gales_magma_create(const gales_magma_desc* comps, int32_t nb_comp, gales_magma** out);
+/* Mixture-of-magmas properties at n points (p[i], T[i], all nb_comp mass fractions
+ * Y[i * nb_comp + c], shear rate shear[i] or NULL = 0), one GPU thread per point:
+ * out[f * n + i] for f = rho, mu, cp, cv, kappa, sound speed, alpha, beta; comp (may be
+ * NULL) [(c * 4 + k) * n + i] for k = rho_c, e_c = cv_c T, chemical diffusivity, gas
+ * volume fraction of magma c.  Host or device arrays; synchronises the stream.  Returns
+ * 0, or GALES_ERR_BAD_INPUT with the GALES_MAGMA_* bits in gales_magma_status. */
+int gales_magma_properties(gales_magma* m, const double* p, const double* T, const double* Y, const double* shear,
+                           int64_t n, double* out, double* comp, void* stream);
+int gales_magma_status(gales_magma* m);
+const char* gales_magma_last_error(gales_magma* m);
+void gales_magma_destroy(gales_magma* m);
+
 /* Status of the last call: error bits and the first offending element (-1 if none). */
 int gales_asm_status(gales_asm* h, int64_t* first_bad_element);
 const char* gales_asm_last_error(gales_asm* h);

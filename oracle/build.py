@@ -1,5 +1,5 @@
-"""Build recipe of the CPU oracle (test infrastructure; see gales_oracle.cpp and
-solver_oracle.cpp).
+"""Build recipe of the CPU oracle (test infrastructure; see gales_oracle.cpp,
+solver_oracle.cpp and magma_oracle.cpp).
 
 Compiled without floating-point contraction so that x86_64 and aarch64 hosts
 give bit-identical results.  Output: oracle/_build/libgales_oracle.so.
@@ -12,7 +12,7 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-SRCS = [HERE / "gales_oracle.cpp", HERE / "solver_oracle.cpp"]
+SRCS = [HERE / "gales_oracle.cpp", HERE / "solver_oracle.cpp", HERE / "magma_oracle.cpp"]
 OUT = HERE / "_build" / "libgales_oracle.so"
 
 

@@ -54,6 +54,8 @@ def lib() -> C.CDLL:
         L.gor_fgmres.argtypes = [C.c_int64, i64p, i32p, dp, dp, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                  C.c_int32, C.c_int64, dp, dp]
         L.gor_fgmres.restype = C.c_int64
+        L.gor_magma_properties.argtypes = [C.POINTER(abi.MagmaDesc), C.c_int32, dp, dp, dp, dp, C.c_int64, dp, dp]
+        L.gor_magma_properties.restype = C.c_int
         for f in ("gor_properties", "gor_inverse", "gor_quad", "gor_gauss", "gor_pattern", "gor_colouring",
                   "gor_element", "gor_assemble", "gor_adaptive_dt"):
             getattr(L, f).restype = C.c_int
@@ -222,6 +224,23 @@ def fgmres(row_ptr, col, vals, b, tol=1e-9, maxsubspace=200, maxrestarts=5, maxi
         raise ZeroDivisionError(f"zero pivot in row {bad - 1}")
     return x, dict(iterations=int(out[0]), abs_res=float(out[1]), rel_res=float(out[2]), converged=bool(out[3]),
                    cycles=int(out[4]))
+
+
+def magma_properties(comps, p, T, Y, shear=None):
+    """fluid_properties' mix_of_mix of magma mixtures on the CPU (magma_oracle.cpp):
+    (out[8, n], comp[nc, 4, n], status bits)."""
+    magma = importlib.import_module("gales-multi-fluid_gb300.magma")
+    arr = magma.descs(comps)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    n = len(p)
+    out = np.zeros((8, n))
+    comp = np.zeros((len(comps), 4, n))
+    sh = None if shear is None else np.ascontiguousarray(shear, dtype=np.float64)
+    st = lib().gor_magma_properties(arr, len(comps), _d(p), _d(T), _d(Y), _d(sh) if sh is not None else None, n,
+                                    _d(out), _d(comp))
+    return out, comp, int(st)
 
 
 def pressure_profile(material, p0, h, T, T1, Y, Y1):
