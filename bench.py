@@ -388,6 +388,46 @@ def _solve_once(gm, fa, lp, torch, dev, tstream, precond):
         return {"error": f"{type(e).__name__}: {e}"}
 
 
+def magma_block(torch, dev, with_cpu, n=4_000_000):
+    """Magma mixture properties (two magma_mix components with synthetic solubility
+    tables, Ishii-Zuber gas correction) at n device-resident (p, T, Y) points: CUDA-event
+    time of the evaluation (the call also reads back a 4-byte status); the oracle on a
+    20,000-point sample on one host core beside it."""
+    try:
+        magma = importlib.import_module("gales-multi-fluid_gb300.magma")
+        syn = importlib.import_module("gales-multi-fluid_gb300.synthetic")
+        comps = syn.magma_pair()
+        mat = magma.MagmaMaterial(comps)
+        g = torch.Generator(device="cpu").manual_seed(0)
+        p = (6.1e7 + 2.38e8 * torch.rand(n, generator=g, dtype=torch.float64)).to(dev)
+        T = (1150.0 + 300.0 * torch.rand(n, generator=g, dtype=torch.float64)).to(dev)
+        y = torch.rand(n, generator=g, dtype=torch.float64)
+        Y = torch.stack([y, 1.0 - y], 1).contiguous().to(dev)
+        for _ in range(2):
+            mat.properties(p, T, Y)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k = 5
+        e0.record()
+        for _ in range(k):
+            mat.properties(p, T, Y)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / k
+        out = {"workload": f"{n} points, 2 magmas (mix_of_mix), 2401-point pressure tables, Ishii-Zuber",
+               "ms": ms, "points_per_s": n / (ms * 1e-3)}
+        if with_cpu:
+            import oracle
+            m = 20000
+            t0 = time.perf_counter()
+            oracle.magma_properties(comps, p[:m].cpu().numpy(), T[:m].cpu().numpy(), Y[:m].cpu().numpy())
+            out["cpu_oracle_points_per_s"] = m / (time.perf_counter() - t0)
+            out["cpu_oracle_cores"] = 1
+        return out
+    except Exception as e:  # reported, never fatal to the assembly line
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def vjp_block(gm, syn, torch, dev, n=32):
     """Adjoint workload: ~200k tets, 3 components.  Exact and frozen VJP against the
     forward residual (FP64 and mixed), and the memory a stored-point design would need."""
@@ -584,6 +624,8 @@ def main():
         line["adaptive_dt"] = adaptive_dt_block(gm, fa, mesh, mat, setup, I, dt, torch, dev, not args.no_cpu)
     if rank == 0 and not args.no_solve:
         line["linear_solve"] = linear_solve_block(gm, fa, lp, torch, dev, stream)
+    if rank == 0:
+        line["magma_properties"] = magma_block(torch, dev, not args.no_cpu)
     if rank == 0 and not args.no_cpu:
         rate, cores, n = cpu_oracle_rate(mesh, mat, setup, I, P, dt, None, None, None, 0)
         line["cpu_baseline"] = {"value": rate, "unit": "elements/s", "cores": cores, "kind": "port",

@@ -375,3 +375,41 @@ def test_newton_device_loop_equals_host_loop(cuda_lib):
     assert np.allclose(host["history"], dev["history"], rtol=1e-8, atol=0)
     S, R = dev["state"].cpu().numpy(), host["state"]
     assert np.linalg.norm(S - R) <= 1e-8 * np.linalg.norm(R)
+
+
+def _iluk_python(n, rows, fill):
+    """Level-of-fill ILU(k) pattern, written directly from the rule (dicts per row)."""
+    pat = []
+    for i in range(n):
+        lev = {j: 0 for j in rows[i]}
+        lev.setdefault(i, 0)
+        k = min(lev)
+        while k < i:
+            lik = lev[k]
+            for j, lkj in pat[k].items():
+                if j > k and lik + lkj + 1 <= fill:
+                    lev[j] = min(lev.get(j, 99), lik + lkj + 1)
+            k = min((c for c in lev if c > k), default=i)
+        pat.append(lev)
+    return pat
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+@pytest.mark.parametrize("fill", [0, 1, 3])
+def test_iluk_pattern_random_graphs(seed, fill):
+    """The library's linked-list symbolic factorisation on irregular graphs (some rows
+    without their diagonal, unsymmetric couplings) against the rule written with dicts."""
+    rng = np.random.default_rng(seed)
+    n = 60
+    rows = []
+    for i in range(n):
+        c = set(rng.choice(n, size=rng.integers(1, 6), replace=False).tolist())
+        if rng.random() < 0.7:
+            c.add(i)
+        rows.append(sorted(c))
+    rp = np.cumsum([0] + [len(r) for r in rows])
+    col = np.concatenate([np.array(r, dtype=np.int32) for r in rows])
+    f_rp, f_col, lf, lb, nl = gm.iluk_pattern(rp, col, fill)
+    ref = _iluk_python(n, rows, fill)
+    for i in range(n):
+        assert list(f_col[f_rp[i]:f_rp[i + 1]]) == sorted(ref[i]), i
