@@ -34,6 +34,10 @@
 #include <cstring>
 #include <vector>
 
+// magma mixtures replacing the chemicals (magma_oracle.cpp, gor_set_magma)
+bool gor_magma_active();
+int gor_magma_point(double p, double T, const double* Y, double* f, double (*comp)[3]);
+
 namespace {
 
 constexpr int MD = GALES_MAX_ND;
@@ -412,6 +416,20 @@ struct Props {
 void properties(const gales_material_desc& mat, double p, double T, const double* Y, Props& o) {
   const int nc = mat.nb_comp;
   o.rho = o.cv = o.cp = o.kappa = o.D = o.mu = o.c = o.alpha = o.beta = 0.0;
+  if (gor_magma_active()) {
+    // fluid_properties.hpp:171-200: mix_of_mix; the mixture's own chemical diffusivity
+    // is not accumulated there and stays 0 from clear() (base_mixture.hpp:50-65)
+    double f[8], cc[GALES_MAX_COMP][3];
+    gor_magma_point(p, T, Y, f, cc);
+    o.rho = f[0]; o.mu = f[1]; o.cp = f[2]; o.cv = f[3]; o.kappa = f[4]; o.c = f[5];
+    o.alpha = f[6]; o.beta = f[7];
+    for (int c = 0; c < nc; ++c) {
+      o.rho_c[c] = cc[c][0];
+      o.e_c[c] = cc[c][1];
+      o.D_c[c] = cc[c][2];
+    }
+    return;
+  }
   double crho[GALES_MAX_COMP], cc[GALES_MAX_COMP], calpha[GALES_MAX_COMP], cbeta[GALES_MAX_COMP];
   for (int c = 0; c < nc; ++c) {
     const gales_chemical_desc& ch = mat.comp[c];

@@ -318,9 +318,57 @@ void build(const gales_magma_desc& d, Magma& g) {
   }
 }
 
+std::vector<Magma> g_active;  // magmas that replace the chemicals in the assembly (gor_set_magma)
+
 }  // namespace
 
+// Used by the assembly restatement (gales_oracle.cpp) when magmas are set: the mixture
+// of sub-mixtures at (p, T, Y) with shear rate 0, f = rho, mu, cp, cv, kappa, sound speed,
+// alpha, beta; comp[c] = rho_c, cv_c T, D_c.  Returns the status bits.
+bool gor_magma_active() { return !g_active.empty(); }
+
+int gor_magma_point(double p, double T, const double* Y, double* f, double (*comp)[3]) {
+  const int nc = (int)g_active.size();
+  int st = 0;
+  double rho = 0, mu = 0, cp = 0, cv = 0, kappa = 0, ss = 0;
+  Chem m[GALES_MAX_COMP];
+  for (int c = 0; c < nc; ++c) {
+    double vfg = 0.0;
+    st |= magma_props(g_active[c], p, T, 0.0, m[c], vfg);
+    rho += Y[c] / m[c].rho;
+    mu += Y[c] * m[c].mu;
+    cp += Y[c] * m[c].cp;
+    cv += Y[c] * m[c].cv;
+    kappa += Y[c] * m[c].kappa;
+    ss += Y[c] / (std::pow(m[c].rho, 2) * std::pow(m[c].c, 2));
+    comp[c][0] = m[c].rho;
+    comp[c][1] = m[c].cv * T;
+    comp[c][2] = m[c].D;
+  }
+  rho = 1.0 / rho;
+  double cs = std::sqrt(1. / ss);
+  cs /= rho;
+  double alpha = 0.0, beta = 0.0;
+  for (int c = 0; c < nc; ++c) {
+    alpha += Y[c] * m[c].alpha * rho / m[c].rho;
+    beta += Y[c] * m[c].beta * rho / m[c].rho;
+  }
+  const double o[8] = {rho, mu, cp, cv, kappa, cs, alpha, beta};
+  for (int k = 0; k < 8; ++k) f[k] = o[k];
+  return st;
+}
+
 extern "C" {
+
+// Replace the material's chemicals by nc magma mixtures in every later assembly,
+// element and property call of the oracle (nc = 0 restores the chemicals).
+int gor_set_magma(const gales_magma_desc* comps, int32_t nc) {
+  g_active.clear();
+  if (nc <= 0) return 0;
+  g_active.resize(nc);
+  for (int c = 0; c < nc; ++c) build(comps[c], g_active[c]);
+  return 0;
+}
 
 // fluid_properties::properties, mix_of_mix branch (fluid_properties.hpp:171-200), for n
 // points: out[f * n + i] with f = rho, mu, cp, cv, kappa, sound speed, alpha, beta;

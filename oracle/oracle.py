@@ -56,6 +56,8 @@ def lib() -> C.CDLL:
         L.gor_fgmres.restype = C.c_int64
         L.gor_magma_properties.argtypes = [C.POINTER(abi.MagmaDesc), C.c_int32, dp, dp, dp, dp, C.c_int64, dp, dp]
         L.gor_magma_properties.restype = C.c_int
+        L.gor_set_magma.argtypes = [C.POINTER(abi.MagmaDesc), C.c_int32]
+        L.gor_set_magma.restype = C.c_int
         for f in ("gor_properties", "gor_inverse", "gor_quad", "gor_gauss", "gor_pattern", "gor_colouring",
                   "gor_element", "gor_assemble", "gor_adaptive_dt"):
             getattr(L, f).restype = C.c_int
@@ -241,6 +243,25 @@ def magma_properties(comps, p, T, Y, shear=None):
     st = lib().gor_magma_properties(arr, len(comps), _d(p), _d(T), _d(Y), _d(sh) if sh is not None else None, n,
                                     _d(out), _d(comp))
     return out, comp, int(st)
+
+
+class magma_material:
+    """Context manager: the oracle's assembly, element and property calls use the given
+    magma mixtures (mix_of_mix) instead of the material's chemicals."""
+
+    def __init__(self, comps):
+        magma = importlib.import_module("gales-multi-fluid_gb300.magma")
+        self._comps = list(comps)  # owns the tables the descriptors point to
+        self._arr = magma.descs(self._comps)
+        self._n = len(comps)
+
+    def __enter__(self):
+        lib().gor_set_magma(self._arr, self._n)
+        return self
+
+    def __exit__(self, *exc):
+        lib().gor_set_magma(None, 0)
+        return False
 
 
 def pressure_profile(material, p0, h, T, T1, Y, Y1):

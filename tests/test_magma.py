@@ -201,3 +201,29 @@ def test_gpu_device_buffers_and_range_status(cuda_lib):
     with pytest.raises(gm.GalesError):
         mat.properties(np.array([5.0e7, 1.0e8]), np.array([1300.0, 1300.0]), np.full((2, 2), 0.5))
     assert gm.abi.lib().gales_magma_status(mat._h) == gm.abi.MAGMA_LOOKUP_RANGE
+
+
+def test_oracle_assembly_with_magma_material():
+    """The oracle's assembly with the chemicals replaced by two magma mixtures (the
+    shipped cases' mix_of_mix; shear-independent Ishii-Zuber): finite blocks with the
+    mixture's density in the mass rows, and the chemicals restored afterwards."""
+    mesh = syn.box_tet_delaunay(4, seed=2)
+    mat = syn.material_for(2, 0)
+    setup = syn.setup_for(3, 2)
+    I, _ = syn.state_for(mesh, 2, 0)
+    S = I.reshape(-1, 6)
+    S[:, 0] = np.clip(S[:, 0], 7.0e7, 2.5e8)
+    S[:, 4] = 1300.0
+    P = I.copy()
+    nd = 6
+    nrp, ncol, rp, col = oracle.pattern(mesh, nd)
+    v0, r0, s0, _ = oracle.assemble(mesh, mat, setup, I, P, 1e-3, rp, col)
+    with oracle.magma_material(syn.magma_pair()):
+        v1, r1, s1, _ = oracle.assemble(mesh, mat, setup, I, P, 1e-3, rp, col)
+        pr = oracle.properties(mat, 1.0e8, 1300.0, np.array([0.5, 0.5]))
+    ref, _, _ = oracle.magma_properties(syn.magma_pair(), np.array([1.0e8]), np.array([1300.0]), np.array([[0.5, 0.5]]))
+    assert s0 == s1 == 0 and np.isfinite(v1).all() and np.isfinite(r1).all()
+    assert not np.allclose(v1, v0)
+    assert pr["rho"] == ref[0, 0] and pr["mu"] == ref[1, 0] and pr["D"] == 0.0
+    v2, _, _, _ = oracle.assemble(mesh, mat, setup, I, P, 1e-3, rp, col)
+    assert np.array_equal(v2, v0)
