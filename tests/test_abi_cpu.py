@@ -59,6 +59,31 @@ def test_struct_layouts_match_c(gm, tmp_path):
                    a.SetupDesc.dirichlet_mask.offset]
 
 
+def test_solver_and_magma_struct_layouts_match_c(gm, tmp_path):
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "sz2.c"
+    fields = [("gales_solver_params", "rel_res_tol"), ("gales_solver_params", "maxiters"),
+              ("gales_solver_params", "precond"), ("gales_solver_result", "iterations"),
+              ("gales_solver_result", "seconds"), ("gales_solver_result", "cycles"),
+              ("gales_magma_desc", "melt_kappa"), ("gales_magma_desc", "gas_on_mu"),
+              ("gales_magma_desc", "n_T"), ("gales_magma_desc", "p_table"), ("gales_magma_desc", "wf_l_co2")]
+    body = " ".join(f'printf("%zu ", offsetof({t}, {f}));' for t, f in fields)
+    body += ' printf("%zu %zu %zu' + chr(92) + 'n", sizeof(gales_solver_params), sizeof(gales_solver_result),' \
+            ' sizeof(gales_magma_desc));'
+    src.write_text(f'#include <stdio.h>\n#include <stddef.h>\n#include "{HEADER}"\nint main(){{{body} return 0;}}\n')
+    exe = tmp_path / "sz2"
+    subprocess.run([cc, str(src), "-o", str(exe)], check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    a = gm.abi
+    types = {"gales_solver_params": a.SolverParams, "gales_solver_result": a.SolverResult,
+             "gales_magma_desc": a.MagmaDesc}
+    want = [getattr(types[t], f).offset for t, f in fields]
+    want += [C.sizeof(a.SolverParams), C.sizeof(a.SolverResult), C.sizeof(a.MagmaDesc)]
+    assert out == want
+
+
 def test_c_constructors_match_python(lib, gm):
     a = gm.abi
     c = a.ChemicalDesc()
