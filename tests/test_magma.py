@@ -227,3 +227,56 @@ def test_oracle_assembly_with_magma_material():
     assert pr["rho"] == ref[0, 0] and pr["mu"] == ref[1, 0] and pr["D"] == 0.0
     v2, _, _, _ = oracle.assemble(mesh, mat, setup, I, P, 1e-3, rp, col)
     assert np.array_equal(v2, v0)
+
+
+def _melt_only(oxide_wf, n_p=11):
+    """A volatile-free magma: no H2O or CO2, so the mixture is the melt alone."""
+    p = np.linspace(6.0e7, 3.0e8, n_p)
+    m = magma.MagmaMix(name="dry", oxide_wf=oxide_wf, h2o_wf=0.0, co2_wf=0.0)
+    return m.with_tables(p, np.zeros(n_p), np.zeros(n_p))
+
+
+OXIDE_MM = np.array([60.084, 79.876, 101.956, 159.692, 71.846, 70.937, 40.304, 56.078, 61.979, 94.195])
+
+
+def test_pin_dry_melt_density_and_heat_capacity():
+    """Lange-Carmichael molar volume (chemicals.hpp:62-103, 110-120) of a dry melt,
+    computed here from the oxide tables: rho = M / (V + dV/dT (T - 1673) + dV/dp (p - 1e5))."""
+    wf = np.array(syn.BASALT_LIKE) / np.sum(syn.BASALT_LIKE)
+    mm = OXIDE_MM * 1e-3
+    M = 1.0 / np.sum(wf / mm)
+    x = wf * M / mm
+    V = np.sum(x * np.array([26.86, 23.16, 37.42, 42.13, 13.65, 0.0, 11.69, 16.53, 28.88, 45.07]) * 1e-6)
+    dT = np.sum(x * np.array([0.0, 7.24, 0.0, 9.09, 2.92, 0.0, 3.27, 3.74, 7.68, 12.08]) * 1e-9)
+    dp = np.sum(x * np.array([-1.89, -2.31, -2.26, -2.53, -0.45, 0.0, 0.27, 0.34, -2.4, -6.75]) * 1e-15)
+    cp = np.sum(x * np.array([1331.0, 1392.0, 1545.0, 1434.0, 1100.0, 0.0, 2424.0, 1781.0, 1651.0, 1030.0]))
+    p, T = np.array([1.0e8, 2.0e8]), np.array([1473.0, 1673.0])
+    out, _, st = oracle.magma_properties([_melt_only(syn.BASALT_LIKE)], p, T, np.ones((2, 1)))
+    mv = V + dT * (T - 1673.0) + dp * (p - 1e5)
+    np.testing.assert_allclose(out[0], M / mv, rtol=1e-13)
+    np.testing.assert_allclose(out[2], cp, rtol=1e-13)
+    np.testing.assert_allclose(out[6], dT / mv, rtol=1e-12)     # alpha
+    np.testing.assert_allclose(out[7], -dp / mv, rtol=1e-12)    # beta
+    assert 2500.0 < out[0][0] < 2900.0
+
+
+def test_pin_dry_melt_viscosity_vft():
+    """Giordano et al. (2008) for a dry melt (GiordanoEtAlViscosityModel.hpp:36-116):
+    log10 mu = -4.55 + B / (T - C) with B and C from the mole percents (Fe as FeO)."""
+    wf = np.array(syn.TRACHYTE_LIKE, dtype=float) / np.sum(syn.TRACHYTE_LIKE)
+    w = wf.copy()
+    w[4] = 0.9309 * (w[3] + w[4])
+    w[3] = 0.0
+    w /= w.sum()
+    Mv = 1.0 / np.sum(w / OXIDE_MM)
+    m = 100.0 * w * Mv / OXIDE_MM
+    B = (159.6 * (m[0] + m[1]) - 173.3 * m[2] + 72.1 * (m[4] + m[5]) + 75.7 * m[6] - 39.0 * m[7] - 84.1 * m[8]
+         - 2.43 * (m[0] + m[1]) * (m[4] + m[5] + m[6]) - 0.91 * (m[0] + m[1] + m[2]) * (m[8] + m[9])
+         + 17.6 * m[2] * (m[8] + m[9]))
+    C = (2.75 * m[0] + 15.7 * (m[1] + m[2]) + 8.3 * (m[4] + m[5] + m[6]) + 10.2 * m[7] - 12.3 * (m[8] + m[9])
+         + 0.3 * (m[2] + m[4] + m[5] + m[6] + m[7]) * (m[8] + m[9]))
+    T = np.array([1200.0, 1400.0])
+    out, _, st = oracle.magma_properties([_melt_only(syn.TRACHYTE_LIKE)], np.full(2, 1.0e8), T, np.ones((2, 1)))
+    assert st == 0
+    np.testing.assert_allclose(np.log10(out[1]), -4.55 + B / (T - C), rtol=1e-12)
+    assert out[1][0] > out[1][1] > 1.0    # viscosity falls with temperature
