@@ -413,3 +413,21 @@ def test_iluk_pattern_random_graphs(seed, fill):
     ref = _iluk_python(n, rows, fill)
     for i in range(n):
         assert list(f_col[f_rp[i]:f_rp[i + 1]]) == sorted(ref[i]), i
+
+
+def test_oracle_full_fill_is_exact_lu():
+    """With a level of fill as large as the matrix, ILU(k) is the LU factorisation
+    without pivoting: L U = A everywhere and FGMRES converges in one step to the
+    direct solution (a pin of the restated elimination and of the Krylov loop)."""
+    *_, nd, nrp, ncol, rp, col, vals, rhs = _system("quad", 1)
+    n = len(rp) - 1
+    A = sp.csr_matrix((vals, col, rp), shape=(n, n))
+    f_rp, f_col, f_val, bad = oracle.iluk(rp, col, vals, n)
+    assert bad == -1
+    F = sp.csr_matrix((f_val, f_col, f_rp), shape=(n, n))
+    LU = ((sp.tril(F, -1) + sp.eye(n)) @ sp.triu(F)).toarray()
+    assert np.abs(LU - A.toarray()).max() <= 1e-11 * abs(A).max()
+    x, info = oracle.fgmres(rp, col, vals, rhs, fill=n)
+    assert info["iterations"] == 1 and info["converged"]
+    xd = sla.spsolve(A.tocsc(), rhs)
+    assert np.linalg.norm(x - xd) <= 1e-9 * np.linalg.norm(xd)
