@@ -126,3 +126,31 @@ def test_null_handle_calls_are_safe(lib):
     assert lib.gales_asm_assemble(None, None, None, 1e-3, 0, None, None, None) == 1
     assert lib.gales_asm_status(None, None) == 1
     assert lib.gales_asm_last_error(None) == b"null handle"
+
+
+def test_solver_and_magma_entry_points_reject_bad_input(lib, gm):
+    """Null handles and invalid descriptors return GALES_ERR_BAD_INPUT before any device
+    work; the host-only ILU pattern checks its arguments."""
+    a = gm.abi
+    out = C.c_void_p()
+    assert lib.gales_solver_create(None, None, C.byref(out)) == 1
+    assert lib.gales_solver_solve(None, None, None, None, None, None) == 1
+    assert lib.gales_solver_last_error(None) == b"null handle"
+    lib.gales_solver_destroy(None)
+    d = a.MagmaDesc()
+    d.n_p = 1  # a table needs two pressures
+    assert lib.gales_magma_create(C.byref(d), 1, C.byref(out)) == 1 and not out.value
+    d.n_p = 3
+    assert lib.gales_magma_create(C.byref(d), 1, C.byref(out)) == 1  # tables missing
+    assert lib.gales_magma_create(C.byref(d), 0, C.byref(out)) == 1
+    assert lib.gales_magma_properties(None, None, None, None, None, 0, None, None, None) == 1
+    assert lib.gales_magma_last_error(None) == b"null handle"
+    lib.gales_magma_destroy(None)
+    rp = np.array([0, 1], dtype=np.int64)
+    col = np.array([0], dtype=np.int32)
+    nnz = C.c_int64()
+    i64p, i32p = C.POINTER(C.c_int64), C.POINTER(C.c_int32)
+    assert lib.gales_iluk_pattern(1, rp.ctypes.data_as(i64p), col.ctypes.data_as(i32p), -1, C.byref(nnz),
+                                  None, None, None, None, None) == 1
+    assert lib.gales_iluk_pattern(1, rp.ctypes.data_as(i64p), col.ctypes.data_as(i32p), 0, C.byref(nnz),
+                                  None, None, None, None, None) == 0 and nnz.value == 1
