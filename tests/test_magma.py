@@ -280,3 +280,25 @@ def test_pin_dry_melt_viscosity_vft():
     assert st == 0
     np.testing.assert_allclose(np.log10(out[1]), -4.55 + B / (T - C), rtol=1e-12)
     assert out[1][0] > out[1][1] > 1.0    # viscosity falls with temperature
+
+
+REF_CASE = pathlib.Path("/root/reference/sim/fluid_mc/P0")
+
+
+@pytest.mark.skipif(not (REF_CASE / "props.txt").exists(), reason="the reference's case files are not present")
+def test_reads_the_reference_case_files():
+    """The shipped case's own props.txt (two magma_mix blocks) and input/lookuptable
+    files parse, and the mixture's properties over the tables' pressure range are finite
+    and physical (format compatibility with the reference's inputs; no expected values
+    ship with them)."""
+    mixes = magma.read_props(REF_CASE / "props.txt")
+    assert [m.name for m in mixes] == ["shoshonite", "phonolite"]
+    assert all(m.gas_on_mu == "Ishii_Zuber" and m.crystal_on_mu == "none" for m in mixes)
+    for m in mixes:
+        magma.read_lookup_tables(REF_CASE / "input" / "lookuptable", m)
+        assert len(m.p_table) == len(m.wf_l_h2o) == len(m.wf_l_co2) > 2 and m.T_table is None
+    p = np.linspace(m.p_table[0] * 1.01, m.p_table[-1] * 0.99, 50)
+    out, comp, st = oracle.magma_properties(mixes, p, np.full(50, 1300.0), np.full((50, 2), 0.5))
+    assert st == 0 and np.isfinite(out).all()
+    assert np.all((out[0] > 2000.0) & (out[0] < 3000.0)) and np.all(out[1] > 1.0)
+    assert np.all(np.diff(comp[:, 3], axis=1) <= 0.0)   # less gas at higher pressure
