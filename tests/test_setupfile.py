@@ -69,3 +69,19 @@ def test_unsupported_solver_choices_raise():
         sf.parse_setup("ls_precond ML\n").solver_params()
     with pytest.raises(ValueError):
         sf.parse_setup("ls_solver GMRES\n").solver_params()
+
+
+REF_SETUP = __import__("pathlib").Path("/root/reference/sim/fluid_mc/P0/setup.txt")
+
+
+@pytest.mark.skipif(not REF_SETUP.exists(), reason="the reference's case files are not present")
+def test_reads_the_reference_case_setup():
+    """The shipped case's own setup.txt maps onto the library defaults: Flexible GMRES
+    with ILU(1), 1e-9, 200 vectors, 5 restarts, maxiters -1; tau 2019, dc_2006, sharpness 2."""
+    s = sf.read_setup(REF_SETUP)
+    p = s.solver_params()
+    d = gm.SolverParams()
+    assert (p.rel_res_tol, p.maxsubspace, p.maxrestarts, p.maxiters, p.fill, p.precond) == \
+        (d.rel_res_tol, d.maxsubspace, d.maxrestarts, d.maxiters, d.fill, d.precond)
+    assert s.tau == gm.TAU_2019 and s.dc_2006 and s.dc_sharp == 2.0 and s.dc_scale_fact == 1.0
+    assert not s.steady_state and s.n_max_it == 3 and s.delta_t == 0.01
