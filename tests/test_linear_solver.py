@@ -431,3 +431,33 @@ def test_oracle_full_fill_is_exact_lu():
     assert info["iterations"] == 1 and info["converged"]
     xd = sla.spsolve(A.tocsc(), rhs)
     assert np.linalg.norm(x - xd) <= 1e-9 * np.linalg.norm(xd)
+
+
+def test_oracle_ilu_values_equal_plain_python_elimination():
+    """The oracle's numeric ILU(1) equals a plain-Python row-oriented (ikj) elimination
+    restricted to the same pattern, bit for bit (Python floats are IEEE binary64 without
+    contraction, as the oracle is compiled)."""
+    mesh = syn.channel_tri(4, 2)
+    nd = gm.nb_dofs(2, 2)
+    nrp, ncol, rp, col = oracle.pattern(mesh, nd)
+    vals, rhs, s, _ = oracle.assemble(mesh, syn.material_for(2, 0), syn.setup_for(2, 2), *syn.state_for(mesh, 2, 0),
+                                      1e-3, rp, col)
+    f_rp, f_col, f_val, bad = oracle.iluk(rp, col, vals, 1)
+    n = len(rp) - 1
+    rows = []
+    for i in range(n):
+        pat = [int(c) for c in f_col[f_rp[i]:f_rp[i + 1]]]
+        w = {c: 0.0 for c in pat}
+        for p in range(rp[i], rp[i + 1]):
+            w[int(col[p])] += float(vals[p])
+        for k in pat:
+            if k >= i:
+                break
+            lik = w[k] / rows[k][k]
+            w[k] = lik
+            for j, u in rows[k].items():
+                if j > k and j in w:
+                    w[j] -= lik * u
+        rows.append(w)
+    ref = np.array([rows[i][int(c)] for i in range(n) for c in f_col[f_rp[i]:f_rp[i + 1]]])
+    assert np.array_equal(ref, f_val)
