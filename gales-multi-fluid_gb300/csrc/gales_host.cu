@@ -1823,7 +1823,9 @@ namespace {
 
 // Device address of g_noalloc_scratch per device.  In host code the array's name
 // is only a host-side stand-in, so the address is looked up once per device, with
-// that device current, by the first gales_asm_assemble_noalloc call on it.
+// that device current, by the first gales_asm_assemble_noalloc call on it, and kept
+// for the life of the process.  A device reset frees the handles' memory as well and
+// would leave this address stale; the header rules out use after a reset.
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[64] = {nullptr};
 

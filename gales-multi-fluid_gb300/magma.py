@@ -200,6 +200,8 @@ def read_props(path) -> List[MagmaMix]:
 
 def _read_table(path: Path, count: Optional[int] = None):
     vals = np.array(Path(path).read_text().split(), dtype=np.float64)
+    if count is not None and len(vals) < count:
+        raise ValueError(f"{path}: {len(vals)} values, the table needs {count}")
     return vals if count is None else vals[:count]
 
 
@@ -209,6 +211,8 @@ def read_lookup_tables(directory, mix: MagmaMix) -> MagmaMix:
     d = Path(directory)
     pv = _read_table(d / "pressure.txt")
     n_p = int(pv[0])
+    if len(pv) < 1 + n_p:
+        raise ValueError(f"{d / 'pressure.txt'}: {len(pv) - 1} pressures, the header declares {n_p}")
     p = pv[1:1 + n_p]
     T = None
     n = n_p

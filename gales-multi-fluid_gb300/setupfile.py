@@ -111,7 +111,10 @@ def parse_setup(text: str) -> SetupFile:
         elif hasattr(out, key):
             cur = getattr(out, key)
             if isinstance(cur, bool):
-                setattr(out, key, val in _TRUE)
+                # read_setup.hpp sets a flag only to true (e.g. 104-105): a false
+                # word leaves the default, so t_dependent_dirichlet_bc F stays true
+                if val in _TRUE:
+                    setattr(out, key, True)
             elif isinstance(cur, int):
                 setattr(out, key, int(val))
             elif isinstance(cur, float):

@@ -198,7 +198,10 @@ int gales_asm_assemble(gales_asm* h, const double* I, const double* P, double dt
  * GALES_ERR_UNSUPPORTED; larger meshes are processed in chunks of a multiple of four
  * elements.
  * The first call on a device looks up the array's device address (once per
- * device); make that first call before any stream capture.  All calls, from every
+ * device) and keeps it for the life of the process; make that first call before any
+ * stream capture.  A reset of the device (cudaDeviceReset, or any reset of its
+ * primary context) frees every handle's device memory and leaves that address
+ * stale: do not use the library on a device after resetting it.  All calls, from every
  * handle, share the one array and it keeps the last call's contents: calls that
  * overlap on the GPU (concurrent streams or threads) race on it, so order them. */
 #define GALES_NOALLOC_SCRATCH_BYTES (8u << 20)

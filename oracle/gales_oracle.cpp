@@ -844,7 +844,8 @@ int tau_matrix(const Ctx& cx, const Quad& q, const Props& pr, const double* vel,
     for (int r = 0; r < nd; ++r)
       for (int cc = 0; cc < nd; ++cc) tau[r][cc] = inv[r * nd + cc] * t[cc];
     if (v_nrm / c < 0.1) {
-      tau[0][0] = 1.0 / (1.0 / tau[0][0] + 1.0 / (rho * tau[1][1] * (trG)));
+      // fluid_2d.hpp:953 in its own form: pow(pow(a,-1) + pow(b,-1), -1)
+      tau[0][0] = pow(pow(tau[0][0], -1.0) + pow(rho * tau[1][1] * (trG), -1.0), -1.0);
       for (int cc = 1; cc < nd; ++cc) tau[0][cc] = 0.0;
     }
   };
@@ -909,9 +910,9 @@ int tau_matrix(const Ctx& cx, const Quad& q, const Props& pr, const double* vel,
           ta += q.G[k][l] * (f.A[k][i][i] * f.A[l][i][i]);
           td += q.G[k][l] * q.G[k][l] * (f.K[k][l][i][i] * f.K[k][l][i][i]);
         }
-      tau[i][i] = 1.0 / (sqrt(tt) + sqrt(ta) + sqrt(td) + 1.e-8);
+      tau[i][i] = pow(sqrt(tt) + sqrt(ta) + sqrt(td) + 1.e-8, -1.0);   // fluid_2d.hpp:1018
     }
-    tau[0][0] = 1.0 / (tau[0][0] + rho * tau[1][1] * (trG));
+    tau[0][0] = pow(tau[0][0] + rho * tau[1][1] * (trG), -1.0);          // fluid_2d.hpp:1020
   }
   return singular;
 }
@@ -962,9 +963,10 @@ void dc(const Ctx& cx, const Quad& q, const double dI[3][MD], const Fluxes& f, d
   }
   const double a = cx.setup->dc_sharp;
   double nu = 0.0;
-  if (a == 1.0) nu = Znrm * h * (1.0 / sqrt(use1));
+  // fluid_2d.hpp:1055-1057 in its own form: pow(use1, -0.5)
+  if (a == 1.0) nu = Znrm * h * pow(use1, -0.5);
   else if (a == 2.0) nu = Znrm * h * h / Unrm;
-  else if (a == 1.5) nu = Znrm * h * ((1.0 / sqrt(use1)) + h / Unrm) / 2.0;
+  else if (a == 1.5) nu = Znrm * h * (pow(use1, -0.5) + h / Unrm) / 2.0;
   for (int r = 0; r < nd; ++r)
     for (int c = 0; c < nd; ++c) shock[r][c] = cx.setup->dc_scale_fact * (nu * f.DUDY[r][c]);
 }

@@ -10,6 +10,7 @@ the CUDA and host math libraries.
 """
 import ctypes as C
 import importlib
+import os
 import pathlib
 import shutil
 import subprocess
@@ -282,7 +283,8 @@ def test_pin_dry_melt_viscosity_vft():
     assert out[1][0] > out[1][1] > 1.0    # viscosity falls with temperature
 
 
-REF_CASE = pathlib.Path("/root/reference/sim/fluid_mc/P0")
+# the reference project's checkout, when one is present (GALES_REFERENCE_DIR)
+REF_CASE = pathlib.Path(os.environ.get("GALES_REFERENCE_DIR", "-"), "sim/fluid_mc/P0")
 
 
 @pytest.mark.skipif(not (REF_CASE / "props.txt").exists(), reason="the reference's case files are not present")

@@ -14,6 +14,7 @@ delta_t           0.02
 final_time        2.0
 restart           F
 n_max_it          4
+t_dependent_dirichlet_bc  F
 
 ls_solver         Flexible GMRES
 ls_precond        ILU
@@ -42,6 +43,8 @@ def test_parse_and_map():
     s = sf.parse_setup(TEXT)
     assert s.fluid_mesh_file == "input/mesh_8core.txt" and s.delta_t == 0.02 and s.final_time == 2.0
     assert s.n_max_it == 4 and not s.restart and s.adaptive_time_step and s.CFL == 0.4 and s.dt_max == 0.25
+    # a flag is only ever set to true (read_setup.hpp:104-105); its default is true
+    assert s.t_dependent_dirichlet_bc
     # "Flexible GMRES" splits to "Flexible", which falls back to Flexible GMRES
     assert s.ls_solver == "Flexible GMRES" and s.ls_precond == "ILU"
     p = s.solver_params()
@@ -71,7 +74,9 @@ def test_unsupported_solver_choices_raise():
         sf.parse_setup("ls_solver GMRES\n").solver_params()
 
 
-REF_SETUP = __import__("pathlib").Path("/root/reference/sim/fluid_mc/P0/setup.txt")
+# the reference project's checkout, when one is present (GALES_REFERENCE_DIR)
+REF_SETUP = __import__("pathlib").Path(__import__("os").environ.get("GALES_REFERENCE_DIR", "-"),
+                                       "sim/fluid_mc/P0/setup.txt")
 
 
 @pytest.mark.skipif(not REF_SETUP.exists(), reason="the reference's case files are not present")
@@ -85,3 +90,4 @@ def test_reads_the_reference_case_setup():
         (d.rel_res_tol, d.maxsubspace, d.maxrestarts, d.maxiters, d.fill, d.precond)
     assert s.tau == gm.TAU_2019 and s.dc_2006 and s.dc_sharp == 2.0 and s.dc_scale_fact == 1.0
     assert not s.steady_state and s.n_max_it == 3 and s.delta_t == 0.01
+    assert s.t_dependent_dirichlet_bc     # the file says F; the reader keeps the true default

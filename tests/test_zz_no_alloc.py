@@ -49,8 +49,12 @@ def test_noalloc_many_scratch_chunks(form, cuda_lib, gm):
     ref = fa.linear_system(device="cuda")
     fa.execute(Id, Pd, 1e-3, ref, form=form)
     lp = fa.linear_system(device="cuda")
+    n0 = fa.launch_count()
     fa.execute_noalloc(Id, Pd, 1e-3, lp, form=form)
     torch.cuda.synchronize()
+    # one point and one matrix launch per scratch chunk (plus the boundary pass): more
+    # than two interior launches means the records went through several chunks
+    assert fa.launch_count() - n0 >= 6
     tol = 1e-12 if form == 0 else 1e-6
     assert rel(lp.vals.cpu().numpy(), ref.vals.cpu().numpy()) <= tol
     assert rel(lp.rhs.cpu().numpy(), ref.rhs.cpu().numpy()) <= tol
