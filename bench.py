@@ -16,6 +16,11 @@ roofline : interior kernel (mixed form), algorithmic bytes per element x element
            / its CUDA-event duration, against the measured HBM copy bandwidth
 cpu_baseline / --impl reference : the CPU oracle (a restatement of the reference's
            assembly, OpenMP over element colours) on the host cores
+hex      : 3,993,600 trilinear hexahedra, 4 components, 8 dofs: 10 mixed assemblies
+           replayed from one CUDA graph, FP64 beside them, the mixed form's error, the
+           roofline and the top-face gas-flux VJP
+newton   : Newton iterations of a time step on the tet mesh, on the GPU, FP64 tangent
+           against the mixed tangent (diagonal tau to 1e-8; shipped tau with n_max_it 3)
 
 Multi-GPU: every rank assembles its own replica (one process per GPU, no data-path
 collective); value = all ranks' elements / the slowest rank's time.
@@ -208,15 +213,13 @@ def top_gas_flux_lambda(mesh, mat, I, nd):
     return lam.ravel(), float(J(S.astype(np.complex128)).real.sum())
 
 
-def run_hex(args):
+def hex_block(args, torch, dev, with_clocks=False):
     """Large hex workload: 160x160x156 trilinear hexahedra (3,993,600) with 10% node
     jitter, 4 components, 8 dofs, 64x64 blocks; 10 mixed assemblies captured in one
-    CUDA graph, FP64 beside it, and the VJP of the top-face gas mass flux."""
-    import torch
-    dev = torch.device("cuda", 0)
+    CUDA graph, FP64 beside it, the mixed form's error against the FP64 form, and the
+    VJP of the top-face gas mass flux."""
     gm = importlib.import_module("gales-multi-fluid_gb300")
     syn = importlib.import_module("gales-multi-fluid_gb300.synthetic")
-    importlib.import_module("gales-multi-fluid_gb300.build").build()
     nx, ny, nz = args.hex_dims
     t0 = time.perf_counter()
     mesh = syn.box_hex(nx, ny, nz, jitter=0.1, seed=4)
@@ -225,7 +228,7 @@ def run_hex(args):
     I, P = syn.state_for(mesh, 4, 0)
     t_mesh = time.perf_counter() - t0
     t0 = time.perf_counter()
-    fa = gm.FluidAssembly(mesh, mat, setup)
+    fa = gm.FluidAssembly(mesh, mat, setup, device=dev.index or 0)
     t_create = time.perf_counter() - t0
     lp = fa.device_system(dev)
     nnz = lp.vals.numel()
@@ -247,8 +250,22 @@ def run_hex(args):
         torch.cuda.synchronize(dev)
         return a.elapsed_time(b) / k, fa.phase_ms(1)
 
-    ms64, k64 = sync_timed(gm.FORM_FP64, max(1, args.fp64_steps), 1)
+    ms64, k64 = sync_timed(gm.FORM_FP64, max(1, args.fp64_steps - 1), 1)
+    # error of the mixed form against the FP64 values this step left (norms in slices,
+    # so the difference never needs a second full copy)
+    with torch.cuda.stream(s):
+        v64, b64 = lp.vals.clone(), lp.rhs.clone()
     ms_sync, k_mx = sync_timed(gm.FORM_MIXED, 2, 1)
+    sl = 1 << 28
+    dA = nA = 0.0
+    for i in range(0, nnz, sl):
+        d = lp.vals[i:i + sl] - v64[i:i + sl]
+        dA += float(torch.dot(d, d))
+        nA += float(torch.dot(v64[i:i + sl], v64[i:i + sl]))
+        del d
+    err = {"matrix": (dA / nA) ** 0.5, "rhs": float(torch.linalg.norm(lp.rhs - b64) / torch.linalg.norm(b64)),
+           "reference": "the GPU FP64 form of this run"}
+    del v64, b64
     # 10 Newton-iteration assemblies in one CUDA graph
     n_in_graph = 10
     g = torch.cuda.CUDAGraph()
@@ -259,16 +276,21 @@ def run_hex(args):
         g.replay()
     torch.cuda.synchronize(dev)
     reps = max(1, args.steps // 5)
-    with ClockSampler(0) as clk:
-        a, b = ev(), ev()
-        a.record(s)
-        with torch.cuda.stream(s):
-            for _ in range(reps):
-                g.replay()
-        b.record(s)
-        torch.cuda.synchronize(dev)
+    clk = ClockSampler(dev.index or 0) if with_clocks else None
+    if clk:
+        clk.__enter__()
+    a, b = ev(), ev()
+    a.record(s)
+    with torch.cuda.stream(s):
+        for _ in range(reps):
+            g.replay()
+    b.record(s)
+    torch.cuda.synchronize(dev)
+    if clk:
+        clk.__exit__()
     fa.sync(stream=sh)
     ms_graph = a.elapsed_time(b) / (reps * n_in_graph)
+    del g
     # objective VJP: lambda = dJ/dI of the top-face gas mass flux, gradient w.r.t. theta
     lam, Jval = top_gas_flux_lambda(mesh, mat, I, fa.nd)
     lamd = torch.tensor(lam, device=dev)
@@ -278,21 +300,17 @@ def run_hex(args):
     torch.cuda.synchronize(dev)
     vjp_ms = fa.device_ms()
     ne = mesh.n_elements
-    pk = peaks()
-    hbm = pk.get("hbm_gbs")
+    hbm = peaks().get("hbm_gbs")
     ach = BYTES_PER_ELEM_HEX * ne / (k_mx * 1e-3) / 1e9
-    line = {
-        "metric": METRIC, "value": ne / (ms_graph * 1e-3), "unit": "elements/s", "n_gpus": 1,
-        "steps": reps * n_in_graph, "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 element integrals + f64 EOS/tau/accumulation (mixed)", "data": "synthetic",
-        "config": {"workload": f"3D hex assembly, {ne} trilinear hexahedra ({nx}x{ny}x{nz}, 10% jitter), "
-                               f"4 components, 8 dofs, 64x64 blocks, 10 mixed assemblies per CUDA graph",
-                   "n_elements": int(ne), "n_nodes": int(mesh.n_nodes), "dofs_per_node": 8, "nnz": int(nnz),
-                   "csr_values_gb": nnz * 8 / 1e9, "l2": "CSR values > L2", "seed": 0},
-        "mixed_sync_ms": ms_sync,
+    out = {
+        "workload": f"3D hex assembly, {ne} trilinear hexahedra ({nx}x{ny}x{nz}, 10% jitter), 4 components, "
+                    f"8 dofs, 64x64 blocks, 10 mixed assemblies per CUDA graph",
+        "n_elements": int(ne), "n_nodes": int(mesh.n_nodes), "nnz": int(nnz), "csr_values_gb": nnz * 8 / 1e9,
+        "value": ne / (ms_graph * 1e-3), "unit": "elements/s", "ms_per_assembly": ms_graph,
+        "graph_replays": reps, "assemblies_timed": reps * n_in_graph, "mixed_stream_ms": ms_sync,
         "fp64": {"value": ne / (ms64 * 1e-3), "unit": "elements/s", "ms_per_step": ms64, "interior_kernel_ms": k64},
         "mixed_over_fp64": ms64 / ms_graph,
+        "mixed_rel_err_vs_fp64": err,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm if hbm else None, "traffic": TRAFFIC_BYTES_PER_ELEM_HEX * ne,
                      "traffic_source": "ncu DRAM bytes per element of a 64,000-hex assembly x elements",
@@ -304,8 +322,27 @@ def run_hex(args):
                           "note": "lambda = dJ/dU seeded VJP (the transpose solve is outside the path)"},
         "host_setup_s": {"mesh": t_mesh, "create": t_create},
         "device_memory_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
-        "clocks": clk.summary(),
     }
+    if clk:
+        out["clocks"] = clk.summary()
+    fa.close()
+    return out
+
+
+def run_hex(args):
+    """--workload hex: the hex workload as the line's headline."""
+    import torch
+    dev = torch.device("cuda", 0)
+    importlib.import_module("gales-multi-fluid_gb300.build").build()
+    h = hex_block(args, torch, dev, with_clocks=True)
+    line = {"metric": METRIC, "value": h["value"], "unit": "elements/s", "n_gpus": 1,
+            "steps": h["assemblies_timed"], "warmup": args.warmup, "ms_per_step": h["ms_per_assembly"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 element integrals + f64 EOS/tau/accumulation (mixed)", "data": "synthetic",
+            "config": {"workload": h["workload"], "n_elements": h["n_elements"], "n_nodes": h["n_nodes"],
+                       "dofs_per_node": 8, "nnz": h["nnz"], "csr_values_gb": h["csr_values_gb"],
+                       "l2": "CSR values > L2", "seed": 0},
+            "roofline": h["roofline"], "clocks": h.get("clocks"), "hex": h}
     print(json.dumps(line), flush=True)
 
 
@@ -334,6 +371,44 @@ def adaptive_dt_block(gm, fa, mesh, mat, setup, I, dt, torch, dev, with_cpu):
         oracle.adaptive_dt(sub, mat, setup, I, dt, 0.5)
         out["cpu_oracle_elements_per_s"] = n / (time.perf_counter() - t0)
         out["cpu_oracle_cores"] = 1
+    return out
+
+
+def newton_block(gm, syn, mesh, mat, torch, dev):
+    """Newton iterations of one time step (main.cpp:216-245) on the benchmark mesh,
+    entirely on the GPU (newton.time_step_device: assembly, ||b|| on the device, the
+    residual check of residual_check.hpp:42-80, flexible GMRES + ILU(1) with an FP32
+    factor, corrector and dof trimmer), from the near-rest state (hydrostatic p, I = P).
+    The FP64 tangent against the mixed tangent (residual in FP64):
+      tau_2014: the reference's diagonal tau (dc_2006 on, sharpness 2), to the reference's
+                criterion ||b|| <= 1e-8 ||b_0||, at most 8 iterations;
+      tau_2019: the shipped non-diagonal tau with the shipped n_max_it = 3.  It enters the
+                tangent frozen and its dependence on the state is not differentiated;
+                the oracle's own loop (CPU assembly + exact solves) stalls the same way."""
+    newton = importlib.import_module("gales-multi-fluid_gb300.newton")
+    I0, _ = syn.state_near_rest(mesh, 3, 0)
+    Id = torch.tensor(I0, device=dev)
+    out = {"workload": f"{mesh.n_elements} tets, near-rest state, dt 1e-3, FGMRES(200)+ILU(1) FP32 factor, 1e-9"}
+    for name, tau, max_it in (("tau_2014", gm.TAU_2014, 8), ("tau_2019_shipped", gm.TAU_2019, 3)):
+        try:
+            fa = gm.FluidAssembly(mesh, mat, syn.setup_for(3, 3, tau=tau), device=dev.index or 0)
+            sol = fa.linear_solver(gm.SolverParams(precond=gm.PRECOND_ILU_FP32))
+            lp = fa.device_system(dev)
+            blk = {}
+            for form, label, rform in ((gm.FORM_FP64, "fp64", None), (gm.FORM_MIXED, "mixed_tangent", gm.FORM_FP64)):
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                r = newton.time_step_device(fa, sol, Id, 1e-3, form, max_it=max_it, residual_form=rform, lp=lp)
+                torch.cuda.synchronize(dev)
+                blk[label] = {"converged": r["converged"], "iterations": r["iterations"],
+                              "history": r["history"], "linear_iterations": r["linear_iterations"],
+                              "s": time.perf_counter() - t0}
+            blk["same_iterations"] = blk["fp64"]["iterations"] == blk["mixed_tangent"]["iterations"]
+            out[name] = blk
+            sol.close()
+            fa.close()
+        except Exception as e:  # reported, never fatal to the assembly line
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
     return out
 
 
@@ -505,6 +580,8 @@ def main():
                     help="tet: 1.0M tets (default); hex: 4.0M hexahedra with a CUDA graph of 10 assemblies")
     ap.add_argument("--hex-dims", type=int, nargs=3, default=[160, 160, 156])
     ap.add_argument("--no-vjp", action="store_true", help="skip the adjoint block")
+    ap.add_argument("--no-hex", action="store_true", help="skip the 4.0M-hex block")
+    ap.add_argument("--no-newton", action="store_true", help="skip the Newton block")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -587,9 +664,14 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize(dev)
+    # a host-buffer call returns when A and b are in host memory, so each step is timed
+    # on its own as well as the whole run
+    e2e_steps = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        ts = time.perf_counter()
         fa.execute(Ih, Ph, dt, lph, form=gm.FORM_MIXED, stream=sh)
+        e2e_steps.append((time.perf_counter() - ts) * 1e3)
     torch.cuda.synchronize(dev)
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dist, dev)
 
@@ -606,14 +688,20 @@ def main():
         "fp64": {"value": whole_job_rate(ne, ms64, world), "unit": "elements/s", "ms_per_step": ms64,
                  "interior_kernel_ms": k64},
         "mixed_over_fp64": ms64 / ms_mx,
-        "mixed_rel_err_vs_fp64": {"matrix": err_A, "rhs": err_b},
+        "mixed_rel_err_vs_fp64": {"matrix": err_A, "rhs": err_b,
+                                  "reference": "the GPU FP64 form of this run, which the -m gpu tests check "
+                                               "against the oracle on this mesh (<= 1e-12)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if hbm else None, "traffic": TRAFFIC_BYTES_PER_ELEM_TET * ne,
                      "traffic_source": "ncu DRAM bytes per element of a 163,618-tet assembly x elements",
                      "kernel": "interior_kernel (mixed form)", "kernel_ms": k_mx,
                      "bytes_per_element": BYTES_PER_ELEM_TET, "peak_source": "measured (MEASURED_PEAKS.json)"},
         "e2e": {"value": whole_job_rate(ne, e2e_s * 1e3, world), "unit": "elements/s",
-                "h2d_bytes_per_step": 2 * fa.n_rows * 8, "d2h_bytes_per_step": (nnz + fa.n_rows) * 8},
+                "h2d_bytes_per_step": 2 * fa.n_rows * 8, "d2h_bytes_per_step": (nnz + fa.n_rows) * 8,
+                "ms_per_step": e2e_s * 1e3,
+                "step_ms": {"median": statistics.median(e2e_steps), "min": min(e2e_steps),
+                            "max": max(e2e_steps)},
+                "over_device_buffers": (e2e_s * 1e3) / ms_mx},
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
@@ -626,6 +714,19 @@ def main():
         line["linear_solve"] = linear_solve_block(gm, fa, lp, torch, dev, stream)
     if rank == 0:
         line["magma_properties"] = magma_block(torch, dev, not args.no_cpu)
+    if rank == 0 and not args.no_newton:
+        syn = importlib.import_module("gales-multi-fluid_gb300.synthetic")
+        line["newton"] = newton_block(gm, syn, mesh, mat, torch, dev)
+    if rank == 0 and not args.no_hex:
+        # the hex workload after the tet workload's buffers are released
+        del lph, Ih, Ph
+        fa.close()
+        lp = None
+        torch.cuda.empty_cache()
+        try:
+            line["hex"] = hex_block(args, torch, dev)
+        except Exception as e:  # reported, never fatal to the assembly line
+            line["hex"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0 and not args.no_cpu:
         rate, cores, n = cpu_oracle_rate(mesh, mat, setup, I, P, dt, None, None, None, 0)
         line["cpu_baseline"] = {"value": rate, "unit": "elements/s", "cores": cores, "kind": "port",

@@ -4,9 +4,10 @@ The mixed tangent must leave the nonlinear convergence unchanged: the same numbe
 of iterations to the reference's residual check (||b|| <= 1e-8 ||b_0||) when the
 residual is evaluated in FP64 (the FP32 residual of a nearly converged state is
 dominated by rounding of large cancelling terms and stalls above 1e-8; checked
-below as well).  The shipped tau (2019) enters the tangent frozen, and on these
-synthetic states Newton then stalls near 10% in both forms; the comparison runs
-with tau off, where it converges.
+below as well).  The shipped non-diagonal tau (2019) enters the tangent frozen and
+the reference's own loop stalls with it (test_newton_oracle.py): the GPU loops follow
+the oracle's loop there, and reach 1e-8 in the oracle's iteration count with the
+diagonal tau (2014) and with tau off.
 """
 import importlib
 
@@ -38,3 +39,54 @@ def test_mixed_form_keeps_newton_iteration_count(kind, cuda_lib):
     # the all-FP32 residual reaches the first iterations' reduction but not 1e-8
     r32 = newton.time_step(fa, I0, 1e-3, gm.FORM_MIXED, max_it=8)
     assert r32["history"][1] == pytest.approx(r64["history"][1], rel=1e-3)
+
+
+def _tet_near_rest(tau):
+    mesh, nc = syn.box_tet_delaunay(8, seed=1), 3
+    mat = syn.material_for(nc, 0)
+    setup = syn.setup_for(3, nc, tau=tau)
+    I0, _ = syn.state_near_rest(mesh, nc, 0)
+    return mesh, mat, setup, I0
+
+
+def _close(h, r):
+    """Residual histories agree to the solve tolerance: 1e-4 relative while the
+    residual is large, 1e-9 absolute once it reaches the Krylov tolerance."""
+    return len(h) == len(r) and all(abs(a - b) <= max(1e-4 * abs(b), 1e-9) for a, b in zip(h, r))
+
+
+@pytest.mark.gpu
+def test_device_newton_with_diagonal_tau_matches_oracle_iterations(cuda_lib):
+    """tau_diag_2014 with the shipped dc_2006: the oracle's loop (host assembly, FGMRES +
+    ILU(1)) reaches ||b|| <= 1e-8 ||b_0||; the GPU loop does too, in the same number of
+    iterations with the FP64 tangent and with the mixed tangent (residual in FP64)."""
+    import torch
+    mesh, mat, setup, I0 = _tet_near_rest(gm.TAU_2014)
+    import cases
+    ref = cases.oracle_newton(mesh, mat, setup, I0, 1e-3, 8, (5, 6))
+    assert ref["converged"]
+    fa = gm.FluidAssembly(mesh, mat, setup)
+    sol = fa.linear_solver()
+    Id = torch.tensor(I0, device="cuda:0")
+    r64 = newton.time_step_device(fa, sol, Id, 1e-3, gm.FORM_FP64, max_it=8)
+    rmx = newton.time_step_device(fa, sol, Id, 1e-3, gm.FORM_MIXED, max_it=8, residual_form=gm.FORM_FP64)
+    for r in (r64, rmx):
+        assert r["converged"] and r["iterations"] == ref["iterations"], (r["history"], ref["history"])
+        assert _close(r["history"], ref["history"]), (r["history"], ref["history"])
+
+
+@pytest.mark.gpu
+def test_device_newton_with_shipped_tau_follows_oracle(cuda_lib):
+    """The shipped tau (2019) and n_max_it = 3: the GPU loop's residual history equals
+    the oracle's loop (the stall is the reference algorithm's, test_newton_oracle.py)."""
+    import torch
+    mesh, mat, setup, I0 = _tet_near_rest(gm.TAU_2019)
+    import cases
+    ref = cases.oracle_newton(mesh, mat, setup, I0, 1e-3, 3, (5, 6))
+    fa = gm.FluidAssembly(mesh, mat, setup)
+    sol = fa.linear_solver()
+    Id = torch.tensor(I0, device="cuda:0")
+    for form, rform in ((gm.FORM_FP64, None), (gm.FORM_MIXED, gm.FORM_FP64)):
+        r = newton.time_step_device(fa, sol, Id, 1e-3, form, max_it=3, residual_form=rform)
+        assert r["converged"] == ref["converged"]
+        assert _close(r["history"], ref["history"]), (form, r["history"], ref["history"])

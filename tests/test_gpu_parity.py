@@ -83,6 +83,17 @@ def test_tau_variants(variant, kind, cuda_lib, gm, orc):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("variant", [2001, 2007, 2014, 0])
+@pytest.mark.parametrize("kind", ["tri", "tet", "hex"])
+def test_mixed_tau_variants(variant, kind, cuda_lib, gm, orc):
+    nc = 4 if kind == "hex" else 3
+    mesh, mat, setup, I, P, dt = cases.make(kind, nc, setup_kw=dict(tau=variant))
+    fa, lp, vals, rhs = _run(gm, orc, mesh, mat, setup, I, P, dt, gm.FORM_MIXED)
+    assert rel(lp.vals, vals) <= MIXED_TOL
+    assert rel(lp.rhs, rhs) <= MIXED_TOL
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("sharp", [1.0, 1.5, 2.0])
 @pytest.mark.parametrize("steady", [False, True])
 def test_dc_and_steady(sharp, steady, cuda_lib, gm, orc):

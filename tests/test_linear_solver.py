@@ -301,30 +301,6 @@ def test_correct_trims_one_dof(cuda_lib):
     assert np.array_equal(dI.cpu().numpy().reshape(-1, nd), ref)
 
 
-def _oracle_newton(mesh, mat, setup, I0, dt, max_it, trim):
-    nd = gm.nb_dofs(mesh.dim, mat.nb_comp)
-    nrp, ncol, rp, col = oracle.pattern(mesh, nd)
-    P = I0.copy()
-    I = P.copy()
-    res0, its, hist = 0.0, [], []
-    for it in range(max_it):
-        vals, rhs, s, _ = oracle.assemble(mesh, mat, setup, I, P, dt, rp, col)
-        nb = float(np.linalg.norm(rhs))
-        if it == 0:
-            res0 = nb
-            hist.append(1.0)
-        else:
-            hist.append(nb / res0)
-            if nb <= max(1e-8 * res0, 1e-5):
-                return dict(converged=True, iterations=it, history=hist, linear_iterations=its, state=I)
-        x, info = oracle.fgmres(rp, col, vals, rhs)
-        its.append(info["iterations"])
-        I = I + x
-        S = I.reshape(-1, nd)
-        S[:, trim[0]:trim[1]] = np.maximum(0.0, np.minimum(S[:, trim[0]:trim[1]], 1.0))
-    return dict(converged=False, iterations=max_it, history=hist, linear_iterations=its, state=I)
-
-
 @pytest.mark.gpu
 @pytest.mark.parametrize("kind, nc", [("quad", 1), ("hex", 2)])
 def test_newton_on_device_matches_oracle(kind, nc, cuda_lib):
@@ -340,7 +316,7 @@ def test_newton_on_device_matches_oracle(kind, nc, cuda_lib):
     trim = (mesh.dim + 2, mesh.dim + 3) if nc > 1 else (0, 0)
     dev = newton.time_step_device(fa, sol, torch.tensor(I0, device="cuda:0"), dt, gm.FORM_FP64, max_it=3,
                                   trim=trim)
-    ref = _oracle_newton(mesh, mat, setup, I0, dt, 3, trim)
+    ref = cases.oracle_newton(mesh, mat, setup, I0, dt, 3, trim)
     assert dev["converged"] == ref["converged"] and dev["iterations"] == ref["iterations"]
     assert ref["history"][-1] < 0.5  # the iteration makes progress on this state
     assert np.allclose(dev["history"], ref["history"], rtol=1e-5, atol=0)
