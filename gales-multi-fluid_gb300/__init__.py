@@ -467,6 +467,13 @@ class FluidAssembly:
 
     SECONDARY_FIELDS = ("rho", "mu", "cp", "cv", "alpha", "beta", "kappa", "sound_speed")
 
+    @staticmethod
+    def MAGMA_FRACTION_FIELDS(nb_comp: int):
+        """Row names of magma_fractions (the names secondary_dofs.hpp:163-176 prints)."""
+        per = [n for c in range(nb_comp) for n in (f"vf_g_comp_{c}", f"vf_comp_{c}")]
+        return tuple(per) + ("vf_g_on_total", "vf_h2o_g_on_total", "vf_co2_g_on_total", "wf_g_on_total",
+                             "wf_h2o_g_on_total", "wf_co2_g_on_total")
+
     def secondary_dofs(self, I, out=None, stream: int = 0):
         """secondary_dofs::execute (secondary_dofs.hpp:56-101): the mixture at every
         node, an (8, n_nodes) array (or the given host/device buffer) in the order of
@@ -474,6 +481,24 @@ class FluidAssembly:
         if out is None:
             out = np.zeros((8, self.mesh.n_nodes))
         self._check(self._L.gales_asm_secondary_dofs(self._h, _addr(I), _addr(out), stream or None))
+        return out
+
+    def set_magma(self, magma_material=None):
+        """Attach magma mixtures (magma.MagmaMaterial, props.txt's mix_of_mix of
+        magma_mix) as the material of every later call, or detach them (None).  The
+        material must have this handle's number of components and outlive the
+        attachment (the handle keeps a reference)."""
+        h = None if magma_material is None else magma_material._h
+        self._check(self._L.gales_asm_set_magma(self._h, h))
+        self._magma = magma_material
+
+    def magma_fractions(self, I, out=None, stream: int = 0):
+        """The gas fractions of secondary_dofs::execute with pp_vf_g
+        (secondary_dofs.hpp:56-131) at every node: a (2 nb_comp + 6, n_nodes) array (or
+        the given buffer), rows MAGMA_FRACTION_FIELDS(nb_comp)."""
+        if out is None:
+            out = np.zeros((2 * self.nb_comp + 6, self.mesh.n_nodes))
+        self._check(self._L.gales_asm_magma_fractions(self._h, _addr(I), _addr(out), stream or None))
         return out
 
     def element_blocks(self, I, P, dt: float, elements, which: int = 0, form: int = FORM_FP64,

@@ -24,6 +24,7 @@ ERR_NONFINITE = 8
 ERR_CUDA = 16
 ERR_UNSUPPORTED = 32
 ERR_NO_MEMORY = 64
+ERR_MAGMA = 128
 NOALLOC_SCRATCH_BYTES = 8 << 20
 
 FORM_FP64 = 0
@@ -217,6 +218,10 @@ def lib() -> C.CDLL:
     L.gales_magma_last_error.restype = C.c_char_p
     L.gales_magma_destroy.argtypes = [vp]
     L.gales_magma_destroy.restype = None
+    L.gales_asm_set_magma.argtypes = [vp, vp]
+    L.gales_asm_set_magma.restype = C.c_int
+    L.gales_asm_magma_fractions.argtypes = [vp, vp, vp, vp]
+    L.gales_asm_magma_fractions.restype = C.c_int
     _lib = L
     return L
 
@@ -234,5 +239,5 @@ EXPORTED = [
     "gales_solver_apply", "gales_solver_factor", "gales_solver_levels", "gales_solver_correct",
     "gales_solver_launches", "gales_solver_last_error", "gales_solver_destroy", "gales_iluk_pattern",
     "gales_magma_create", "gales_magma_properties", "gales_magma_status", "gales_magma_last_error",
-    "gales_magma_destroy",
+    "gales_magma_destroy", "gales_asm_set_magma", "gales_asm_magma_fractions",
 ]

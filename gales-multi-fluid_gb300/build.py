@@ -18,7 +18,8 @@ CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = HERE / "libgales_asm.so"
 SOURCES = (["gales_host.cu", "gales_mesh_io.cu", "gales_solver.cu", "gales_magma.cu"] + [f"gales_{t}_{f}.cu" for t in ("hex8", "tet4", "tri3", "quad4") for f in ("fp64", "mixed")]
-           + [f"gales_vjp_{t}.cu" for t in ("hex8", "tet4", "tri3", "quad4")])
+           + [f"gales_vjp_{t}.cu" for t in ("hex8", "tet4", "tri3", "quad4")]
+           + [f"gales_{t}_magma_{f}.cu" for t in ("hex8", "tet4", "tri3", "quad4") for f in ("fp64", "mixed")])
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no implicit contraction in the FP64 form's units, which perform the
 # reference's IEEE operations (see gales_physics.cuh); the mixed form's units contract

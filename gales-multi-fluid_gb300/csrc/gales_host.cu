@@ -252,6 +252,11 @@ struct gales_asm {
   // interior pass: point-record chunk buffers (scratch) and, for the FP64 form, two
   // internal streams
   InteriorOps ops[2];
+  // magma mixtures (gales_asm_set_magma): the kernels compiled with the magma EOS replace
+  // ops[] while a magma material is attached; ops_ch keeps the chemicals' kernels
+  InteriorOps ops_ch[2];
+  const magma_mix::DevMagma* mg = nullptr;
+  MagmaOps mops{};
   DevBuf<unsigned char> qpbuf[kRing];
   long long chunk_elems[2] = {1, 1};   // elements per chunk, per form
   int sms = 1;                          // multiprocessors of the device
@@ -315,10 +320,12 @@ bool is_pinned_host_ptr(const void* p) {
 
 // Reference fluid properties at the dc_2006 reference state (fluid_2d.hpp:123-135):
 // props at (p_ref, T_ref, Y = 0.5 for every component), U at v_ref.
+void u_ref_inv_from(gales_asm* h, double rho, double cv);
+
 void compute_u_ref_inv(gales_asm* h) {
   for (int i = 0; i < GALES_MAX_ND; ++i) h->u_ref_inv[i] = 0.0;
   if (!h->setup.dc_2006) return;
-  const int nc = h->nc, dim = h->dim;
+  const int nc = h->nc;
   const double p = h->setup.p_ref, T = h->setup.T_ref;
   double rho = 0.0, cv = 0.0;
   for (int c = 0; c < nc; ++c) {
@@ -335,6 +342,15 @@ void compute_u_ref_inv(gales_asm* h) {
     cv += 0.5 * v;
   }
   rho = 1. / rho;
+  u_ref_inv_from(h, rho, cv);
+}
+
+// U at (rho, cv, T_ref, v_ref, Y_ref = 0.5) and its inverse where U >= DBL_EPSILON.
+void u_ref_inv_from(gales_asm* h, double rho, double cv) {
+  for (int i = 0; i < GALES_MAX_ND; ++i) h->u_ref_inv[i] = 0.0;
+  if (!h->setup.dc_2006) return;
+  const int nc = h->nc, dim = h->dim;
+  const double T = h->setup.T_ref;
   double v2 = 0.0;
   for (int k = 0; k < dim; ++k) v2 += h->setup.v_ref[k] * h->setup.v_ref[k];
   const double E = cv * T + 0.5 * (v2);
@@ -793,6 +809,8 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   }
   h->ops[GALES_FORM_FP64] = interior_ops(h->dim, h->nen, GALES_FORM_FP64);
   h->ops[GALES_FORM_MIXED] = interior_ops(h->dim, h->nen, GALES_FORM_MIXED);
+  h->ops_ch[GALES_FORM_FP64] = h->ops[GALES_FORM_FP64];
+  h->ops_ch[GALES_FORM_MIXED] = h->ops[GALES_FORM_MIXED];
   {  // chunk size per form from the point kernel's occupancy; record buffers for the larger
     int sms = 0;
     if ((ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
@@ -986,6 +1004,7 @@ void fill_chem(const gales_chemical_desc& q, DevChem& d) {
 KParams base_params(gales_asm* h, double dt) {
   KParams k;
   memset(&k, 0, sizeof(k));
+  k.mg = h->mg;
   for (int c = 0; c < h->nc; ++c) {
     const gales_chemical_desc& q = h->mat.comp[c];
     fill_chem(q, k.ch[c]);
@@ -1128,6 +1147,7 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
 }
 
 LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, int form, long long n, cudaStream_t st) {
+  if (h->mg) return h->mops.boundary(k, h->nc, form, n, st);
   if (h->dim == 2 && h->nen == 3) return boundary_tri3(k, h->nc, form, n, st);
   if (h->dim == 2 && h->nen == 4) return boundary_quad4(k, h->nc, form, n, st);
   if (h->dim == 3 && h->nen == 4) return boundary_tet4(k, h->nc, form, n, st);
@@ -1136,6 +1156,7 @@ LaunchResult dispatch_boundary(gales_asm* h, const KParams& k, int form, long lo
 
 LaunchResult dispatch_adaptive_dt(gales_asm* h, const KParams& k, double cfl, double* dt_el, long long n,
                                   cudaStream_t st) {
+  if (h->mg) return h->mops.adaptive_dt(k, h->nc, cfl, dt_el, n, st);
   if (h->dim == 2 && h->nen == 3) return adaptive_dt_tri3(k, h->nc, cfl, dt_el, n, st);
   if (h->dim == 2 && h->nen == 4) return adaptive_dt_quad4(k, h->nc, cfl, dt_el, n, st);
   if (h->dim == 3 && h->nen == 4) return adaptive_dt_tet4(k, h->nc, cfl, dt_el, n, st);
@@ -1530,6 +1551,8 @@ int gales_asm_vjp(gales_asm* h, const double* I, const double* P, double dt, con
   if (!(dt > 0.0)) return fail(h, GALES_ERR_BAD_INPUT, "dt must be positive");
   if (mode == GALES_VJP_EXACT && h->setup.tau != GALES_TAU_NON_DIAG_COMP_2019 && h->setup.tau != GALES_TAU_NONE)
     return fail(h, GALES_ERR_UNSUPPORTED, "the exact VJP is available for tau 2019 and tau none");
+  if (mode == GALES_VJP_EXACT && h->mg)
+    return fail(h, GALES_ERR_UNSUPPORTED, "the exact VJP differentiates the chemicals' EOS, not magma mixtures");
   CK(h, cudaSetDevice(h->device), "cudaSetDevice");
   cudaStream_t st = (cudaStream_t)stream;
   const size_t sb = (size_t)h->n_rows * sizeof(double);
@@ -1675,6 +1698,10 @@ int gales_asm_adaptive_dt(gales_asm* h, const double* I, double dt, double cfl, 
   }
   KParams k = base_params(h, dt);
   k.I = dI;
+  if (h->mg) {  // magma lookups report through the status word
+    CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
+    CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  }
   LaunchResult r = dispatch_adaptive_dt(h, k, cfl, del, h->n_el, st);
   if (r.err != cudaSuccess) return cuda_fail(h, r.err, "adaptive dt kernel");
   h->launches += r.launches;
@@ -1687,9 +1714,11 @@ int gales_asm_adaptive_dt(gales_asm* h, const double* I, double dt, double cfl, 
      "copy min");
   if (dt_el && !dev_el)
     CK(h, cudaMemcpyAsync(dt_el, del, (size_t)h->n_el * sizeof(double), cudaMemcpyDeviceToHost, st), "copy dt");
-  CK(h, cudaStreamSynchronize(st), "synchronize");
+  int rc = 0;
+  if (h->mg) rc = finish(h, st);
+  else CK(h, cudaStreamSynchronize(st), "synchronize");
   *dt_new = gales_dt_update(*h->h_aux, dt, dt_min, dt_max);
-  return 0;
+  return rc;
 }
 
 int gales_asm_secondary_dofs(gales_asm* h, const double* I, double* out, void* stream) {
@@ -1712,13 +1741,95 @@ int gales_asm_secondary_dofs(gales_asm* h, const double* I, double* out, void* s
   }
   KParams k = base_params(h, 1.0);
   k.I = dI;
-  LaunchResult r = h->dim == 2 ? secondary_dofs_2d(k, h->nc, dout, n, st) : secondary_dofs_3d(k, h->nc, dout, n, st);
+  if (h->mg) {  // magma lookups report through the status word
+    CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
+    CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  }
+  LaunchResult r = h->mg ? h->mops.secondary_dofs(k, h->nc, dout, n, st)
+                         : (h->dim == 2 ? secondary_dofs_2d(k, h->nc, dout, n, st)
+                                        : secondary_dofs_3d(k, h->nc, dout, n, st));
   if (r.err != cudaSuccess) return cuda_fail(h, r.err, "secondary dofs kernel");
   h->launches += r.launches;
   if (!dev_out)
     CK(h, cudaMemcpyAsync(out, dout, (size_t)(8 * n) * sizeof(double), cudaMemcpyDeviceToHost, st), "copy output");
+  if (h->mg) return finish(h, st);
   CK(h, cudaStreamSynchronize(st), "synchronize");
   return 0;
+}
+
+int gales_asm_set_magma(gales_asm* h, gales_magma* m) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  if (!m) {  // back to the material's chemicals
+    h->mg = nullptr;
+    h->ops[GALES_FORM_FP64] = h->ops_ch[GALES_FORM_FP64];
+    h->ops[GALES_FORM_MIXED] = h->ops_ch[GALES_FORM_MIXED];
+    compute_u_ref_inv(h);
+    return 0;
+  }
+  int nc = 0, dev = -1;
+  const magma_mix::DevMagma* tab = magma_device_table(m, &nc, &dev);
+  if (nc != h->nc)
+    return fail(h, GALES_ERR_BAD_INPUT, "the magma material has " + std::to_string(nc) +
+                                            " components, the handle " + std::to_string(h->nc));
+  if (dev != h->device) return fail(h, GALES_ERR_BAD_INPUT, "the magma material lives on another device");
+  MagmaOps mo = h->dim == 2 ? (h->nen == 3 ? magma_ops_tri3() : magma_ops_quad4())
+                            : (h->nen == 4 ? magma_ops_tet4() : magma_ops_hex8());
+  for (int f = 0; f < 2; ++f) {  // kernel attributes, once, outside any stream capture
+    if (mo.interior[f].rec_bytes(h->nc) != h->ops_ch[f].rec_bytes(h->nc))
+      return fail(h, GALES_ERR_UNSUPPORTED, "magma point records differ from the chemicals'");
+    CK(h, mo.interior[f].prepare(h->nc), "kernel attributes");
+    KParams k0;
+    memset(&k0, 0, sizeof(k0));
+    LaunchResult r = mo.boundary(k0, h->nc, f, -1, 0);
+    if (r.err != cudaSuccess) return cuda_fail(h, r.err, "kernel attributes");
+  }
+  // u_ref_inv from the magma mixture at (p_ref, T_ref, Y_ref = 0.5, shear rate 0)
+  // (fluid_2d.hpp:123-135)
+  double p = h->setup.p_ref, T = h->setup.T_ref, Y[GALES_MAX_COMP], f[8];
+  for (int c = 0; c < nc; ++c) Y[c] = 0.5;
+  int rc = gales_magma_properties(m, &p, &T, Y, nullptr, 1, f, nullptr, nullptr);
+  if (rc) return fail(h, GALES_ERR_MAGMA, std::string("magma properties at the reference state: ") +
+                                              gales_magma_last_error(m));
+  h->mops = mo;
+  h->mg = tab;
+  h->ops[GALES_FORM_FP64] = mo.interior[GALES_FORM_FP64];
+  h->ops[GALES_FORM_MIXED] = mo.interior[GALES_FORM_MIXED];
+  u_ref_inv_from(h, f[0], f[3]);
+  return 0;
+}
+
+int gales_asm_magma_fractions(gales_asm* h, const double* I, double* out, void* stream) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (!I || !out) return fail(h, GALES_ERR_BAD_INPUT, "null state or output pointer");
+  if (!h->mg) return fail(h, GALES_ERR_BAD_INPUT, "no magma material attached (gales_asm_set_magma)");
+  CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t st = (cudaStream_t)stream;
+  const double* dI = I;
+  if (!is_device_ptr(I)) {
+    CK(h, h->s_I.alloc(h->n_rows), "staging I");
+    CK(h, cudaMemcpyAsync(h->s_I.p, I, (size_t)h->n_rows * sizeof(double), cudaMemcpyHostToDevice, st), "copy I");
+    dI = h->s_I.p;
+  }
+  const int64_t n = h->n_nodes, nf = 2 * h->nc + 6;
+  const bool dev_out = is_device_ptr(out);
+  double* dout = out;
+  if (!dev_out) {
+    CK(h, h->s_aux.alloc(std::max<int64_t>(nf * n, 1)), "staging output");
+    dout = h->s_aux.p;
+  }
+  KParams k = base_params(h, 1.0);
+  k.I = dI;
+  if (h->mg) {  // magma lookups report through the status word
+    CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
+    CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
+  }
+  LaunchResult r = h->mops.fractions(k, h->nc, dout, n, st);
+  if (r.err != cudaSuccess) return cuda_fail(h, r.err, "magma fractions kernel");
+  h->launches += r.launches;
+  if (!dev_out)
+    CK(h, cudaMemcpyAsync(out, dout, (size_t)(nf * n) * sizeof(double), cudaMemcpyDeviceToHost, st), "copy output");
+  return finish(h, st);
 }
 
 int gales_pressure_profile(const gales_material_desc* mat, double p0, double h, int32_t n_steps, const double* T,

@@ -38,6 +38,7 @@ struct KParams {
   double W_in, W_bd;
   int32_t tau, dc_2006, steady;
   int32_t has_gas;             // some component is an ideal gas (mixed-form EOS)
+  const magma_mix::DevMagma* mg;  // magma sub-mixtures (kernels compiled with kEosMagma)
   int32_t n_sides, n_side_nodes, n_side_q;
   uint32_t dirichlet_mask[GALES_MAX_FLAGS];
   double sgp[6][4][3];
@@ -420,7 +421,7 @@ __device__ __noinline__ double compute_h_reference(const double* __restrict__ I,
 //   GALES_FORM_MIXED: FP64 for the mixture EOS and its derivatives, U - U_P, the
 //                     element size h and tau with the closed-form DUDY inverse; the
 //                     fluxes, least-squares residual and dc viscosity in FP32.
-template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, int BP>
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, int BP, int EOS = kEosChemicals>
 __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<QP<DIM, NEN, NC, S>, BP>& out) {
   using L = Layout<DIM, NC>;
   using QPT = QP<DIM, NEN, NC, S>;
@@ -588,11 +589,22 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
   double v_nrm, iv = 0.0;
   if constexpr (FORM == GALES_FORM_FP64) {
     assign<DIM, NC>(Pq, p, v, T, Y);
-    double rhoP, cvP;
-    mixture_rho_cv<NC>(k.ch, p, T, Y, rhoP, cvP);
-    conservative<DIM, NC>(rhoP, cvP, v, T, Y, UP);
-    assign<DIM, NC>(Iq, p, v, T, Y);
-    mixture<NC>(k.ch, p, T, Y, pr);
+    if constexpr (EOS == kEosMagma) {
+      // props at P with shear rate 0 (fluid_2d.hpp:186), at I with the point's shear
+      // rate (fluid_2d.hpp:193-194)
+      Props<NC> prP;
+      unsigned st = magma_mixture<NC>(k.mg, p, T, Y, 0.0, prP);
+      conservative<DIM, NC>(prP.rho, prP.cv, v, T, Y, UP);
+      assign<DIM, NC>(Iq, p, v, T, Y);
+      st |= magma_mixture<NC>(k.mg, p, T, Y, shear_rate<DIM>(dv), pr);
+      if (st) flag_error(k, GALES_ERR_MAGMA, e);
+    } else {
+      double rhoP, cvP;
+      mixture_rho_cv<NC>(k.ch, p, T, Y, rhoP, cvP);
+      conservative<DIM, NC>(rhoP, cvP, v, T, Y, UP);
+      assign<DIM, NC>(Iq, p, v, T, Y);
+      mixture<NC>(k.ch, p, T, Y, pr);
+    }
     make_coef<DIM, NC>(pr, p, v, T, Y, c);
     conservative<DIM, NC>(pr.rho, pr.cv, v, T, Y, U);
     v_nrm = sqrt(vsq<DIM>(v));
@@ -601,7 +613,19 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
     assign<DIM, NC>(Pq, pP, vP, TP, YP);
     assign<DIM, NC>(Iq, p, v, T, Y);
     double rhoP, cvP;
-    mixture_pair_fast<NC>(k.ch, k.has_gas != 0, pP, TP, YP, p, T, Y, rhoP, cvP, pr);
+    if constexpr (EOS == kEosMagma) {
+      Props<NC> prP;
+      unsigned st = magma_mixture<NC>(k.mg, pP, TP, YP, 0.0, prP);
+      st |= magma_mixture<NC>(k.mg, p, T, Y, shear_rate<DIM>(dv), pr);
+      if (st) flag_error(k, GALES_ERR_MAGMA, e);
+      rhoP = prP.rho;
+      cvP = prP.cv;
+      pr.irho = 1.0 / pr.rho;
+#pragma unroll
+      for (int i = 0; i < NC; ++i) pr.irho_c[i] = 1.0 / pr.rho_c[i];
+    } else {
+      mixture_pair_fast<NC>(k.ch, k.has_gas != 0, pP, TP, YP, p, T, Y, rhoP, cvP, pr);
+    }
     conservative<DIM, NC>(rhoP, cvP, vP, TP, YP, UP);
     double vv = v[0] * v[0];
 #pragma unroll
@@ -715,7 +739,8 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
       for (int d = 0; d < DIM; ++d) td[1 + d] = tm;
       td[L::iT] = fmin(use, hh12 * rho * cv * mu * imk);
 #pragma unroll
-      for (int i = 0; i < NC - 1; ++i) td[L::iY + i] = fmin(use, hh12 * k.ch[i].inv_D);
+      for (int i = 0; i < NC - 1; ++i)
+        td[L::iY + i] = fmin(use, hh12 * (EOS == kEosMagma ? 1.0 / pr.D_c[i] : k.ch[i].inv_D));
       nondiag = true;
     } else if (k.tau == GALES_TAU_NON_DIAG_COMP_2019) {
       double use;
@@ -1038,7 +1063,7 @@ __device__ __forceinline__ double widen(double d) { return d; }
 // point record of that point to a chunk buffer (L2-resident).  The mixed form is
 // held to 128 registers (4 CTAs per SM): more warps hide the FP64 latency better
 // than the spilled values cost.
-template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, int EOS = kEosChemicals>
 __device__ __forceinline__ void point_block(const KParams& k, QP<DIM, NEN, NC, S>* __restrict__ out, long long first,
                                             long long n, int bid) {
   // chunk-local indices fit 32 bits (a chunk is one wave of CTAs); 64-bit shifts and
@@ -1054,13 +1079,20 @@ __device__ __forceinline__ void point_block(const KParams& k, QP<DIM, NEN, NC, S
   constexpr int RW = RecOut<QPT, BP>::RW;
   const int blk = t / BP;
   const RecOut<QPT, BP> o{reinterpret_cast<S*>(out) + (size_t)blk * (size_t)(RW * BP), t - blk * BP};
-  point_phase<DIM, NEN, NC, NQ, FORM, S, BP>(k, e, iq, o);
+  point_phase<DIM, NEN, NC, NQ, FORM, S, BP, EOS>(k, e, iq, o);
 }
 
-template <int DIM, int NEN, int NC, int NQ, int FORM, typename S>
-__global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1) point_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ out,
+// Resident point-stage CTAs the register budget is set for: 4 for the mixed form with
+// the chemicals' EOS, 2 with the (out-of-line, register-hungry) magma EOS, 1 for FP64.
+template <int FORM, int EOS>
+constexpr int point_min_ctas() {
+  return FORM == GALES_FORM_MIXED ? (EOS == kEosMagma ? 2 : 4) : 1;
+}
+
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, int EOS = kEosChemicals>
+__global__ void __launch_bounds__(128, point_min_ctas<FORM, EOS>()) point_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ out,
                                                      long long first, long long n) {
-  point_block<DIM, NEN, NC, NQ, FORM, S>(k, out, first, n, (int)blockIdx.x);
+  point_block<DIM, NEN, NC, NQ, FORM, S, EOS>(k, out, first, n, (int)blockIdx.x);
 }
 
 // Interior pass, stage 2: element matrices.  Lane (b, r, g) owns row (b, r) of the
@@ -1519,14 +1551,14 @@ __device__ __forceinline__ void griddep_launch_dependents() {
 // the same schedule inside a CUDA graph (whose replay of a two-stream pipeline
 // overlapped the stages less).  Every matrix CTA shape is at most 128 threads; threads
 // beyond it leave at once.
-template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, bool WANT_M>
-__global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1)
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, bool WANT_M, int EOS = kEosChemicals>
+__global__ void __launch_bounds__(128, point_min_ctas<FORM, EOS>())
     interior_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ pt_out, long long pt_first, long long pt_n,
                     int pt_ctas, const QP<DIM, NEN, NC, S>* __restrict__ mx_in, long long mx_first, long long mx_n) {
   static_assert(MatShape<DIM, NEN, NC>::CTA <= 128, "matrix CTA fits the 128-thread launch");
   if ((int)blockIdx.x < pt_ctas) {
     griddep_launch_dependents();
-    point_block<DIM, NEN, NC, NQ, FORM, S>(k, pt_out, pt_first, pt_n, (int)blockIdx.x);
+    point_block<DIM, NEN, NC, NQ, FORM, S, EOS>(k, pt_out, pt_first, pt_n, (int)blockIdx.x);
     return;
   }
   if ((int)threadIdx.x >= MatShape<DIM, NEN, NC>::CTA) return;
@@ -1545,7 +1577,7 @@ __global__ void __launch_bounds__(128, FORM == GALES_FORM_MIXED ? 4 : 1)
 // sqrt(|v|^2 + 1.5 c^2 + c sqrt(16|v|^2 + c^2)) in 2D, sqrt(|v|^2 + 2 c^2 +
 // c sqrt(4|v|^2 + c^2)) in 3D), use = 2 max(2 mu/rho, kappa/(rho cv))/h^2 + v_tau/h and
 // CFL/use.  dt_el[e] = the first smallest of the element's values (min_element).
-template <int DIM, int NEN, int NC, int NQ>
+template <int DIM, int NEN, int NC, int NQ, int EOS = kEosChemicals>
 __global__ void __launch_bounds__(128) adaptive_dt_kernel(const KParams k, double cfl, double* __restrict__ dt_el,
                                                           long long n) {
   using L = Layout<DIM, NC>;
@@ -1582,7 +1614,11 @@ __global__ void __launch_bounds__(128) adaptive_dt_kernel(const KParams k, doubl
     double p, v[DIM], T, Y[NC];
     assign<DIM, NC>(Iq, p, v, T, Y);
     Props<NC> pr;
-    mixture<NC>(k.ch, p, T, Y, pr);
+    if constexpr (EOS == kEosMagma) {  // shear rate 0 (adaptive_time_step.hpp:197, 226)
+      if (magma_mixture<NC>(k.mg, p, T, Y, 0.0, pr)) flag_error(k, GALES_ERR_MAGMA, e);
+    } else {
+      mixture<NC>(k.ch, p, T, Y, pr);
+    }
     const double v_nrm = sqrt(vsq<DIM>(v));
     double dtg;
     if (v_nrm < kEps) {
@@ -1615,7 +1651,7 @@ __global__ void __launch_bounds__(128) adaptive_dt_kernel(const KParams k, doubl
 // the mixture properties of every node's state at shear rate 0, written word-major:
 // out[f * n + node] for f = rho, mu, cp, cv, alpha, beta, kappa, sound speed (the
 // order of 146-153).  FP64 with the reference's operations (FP64 units).
-template <int DIM, int NC>
+template <int DIM, int NC, int EOS = kEosChemicals>
 __global__ void __launch_bounds__(128) secondary_dofs_kernel(const KParams k, double* __restrict__ out, long long n) {
   using L = Layout<DIM, NC>;
   const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
@@ -1626,10 +1662,35 @@ __global__ void __launch_bounds__(128) secondary_dofs_kernel(const KParams k, do
   double p, v[DIM], T, Y[NC];
   assign<DIM, NC>(w, p, v, T, Y);
   Props<NC> pr;
-  mixture<NC>(k.ch, p, T, Y, pr);
+  if constexpr (EOS == kEosMagma) {  // shear rate 0 (secondary_dofs.hpp:85)
+    if (magma_mixture<NC>(k.mg, p, T, Y, 0.0, pr)) flag_error(k, GALES_ERR_MAGMA, i);
+  } else {
+    mixture<NC>(k.ch, p, T, Y, pr);
+  }
   const double f[8] = {pr.rho, pr.mu, pr.cp, pr.cv, pr.alpha, pr.beta, pr.kappa, pr.c};
 #pragma unroll
   for (int q = 0; q < 8; ++q) out[q * n + i] = f[q];
+}
+
+// The magma gas fractions of secondary_dofs::execute (pp_vf_g, secondary_dofs.hpp:
+// 113-131) at every node, shear rate 0, written word-major: out[f * n + node] for
+// f = vf_g_comp_c, vf_comp_c (c = 0..NC-1, interleaved), then vf_g_on_total,
+// vf_h2o_g_on_total, vf_co2_g_on_total, wf_g_on_total, wf_h2o_g_on_total,
+// wf_co2_g_on_total.  FP64 with the reference's operations (magma units).
+template <int DIM, int NC>
+__global__ void __launch_bounds__(128) magma_fractions_kernel(const KParams k, double* __restrict__ out, long long n) {
+  using L = Layout<DIM, NC>;
+  const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
+  if (i >= n) return;
+  double w[L::ND];
+#pragma unroll
+  for (int j = 0; j < L::ND; ++j) w[j] = __ldg(k.I + i * L::ND + j);
+  double p, v[DIM], T, Y[NC];
+  assign<DIM, NC>(w, p, v, T, Y);
+  double f[2 * NC + 6];
+  if (magma_mix::mix_fractions(k.mg, NC, p, T, Y, f)) flag_error(k, GALES_ERR_MAGMA, i);
+#pragma unroll
+  for (int q = 0; q < 2 * NC + 6; ++q) out[q * n + i] = f[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -1713,10 +1774,10 @@ struct BoundarySmem {
 // Boundary point physics (fluid_2d.hpp:341-349, 610-817) at one side point with
 // the given geometry (shape values, gradients, JN W_bd): the coefficients, shape data
 // and the boundary residual rb = sum_k (F_adv,k - F_dif,k) JNxW_k, in FP64.
-template <int DIM, int NEN, int NC, typename S>
+template <int DIM, int NEN, int NC, typename S, int EOS = kEosChemicals>
 __device__ __forceinline__ void bpoint_phase(const KParams& k, const int* nodes, int flag, const double* sh,
                                              const double (&ds)[DIM][NEN], const double* JNxW,
-                                             BPoint<DIM, NEN, NC, S>& P) {
+                                             BPoint<DIM, NEN, NC, S>& P, long long e) {
   using L = Layout<DIM, NC>;
   constexpr int ND = L::ND;
   const gales_side_bc& bc = k.side_bc[flag < GALES_MAX_FLAGS ? flag : 0];
@@ -1753,7 +1814,16 @@ __device__ __forceinline__ void bpoint_phase(const KParams& k, const int* nodes,
   double p, v[DIM], T, Y[NC];
   assign<DIM, NC>(Iq, p, v, T, Y);
   Props<NC> pr;
-  mixture<NC>(k.ch, p, T, Y, pr);
+  if constexpr (EOS == kEosMagma) {  // the side point's shear rate (fluid_2d.hpp:234-235)
+    double dv[DIM][DIM];
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) dv[a][d] = dI[d][1 + a];
+    if (magma_mixture<NC>(k.mg, p, T, Y, shear_rate<DIM>(dv), pr)) flag_error(k, GALES_ERR_MAGMA, e);
+  } else {
+    mixture<NC>(k.ch, p, T, Y, pr);
+  }
   Coef<DIM, NC> c;
   make_coef<DIM, NC>(pr, p, v, T, Y, c);
   if constexpr (sizeof(S) == 4) P.c = narrow<DIM, NC>(c);
@@ -1880,7 +1950,7 @@ __global__ void __launch_bounds__(128) bgeo_kernel(const KParams k, BGeo<DIM, NE
 }
 
 // Boundary pass, stage 1: one thread per flagged side point writes its point record.
-template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
+template <int DIM, int NEN, int NC, int NS, int NSQ, typename S, int EOS = kEosChemicals>
 __global__ void __launch_bounds__(128) bpoint_kernel(const KParams k) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= k.n_bpt) return;
@@ -1900,7 +1970,7 @@ __global__ void __launch_bounds__(128) bpoint_kernel(const KParams k) {
 #pragma unroll
   for (int d = 0; d < DIM; ++d) JN[d] = g.JNxW[d];
   BPoint<DIM, NEN, NC, S> P;
-  bpoint_phase<DIM, NEN, NC, S>(k, nodes, (int)k.bd_sides[li * NS + ip / NSQ], sh, ds, JN, P);
+  bpoint_phase<DIM, NEN, NC, S, EOS>(k, nodes, (int)k.bd_sides[li * NS + ip / NSQ], sh, ds, JN, P, e);
   reinterpret_cast<BPoint<DIM, NEN, NC, S>*>(k.bpt_rec)[t] = P;
 }
 
@@ -1910,7 +1980,7 @@ __global__ void __launch_bounds__(128) bpoint_kernel(const KParams k) {
 // matrix type S and accumulate
 //   m_ba += N_b (N_a BA - sum_l dN_a/dx_l BK_l)                 (fluid_2d.hpp:351-363)
 // before the element's own Dirichlet pass and scatter (fluid_assembly.hpp:57-63).
-template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
+template <int DIM, int NEN, int NC, int NS, int NSQ, typename S, int EOS = kEosChemicals>
 __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   using L = Layout<DIM, NC>;
   constexpr int ND = L::ND;
@@ -1959,7 +2029,7 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
       double JNxW[DIM];
 #pragma unroll
       for (int d = 0; d < DIM; ++d) JNxW[d] = q.JN[d] * k.W_bd;
-      bpoint_phase<DIM, NEN, NC, S>(k, nodes, flag, q.sh, q.ds, JNxW, P);
+      bpoint_phase<DIM, NEN, NC, S, EOS>(k, nodes, flag, q.sh, q.ds, JNxW, P, e);
     }
   }
   __syncwarp();

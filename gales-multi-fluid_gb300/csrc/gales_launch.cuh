@@ -15,7 +15,7 @@ struct LaunchResult {
   int launches;
 };
 
-template <int DIM, int NEN, int NC, int NQ, int FORM>
+template <int DIM, int NEN, int NC, int NQ, int FORM, int EOS = kEosChemicals>
 struct InteriorInst {
   using S = typename std::conditional<FORM == GALES_FORM_FP64, double, float>::type;
   using Rec = QP<DIM, NEN, NC, S>;
@@ -25,7 +25,7 @@ struct InteriorInst {
   // resident point-kernel CTAs (128 threads) per SM
   static int point_occupancy() {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, point_kernel<DIM, NEN, NC, NQ, FORM, S>, 128, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, point_kernel<DIM, NEN, NC, NQ, FORM, S, EOS>, 128, 0) !=
         cudaSuccess)
       return 1;
     return nb > 0 ? nb : 1;
@@ -33,7 +33,7 @@ struct InteriorInst {
   static LaunchResult point(const KParams& k, void* buf, long long first, long long n, cudaStream_t st) {
     if (n <= 0) return {cudaSuccess, 0};
     const long long threads = n * NQ;
-    point_kernel<DIM, NEN, NC, NQ, FORM, S><<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(
+    point_kernel<DIM, NEN, NC, NQ, FORM, S, EOS><<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(
         k, reinterpret_cast<Rec*>(buf), first, n);
     return {cudaGetLastError(), 1};
   }
@@ -47,10 +47,10 @@ struct InteriorInst {
     e = cudaFuncSetAttribute(matrix_kernel<DIM, NEN, NC, NQ, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(interior_kernel<DIM, NEN, NC, NQ, FORM, S, true>,
+    e = cudaFuncSetAttribute(interior_kernel<DIM, NEN, NC, NQ, FORM, S, true, EOS>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(interior_kernel<DIM, NEN, NC, NQ, FORM, S, false>,
+    return cudaFuncSetAttribute(interior_kernel<DIM, NEN, NC, NQ, FORM, S, false, EOS>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   }
   // point stage of pt_n elements into pt_buf and matrix stage of mx_n elements from
@@ -74,10 +74,10 @@ struct InteriorInst {
     const Rec* mi = reinterpret_cast<const Rec*>(mx_buf);
     const int pc = (int)pt_ctas;
     cudaError_t e = want_m
-        ? cudaLaunchKernelEx(&cfg, interior_kernel<DIM, NEN, NC, NQ, FORM, S, true>, k, po, pt_first, pt_n, pc, mi,
-                             mx_first, mx_n)
-        : cudaLaunchKernelEx(&cfg, interior_kernel<DIM, NEN, NC, NQ, FORM, S, false>, k, po, pt_first, pt_n, pc, mi,
-                             mx_first, mx_n);
+        ? cudaLaunchKernelEx(&cfg, interior_kernel<DIM, NEN, NC, NQ, FORM, S, true, EOS>, k, po, pt_first, pt_n, pc,
+                             mi, mx_first, mx_n)
+        : cudaLaunchKernelEx(&cfg, interior_kernel<DIM, NEN, NC, NQ, FORM, S, false, EOS>, k, po, pt_first, pt_n, pc,
+                             mi, mx_first, mx_n);
     return {e != cudaSuccess ? e : cudaGetLastError(), 1};
   }
   static LaunchResult matrix(const KParams& k, bool want_m, const void* buf, long long first, long long n,
@@ -92,24 +92,25 @@ struct InteriorInst {
   }
 };
 
-template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
+template <int DIM, int NEN, int NC, int NS, int NSQ, typename S, int EOS = kEosChemicals>
 cudaError_t prepare_boundary_nc() {
-  return cudaFuncSetAttribute(boundary_kernel<DIM, NEN, NC, NS, NSQ, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(boundary_kernel<DIM, NEN, NC, NS, NSQ, S, EOS>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)sizeof(BoundarySmem<DIM, NEN, NC, NS, NSQ, S>));
 }
 
 // Boundary pass: with point records (k.bpt_rec) the point stage runs first, one thread
 // per flagged side point; the element stage then reads the records.
-template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
+template <int DIM, int NEN, int NC, int NS, int NSQ, typename S, int EOS = kEosChemicals>
 LaunchResult launch_boundary_nc(const KParams& k, long long n_items, cudaStream_t st) {
   if (n_items == 0) return {cudaSuccess, 0};
   int launches = 0;
   if (k.bpt_rec && k.n_bpt > 0) {
-    bpoint_kernel<DIM, NEN, NC, NS, NSQ, S><<<(unsigned)((k.n_bpt + 127) / 128), 128, 0, st>>>(k);
+    bpoint_kernel<DIM, NEN, NC, NS, NSQ, S, EOS><<<(unsigned)((k.n_bpt + 127) / 128), 128, 0, st>>>(k);
     ++launches;
   }
   const size_t smem = sizeof(BoundarySmem<DIM, NEN, NC, NS, NSQ, S>);
-  boundary_kernel<DIM, NEN, NC, NS, NSQ, S><<<(unsigned)n_items, 32, smem, st>>>(k);
+  boundary_kernel<DIM, NEN, NC, NS, NSQ, S, EOS><<<(unsigned)n_items, 32, smem, st>>>(k);
   return {cudaGetLastError(), launches + 1};
 }
 
@@ -135,35 +136,35 @@ struct InteriorOps {
     default: break;                    \
   }
 
-template <int DIM, int NEN, int NQ, int FORM>
+template <int DIM, int NEN, int NQ, int FORM, int EOS = kEosChemicals>
 struct InteriorDispatch {
   static cudaError_t prepare(int nc) {
-#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::prepare()
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM, EOS>::prepare()
     GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
     return cudaErrorInvalidValue;
   }
   static int point_occupancy(int nc) {
-#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::point_occupancy()
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM, EOS>::point_occupancy()
     GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
     return 1;
   }
   static size_t rec_bytes(int nc) {
-#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::rec_bytes()
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM, EOS>::rec_bytes()
     GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
     return 0;
   }
   static LaunchResult point(const KParams& k, int nc, void* buf, long long first, long long n, cudaStream_t st) {
-#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::point(k, buf, first, n, st)
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM, EOS>::point(k, buf, first, n, st)
     GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
     return {cudaErrorInvalidValue, 0};
   }
   static LaunchResult matrix(const KParams& k, int nc, bool want_m, const void* buf, long long first, long long n,
                              cudaStream_t st) {
-#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM>::matrix(k, want_m, buf, first, n, st)
+#define GALES_C(NC) return InteriorInst<DIM, NEN, NC, NQ, FORM, EOS>::matrix(k, want_m, buf, first, n, st)
     GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
     return {cudaErrorInvalidValue, 0};
@@ -172,7 +173,7 @@ struct InteriorDispatch {
                                long long pt_n, const void* mx_buf, long long mx_first, long long mx_n, bool pdl,
                                cudaStream_t st) {
 #define GALES_C(NC)                                                                                              \
-  return InteriorInst<DIM, NEN, NC, NQ, FORM>::interior(k, want_m, pt_buf, pt_first, pt_n, mx_buf, mx_first, mx_n, \
+  return InteriorInst<DIM, NEN, NC, NQ, FORM, EOS>::interior(k, want_m, pt_buf, pt_first, pt_n, mx_buf, mx_first, mx_n, \
                                                         pdl, st)
     GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
@@ -183,27 +184,27 @@ struct InteriorDispatch {
 
 // Boundary pass of one element type; S is the matrix arithmetic type of the form.
 // n < 0 only prepares the kernel (shared-memory limit) and launches nothing.
-template <int DIM, int NEN, int NS, int NSQ, typename S>
+template <int DIM, int NEN, int NS, int NSQ, typename S, int EOS = kEosChemicals>
 LaunchResult boundary_dispatch(const KParams& k, int nc, long long n, cudaStream_t st) {
   if (n < 0) {
-#define GALES_C(NC) return {prepare_boundary_nc<DIM, NEN, NC, NS, NSQ, S>(), 0}
+#define GALES_C(NC) return {prepare_boundary_nc<DIM, NEN, NC, NS, NSQ, S, EOS>(), 0}
     GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
     return {cudaErrorInvalidValue, 0};
   }
-#define GALES_C(NC) return launch_boundary_nc<DIM, NEN, NC, NS, NSQ, S>(k, n, st)
+#define GALES_C(NC) return launch_boundary_nc<DIM, NEN, NC, NS, NSQ, S, EOS>(k, n, st)
   GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
   return {cudaErrorInvalidValue, 0};
 }
 
 // Adaptive time step (f_mc) per element of one element type.
-template <int DIM, int NEN, int NQ>
+template <int DIM, int NEN, int NQ, int EOS = kEosChemicals>
 LaunchResult adaptive_dt_dispatch(const KParams& k, int nc, double cfl, double* dt_el, long long n, cudaStream_t st) {
   if (n <= 0) return {cudaSuccess, 0};
   const unsigned blocks = (unsigned)((n + 127) / 128);
 #define GALES_C(NC)                                                                       \
-  adaptive_dt_kernel<DIM, NEN, NC, NQ><<<blocks, 128, 0, st>>>(k, cfl, dt_el, n); \
+  adaptive_dt_kernel<DIM, NEN, NC, NQ, EOS><<<blocks, 128, 0, st>>>(k, cfl, dt_el, n); \
   return {cudaGetLastError(), 1}
   GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
@@ -211,17 +212,39 @@ LaunchResult adaptive_dt_dispatch(const KParams& k, int nc, double cfl, double* 
 }
 
 // Secondary variables at the nodes (any element type of the dimension).
-template <int DIM>
+template <int DIM, int EOS = kEosChemicals>
 LaunchResult secondary_dofs_dispatch(const KParams& k, int nc, double* out, long long n, cudaStream_t st) {
   if (n <= 0) return {cudaSuccess, 0};
   const unsigned blocks = (unsigned)((n + 127) / 128);
 #define GALES_C(NC)                                                            \
-  secondary_dofs_kernel<DIM, NC><<<blocks, 128, 0, st>>>(k, out, n); \
+  secondary_dofs_kernel<DIM, NC, EOS><<<blocks, 128, 0, st>>>(k, out, n); \
   return {cudaGetLastError(), 1}
   GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
   return {cudaErrorInvalidValue, 0};
 }
+
+// Magma gas fractions at the nodes (pp_vf_g).
+template <int DIM>
+LaunchResult magma_fractions_dispatch(const KParams& k, int nc, double* out, long long n, cudaStream_t st) {
+  if (n <= 0) return {cudaSuccess, 0};
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+#define GALES_C(NC)                                                            \
+  magma_fractions_kernel<DIM, NC><<<blocks, 128, 0, st>>>(k, out, n); \
+  return {cudaGetLastError(), 1}
+  GALES_NC_SWITCH(nc, GALES_C)
+#undef GALES_C
+  return {cudaErrorInvalidValue, 0};
+}
+
+// Every kernel of one element type compiled with the magma EOS (gales_<type>_magma.cu).
+struct MagmaOps {
+  InteriorOps interior[2];   // per form (FP64, mixed)
+  LaunchResult (*boundary)(const KParams&, int nc, int form, long long n, cudaStream_t);
+  LaunchResult (*adaptive_dt)(const KParams&, int nc, double cfl, double* dt_el, long long n, cudaStream_t);
+  LaunchResult (*secondary_dofs)(const KParams&, int nc, double* out, long long n, cudaStream_t);
+  LaunchResult (*fractions)(const KParams&, int nc, double* out, long long n, cudaStream_t);
+};
 
 // Boundary side-point geometry (handle creation) and record sizes.
 struct BoundaryInfo {
@@ -311,5 +334,12 @@ LaunchResult boundary_hex8_mixed(const KParams&, int nc, long long n, cudaStream
 GeometryOps geometry_ops_hex8();
 BoundaryInfo boundary_info_hex8(int nc);
 LaunchResult adaptive_dt_hex8(const KParams&, int nc, double cfl, double* dt_el, long long n, cudaStream_t);
+// The device array of a magma material's sub-mixtures, its count and its device
+// (gales_magma.cu).
+const magma_mix::DevMagma* magma_device_table(const gales_magma* m, int* nc, int* device);
+MagmaOps magma_ops_tri3();
+MagmaOps magma_ops_quad4();
+MagmaOps magma_ops_tet4();
+MagmaOps magma_ops_hex8();
 
 }  // namespace gales

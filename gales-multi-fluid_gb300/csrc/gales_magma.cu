@@ -56,6 +56,16 @@ struct gales_magma {
   std::string err;
 };
 
+namespace gales {
+
+const magma_mix::DevMagma* magma_device_table(const gales_magma* m, int* nc, int* device) {
+  *nc = m->nc;
+  *device = m->device;
+  return m->d_mg;
+}
+
+}  // namespace gales
+
 extern "C" {
 
 int gales_magma_create(const gales_magma_desc* comps, int32_t nb_comp, gales_magma** out) {

@@ -15,9 +15,9 @@
 #include "../../include/gales_asm.h"
 
 #ifdef __CUDACC__
-#define GALES_MAGMA_HD __host__ __device__
+#define GALES_MAGMA_HD __host__ __device__ inline
 #else
-#define GALES_MAGMA_HD
+#define GALES_MAGMA_HD inline
 #endif
 
 namespace magma_mix {
@@ -221,9 +221,11 @@ GALES_MAGMA_HD double giordano_mu(const DevMagma& g, double T, double wf_h2o_l, 
   return pow(10., P[0] + Bv / (T - Cv));
 }
 
-// magma_mixture::properties (mixtures.hpp:163-176, submix_of_comp 187-250)
+// magma_mixture::properties (mixtures.hpp:163-176, submix_of_comp 187-250).  fr
+// (optional): wf_ph_[g], wf_[3], wf_[4], vf_ph_[g], vf_[3], vf_[4] (mixtures.hpp:225-258),
+// the fractions secondary_dofs.hpp:113-131 reads.
 GALES_MAGMA_HD void magma_props(const DevMagma& g, double p, double T, double sr, Props& o, double& vf_gas,
-                            unsigned& st) {
+                            unsigned& st, double* fr = nullptr) {
   double wl1, wl2;
   if (g.n_T == 0) {
     wl1 = lookup_p(g, g.h2o_tab, p, st);
@@ -264,7 +266,16 @@ GALES_MAGMA_HD void magma_props(const DevMagma& g, double p, double T, double sr
   }
   double cs = sqrt(1. / ss);
   cs /= rho;
-  vf_gas = wf[3] * rho / ch[3].rho + wf[4] * rho / ch[4].rho;
+  const double vf3 = wf[3] * rho / ch[3].rho, vf4 = wf[4] * rho / ch[4].rho;
+  vf_gas = vf3 + vf4;
+  if (fr) {
+    fr[0] = 1.0 - wl_ph;
+    fr[1] = wf[3];
+    fr[2] = wf[4];
+    fr[3] = vf_gas;
+    fr[4] = vf3;
+    fr[5] = vf4;
+  }
   double mu = giordano_mu(g, T, wl1, wl2, st);
   if (g.gas_on_mu == GALES_GAS_MU_ISHII_ZUBER) {
     mu = mu / (1.0 - vf_gas);
@@ -352,6 +363,43 @@ GALES_MAGMA_HD unsigned mix_point(const DevMagma* mg, int nc, double p, double T
   f[5] = cs;
   f[6] = alpha;
   f[7] = beta;
+  return st;
+}
+
+// secondary_dofs::execute's gas fractions (pp_vf_g, secondary_dofs.hpp:56-131) at one
+// node (shear rate 0): out[2c] = vf_g_comp_c, out[2c + 1] = vf_comp_c for every magma c,
+// then vf_g_on_total, vf_h2o_g_on_total, vf_co2_g_on_total, wf_g_on_total,
+// wf_h2o_g_on_total, wf_co2_g_on_total (2 nc + 6 values).  Returns the status bits.
+GALES_MAGMA_HD unsigned mix_fractions(const DevMagma* mg, int nc, double p, double T, const double* Y,
+                                      double* out) {
+  unsigned st = 0;
+  double rho = 0.0, rho_c[GALES_MAX_COMP], fr[GALES_MAX_COMP][6];
+  for (int c = 0; c < nc; ++c) {
+    Props m;
+    double vfg;
+    magma_props(mg[c], p, T, 0.0, m, vfg, st, fr[c]);
+    rho += Y[c] / m.rho;
+    rho_c[c] = m.rho;
+  }
+  rho = 1.0 / rho;
+  double vf_g = 0.0, vf_h2o = 0.0, vf_co2 = 0.0, wf_g = 0.0, wf_h2o = 0.0, wf_co2 = 0.0;
+  for (int c = 0; c < nc; ++c) {
+    const double vf_comp = Y[c] * rho / rho_c[c];
+    out[2 * c] = fr[c][3] * vf_comp;
+    out[2 * c + 1] = vf_comp;
+    vf_g += fr[c][3] * vf_comp;
+    vf_h2o += fr[c][4] * vf_comp;
+    vf_co2 += fr[c][5] * vf_comp;
+    wf_g += fr[c][0] * Y[c];
+    wf_h2o += fr[c][1] * Y[c];
+    wf_co2 += fr[c][2] * Y[c];
+  }
+  out[2 * nc] = vf_g;
+  out[2 * nc + 1] = vf_h2o;
+  out[2 * nc + 2] = vf_co2;
+  out[2 * nc + 3] = wf_g;
+  out[2 * nc + 4] = wf_h2o;
+  out[2 * nc + 5] = wf_co2;
   return st;
 }
 

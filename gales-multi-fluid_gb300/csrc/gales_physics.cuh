@@ -13,6 +13,7 @@
 #include <cstdint>
 
 #include "../../include/gales_asm.h"
+#include "gales_magma.cuh"
 
 namespace gales {
 
@@ -207,6 +208,53 @@ __device__ __forceinline__ void mixture_pair_fast(const DevChem* ch, bool has_ga
   o.c = rsqrt(c2) * irho;
   o.alpha = rho * al;
   o.beta = rho * be;
+}
+
+// The equation of state a kernel instance is compiled for: the material's chemicals
+// (custom_chemical / ideal_gas, mix_of_ch) or a mixture of magma sub-mixtures
+// (mix_of_mix of magma_mix).  The chemical kernels are untouched by the magma ones.
+constexpr int kEosChemicals = 0;
+constexpr int kEosMagma = 1;
+
+// The mixture of magma sub-mixtures at one point (fluid_properties.hpp:171-200 over
+// magma_mixture::properties, mixtures.hpp:175-261), out of line: the evaluation (five
+// chemicals per magma, table lookups, Giordano viscosity, gas and crystal corrections)
+// is long, and one copy per kernel keeps the call sites small.  Returns the
+// GALES_MAGMA_* bits.
+static __device__ __noinline__ unsigned magma_point(const magma_mix::DevMagma* mg, int nc, double p, double T,
+                                                    const double* Y, double sr, double* f, double (*comp)[4]) {
+  return magma_mix::mix_point(mg, nc, p, T, Y, sr, f, comp);
+}
+
+// Props of the magma mixture; the mixture's own chemical diffusivity is not formed by
+// fluid_properties' mix_of_mix (it stays 0 there), the components' are kept in D_c.
+template <int NC>
+__device__ __forceinline__ unsigned magma_mixture(const magma_mix::DevMagma* mg, double p, double T, const double* Y,
+                                                  double sr, Props<NC>& o) {
+  double f[8], comp[NC][4];
+  const unsigned st = magma_point(mg, NC, p, T, Y, sr, f, comp);
+  o.rho = f[0]; o.mu = f[1]; o.cp = f[2]; o.cv = f[3]; o.kappa = f[4]; o.c = f[5]; o.alpha = f[6]; o.beta = f[7];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    o.rho_c[c] = comp[c][0];
+    o.e_c[c] = comp[c][1];
+    o.D_c[c] = comp[c][2];
+  }
+  return st;
+}
+
+// compute_shear_rate (non_newtonian.hpp:23-29 in 2D, 32-39 in 3D) from the velocity
+// gradient dv[i][j] = d v_i / d x_j; std::pow(x, 2) is the correctly rounded x*x.
+template <int DIM>
+__host__ __device__ __forceinline__ double shear_rate(const double (&dv)[DIM][DIM]) {
+  if constexpr (DIM == 2) {
+    const double a = dv[0][1] + dv[1][0];
+    return sqrt(dv[0][0] * dv[0][0] + dv[1][1] * dv[1][1] + 2 * (a * a));
+  } else {
+    const double a = dv[0][1] + dv[1][0], b = dv[0][2] + dv[2][0], c = dv[1][2] + dv[2][1];
+    return sqrt(dv[0][0] * dv[0][0] + dv[1][1] * dv[1][1] + dv[2][2] * dv[2][2] + 2 * (a * a) + 2 * (b * b) +
+                2 * (c * c));
+  }
 }
 
 // Only rho and cv (what U(P) needs); same operations as mixture().

@@ -1,0 +1,15 @@
+// Kernel instances for the quad4 element with the magma EOS, mixed form (dim 2, 4 nodes,
+// 4 interior points, 4 sides with 2 points each): interior pass and boundary pass.
+#include "gales_launch.cuh"
+
+namespace gales {
+
+InteriorOps interior_ops_quad4_magma_mixed() {
+  return InteriorDispatch<2, 4, 4, GALES_FORM_MIXED, kEosMagma>::ops();
+}
+
+LaunchResult boundary_quad4_magma_mixed(const KParams& k, int nc, long long n, cudaStream_t st) {
+  return boundary_dispatch<2, 4, 4, 2, float, kEosMagma>(k, nc, n, st);
+}
+
+}  // namespace gales

@@ -55,6 +55,9 @@ extern "C" {
 #define GALES_ERR_CUDA 16
 #define GALES_ERR_UNSUPPORTED 32
 #define GALES_ERR_NO_MEMORY 64
+#define GALES_ERR_MAGMA 128        /* a magma property outside its lookup tables or a zero
+                                      viscosity denominator (mixtures.hpp:342-412,
+                                      GiordanoEtAlViscosityModel.hpp; the reference stops) */
 
 /* numerical forms */
 #define GALES_FORM_FP64 0    /* every operation in FP64 (the reference's arithmetic) */
@@ -399,6 +402,25 @@ int gales_magma_properties(gales_magma* m, const double* p, const double* T, con
 int gales_magma_status(gales_magma* m);
 const char* gales_magma_last_error(gales_magma* m);
 void gales_magma_destroy(gales_magma* m);
+/* Attach magma mixtures as the assembly's material (m == NULL detaches them): from then
+ * on the handle's assembly, residual, frozen VJP, element blocks, adaptive time step and
+ * secondary variables evaluate every point's properties with fluid_properties'
+ * mix_of_mix of magma_mix (fluid_properties.hpp:171-200), at P with shear rate 0 and at
+ * I and the boundary points with the point's shear rate (fluid_2d.hpp:186, 193-194,
+ * 234-235; compute_shear_rate, non_newtonian.hpp:23-39), instead of the chemicals given
+ * at creation; u_ref_inv is recomputed from the magmas (fluid_2d.hpp:123-135).  The
+ * reference selects this with props.txt's "mix_of_mix" (fluid_properties_reader.hpp).
+ * m must have the handle's number of components, live on its device and outlive the
+ * attachment.  A point outside a magma's lookup tables sets GALES_ERR_MAGMA (the
+ * reference stops).  The exact VJP returns GALES_ERR_UNSUPPORTED while magmas are
+ * attached.  Call outside any stream capture. */
+int gales_asm_set_magma(gales_asm* h, gales_magma* m);
+/* The gas fractions of secondary_dofs::execute with pp_vf_g (secondary_dofs.hpp:56-131)
+ * at every node's state I (shear rate 0), with magmas attached: out[f * n_nodes + node]
+ * for f = vf_g_comp_c, vf_comp_c (c = 0..nb_comp-1, interleaved), then vf_g_on_total,
+ * vf_h2o_g_on_total, vf_co2_g_on_total, wf_g_on_total, wf_h2o_g_on_total,
+ * wf_co2_g_on_total: 2 nb_comp + 6 fields.  Host or device buffers. */
+int gales_asm_magma_fractions(gales_asm* h, const double* I, double* out, void* stream);
 
 /* Status of the last call: error bits and the first offending element (-1 if none). */
 int gales_asm_status(gales_asm* h, int64_t* first_bad_element);

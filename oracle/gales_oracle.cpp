@@ -36,7 +36,7 @@
 
 // magma mixtures replacing the chemicals (magma_oracle.cpp, gor_set_magma)
 bool gor_magma_active();
-int gor_magma_point(double p, double T, const double* Y, double* f, double (*comp)[3]);
+int gor_magma_point(double p, double T, const double* Y, double sr, double* f, double (*comp)[3]);
 
 namespace {
 
@@ -405,6 +405,21 @@ double compute_h(const Quad& q, int dim, const double* v, const double del_v[3][
   return h;
 }
 
+/* compute_shear_rate: non_newtonian.hpp:23-29 (2D), 32-39 (3D), from the gradients
+ * dI[k][j] = d I_j / d x_k (dI_dx, dI_dy, dI_dz); std::pow(x, 2) as written there. */
+double compute_shear_rate(int dim, const double dI[3][MD]) {
+  if (dim == 2) {
+    const double dv1_1 = dI[0][1], dv2_1 = dI[0][2];
+    const double dv1_2 = dI[1][1], dv2_2 = dI[1][2];
+    return std::sqrt(std::pow(dv1_1, 2) + std::pow(dv2_2, 2) + 2 * std::pow(dv1_2 + dv2_1, 2));
+  }
+  const double dv1_1 = dI[0][1], dv2_1 = dI[0][2], dv3_1 = dI[0][3];
+  const double dv1_2 = dI[1][1], dv2_2 = dI[1][2], dv3_2 = dI[1][3];
+  const double dv1_3 = dI[2][1], dv2_3 = dI[2][2], dv3_3 = dI[2][3];
+  return std::sqrt(std::pow(dv1_1, 2) + std::pow(dv2_2, 2) + std::pow(dv3_3, 2) + 2 * std::pow(dv1_2 + dv2_1, 2) +
+                   2 * std::pow(dv1_3 + dv3_1, 2) + 2 * std::pow(dv2_3 + dv3_2, 2));
+}
+
 /* ------------------------------------------------------------------------- */
 /* Properties: fluid_properties.hpp:199-227 (mix_of_ch), chemicals.hpp:43-47,
  * 258-264, base_mixture.hpp:50-65.                                            */
@@ -413,14 +428,16 @@ struct Props {
   double rho_c[GALES_MAX_COMP], e_c[GALES_MAX_COMP], D_c[GALES_MAX_COMP];
 };
 
-void properties(const gales_material_desc& mat, double p, double T, const double* Y, Props& o) {
+/* sr: the point's shear rate (non_newtonian.hpp:23-39); only magma viscosity models use
+ * it (custom and ideal-gas chemicals ignore it, chemicals.hpp:19-49, 198-271). */
+void properties(const gales_material_desc& mat, double p, double T, const double* Y, Props& o, double sr = 0.0) {
   const int nc = mat.nb_comp;
   o.rho = o.cv = o.cp = o.kappa = o.D = o.mu = o.c = o.alpha = o.beta = 0.0;
   if (gor_magma_active()) {
     // fluid_properties.hpp:171-200: mix_of_mix; the mixture's own chemical diffusivity
     // is not accumulated there and stays 0 from clear() (base_mixture.hpp:50-65)
     double f[8], cc[GALES_MAX_COMP][3];
-    gor_magma_point(p, T, Y, f, cc);
+    gor_magma_point(p, T, Y, sr, f, cc);
     o.rho = f[0]; o.mu = f[1]; o.cp = f[2]; o.cv = f[3]; o.kappa = f[4]; o.c = f[5];
     o.alpha = f[6]; o.beta = f[7];
     for (int c = 0; c < nc; ++c) {
@@ -1025,7 +1042,7 @@ int element_interior(const Ctx& cx, const double X[8][3], const double* Ie, cons
         dI[k][j] = a;
       }
     assign(cx, Iq, p, vel, T, Y);
-    properties(*cx.mat, p, T, Y, pr);
+    properties(*cx.mat, p, T, Y, pr, compute_shear_rate(dim, dI));   // fluid_2d.hpp:193-194
     Fluxes f;
     fluxes(cx, pr, p, vel, T, Y, dI, f);
     // Galerkin residual (fluid_2d.hpp:253-262)
@@ -1159,7 +1176,7 @@ int element_boundary(const Ctx& cx, const double X[8][3], const double* Ie, cons
       double p, vel[3] = {0, 0, 0}, T, Y[GALES_MAX_COMP];
       assign(cx, Iq, p, vel, T, Y);
       Props pr;
-      properties(*cx.mat, p, T, Y, pr);
+      properties(*cx.mat, p, T, Y, pr, compute_shear_rate(dim, dI));   // fluid_2d.hpp:234-235
       Fluxes f;
       fluxes_boundary(cx, pr, p, vel, T, Y, dI, bc, f);
       for (int b = 0; b < nen; ++b)
@@ -1253,6 +1270,14 @@ void side_table(const gales_mesh_desc& mesh, int nsides, std::vector<int32_t>& o
 }  // namespace
 
 extern "C" {
+
+/* compute_shear_rate at a point from dI[k][j] = d I_j / d x_k (3 x GALES_MAX_ND). */
+double gor_shear_rate(int dim, const double* dI) {
+  double g[3][MD];
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < MD; ++j) g[k][j] = dI[k * MD + j];
+  return compute_shear_rate(dim, g);
+}
 
 int gor_properties(const gales_material_desc* mat, double p, double T, const double* Y, double* out) {
   Props pr;

@@ -199,7 +199,9 @@ double interp2(double T, double p, const std::vector<double>& Tt, const std::vec
 }
 
 // status bits: 1 lookup out of range, 2 viscosity model division, 4 Pal 2003 not converged
-int magma_props(const Magma& g, double p, double T, double sr, Chem& o, double& vf_gas) {
+// fr (optional): the phase and chemical fractions secondary_dofs.hpp:113-131 reads,
+// wf_ph_[g], wf_[3], wf_[4], vf_ph_[g], vf_[3], vf_[4] (mixtures.hpp:225-258).
+int magma_props(const Magma& g, double p, double T, double sr, Chem& o, double& vf_gas, double* fr = nullptr) {
   int st = 0;
   bool ok = true;
   double wl[3];
@@ -248,6 +250,14 @@ int magma_props(const Magma& g, double p, double T, double sr, Chem& o, double& 
   double vf[5];
   for (int c = 0; c < 5; ++c) vf[c] = wf[c] * o.rho / ch[c].rho;
   vf_gas = vf[3] + vf[4];
+  if (fr) {
+    fr[0] = wg_ph;
+    fr[1] = wf[3];
+    fr[2] = wf[4];
+    fr[3] = vf_gas;
+    fr[4] = vf[3];
+    fr[5] = vf[4];
+  }
   double mu = 0.0;
   if (!g.visc.mu(T, wl[1], wl[2], mu)) st |= 2;
   if (g.gas_on_mu == GALES_GAS_MU_ISHII_ZUBER) {
@@ -323,18 +333,18 @@ std::vector<Magma> g_active;  // magmas that replace the chemicals in the assemb
 }  // namespace
 
 // Used by the assembly restatement (gales_oracle.cpp) when magmas are set: the mixture
-// of sub-mixtures at (p, T, Y) with shear rate 0, f = rho, mu, cp, cv, kappa, sound speed,
+// of sub-mixtures at (p, T, Y) with shear rate sr, f = rho, mu, cp, cv, kappa, sound speed,
 // alpha, beta; comp[c] = rho_c, cv_c T, D_c.  Returns the status bits.
 bool gor_magma_active() { return !g_active.empty(); }
 
-int gor_magma_point(double p, double T, const double* Y, double* f, double (*comp)[3]) {
+int gor_magma_point(double p, double T, const double* Y, double sr, double* f, double (*comp)[3]) {
   const int nc = (int)g_active.size();
   int st = 0;
   double rho = 0, mu = 0, cp = 0, cv = 0, kappa = 0, ss = 0;
   Chem m[GALES_MAX_COMP];
   for (int c = 0; c < nc; ++c) {
     double vfg = 0.0;
-    st |= magma_props(g_active[c], p, T, 0.0, m[c], vfg);
+    st |= magma_props(g_active[c], p, T, sr, m[c], vfg);
     rho += Y[c] / m[c].rho;
     mu += Y[c] * m[c].mu;
     cp += Y[c] * m[c].cp;
@@ -414,3 +424,37 @@ int gor_magma_properties(const gales_magma_desc* comps, int32_t nc, const double
 }
 
 }  // extern "C"
+
+// secondary_dofs::execute's gas fractions (pp_vf_g, secondary_dofs.hpp:56-131) at one
+// node's (p, T, Y) with the set magmas, shear rate 0: out[2c] = vf_g_comp_c,
+// out[2c + 1] = vf_comp_c for every magma c, then vf_g_on_total, vf_h2o_g_on_total,
+// vf_co2_g_on_total, wf_g_on_total, wf_h2o_g_on_total, wf_co2_g_on_total.
+extern "C" int gor_magma_fractions(double p, double T, const double* Y, double* out) {
+  const int nc = (int)g_active.size();
+  if (nc == 0) return -1;
+  int st = 0;
+  Chem m[GALES_MAX_COMP];
+  double fr[GALES_MAX_COMP][6];
+  double rho = 0.0;
+  for (int c = 0; c < nc; ++c) {
+    double vfg = 0.0;
+    st |= magma_props(g_active[c], p, T, 0.0, m[c], vfg, fr[c]);
+    rho += Y[c] / m[c].rho;   // fluid_properties.hpp:174, 185
+  }
+  rho = 1.0 / rho;
+  double vf_g = 0.0, vf_h2o = 0.0, vf_co2 = 0.0, wf_g = 0.0, wf_h2o = 0.0, wf_co2 = 0.0;
+  for (int c = 0; c < nc; ++c) {
+    const double vf_comp = Y[c] * rho / m[c].rho;
+    out[2 * c] = fr[c][3] * vf_comp;
+    out[2 * c + 1] = vf_comp;
+    vf_g += (fr[c][3]) * vf_comp;
+    vf_h2o += (fr[c][4]) * vf_comp;
+    vf_co2 += (fr[c][5]) * vf_comp;
+    wf_g += (fr[c][0]) * Y[c];
+    wf_h2o += (fr[c][1]) * Y[c];
+    wf_co2 += (fr[c][2]) * Y[c];
+  }
+  const double tot[6] = {vf_g, vf_h2o, vf_co2, wf_g, wf_h2o, wf_co2};
+  for (int k = 0; k < 6; ++k) out[2 * nc + k] = tot[k];
+  return st;
+}

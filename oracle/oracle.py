@@ -58,6 +58,10 @@ def lib() -> C.CDLL:
         L.gor_magma_properties.restype = C.c_int
         L.gor_set_magma.argtypes = [C.POINTER(abi.MagmaDesc), C.c_int32]
         L.gor_set_magma.restype = C.c_int
+        L.gor_shear_rate.argtypes = [C.c_int, dp]
+        L.gor_shear_rate.restype = C.c_double
+        L.gor_magma_fractions.argtypes = [C.c_double, C.c_double, dp, dp]
+        L.gor_magma_fractions.restype = C.c_int
         for f in ("gor_properties", "gor_inverse", "gor_quad", "gor_gauss", "gor_pattern", "gor_colouring",
                   "gor_element", "gor_assemble", "gor_adaptive_dt"):
             getattr(L, f).restype = C.c_int
@@ -262,6 +266,26 @@ class magma_material:
     def __exit__(self, *exc):
         lib().gor_set_magma(None, 0)
         return False
+
+
+def shear_rate(dim, dI):
+    """compute_shear_rate (non_newtonian.hpp:23-39) from dI[k][j] = dI_j/dx_k, shape
+    (3, GALES_MAX_ND)."""
+    dI = np.ascontiguousarray(dI, dtype=np.float64)
+    return float(lib().gor_shear_rate(int(dim), _d(dI)))
+
+
+def magma_fractions(p, T, Y):
+    """secondary_dofs::execute's gas fractions (pp_vf_g, secondary_dofs.hpp:56-131) with
+    the magmas set by magma_material, at points (p[i], T[i], Y[i, :]): (2 nc + 6, n)."""
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    n, nc = Y.shape
+    out = np.zeros((n, 2 * nc + 6))
+    for i in range(n):
+        st = lib().gor_magma_fractions(float(p[i]), float(T[i]), _d(Y[i]), _d(out[i]))
+        if st < 0:
+            raise RuntimeError("no magma material set")
+    return out.T.copy()
 
 
 def pressure_profile(material, p0, h, T, T1, Y, Y1):

@@ -27,3 +27,24 @@ extern "C" int magma_host_properties(const gales_magma_desc* comps, int32_t nc, 
   }
   return (int)st;
 }
+
+// secondary_dofs' gas fractions (mix_fractions) at n points: out[k * n + i], 2 nc + 6 fields.
+extern "C" int magma_host_fractions(const gales_magma_desc* comps, int32_t nc, const double* p, const double* T,
+                                    const double* Y, int64_t n, double* out) {
+  std::vector<DevMagma> mg(nc);
+  for (int c = 0; c < nc; ++c) {
+    build_constants(comps[c], mg[c]);
+    mg[c].p_tab = comps[c].p_table;
+    mg[c].T_tab = comps[c].n_T > 0 ? comps[c].T_table : nullptr;
+    mg[c].h2o_tab = comps[c].wf_l_h2o;
+    mg[c].co2_tab = comps[c].wf_l_co2;
+  }
+  unsigned st = 0;
+  const int nf = 2 * nc + 6;
+  for (int64_t i = 0; i < n; ++i) {
+    double f[2 * GALES_MAX_COMP + 6];
+    st |= mix_fractions(mg.data(), nc, p[i], T[i], Y + i * nc, f);
+    for (int k = 0; k < nf; ++k) out[k * n + i] = f[k];
+  }
+  return (int)st;
+}

@@ -50,6 +50,8 @@ def host_lib(tmp_path_factory):
     dp = C.POINTER(C.c_double)
     L.magma_host_properties.argtypes = [C.POINTER(gm.abi.MagmaDesc), C.c_int32, dp, dp, dp, dp, C.c_int64, dp, dp]
     L.magma_host_properties.restype = C.c_int
+    L.magma_host_fractions.argtypes = [C.POINTER(gm.abi.MagmaDesc), C.c_int32, dp, dp, dp, C.c_int64, dp]
+    L.magma_host_fractions.restype = C.c_int
     return L
 
 
@@ -72,6 +74,46 @@ def test_kernel_code_equals_oracle_on_host(gas, crystal, cf, n_T, host_lib):
     o2, c2, s2 = oracle.magma_properties(comps, p, T, Y, shear)
     assert s1 == s2 == 0
     assert np.array_equal(o1, o2, equal_nan=True) and np.array_equal(c1, c2, equal_nan=True)
+
+
+@pytest.mark.parametrize("n_T", [0, 7])
+def test_gas_fractions_kernel_code_equals_oracle(n_T, host_lib):
+    """secondary_dofs' pp_vf_g fractions (secondary_dofs.hpp:113-131): the kernel's code on
+    the host equals the oracle bit for bit, and the totals agree with the mixture's own
+    outputs (vf_g_on_total = sum_c Y_c rho / rho_c vf_gas_c)."""
+    comps = syn.magma_pair(n_T=n_T)
+    p, T, Y, _ = _points()
+    n, nc = len(p), len(comps)
+    got = np.zeros((2 * nc + 6, n))
+    d = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    Yc = np.ascontiguousarray(Y)
+    st = host_lib.magma_host_fractions(magma.descs(comps), nc, d(p), d(T), d(Yc), n, d(got))
+    with oracle.magma_material(comps):
+        ref = oracle.magma_fractions(p, T, Y)
+    assert st == 0 and np.array_equal(got, ref)
+    out, comp, _ = oracle.magma_properties(comps, p, T, Y)
+    vf = sum(Y[:, c] * out[0] / comp[c, 0] * comp[c, 3] for c in range(nc))
+    np.testing.assert_allclose(ref[2 * nc], vf, rtol=1e-13)
+    np.testing.assert_allclose(ref[2 * nc], ref[2 * nc + 1] + ref[2 * nc + 2], rtol=1e-12)
+    assert np.all((ref[2 * nc + 3] > 0) & (ref[2 * nc + 3] < 1))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_shear_rate_formula(dim):
+    """compute_shear_rate (non_newtonian.hpp:23-29, 32-39), which the magma viscosity
+    models read at I and at the boundary points: sqrt(u_x^2 + v_y^2 (+ w_z^2)
+    + 2 (u_y + v_x)^2 (+ 2 (u_z + w_x)^2 + 2 (v_z + w_y)^2)), from dI[k][j] = dI_j/dx_k."""
+    rng = np.random.default_rng(dim)
+    for _ in range(20):
+        dI = np.zeros((3, gm.abi.MAX_ND))
+        dI[:dim, :] = rng.normal(size=(dim, gm.abi.MAX_ND))
+        g = dI[:dim, 1:1 + dim].T          # g[i][j] = d v_i / d x_j
+        if dim == 2:
+            ref = np.sqrt(g[0, 0] ** 2 + g[1, 1] ** 2 + 2 * (g[0, 1] + g[1, 0]) ** 2)
+        else:
+            ref = np.sqrt(g[0, 0] ** 2 + g[1, 1] ** 2 + g[2, 2] ** 2 + 2 * (g[0, 1] + g[1, 0]) ** 2
+                          + 2 * (g[0, 2] + g[2, 0]) ** 2 + 2 * (g[1, 2] + g[2, 1]) ** 2)
+        assert oracle.shear_rate(dim, dI) == pytest.approx(ref, rel=1e-15)
 
 
 def test_physical_consistency():
