@@ -33,6 +33,7 @@ CH_CUSTOM = 0
 CH_IDEAL_GAS = 1
 TAU_NONE = 0
 MAGMA_LOOKUP_RANGE, MAGMA_VISCOSITY, MAGMA_PAL_ITER = 1, 2, 4  # gales_magma_status bits
+SUBMIX_MAGMA, SUBMIX_CUSTOM, SUBMIX_CHEMICAL = 0, 1, 2
 TAU_2001 = 2001
 TAU_2019 = 2019
 TAU_2007 = 2007
@@ -95,7 +96,8 @@ class MagmaDesc(C.Structure):
                 ("crystal_fraction", C.c_double), ("crystal_rho", C.c_double),
                 ("gas_on_mu", C.c_int32), ("crystal_on_mu", C.c_int32), ("n_p", C.c_int32), ("n_T", C.c_int32),
                 ("p_table", C.POINTER(C.c_double)), ("T_table", C.POINTER(C.c_double)),
-                ("wf_l_h2o", C.POINTER(C.c_double)), ("wf_l_co2", C.POINTER(C.c_double))]
+                ("wf_l_h2o", C.POINTER(C.c_double)), ("wf_l_co2", C.POINTER(C.c_double)),
+                ("kind", C.c_int32), ("reserved", C.c_int32), ("chemical", ChemicalDesc)]
 
 
 class SolverParams(C.Structure):

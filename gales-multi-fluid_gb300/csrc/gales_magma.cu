@@ -73,8 +73,18 @@ int gales_magma_create(const gales_magma_desc* comps, int32_t nb_comp, gales_mag
   *out = nullptr;
   for (int c = 0; c < nb_comp; ++c) {
     const gales_magma_desc& d = comps[c];
-    if (d.n_p < 2 || d.n_T < 0 || d.n_T == 1 || !d.p_table || !d.wf_l_h2o || !d.wf_l_co2 ||
-        (d.n_T > 0 && !d.T_table) || d.gas_on_mu < 0 || d.gas_on_mu > 2 || d.crystal_on_mu < 0 ||
+    if (d.kind == GALES_SUBMIX_CUSTOM) {
+      if (!(d.chemical.rho > 0.0)) return GALES_ERR_BAD_INPUT;
+      continue;
+    }
+    if (d.kind == GALES_SUBMIX_CHEMICAL) {
+      if (d.chemical.kind == GALES_CH_CUSTOM ? !(d.chemical.rho > 0.0)
+                                              : (d.chemical.kind != GALES_CH_IDEAL_GAS || !(d.chemical.R > 0.0)))
+        return GALES_ERR_BAD_INPUT;
+      continue;
+    }
+    if (d.kind != GALES_SUBMIX_MAGMA || d.n_p < 2 || d.n_T < 0 || d.n_T == 1 || !d.p_table || !d.wf_l_h2o ||
+        !d.wf_l_co2 || (d.n_T > 0 && !d.T_table) || d.gas_on_mu < 0 || d.gas_on_mu > 2 || d.crystal_on_mu < 0 ||
         d.crystal_on_mu > 2)
       return GALES_ERR_BAD_INPUT;
   }
@@ -94,8 +104,12 @@ int gales_magma_create(const gales_magma_desc* comps, int32_t nb_comp, gales_mag
   for (int c = 0; c < nb_comp && ok; ++c) {
     const gales_magma_desc& d = comps[c];
     build_constants(d, h[c]);
-    const size_t tn = d.n_T > 0 ? (size_t)d.n_T * d.n_p : (size_t)d.n_p;
     h[c].T_tab = nullptr;
+    if (d.kind != GALES_SUBMIX_MAGMA) {  // no tables
+      h[c].p_tab = h[c].h2o_tab = h[c].co2_tab = nullptr;
+      continue;
+    }
+    const size_t tn = d.n_T > 0 ? (size_t)d.n_T * d.n_p : (size_t)d.n_p;
     ok = upload(d.p_table, d.n_p, &h[c].p_tab) && upload(d.wf_l_h2o, tn, &h[c].h2o_tab) &&
          upload(d.wf_l_co2, tn, &h[c].co2_tab) && (d.n_T == 0 || upload(d.T_table, d.n_T, &h[c].T_tab));
   }

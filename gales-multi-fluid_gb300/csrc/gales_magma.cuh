@@ -31,6 +31,9 @@ struct DevMagma {
   double crystal_vf, crystal_rho;
   int gas_on_mu, crystal_on_mu;
   int n_p, n_T;
+  // custom_mix / ch_as_mix (kind != GALES_SUBMIX_MAGMA): the chemical's constants
+  int kind, ch_kind;
+  double ch_rho, ch_mu, ch_cp, ch_cv, ch_kappa, ch_alpha, ch_beta, ch_R, ch_gamma;
   const double* p_tab;
   const double* T_tab;
   const double* h2o_tab;
@@ -45,6 +48,17 @@ struct Props {
 // chemicals.hpp:62-103; GiordanoEtAlViscosityModel::set: GiordanoEtAlViscosityModel.hpp:36-83;
 // ideal_gas("H2O"/"CO2"): chemicals.hpp:201-234).
 inline void build_constants(const gales_magma_desc& d, DevMagma& g) {
+  g.kind = d.kind;
+  g.ch_kind = d.kind == GALES_SUBMIX_CUSTOM ? GALES_CH_CUSTOM : d.chemical.kind;
+  g.ch_rho = d.chemical.rho;
+  g.ch_mu = d.chemical.mu;
+  g.ch_cp = d.chemical.cp;
+  g.ch_cv = d.chemical.cv;
+  g.ch_kappa = d.chemical.kappa;
+  g.ch_alpha = d.chemical.alpha;
+  g.ch_beta = d.chemical.beta;
+  g.ch_R = d.chemical.R;
+  g.ch_gamma = d.chemical.gamma;
   g.wf_comp[1] = d.h2o_wf;
   g.wf_comp[2] = d.co2_wf;
   g.wf_comp[0] = 1.0 - g.wf_comp[1] - g.wf_comp[2];
@@ -320,7 +334,44 @@ GALES_MAGMA_HD void magma_props(const DevMagma& g, double p, double T, double sr
   o.mu = mu;
 }
 
-// One point of the mixture of magma sub-mixtures (fluid_properties.hpp:171-200):
+// A sub-mixture of any kind at (p, T): magma_mix above; custom_mix
+// (custom_mixture, mixtures.hpp:69-101: constant properties, sound speed 1e20 or
+// 1/sqrt(rho beta), cv = cp or cp - T alpha^2/(rho beta)); ch_as_mix (mixtures.hpp:25-53:
+// the chemical's properties, chemicals.hpp:19-49 custom, 198-271 ideal gas).  The last
+// two keep base_chemical's diffusivity 1e-10 (base_chemical.hpp:86; they never clear()
+// it) and have no gas phase.
+GALES_MAGMA_HD void sub_props(const DevMagma& g, double p, double T, double sr, Props& o, double& vf_gas,
+                              unsigned& st, double* fr = nullptr) {
+  if (g.kind == GALES_SUBMIX_MAGMA) {
+    magma_props(g, p, T, sr, o, vf_gas, st, fr);
+    return;
+  }
+  vf_gas = 0.0;
+  if (fr)
+    for (int k = 0; k < 6; ++k) fr[k] = 0.0;
+  o.D = 1.e-10;
+  if (g.ch_kind == GALES_CH_CUSTOM) {
+    o.rho = g.ch_rho;
+    o.mu = g.ch_mu;
+    o.cp = g.ch_cp;
+    o.kappa = g.ch_kappa;
+    o.alpha = g.ch_alpha;
+    o.beta = g.ch_beta;
+    o.c = (o.beta == 0.0) ? 1.e20 : 1.0 / sqrt(o.rho * o.beta);
+    o.cv = (o.beta == 0.0) ? o.cp : o.cp - T * o.alpha * o.alpha / (o.rho * o.beta);
+  } else {
+    o.rho = p / (g.ch_R * T);
+    o.beta = 1.0 / p;
+    o.alpha = 1.0 / T;
+    o.c = sqrt(g.ch_gamma * g.ch_R * T);
+    o.cv = g.ch_cv;
+    o.cp = g.ch_cp;
+    o.mu = g.ch_mu;
+    o.kappa = g.ch_kappa;
+  }
+}
+
+// One point of the mixture of sub-mixtures (fluid_properties.hpp:171-200):
 // f = rho, mu, cp, cv, kappa, sound speed, alpha, beta; comp[c] = rho_c, cv_c T, chemical
 // diffusivity, gas volume fraction.  Returns the status bits.
 GALES_MAGMA_HD unsigned mix_point(const DevMagma* mg, int nc, double p, double T, const double* Y, double sr,
@@ -331,7 +382,7 @@ GALES_MAGMA_HD unsigned mix_point(const DevMagma* mg, int nc, double p, double T
   for (int c = 0; c < nc; ++c) {
     Props m;
     double vfg;
-    magma_props(mg[c], p, T, sr, m, vfg, st);
+    sub_props(mg[c], p, T, sr, m, vfg, st);
     const double y = Y[c];
     rho += y / m.rho;
     mu += y * m.mu;
@@ -377,7 +428,7 @@ GALES_MAGMA_HD unsigned mix_fractions(const DevMagma* mg, int nc, double p, doub
   for (int c = 0; c < nc; ++c) {
     Props m;
     double vfg;
-    magma_props(mg[c], p, T, 0.0, m, vfg, st, fr[c]);
+    sub_props(mg[c], p, T, 0.0, m, vfg, st, fr[c]);
     rho += Y[c] / m.rho;
     rho_c[c] = m.rho;
   }

@@ -84,6 +84,43 @@ class MagmaMix:
         return d
 
 
+@dataclass
+class CustomMix:
+    """A custom_mix block (custom_mixture, mixtures.hpp:69-101;
+    fluid_properties_reader.hpp:222-274): a sub-mixture of constant rho, mu, cp, kappa,
+    alpha and beta."""
+    name: str
+    rho: float
+    mu: float
+    cp: float
+    kappa: float
+    alpha: float = 0.0
+    beta: float = 0.0
+
+    def desc(self) -> abi.MagmaDesc:
+        d = abi.MagmaDesc()
+        d.kind = abi.SUBMIX_CUSTOM
+        d.chemical.kind = abi.CH_CUSTOM
+        for k in ("rho", "mu", "cp", "kappa", "alpha", "beta"):
+            setattr(d.chemical, k, float(getattr(self, k)))
+        d.chemical.cv = float(self.cp)
+        return d
+
+
+@dataclass
+class ChemicalAsMix:
+    """A ch_as_mix block (ch_as_mix, mixtures.hpp:25-53; fluid_properties_reader.hpp:
+    175-205): one chemical (custom_chemical or ideal_gas descriptor) as a sub-mixture."""
+    name: str
+    chemical: abi.ChemicalDesc
+
+    def desc(self) -> abi.MagmaDesc:
+        d = abi.MagmaDesc()
+        d.kind = abi.SUBMIX_CHEMICAL
+        d.chemical = self.chemical
+        return d
+
+
 def descs(comps: Sequence[MagmaMix]):
     arr = (abi.MagmaDesc * len(comps))()
     for i, m in enumerate(comps):

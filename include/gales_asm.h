@@ -361,6 +361,10 @@ int gales_iluk_pattern(int64_t n, const int64_t* row_ptr, const int32_t* col, in
 #define GALES_CRYSTAL_MU_NONE 0
 #define GALES_CRYSTAL_MU_EINSTEIN_ROSCOE 1  /* mixtures.hpp:305-308 */
 #define GALES_CRYSTAL_MU_CARICCHI 2         /* mixtures.hpp:314-330 */
+/* sub-mixture kinds of a mix_of_mix (fluid_properties_reader.hpp:17, 127-141) */
+#define GALES_SUBMIX_MAGMA 0      /* magma_mix (mixtures.hpp:114-511) */
+#define GALES_SUBMIX_CUSTOM 1     /* custom_mix: constant properties (mixtures.hpp:69-101) */
+#define GALES_SUBMIX_CHEMICAL 2   /* ch_as_mix: one chemical as a sub-mixture (mixtures.hpp:25-53) */
 /* magma status bits (gales_magma_status) */
 #define GALES_MAGMA_LOOKUP_RANGE 1   /* a pressure or temperature outside the table (the reference stops) */
 #define GALES_MAGMA_VISCOSITY 2      /* a zero denominator of the viscosity model (the reference stops) */
@@ -385,11 +389,20 @@ typedef struct gales_magma_desc {
   const double* T_table;
   const double* wf_l_h2o;
   const double* wf_l_co2;
+  /* The kind of this sub-mixture (GALES_SUBMIX_*; 0 = magma_mix, which reads the fields
+   * above).  custom_mix reads rho, mu, cp, kappa, alpha and beta of `chemical`
+   * (kind GALES_CH_CUSTOM); ch_as_mix reads `chemical` (a custom chemical or an ideal
+   * gas).  Neither copies the chemical's diffusivity: theirs stays base_chemical's
+   * 1e-10 (base_chemical.hpp:86), and their gas fractions (pp_vf_g) are 0. */
+  int32_t kind;
+  int32_t reserved;
+  gales_chemical_desc chemical;
 } gales_magma_desc;
 
 typedef struct gales_magma gales_magma;
 
-/* Upload nb_comp magma mixtures (1..GALES_MAX_COMP) to the current device. */
+/* Upload nb_comp sub-mixtures (1..GALES_MAX_COMP; magma_mix, custom_mix or ch_as_mix)
+ * to the current device. */
 int gales_magma_create(const gales_magma_desc* comps, int32_t nb_comp, gales_magma** out);
 /* Mixture-of-magmas properties at n points (p[i], T[i], all nb_comp mass fractions
  * Y[i * nb_comp + c], shear rate shear[i] or NULL = 0), one GPU thread per point:

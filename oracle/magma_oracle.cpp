@@ -167,7 +167,40 @@ struct Magma {
   double crystal_vf = 0, crystal_rho = 0;
   int gas_on_mu = 0, crystal_on_mu = 0;
   std::vector<double> p_tab, T_tab, h2o_tab, co2_tab;
+  int kind = GALES_SUBMIX_MAGMA;   // magma_mix, custom_mix or ch_as_mix
+  gales_chemical_desc ch{};        // custom_mix / ch_as_mix constants
 };
+
+// custom_mixture::properties (mixtures.hpp:69-101) and ch_as_mix::properties
+// (mixtures.hpp:25-53) over custom_chemical (chemicals.hpp:19-49) or ideal_gas
+// (chemicals.hpp:198-271).  The diffusivity is base_chemical's 1e-10 (base_chemical.hpp:86):
+// neither class clears or copies it.
+void submix_props(const Magma& g, double p, double T, Chem& o) {
+  o = Chem();
+  o.D = 1.e-10;
+  const bool custom = g.kind == GALES_SUBMIX_CUSTOM || g.ch.kind == GALES_CH_CUSTOM;
+  if (custom) {
+    o.rho = g.ch.rho;
+    o.mu = g.ch.mu;
+    o.cp = g.ch.cp;
+    o.alpha = g.ch.alpha;
+    o.beta = g.ch.beta;
+    o.kappa = g.ch.kappa;
+    if (o.beta == 0.0) o.c = 1.e20;
+    else o.c = 1.0 / std::sqrt(o.rho * o.beta);
+    if (o.beta == 0.0) o.cv = o.cp;
+    else o.cv = o.cp - T * o.alpha * o.alpha / (o.rho * o.beta);
+  } else {
+    o.rho = p / (g.ch.R * T);
+    o.beta = 1.0 / p;
+    o.alpha = 1.0 / T;
+    o.c = std::sqrt(g.ch.gamma * g.ch.R * T);
+    o.cv = g.ch.cv;
+    o.cp = g.ch.cp;
+    o.mu = g.ch.mu;
+    o.kappa = g.ch.kappa;
+  }
+}
 
 double interp1(double p, const std::vector<double>& pt, const std::vector<double>& y, bool& ok) {
   const double dp = pt[1] - pt[0];
@@ -202,6 +235,13 @@ double interp2(double T, double p, const std::vector<double>& Tt, const std::vec
 // fr (optional): the phase and chemical fractions secondary_dofs.hpp:113-131 reads,
 // wf_ph_[g], wf_[3], wf_[4], vf_ph_[g], vf_[3], vf_[4] (mixtures.hpp:225-258).
 int magma_props(const Magma& g, double p, double T, double sr, Chem& o, double& vf_gas, double* fr = nullptr) {
+  if (g.kind != GALES_SUBMIX_MAGMA) {
+    submix_props(g, p, T, o);
+    vf_gas = 0.0;
+    if (fr)
+      for (int k = 0; k < 6; ++k) fr[k] = 0.0;
+    return 0;
+  }
   int st = 0;
   bool ok = true;
   double wl[3];
@@ -300,6 +340,9 @@ int magma_props(const Magma& g, double p, double T, double sr, Chem& o, double& 
 }
 
 void build(const gales_magma_desc& d, Magma& g) {
+  g.kind = d.kind;
+  g.ch = d.chemical;
+  if (d.kind != GALES_SUBMIX_MAGMA) return;
   g.wf_comp[1] = d.h2o_wf;
   g.wf_comp[2] = d.co2_wf;
   g.wf_comp[0] = 1.0 - g.wf_comp[1] - g.wf_comp[2];

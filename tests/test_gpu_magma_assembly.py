@@ -161,3 +161,28 @@ def test_magma_adaptive_dt_secondary_dofs_and_fractions(kind, cuda_lib, orc):
     for f in range(got.shape[0]):
         assert rel(got[f], fr[f]) <= 1e-12, f
     assert np.all(got[-6] > 0.0)                 # some gas at these pressures
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["magma+custom", "magma+gas", "custom+chemical", "three"])
+@pytest.mark.parametrize("elem", ["tri", "tet"])
+def test_submixture_kinds_assembly_matches_oracle(kind, elem, cuda_lib, orc):
+    """custom_mix and ch_as_mix sub-mixtures beside magma_mix (fluid_properties_reader.hpp:
+    127-141, mixtures.hpp:25-101) in the assembly, both forms, against the oracle."""
+    import test_magma as tm
+    magma = pytest.importorskip("gales-multi-fluid_gb300.magma")
+    comps = tm._with_submixtures(kind)
+    nc = len(comps)
+    mesh = syn.channel_tri(16, 8) if elem == "tri" else syn.box_tet_delaunay(6, seed=1)
+    mat = syn.material_for(nc, 0)
+    setup = syn.setup_for(mesh.dim, nc)
+    I, P = _magma_state(mesh, nc)
+    mm = magma.MagmaMaterial(comps)
+    fa = gm.FluidAssembly(mesh, mat, setup)
+    fa.set_magma(mm)
+    vals, rhs = _oracle(orc, mesh, comps, mat, setup, I, P, 1e-3, fa.nd)
+    for form, tol in ((gm.FORM_FP64, 1e-12), (gm.FORM_MIXED, 1e-6)):
+        lp = fa.linear_system()
+        fa.execute(I, P, 1e-3, lp, form=form)
+        assert rel(lp.vals, vals) <= tol, (form, rel(lp.vals, vals))
+        assert rel(lp.rhs, rhs) <= tol, (form, rel(lp.rhs, rhs))

@@ -116,6 +116,65 @@ def test_oracle_shear_rate_formula(dim):
         assert oracle.shear_rate(dim, dI) == pytest.approx(ref, rel=1e-15)
 
 
+def _with_submixtures(kind):
+    """Mixtures of sub-mixtures of every kind: magma_mix, custom_mix, ch_as_mix."""
+    mg = syn.magma_pair()[0]
+    melt = magma.CustomMix("melt", rho=2400.0, mu=1.0e3, cp=1200.0, kappa=1.5, alpha=3e-5, beta=1e-10)
+    rigid = magma.CustomMix("rigid", rho=2700.0, mu=1.0e4, cp=1000.0, kappa=2.0)
+    gas = magma.ChemicalAsMix("h2o", gm.ideal_gas_named("H2O"))
+    liquid = magma.ChemicalAsMix("liq", gm.custom_chemical(rho=2300.0, mu=500.0, cp=1100.0, kappa=1.2, alpha=2e-5,
+                                                           beta=2e-10))
+    return {"magma+custom": [mg, melt], "magma+gas": [mg, gas], "custom+chemical": [rigid, liquid],
+            "three": [mg, liquid, gas]}[kind]
+
+
+@pytest.mark.parametrize("kind", ["magma+custom", "magma+gas", "custom+chemical", "three"])
+def test_submixture_kinds_kernel_code_equals_oracle(kind, host_lib):
+    """custom_mix (mixtures.hpp:69-101) and ch_as_mix (mixtures.hpp:25-53) beside magma_mix
+    in a mix_of_mix: the kernel's code on the host equals the oracle bit for bit."""
+    comps = _with_submixtures(kind)
+    p, T, Y, shear = _points(nc=len(comps))
+    o1, c1, s1 = _host(host_lib, comps, p, T, Y, shear)
+    o2, c2, s2 = oracle.magma_properties(comps, p, T, Y, shear)
+    assert s1 == s2 == 0
+    assert np.array_equal(o1, o2) and np.array_equal(c1, c2)
+
+
+def test_custom_mix_closed_forms():
+    """custom_mixture: constant rho, mu, cp, kappa; sound speed 1/sqrt(rho beta) (1e20 for
+    beta = 0); cv = cp - T alpha^2/(rho beta) (cp for beta = 0); diffusivity 1e-10."""
+    cm = magma.CustomMix("m", rho=2400.0, mu=1.0e3, cp=1200.0, kappa=1.5, alpha=3e-5, beta=1e-10)
+    rigid = magma.CustomMix("r", rho=2700.0, mu=1.0e4, cp=1000.0, kappa=2.0)
+    T = np.array([1200.0, 1300.0])
+    out, comp, st = oracle.magma_properties([cm], np.full(2, 1e8), T, np.ones((2, 1)))
+    assert st == 0
+    np.testing.assert_allclose(out[0], 2400.0, rtol=0)
+    np.testing.assert_allclose(out[5], 1.0 / np.sqrt(2400.0 * 1e-10), rtol=1e-15)
+    np.testing.assert_allclose(out[3], 1200.0 - T * 9e-10 / (2400.0 * 1e-10), rtol=1e-15)
+    assert np.all(comp[0, 2] == 1e-10) and np.all(comp[0, 3] == 0.0)
+    out, comp, st = oracle.magma_properties([rigid], np.full(2, 1e8), T, np.ones((2, 1)))
+    assert np.all(out[3] == 1000.0) and np.all(out[5] == 1e20)
+
+
+def test_chemicals_as_submixtures_equal_the_mixture_of_chemicals():
+    """A mix_of_mix of ch_as_mix sub-mixtures (fluid_properties.hpp:171-200) is the
+    mix_of_ch of the same chemicals (fluid_properties.hpp:199-227): the same properties
+    and the same assembled system in the oracle (the mixtures' own diffusivities are not
+    read by the assembly; the components' are 1e-10 in both)."""
+    mat = syn.material_for(3, 0)
+    comps = [magma.ChemicalAsMix(f"c{i}", q) for i, q in enumerate(mat.chemicals)]
+    mesh = syn.box_tet_delaunay(4, seed=2)
+    setup = syn.setup_for(3, 3)
+    I, P = syn.state_for(mesh, 3, 0)
+    nrp, ncol, rp, col = oracle.pattern(mesh, 7)
+    v0, r0, s0, _ = oracle.assemble(mesh, mat, setup, I, P, 1e-3, rp, col)
+    with oracle.magma_material(comps):
+        v1, r1, s1, _ = oracle.assemble(mesh, mat, setup, I, P, 1e-3, rp, col)
+    assert s0 == s1 == 0
+    assert np.linalg.norm(v1 - v0) <= 1e-14 * np.linalg.norm(v0)
+    assert np.linalg.norm(r1 - r0) <= 1e-14 * np.linalg.norm(r0)
+
+
 def test_physical_consistency():
     """rho of the mixture of sub-mixtures is the harmonic Y-average of the components';
     the gas volume fraction grows as the pressure falls; Ishii-Zuber divides mu by
