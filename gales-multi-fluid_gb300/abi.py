@@ -25,6 +25,7 @@ ERR_CUDA = 16
 ERR_UNSUPPORTED = 32
 ERR_NO_MEMORY = 64
 ERR_MAGMA = 128
+ERR_TIMEOUT = 256
 NOALLOC_SCRATCH_BYTES = 8 << 20
 
 FORM_FP64 = 0

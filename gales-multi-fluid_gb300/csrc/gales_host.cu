@@ -146,14 +146,17 @@ void parallel_for(int64_t n, F f) {
 
 // Scratch of the exact VJP: the theta and u_ref_inv cotangents.
 constexpr int kVjpAux = 3 * GALES_MAX_COMP + GALES_MAX_ND;
-// Chunks of the interior pass: one wave of the point stage that leaves one CTA slot per
-// SM to the matrix stage running beside it (with four point CTAs resident per SM the
-// chunk holds three per SM), so that the FP64-bound point stage and the issue-bound
-// matrix stage share every SM.  A chunk's point records (about 44 MB for tets) stay in
-// L2 until the matrix stage reads them.
-constexpr int kRing = 3;    // point-record buffers in flight between the two stages
+// Chunks of the interior pass.  On this GPU an FP64 instruction occupies the FMA
+// pipe that the FP32 instructions issue to, so the FP64-bound point stage and the
+// FP32 matrix stage gain nothing from sharing an SM: each chunk runs the point kernel
+// over all its elements, then the persistent matrix kernel, on the caller's stream.
+// Chunks are as large as kRecordBytes of point records allow (the whole mesh for the
+// 1.0M-tet workload), so that few launch tails remain; the records go through DRAM,
+// which the compute-bound stages leave mostly idle.  A host-buffer call cuts the pass
+// into kCopyChunks chunks, after each of which the finished CSR rows are copied.
+constexpr size_t kRecordBytes = size_t(3) << 30;
+constexpr int kCopyChunks = 8;
 constexpr int kCopyEvents = 24;  // row copies per host-buffer assembly (at most)
-inline int point_ctas_per_chunk_sm(int occupancy) { return occupancy >= 3 ? occupancy - 1 : occupancy; }
 
 GeometryOps geometry_ops(int dim, int nen) {
   if (dim == 2 && nen == 3) return geometry_ops_tri3();
@@ -257,13 +260,10 @@ struct gales_asm {
   InteriorOps ops_ch[2];
   const magma_mix::DevMagma* mg = nullptr;
   MagmaOps mops{};
-  DevBuf<unsigned char> qpbuf[kRing];
+  DevBuf<unsigned char> qpbuf;          // point records of one chunk
   long long chunk_elems[2] = {1, 1};   // elements per chunk, per form
   int sms = 1;                          // multiprocessors of the device
   DevBuf<unsigned char> d_geo;   // element geometry at the interior points (mesh.hpp:468-495)
-  cudaStream_t ist[2] = {nullptr, nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
-  cudaEvent_t ev_pt[kRing] = {}, ev_mx[kRing] = {};   // chunk in a buffer written / consumed
   cudaStream_t bst = nullptr;                  // boundary pass, concurrent with the interior
   cudaStream_t cst = nullptr;                  // device-to-host copies of finished CSR rows
   cudaEvent_t ev_copy[kCopyEvents] = {};
@@ -789,11 +789,6 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   if ((ce = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(ce, "event");
   for (int i = 0; i < 4; ++i)
     if ((ce = cudaEventCreate(&h->evp[i])) != cudaSuccess) return bail(ce, "event");
-  if ((ce = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
-  for (int i = 0; i < kRing; ++i) {
-    if ((ce = cudaEventCreateWithFlags(&h->ev_pt[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
-    if ((ce = cudaEventCreateWithFlags(&h->ev_mx[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
-  }
   if ((ce = cudaEventCreateWithFlags(&h->ev_bfork, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreateWithFlags(&h->ev_bjoin, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaStreamCreateWithFlags(&h->bst, cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
@@ -801,17 +796,20 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   for (int i = 0; i < kCopyEvents; ++i)
     if ((ce = cudaEventCreateWithFlags(&h->ev_copy[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreateWithFlags(&h->ev_cjoin, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
-  for (int i = 0; i < 2; ++i) {
-    if ((ce = cudaEventCreateWithFlags(&h->ev_join[i], cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
-    // ist[0] runs the point stage, ist[1] the matrix stage
-    if ((ce = cudaStreamCreateWithFlags(&h->ist[i], cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
-
-  }
   h->ops[GALES_FORM_FP64] = interior_ops(h->dim, h->nen, GALES_FORM_FP64);
   h->ops[GALES_FORM_MIXED] = interior_ops(h->dim, h->nen, GALES_FORM_MIXED);
   h->ops_ch[GALES_FORM_FP64] = h->ops[GALES_FORM_FP64];
   h->ops_ch[GALES_FORM_MIXED] = h->ops[GALES_FORM_MIXED];
-  {  // chunk size per form from the point kernel's occupancy; record buffers for the larger
+  // the scatter descriptors in the point records hold CSR offsets in units of nd
+  // values as 32-bit integers
+  if (h->nnz_nodes * (int64_t)h->nd >= (int64_t(1) << 31)) {
+    fprintf(stderr, "gales_asm_create: %lld node-graph entries x %d dofs exceed the 32-bit scatter offsets\n",
+            (long long)h->nnz_nodes, h->nd);
+    gales_asm_destroy(h);
+    return GALES_ERR_UNSUPPORTED;
+  }
+  {  // chunk size per form (kRecordBytes of point records, a multiple of four elements);
+     // one record buffer for the larger
     int sms = 0;
     if ((ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
       return bail(ce, "device attribute");
@@ -820,13 +818,12 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
     for (int f = 0; f < 2; ++f) {
       const size_t rb = h->ops[f].rec_bytes(h->nc);
       if (rb == 0) continue;
-      const long long wave = (long long)sms * point_ctas_per_chunk_sm(h->ops[f].point_occupancy(h->nc)) * 128 / h->ei.nq;
-      h->chunk_elems[f] = std::max<long long>(1, std::min<long long>(wave, std::max<int64_t>(h->n_el, 1)));
+      const long long cap = std::max<long long>(4, (long long)(kRecordBytes / rb) / 4 * 4);
+      h->chunk_elems[f] = std::max<long long>(1, std::min<long long>(cap, std::max<int64_t>(h->n_el, 1)));
       // records are written in blocks of (elements per matrix CTA, at most 4) elements
       bytes = std::max(bytes, rb * (size_t)(h->chunk_elems[f] + 4));
     }
-    for (int i = 0; i < kRing; ++i)
-      if ((ce = h->qpbuf[i].alloc(std::max<size_t>(bytes, 16))) != cudaSuccess) return bail(ce, "point-record buffer");
+    if ((ce = h->qpbuf.alloc(std::max<size_t>(bytes, 16))) != cudaSuccess) return bail(ce, "point-record buffer");
   }
   for (int f = 0; f < 2; ++f) {  // kernel attributes, once, outside any stream capture
     if ((ce = h->ops[f].prepare(h->nc)) != cudaSuccess) return bail(ce, "kernel attributes");
@@ -906,7 +903,6 @@ void gales_asm_destroy(gales_asm* h) {
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (int i = 0; i < 4; ++i)
     if (h->evp[i]) cudaEventDestroy(h->evp[i]);
-  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_bfork) cudaEventDestroy(h->ev_bfork);
   if (h->ev_bjoin) cudaEventDestroy(h->ev_bjoin);
   if (h->bst) cudaStreamDestroy(h->bst);
@@ -914,15 +910,7 @@ void gales_asm_destroy(gales_asm* h) {
   for (int i = 0; i < kCopyEvents; ++i)
     if (h->ev_copy[i]) cudaEventDestroy(h->ev_copy[i]);
   if (h->ev_cjoin) cudaEventDestroy(h->ev_cjoin);
-  for (int i = 0; i < kRing; ++i) {
-    h->qpbuf[i].release();
-    if (h->ev_pt[i]) cudaEventDestroy(h->ev_pt[i]);
-    if (h->ev_mx[i]) cudaEventDestroy(h->ev_mx[i]);
-  }
-  for (int i = 0; i < 2; ++i) {
-    if (h->ev_join[i]) cudaEventDestroy(h->ev_join[i]);
-    if (h->ist[i]) cudaStreamDestroy(h->ist[i]);
-  }
+  h->qpbuf.release();
   delete h;
 }
 
@@ -1042,6 +1030,7 @@ KParams base_params(gales_asm* h, double dt) {
   k.side_bc = h->d_side_bc.p;
   k.status = h->d_status.p;
   k.first_bad = h->d_first_bad.p;
+  k.sms = h->sms;
   return k;
 }
 
@@ -1078,69 +1067,29 @@ int copy_finished_rows(gales_asm* h, RowCopy& rc, int64_t elements_done, bool la
   return 0;
 }
 
-// Interior pass over n listed elements (k.el_list, or elements 0..n-1): point stage then
-// matrix stage per chunk.  Mixed form with the atomic scatter: one interior_kernel
-// launch per chunk on the caller's stream (point stage of chunk c beside the matrix
-// stage of chunk c-1, programmatically dependent launches), with the optional
-// device-to-host copy of finished rows (rc).  FP64 form with the atomic scatter: the
-// point stage on ist[0] and the matrix stage on ist[1], chunk c's matrix waiting on its
-// records (ev_pt) and chunk c+kRing's point stage waiting until chunk c's buffer has
-// been consumed (ev_mx).  Otherwise (plain read-modify-write of coloured batches, or
-// element-level output) both stages run on the caller's stream.
+// Interior pass over n listed elements (k.el_list, or elements 0..n-1): per chunk the
+// point kernel, then the matrix kernel, on the caller's stream, with the optional
+// device-to-host copy of finished rows (rc) after each chunk.
 int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long long n, cudaStream_t st,
-                 bool concurrent, RowCopy* rc = nullptr) {
+                 RowCopy* rc = nullptr) {
   const InteriorOps& ops = h->ops[form];
   const size_t rb = ops.rec_bytes(h->nc);
   if (rb == 0) return fail(h, GALES_ERR_UNSUPPORTED, "no interior kernel for this element/component count");
-  const long long chunk = h->chunk_elems[form];
+  long long chunk = h->chunk_elems[form];
+  if (rc) chunk = std::min(chunk, std::max<long long>(4, (n + kCopyChunks - 1) / kCopyChunks));
   const long long nchunks = (n + chunk - 1) / chunk;
-  if (nchunks == 0) return 0;
-  if (concurrent && form == GALES_FORM_MIXED) {
-    // one launch per chunk on the caller's stream: chunk c's point stage (buffer c % 3)
-    // beside chunk c-1's matrix stage (buffer (c-1) % 3), each launch programmatically
-    // dependent on the one before (the first follows the zero fill normally)
-    static_assert(kRing == 3, "the fused interior pass uses three record buffers");
-    for (long long c = 0; c <= nchunks; ++c) {
-      const long long pf = c * chunk, pn = c < nchunks ? std::min(chunk, n - pf) : 0;
-      const long long mf = (c - 1) * chunk, mn = c >= 1 ? std::min(chunk, n - mf) : 0;
-      void* pb = h->qpbuf[c % 3].p;
-      const void* mb = h->qpbuf[(c + 2) % 3].p;
-      LaunchResult r = ops.interior(k, h->nc, want_m, pb, pf, pn, mb, c >= 1 ? mf : 0, mn, c >= 1, st);
-      if (r.err != cudaSuccess) return cuda_fail(h, r.err, "interior kernel");
-      h->launches += r.launches;
-      if (rc && c >= 1) {
-        const int e = copy_finished_rows(h, *rc, mf + mn, c == nchunks, st);
-        if (e) return e;
-      }
-    }
-    return 0;
-  }
-  if (concurrent) {
-    CK(h, cudaEventRecord(h->ev_fork, st), "event");
-    for (int i = 0; i < 2; ++i) CK(h, cudaStreamWaitEvent(h->ist[i], h->ev_fork, 0), "stream wait");
-  }
+  void* buf = h->qpbuf.p;
   for (long long c = 0; c < nchunks; ++c) {
     const long long first = c * chunk, cnt = std::min(chunk, n - first);
-    const int slot = (int)(c % kRing);
-    void* buf = h->qpbuf[concurrent ? slot : 0].p;
-    cudaStream_t sp = concurrent ? h->ist[0] : st, sm = concurrent ? h->ist[1] : st;
-    if (concurrent && c >= kRing) CK(h, cudaStreamWaitEvent(sp, h->ev_mx[slot], 0), "stream wait");
-    LaunchResult r = ops.point(k, h->nc, buf, first, cnt, sp);
+    LaunchResult r = ops.point(k, h->nc, buf, first, cnt, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "point kernel");
     h->launches += r.launches;
-    if (concurrent) {
-      CK(h, cudaEventRecord(h->ev_pt[slot], sp), "event");
-      CK(h, cudaStreamWaitEvent(sm, h->ev_pt[slot], 0), "stream wait");
-    }
-    r = ops.matrix(k, h->nc, want_m, buf, first, cnt, sm);
+    r = ops.matrix(k, h->nc, want_m, buf, first, cnt, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "matrix kernel");
     h->launches += r.launches;
-    if (concurrent) CK(h, cudaEventRecord(h->ev_mx[slot], sm), "event");
-  }
-  if (concurrent) {
-    for (int i = 0; i < 2; ++i) {
-      CK(h, cudaEventRecord(h->ev_join[i], h->ist[i]), "event");
-      CK(h, cudaStreamWaitEvent(st, h->ev_join[i], 0), "stream wait");
+    if (rc) {
+      const int e = copy_finished_rows(h, *rc, first + cnt, c == nchunks - 1, st);
+      if (e) return e;
     }
   }
   return 0;
@@ -1329,13 +1278,13 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
       KParams kc = k;
       kc.el_list = h->d_colour_order.p + h->colour_off[c];
       kc.n_list = h->colour_off[c + 1] - h->colour_off[c];
-      int rc = run_interior(h, kc, form, want_m, kc.n_list, st, false);
+      int rc = run_interior(h, kc, form, want_m, kc.n_list, st);
       if (rc) return rc;
     }
   } else {
     k.el_list = rc ? h->d_sweep_rows.p : h->d_sweep.p;
     k.n_list = h->n_el;
-    int e = run_interior(h, k, form, want_m, h->n_el, st, true, rc);
+    int e = run_interior(h, k, form, want_m, h->n_el, st, rc);
     if (e) return e;
   }
   if (timed) CK(h, cudaEventRecord(h->evp[2], st), "event");
@@ -1521,7 +1470,7 @@ int gales_asm_element_blocks(gales_asm* h, const double* I, const double* P, dou
   CK(h, cudaMemsetAsync(dr, 0, (size_t)n * N * sizeof(double), st), "memset r");
   LaunchResult r;
   if (which == 0) {
-    int rc0 = run_interior(h, k, form, dm != nullptr, n, st, false);
+    int rc0 = run_interior(h, k, form, dm != nullptr, n, st);
     if (rc0) return rc0;
     r = {cudaSuccess, 0};
   } else {
@@ -1617,7 +1566,7 @@ int gales_asm_vjp(gales_asm* h, const double* I, const double* P, double dt, con
     }
   } else {
     // the FP64 tangent, contracted with lambda by the matrix and boundary kernels
-    int rc = run_interior(h, k, GALES_FORM_FP64, true, h->n_el, st, true);
+    int rc = run_interior(h, k, GALES_FORM_FP64, true, h->n_el, st);
     if (rc) return rc;
     if (kb.n_list > 0) {
       LaunchResult r = dispatch_boundary(h, kb, GALES_FORM_FP64, kb.n_list, st);

@@ -64,6 +64,7 @@ struct KParams {
   unsigned int* status;
   unsigned long long* first_bad;
   int32_t scatter_mode;        // 0 atomics, 1 plain read-modify-write (coloured batches)
+  int32_t sms;                 // multiprocessors of the device (persistent grids)
   const void* geo;             // ElemGeo records (per element, or per element and point)
   double sh_tab[8][8];         // shape functions at the interior points [q][node]
   double* local_m;             // element-level output [n_list][(nen*nd)^2] (no scatter) or null
@@ -289,9 +290,15 @@ __device__ __forceinline__ void geometry(const double (&X)[NEN][DIM], const doub
 }
 
 // ---------------------------------------------------------------------------
-// Per-quadrature-point record written by the point phase.
+// Per-quadrature-point record written by the point phase.  The record of point q of
+// an element also carries the scatter descriptor of the element's node b = q (every
+// element type here has as many interior points as nodes): the node, its CSR row
+// length nd * (graph row length), its Dirichlet mask and, per trial node a, the unit
+// offset u = node_rp(b) nd + slot(b, a), so that dof row jb of node b holds node a's
+// columns from nd u + jb rowlen on.  The matrix stage then reads everything it needs
+// from the record block.  Integers are stored as the bit patterns of S words.
 template <int DIM, int NEN, int NC, typename S>
-struct alignas(16) QP {
+struct QP {
   using L = Layout<DIM, NC>;
   using Scalar = S;
   static constexpr int ND = L::ND;
@@ -306,7 +313,13 @@ struct alignas(16) QP {
   S rv[ND];         // coefficient of N_b:    (U - U_P)/dt - S
   S rf[DIM][ND];    // coefficient of dN_b/dx_k:  F_dif,k - F_adv,k + shock dI/dx_k
   S res[ND];        // least-squares residual Res (fluid_2d.hpp:282)
+  S d_node, d_rowlen, d_blocked, d_off[NEN];  // scatter descriptor of node b = q (see above)
 };
+
+__device__ __forceinline__ float int_word(float, int32_t v) { return __int_as_float(v); }
+__device__ __forceinline__ double int_word(double, int32_t v) { return __longlong_as_double((long long)v); }
+__device__ __forceinline__ int32_t word_int(float w) { return __float_as_int(w); }
+__device__ __forceinline__ int32_t word_int(double w) { return (int32_t)__double_as_longlong(w); }
 
 // Lane layout of the matrix stage (see matrix_kernel); the point stage lays its
 // records out in the matrix CTAs' blocks.
@@ -325,22 +338,42 @@ struct MatShape {
   static constexpr bool AFFINE = NEN == DIM + 1;
 };
 
-// Point records in a chunk buffer are stored word-major within blocks of BP points,
-// BP = (elements per matrix CTA) x NQ, the points one matrix CTA reads: word f of
-// point p of block b is at [b][f][p].  A warp of the point stage then stores each word
-// for its 32 consecutive points as runs of BP contiguous words (instead of one word
-// per record, 760 bytes apart), and a matrix CTA reads its block as one contiguous
-// range.  RecOut addresses one point's words.
-template <typename QPT, int BP>
+// Point records are stored in blocks of BP = (elements per matrix CTA) x NQ points, the
+// points one matrix CTA group reads, word-major inside a block: word f of point p is at
+// [f * BPS + p] with the odd stride BPS = BP + 1, so that the lanes of a matrix warp
+// reading word f + i * nd of one point (the rows of tau) hit distinct banks.  A block
+// is padded to a whole number of 16-byte units and is copied to shared memory as it
+// lies (one bulk copy).  A warp of the point stage stores each word for its 32
+// consecutive points as runs of BP contiguous words.
+template <int DIM, int NEN, int NC, int NQ, typename S>
+struct RecBlock {
+  using QPT = QP<DIM, NEN, NC, S>;
+  static constexpr int EPC = MatShape<DIM, NEN, NC>::EPC;
+  static constexpr int BP = EPC * NQ;
+  static constexpr int BPS = BP + 1;
+  static constexpr int RW = (int)(sizeof(QPT) / sizeof(S));   // words per record
+  static constexpr int V = (int)(16 / sizeof(S));
+  static constexpr int WORDS = (RW * BPS + V - 1) / V * V;    // words per block
+  static constexpr size_t BYTES = (size_t)WORDS * sizeof(S);
+  static_assert(sizeof(QPT) % sizeof(S) == 0, "a record is a whole number of words");
+};
+
+// One point's words in a block being written (point stage) or read (matrix stage).
+template <typename QPT, int BPS>
 struct RecOut {
   using S = typename QPT::Scalar;
-  static constexpr int RW = (int)(sizeof(QPT) / sizeof(S));  // words per record
   S* __restrict__ blk;
   int p;
-  __device__ __forceinline__ S& at(size_t off) const { return blk[(off / sizeof(S)) * BP + p]; }
+  __device__ __forceinline__ S& at(size_t off) const { return blk[(off / sizeof(S)) * BPS + p]; }
+};
+template <typename S, int BPS>
+struct RecIn {
+  const S* b;  // word 0 of the point
+  __device__ __forceinline__ S operator[](int f) const { return b[f * BPS]; }
 };
 #define GALES_REC(m) out.at(offsetof(QPT, m))
 #define GALES_RECA(m, i) out.at(offsetof(QPT, m) + (size_t)(i) * sizeof(S))
+#define GALES_W(m) ((int)(offsetof(QPT, m) / sizeof(S)))
 
 // Element geometry at the interior quadrature points, computed once at handle
 // creation as the reference does at mesh load (mesh.hpp:468-495 builds a quad
@@ -421,16 +454,33 @@ __device__ __noinline__ double compute_h_reference(const double* __restrict__ I,
 //   GALES_FORM_MIXED: FP64 for the mixture EOS and its derivatives, U - U_P, the
 //                     element size h and tau with the closed-form DUDY inverse; the
 //                     fluxes, least-squares residual and dc viscosity in FP32.
-template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, int BP, int EOS = kEosChemicals>
-__device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<QP<DIM, NEN, NC, S>, BP>& out) {
+template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, int BPS, int EOS = kEosChemicals>
+__device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<QP<DIM, NEN, NC, S>, BPS>& out) {
   using L = Layout<DIM, NC>;
   using QPT = QP<DIM, NEN, NC, S>;
   constexpr int ND = L::ND;
   constexpr int NG = geo_per_element<DIM, NEN>(NQ);
   using R = typename std::conditional<FORM == GALES_FORM_FP64, double, float>::type;
+  static_assert(NQ == NEN, "point q carries the scatter descriptor of node q");
   int nodes[NEN];
 #pragma unroll
   for (int a = 0; a < NEN; ++a) nodes[a] = __ldg(k.conn + e * NEN + a);
+  {
+    // scatter descriptor of node b = iq (see QP): its graph row, Dirichlet mask and the
+    // positions of the element's nodes in that row (slot table)
+    int nb = nodes[0];
+#pragma unroll
+    for (int a = 1; a < NEN; ++a) nb = (iq == a) ? nodes[a] : nb;
+    const int64_t rr0 = __ldg(k.node_rp + nb), rr1 = __ldg(k.node_rp + nb + 1);
+    const int fl = k.node_flag ? __ldg(k.node_flag + nb) : 0;
+    const uint32_t blocked = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
+    GALES_REC(d_node) = int_word(S(0), nb);
+    GALES_REC(d_rowlen) = int_word(S(0), (int32_t)((rr1 - rr0) * ND));
+    GALES_REC(d_blocked) = int_word(S(0), (int32_t)blocked);
+    const uint16_t* sl = k.slot + ((long long)e * NEN + iq) * NEN;
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) GALES_RECA(d_off, a) = int_word(S(0), (int32_t)(rr0 * ND + __ldg(sl + a)));
+  }
   const ElemGeo<DIM, NEN>& q = reinterpret_cast<const ElemGeo<DIM, NEN>*>(k.geo)[e * NG + (NG == 1 ? 0 : iq)];
   double sh[NEN];
 #pragma unroll
@@ -1066,7 +1116,7 @@ __device__ __forceinline__ double widen(double d) { return d; }
 template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, int EOS = kEosChemicals>
 __device__ __forceinline__ void point_block(const KParams& k, QP<DIM, NEN, NC, S>* __restrict__ out, long long first,
                                             long long n, int bid) {
-  // chunk-local indices fit 32 bits (a chunk is one wave of CTAs); 64-bit shifts and
+  // chunk-local indices fit 32 bits (the host keeps a chunk's points below 2^31); 64-bit
   // divisions would issue on the FP64 pipe.  CTAs of 128 threads.
   const int t = bid * 128 + (int)threadIdx.x;
   const int li = t / NQ;
@@ -1075,11 +1125,10 @@ __device__ __forceinline__ void point_block(const KParams& k, QP<DIM, NEN, NC, S
   const long long g = first + li;
   const long long e = k.el_list ? (long long)k.el_list[g] : g;
   using QPT = QP<DIM, NEN, NC, S>;
-  constexpr int BP = MatShape<DIM, NEN, NC>::EPC * NQ;
-  constexpr int RW = RecOut<QPT, BP>::RW;
-  const int blk = t / BP;
-  const RecOut<QPT, BP> o{reinterpret_cast<S*>(out) + (size_t)blk * (size_t)(RW * BP), t - blk * BP};
-  point_phase<DIM, NEN, NC, NQ, FORM, S, BP, EOS>(k, e, iq, o);
+  using RB = RecBlock<DIM, NEN, NC, NQ, S>;
+  const int blk = t / RB::BP;
+  const RecOut<QPT, RB::BPS> o{reinterpret_cast<S*>(out) + (size_t)blk * (size_t)RB::WORDS, t - blk * RB::BP};
+  point_phase<DIM, NEN, NC, NQ, FORM, S, RB::BPS, EOS>(k, e, iq, o);
 }
 
 // Resident point-stage CTAs the register budget is set for: 4 for the mixed form with
@@ -1129,22 +1178,27 @@ struct PointVecs {
   S tb[NQ][NEN][ND];
 };
 
+// Shared memory of one element slot of a matrix CTA: the per-point vectors t_b, the
+// element block staged for the scatter (FP64), and the per-warp partial traces.
 template <int DIM, int NEN, int NC, int NQ, typename S>
 struct ElemSmem {
   using M = MatShape<DIM, NEN, NC>;
-  struct In {
-    QP<DIM, NEN, NC, S> qp[NQ];
-    PointVecs<DIM, NEN, NC, NQ, S> pv;
-  };
-  union {
-    In in;
-    double stage[M::N * M::NS];
-  } u;
+  PointVecs<DIM, NEN, NC, NQ, S> pv;
+  double stage[M::N * M::NS];
   double wsum[M::WPE];
-  int nodes[NEN];
-  int64_t rowbase[NEN];
-  int32_t rowlen[NEN];
-  uint32_t blocked[NEN];
+};
+
+// Shared memory of a matrix CTA: two record blocks (the group being assembled and the
+// next one, in flight), the element slots and the two transaction barriers of the
+// blocks.  Offsets in bytes; every part 16-byte aligned.
+template <int DIM, int NEN, int NC, int NQ, typename S>
+struct MatSmem {
+  using RB = RecBlock<DIM, NEN, NC, NQ, S>;
+  using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
+  static constexpr size_t ES_BYTES = (sizeof(ES) + 15) / 16 * 16;
+  static constexpr size_t OFF_ES = 2 * RB::BYTES;
+  static constexpr size_t OFF_BAR = OFF_ES + (size_t)MatShape<DIM, NEN, NC>::EPC * ES_BYTES;
+  static constexpr size_t BYTES = OFF_BAR + 16;
 };
 
 template <int WPE>
@@ -1205,73 +1259,50 @@ __device__ __forceinline__ void add_viscous_row(S (&acc)[Layout<DIM, NC>::ND], i
   }
 }
 
+// Element stage of one group of EPC elements (list positions first + li, li = grp EPC
+// + ec) from their record block blk in shared memory; the lanes of slot ec build its
+// rows.  Elements past n are skipped.
 template <int DIM, int NEN, int NC, int NQ, typename S, bool WANT_M>
-__device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN, NC, S>* __restrict__ in,
-                                             long long first, long long n, int bid) {
+__device__ __forceinline__ void matrix_group(const KParams& k, const S* __restrict__ blk,
+                                             ElemSmem<DIM, NEN, NC, NQ, S>& E, long long first, long long n,
+                                             long long grp) {
   using L = Layout<DIM, NC>;
   using M = MatShape<DIM, NEN, NC>;
-  using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
-  constexpr int ND = M::ND, N = M::N, NA = M::NA, NT = N * N, WPE = M::WPE, EPC = M::EPC, ET = M::ET, NS = M::NS;
+  using QPT = QP<DIM, NEN, NC, S>;
+  using RB = RecBlock<DIM, NEN, NC, NQ, S>;
+  constexpr int ND = M::ND, N = M::N, NA = M::NA, NT = N * N, WPE = M::WPE, ET = M::ET, NS = M::NS;
+  constexpr int BPS = RB::BPS;
   constexpr int iT = L::iT, iY = L::iY;
   constexpr bool AFF = M::AFFINE;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x;
   const int ec = tid / ET;      // element slot in the CTA
   const int gl = tid % ET;      // thread index within the element
-  ES& E = reinterpret_cast<ES*>(smem_raw)[ec];
-  const long long li = (long long)bid * EPC + ec;
-  {
-    // the CTA's block of point records ([word][point], see RecOut) into the elements'
-    // records in shared memory, 16-byte loads over the contiguous block
-    using QPT = QP<DIM, NEN, NC, S>;
-    constexpr int BP = EPC * NQ, RW = (int)(sizeof(QPT) / sizeof(S)), V = (int)(16 / sizeof(S));
-    constexpr int NV = RW * BP / V;
-    static_assert((RW * BP) % V == 0, "record block is a whole number of 16-byte words");
-    const int4* src = reinterpret_cast<const int4*>(reinterpret_cast<const S*>(in) + (long long)bid * RW * BP);
-    ES* Es = reinterpret_cast<ES*>(smem_raw);
-    for (int i = tid; i < NV; i += M::CTA) {
-      const int4 x = src[i];
-      const S* xs = reinterpret_cast<const S*>(&x);
-#pragma unroll
-      for (int u = 0; u < V; ++u) {
-        const int w = i * V + u, f = w / BP, pp = w - f * BP;
-        reinterpret_cast<S*>(&Es[pp / NQ].u.in.qp[pp % NQ])[f] = xs[u];
-      }
-    }
-  }
-  __syncthreads();
-  if (li >= n) return;          // whole element groups exit together
+  const long long li = grp * M::EPC + ec;
+  if (li >= n) return;          // whole element groups skip together
   const long long g = first + li;
-  const long long e = k.el_list ? (long long)k.el_list[g] : g;
-  if (gl < NEN) {
-    const int nd_ = __ldg(k.conn + e * NEN + gl);
-    E.nodes[gl] = nd_;
-    const int64_t rr0 = __ldg(k.node_rp + nd_), rr1 = __ldg(k.node_rp + nd_ + 1);
-    E.rowbase[gl] = rr0 * (int64_t)(ND * ND);
-    E.rowlen[gl] = (int32_t)((rr1 - rr0) * ND);
-    const int fl = k.node_flag ? __ldg(k.node_flag + nd_) : 0;
-    E.blocked[gl] = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
-  }
+  const S* el = blk + ec * NQ;  // word f of point q of this element: el[f * BPS + q]
+  auto rec = [&](int q) { return RecIn<S, BPS>{el + q}; };
+  // scatter descriptor words of node b (carried by point b)
+  auto d_int = [&](int b, int f) { return word_int(el[f * BPS + b]); };
   S grav[DIM];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) grav[d] = S(k.gravity[d]);
-  elem_sync<WPE>(ec);
-  auto& pv = E.u.in.pv;
+  auto& pv = E.pv;
   // t_b per point
   for (int t = gl; t < NQ * NEN * ND; t += ET) {
     const int q = t / (NEN * ND), u = t % (NEN * ND), b = u / ND, col = u % ND;
-    const QP<DIM, NEN, NC, S>& c = E.u.in.qp[q];
-    S x = c.ds[0][b] * c.tau[1][col];
+    const RecIn<S, BPS> c = rec(q);
+    S x = c[GALES_W(ds) + b] * c[GALES_W(tau) + ND + col];
 #pragma unroll
-    for (int d = 1; d < DIM; ++d) x = madd(c.ds[d][b], c.tau[1 + d][col], x);
+    for (int d = 1; d < DIM; ++d) x = madd(c[GALES_W(ds) + d * NEN + b], c[GALES_W(tau) + (1 + d) * ND + col], x);
     pv.tb[q][b][col] = x;
   }
   elem_sync<WPE>(ec);
   const bool active = gl < M::LANES;
   const int row = active ? gl % N : 0;
-  const int grp = active ? gl / N : 0;
+  const int grp_a = active ? gl / N : 0;
   const int b = row / ND, r = row % ND;
-  const int a0 = grp * NA;
+  const int a0 = grp_a * NA;
   const bool cV = r >= 1 && r < iT, cE = r == iT, cvy = r >= 1 && r != iT;
   S acc[NA][ND];
 #pragma unroll
@@ -1291,17 +1322,21 @@ __device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN
     for (int y = 0; y < L::NYA; ++y) ksum.rhoD[y] = ksum.rhoDH[y] = S(0);
   }
   const S idt = S(k.inv_dt);
+  const int mrow_f = cvy ? GALES_W(tau) + r * ND : GALES_W(y);
   for (int q = 0; q < NQ; ++q) {
-    const QP<DIM, NEN, NC, S>& c = E.u.in.qp[q];
-    const S rho = c.rho, p = c.p, jx = c.JxW;
-    S gb[DIM];
+    const RecIn<S, BPS> c = rec(q);
+    const S rho = c[GALES_W(rho)], p = c[GALES_W(p)], jx = c[GALES_W(JxW)];
+    S gb[DIM], vq[DIM];
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) gb[d] = c.ds[d][b];
-    const S Nb = c.sh[b];
-    S sb = gb[0] * c.v[0];
+    for (int d = 0; d < DIM; ++d) {
+      gb[d] = c[GALES_W(ds) + d * NEN + b];
+      vq[d] = c[GALES_W(v) + d];
+    }
+    const S Nb = c[GALES_W(sh) + b];
+    S sb = gb[0] * vq[0];
 #pragma unroll
-    for (int d = 1; d < DIM; ++d) sb = madd(gb[d], c.v[d], sb);
-    const S wr = c.w[r];
+    for (int d = 1; d < DIM; ++d) sb = madd(gb[d], vq[d], sb);
+    const S wr = c[GALES_W(w) + r];
     const S ur = madd(rho, wr, cE ? p : S(0));
     S gsel = S(0);
 #pragma unroll
@@ -1309,41 +1344,40 @@ __device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN
     const S kap = (cE ? sb : S(0)) + gsel;
     // row r of FPT_b
     const S cz = sb * wr, cm = (r == 0) ? S(0) : sb * rho, cg = cE ? -Nb * rho : S(0);
-    const S* mrow = cvy ? &c.tau[r][0] : &c.y[0];
     const S* tb = &pv.tb[q][b][0];
     S F[ND];
 #pragma unroll
     for (int j = 0; j < ND; ++j) {
-      S x = cz * c.z[j];
-      x = madd(cm, mrow[j], x);
+      S x = cz * c[GALES_W(z) + j];
+      x = madd(cm, c[mrow_f + j], x);
       x = madd(ur, tb[j], x);
-      x = madd(kap, c.tau[0][j], x);
-      F[j] = madd(cg, c.tg[j], x);
+      x = madd(kap, c[GALES_W(tau) + j], x);
+      F[j] = madd(cg, c[GALES_W(tg) + j], x);
     }
     // residual row: N_b rv + sum_k dN_b/dx_k rf_k + FPT_b Res (fluid_2d.hpp:253-262, 280-290)
     {
-      S x = Nb * c.rv[r];
+      S x = Nb * c[GALES_W(rv) + r];
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) x = madd(gb[d], c.rf[d][r], x);
+      for (int d = 0; d < DIM; ++d) x = madd(gb[d], c[GALES_W(rf) + d * ND + r], x);
 #pragma unroll
-      for (int j = 0; j < ND; ++j) x = madd(F[j], c.res[j], x);
+      for (int j = 0; j < ND; ++j) x = madd(F[j], c[GALES_W(res) + j], x);
       racc = madd(jx, x, racc);
     }
     if constexpr (WANT_M) {
       // FPT_b DUDY, DUDY row r, and the a-independent velocity-column terms
       S fw = F[0];
 #pragma unroll
-      for (int j = 1; j < ND; ++j) fw = madd(F[j], c.w[j], fw);
+      for (int j = 1; j < ND; ++j) fw = madd(F[j], c[GALES_W(w) + j], fw);
       const S fu = madd(rho, fw, p * F[iT]);
       const S rF = rho * F[iT];
       S FD[ND], Dr[ND];
 #pragma unroll
       for (int j = 0; j < ND; ++j) {
         S r0j, mEj;
-        if (j == 0) { r0j = c.drho_dp; mEj = c.de_dp; }
-        else if (j < iT) { r0j = S(0); mEj = c.v[j - 1]; }
-        else if (j == iT) { r0j = c.drho_dT; mEj = c.de_dT; }
-        else { r0j = c.drho_dY[j - iY]; mEj = c.dE_dY[j - iY]; }
+        if (j == 0) { r0j = c[GALES_W(drho_dp)]; mEj = c[GALES_W(de_dp)]; }
+        else if (j < iT) { r0j = S(0); mEj = vq[j - 1]; }
+        else if (j == iT) { r0j = c[GALES_W(drho_dT)]; mEj = c[GALES_W(de_dT)]; }
+        else { r0j = c[GALES_W(drho_dY) + j - iY]; mEj = c[GALES_W(dE_dY) + j - iY]; }
         S x = madd(rF, mEj, (j >= 1 && j != iT) ? rho * F[j] : S(0));
         FD[j] = (j >= 1 && j < iT) ? x : madd(fw, r0j, x);
         S dd = madd(cE ? rho : S(0), mEj, (cvy && r == j) ? rho : S(0));
@@ -1357,23 +1391,26 @@ __device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN
       KSums<DIM, NC, S> ks;
       S nu_j = S(0);
       if constexpr (!AFF) {
-        ks.mu = jx * c.mu; ks.lambda = jx * c.lambda; ks.kappa = jx * c.kappa;
+        ks.mu = jx * c[GALES_W(mu)]; ks.lambda = jx * c[GALES_W(lambda)]; ks.kappa = jx * c[GALES_W(kappa)];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) { ks.muv[d] = ks.mu * c.v[d]; ks.lamv[d] = ks.lambda * c.v[d]; }
+        for (int d = 0; d < DIM; ++d) { ks.muv[d] = ks.mu * vq[d]; ks.lamv[d] = ks.lambda * vq[d]; }
 #pragma unroll
-        for (int y = 0; y < L::NYA; ++y) { ks.rhoD[y] = jx * c.rhoD[y]; ks.rhoDH[y] = jx * c.rhoDH[y]; }
-        nu_j = jx * c.nu;
+        for (int y = 0; y < L::NYA; ++y) {
+          ks.rhoD[y] = jx * c[GALES_W(rhoD) + y];
+          ks.rhoDH[y] = jx * c[GALES_W(rhoDH) + y];
+        }
+        nu_j = jx * c[GALES_W(nu)];
       }
 #pragma unroll
       for (int ai = 0; ai < NA; ++ai) {
         const int a = a0 + ai;
         S ga[DIM];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) ga[d] = c.ds[d][a];
-        const S Na = c.sh[a];
-        S sa = ga[0] * c.v[0];
+        for (int d = 0; d < DIM; ++d) ga[d] = c[GALES_W(ds) + d * NEN + a];
+        const S Na = c[GALES_W(sh) + a];
+        S sa = ga[0] * vq[0];
 #pragma unroll
-        for (int d = 1; d < DIM; ++d) sa = madd(ga[d], c.v[d], sa);
+        for (int d = 1; d < DIM; ++d) sa = madd(ga[d], vq[d], sa);
         S fk = sa * F[iT];
 #pragma unroll
         for (int d = 0; d < DIM; ++d) fk = madd(ga[d], F[1 + d], fk);
@@ -1395,36 +1432,37 @@ __device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN
         }
       }
       if constexpr (AFF) {
-        const S jn = jx * c.nu;
+        const S mu = c[GALES_W(mu)], lam = c[GALES_W(lambda)];
+        const S jn = jx * c[GALES_W(nu)];
 #pragma unroll
         for (int j = 0; j < ND; ++j) Dnu[j] = madd(jn, Dr[j], Dnu[j]);
-        ksum.mu = madd(jx, c.mu, ksum.mu);
-        ksum.lambda = madd(jx, c.lambda, ksum.lambda);
-        ksum.kappa = madd(jx, c.kappa, ksum.kappa);
+        ksum.mu = madd(jx, mu, ksum.mu);
+        ksum.lambda = madd(jx, lam, ksum.lambda);
+        ksum.kappa = madd(jx, c[GALES_W(kappa)], ksum.kappa);
 #pragma unroll
         for (int d = 0; d < DIM; ++d) {
-          ksum.muv[d] = madd(jx * c.mu, c.v[d], ksum.muv[d]);
-          ksum.lamv[d] = madd(jx * c.lambda, c.v[d], ksum.lamv[d]);
+          ksum.muv[d] = madd(jx * mu, vq[d], ksum.muv[d]);
+          ksum.lamv[d] = madd(jx * lam, vq[d], ksum.lamv[d]);
         }
 #pragma unroll
         for (int y = 0; y < L::NYA; ++y) {
-          ksum.rhoD[y] = madd(jx, c.rhoD[y], ksum.rhoD[y]);
-          ksum.rhoDH[y] = madd(jx, c.rhoDH[y], ksum.rhoDH[y]);
+          ksum.rhoD[y] = madd(jx, c[GALES_W(rhoD) + y], ksum.rhoD[y]);
+          ksum.rhoDH[y] = madd(jx, c[GALES_W(rhoDH) + y], ksum.rhoDH[y]);
         }
       }
     }
   }
   if constexpr (WANT_M && AFF) {
     // viscous/diffusive and dc terms of a simplex, from the point sums
-    const QP<DIM, NEN, NC, S>& c = E.u.in.qp[0];
+    const RecIn<S, BPS> c = rec(0);
     S gb[DIM];
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) gb[d] = c.ds[d][b];
+    for (int d = 0; d < DIM; ++d) gb[d] = c[GALES_W(ds) + d * NEN + b];
 #pragma unroll
     for (int ai = 0; ai < NA; ++ai) {
       S ga[DIM];
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) ga[d] = c.ds[d][a0 + ai];
+      for (int d = 0; d < DIM; ++d) ga[d] = c[GALES_W(ds) + d * NEN + a0 + ai];
       add_viscous_row<DIM, NC, S>(acc[ai], r, ksum, gb, ga);
       S gg = gb[0] * ga[0];
 #pragma unroll
@@ -1435,14 +1473,14 @@ __device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN
   }
   // Dirichlet rows (scatter.hpp:62-78) and scatter (scatter.hpp:96-97)
   const bool local = k.local_r != nullptr;
-  const bool blk = !local && ((E.blocked[b] >> r) & 1u);
+  const bool blk_row = !local && (((uint32_t)d_int(b, GALES_W(d_blocked)) >> r) & 1u);
   double avg = 0.0;
   if constexpr (WANT_M) {
     // avg_val = (1 + trace)/n (scatter.hpp:65-68), only where the element has a blocked
     // row (the same for every lane of the element)
     uint32_t any_blocked = 0u;
 #pragma unroll
-    for (int i = 0; i < NEN; ++i) any_blocked |= E.blocked[i];
+    for (int i = 0; i < NEN; ++i) any_blocked |= (uint32_t)d_int(i, GALES_W(d_blocked));
     const bool need_avg = !local && any_blocked != 0u;
     double tr = 0.0;
     if (need_avg) {
@@ -1458,7 +1496,7 @@ __device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN
         if ((gl & 31) == 0) E.wsum[gl >> 5] = tr;
       }
     }
-    elem_sync<WPE>(ec);  // the point records are dead from here on (stage aliases them)
+    elem_sync<WPE>(ec);
     if (need_avg) {
       if constexpr (WPE > 1) {
         tr = E.wsum[0];
@@ -1468,12 +1506,12 @@ __device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN
       avg = (1.0 + tr) * (1.0 / N);
     }
     if (active) {
-      double* srow = E.u.stage + row * NS + a0 * ND;
+      double* srow = E.stage + row * NS + a0 * ND;
 #pragma unroll
       for (int ai = 0; ai < NA; ++ai)
 #pragma unroll
         for (int j = 0; j < ND; ++j)
-          srow[ai * ND + j] = blk ? ((a0 + ai == b && j == r) ? avg : 0.0) : widen(acc[ai][j]);
+          srow[ai * ND + j] = blk_row ? ((a0 + ai == b && j == r) ? avg : 0.0) : widen(acc[ai][j]);
     }
     elem_sync<WPE>(ec);
   }
@@ -1482,26 +1520,24 @@ __device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN
     for (int cx = gl; cx < N; cx += ET) {
       double sum = 0.0;
       for (int rw = 0; rw < N; ++rw)
-        sum += __ldg(k.vjp_lam + (long long)E.nodes[rw / ND] * ND + rw % ND) * E.u.stage[rw * NS + cx];
-      if (sum != 0.0) atomicAdd(k.vjp_g + (long long)E.nodes[cx / ND] * ND + cx % ND, sum);
+        sum += __ldg(k.vjp_lam + (long long)d_int(rw / ND, GALES_W(d_node)) * ND + rw % ND) * E.stage[rw * NS + cx];
+      if (sum != 0.0) atomicAdd(k.vjp_g + (long long)d_int(cx / ND, GALES_W(d_node)) * ND + cx % ND, sum);
     }
     return;
   }
   if (local) {  // element-level output of execute_i (fluid_2d.hpp:200-201): m = m_, r = -r_
-    if (active && grp == 0) k.local_r[g * N + row] = widen(-racc);
+    if (active && grp_a == 0) k.local_r[g * N + row] = widen(-racc);
     if (WANT_M && k.local_m)
-      for (int t = gl; t < NT; t += ET) k.local_m[g * NT + t] = E.u.stage[(t / N) * NS + t % N];
+      for (int t = gl; t < NT; t += ET) k.local_m[g * NT + t] = E.stage[(t / N) * NS + t % N];
     return;
   }
   const int mode = k.scatter_mode;
-  if (active && grp == 0) {
-    const double rv = blk ? avg * 0.0 : widen(-racc);
-    add_to(k.rhs + (long long)E.nodes[b] * ND + r, rv, mode);
-  }
+  if (active && grp_a == 0 && !blk_row)
+    add_to(k.rhs + (long long)d_int(b, GALES_W(d_node)) * ND + r, widen(-racc), mode);
   if constexpr (WANT_M) {
-    // One block row per warp step: lane l covers columns l, l+32, ... of the row, whose
-    // offset within node b's CSR row (slot(b, a) nd + ja) is fixed per (b, column), so
-    // it is formed once per test node; consecutive lanes write the contiguous nd-runs.
+    // One block row per warp step: lane l covers columns l, l+32, ... of the row; node
+    // sb_'s dof row jb holds node a's columns from nd off(sb_, a) + jb rowlen on, so
+    // consecutive lanes write the contiguous nd-runs.
     constexpr int CH = (N + 31) / 32;   // column passes per row
     const int lane = gl & 31, warp = gl >> 5;
 #pragma unroll
@@ -1510,61 +1546,93 @@ __device__ __forceinline__ void matrix_block(const KParams& k, const QP<DIM, NEN
       if (cx >= N) break;
       const int a = cx / ND, ja = cx - a * ND;
       for (int sb_ = 0; sb_ < NEN; ++sb_) {
-        double* row = k.vals + E.rowbase[sb_] + (int64_t)warp * E.rowlen[sb_] +
-                      (int64_t)__ldg(k.slot + (e * NEN + sb_) * NEN + a) * ND + ja;
-        const int64_t step = (int64_t)WPE * E.rowlen[sb_];
-        for (int jb = warp; jb < ND; jb += WPE, row += step) {
-          const double val = E.u.stage[(sb_ * ND + jb) * NS + cx];
-          if ((__double2hiint(val) & 0x7fffffff) | __double2loint(val)) add_to(row, val, mode);
+        const int64_t rl = d_int(sb_, GALES_W(d_rowlen));
+        double* rowp = k.vals + (int64_t)d_int(sb_, GALES_W(d_off) + a) * ND + (int64_t)warp * rl + ja;
+        const int64_t step = (int64_t)WPE * rl;
+        for (int jb = warp; jb < ND; jb += WPE, rowp += step) {
+          const double val = E.stage[(sb_ * ND + jb) * NS + cx];
+          if ((__double2hiint(val) & 0x7fffffff) | __double2loint(val)) add_to(rowp, val, mode);
         }
       }
     }
   }
 }
 
+// Bulk copies of record blocks into shared memory with transaction barriers
+// (cp.async.bulk and mbarrier, sm_90+).  Every wait is bounded.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0u;
+}
+// Bounded wait on phase `parity` of a transaction barrier: false after kMbarTries
+// polls (each poll may suspend the thread for a while), far beyond any bulk copy.
+constexpr long long kMbarTries = 1ll << 24;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long i = 0; i < kMbarTries; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Interior pass, stage 2 (persistent): CTA c assembles the element groups c, c + grid,
+// ... of the n listed elements whose records start at `in`.  One thread issues the bulk
+// copy of the next group's record block into the second buffer before the CTA works
+// on the current one, so the copy overlaps the element arithmetic.  A barrier wait
+// that runs out (it cannot on a working device) sets GALES_ERR_TIMEOUT, waits (again
+// bounded) for the other buffer's copy and ends the CTA.
 template <int DIM, int NEN, int NC, int NQ, typename S, bool WANT_M>
 __global__ void __launch_bounds__(MatShape<DIM, NEN, NC>::CTA)
-    matrix_kernel(const KParams k, const QP<DIM, NEN, NC, S>* __restrict__ in, long long first, long long n) {
-  matrix_block<DIM, NEN, NC, NQ, S, WANT_M>(k, in, first, n, (int)blockIdx.x);
-}
-
-// Programmatic dependent launch (sm_90+): a launch made with programmatic stream
-// serialisation may start once every CTA of the previous launch in the stream has
-// signalled (launch_dependents) or exited; wait blocks until that previous launch has
-// completed and its writes are visible.  Without the launch attribute wait returns at
-// once.
-__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void griddep_launch_dependents() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
-// Both interior stages in one launch (the mixed form with the atomic scatter): CTAs
-// [0, pt_ctas) run the point stage of chunk c into buffer c % 3, the others the matrix
-// stage of chunk c - 1 from buffer (c - 1) % 3.  CTAs are dispatched in index order, so
-// the long FP64-bound point CTAs take their slots first and the short matrix CTAs run
-// in the slot beside them on each SM and then in the slots they free.  Launches follow
-// each other with programmatic dependence: the next launch's CTAs fill the slots this
-// launch's tail frees.  Its matrix CTAs wait for this launch to complete (they read
-// the records its point CTAs wrote); its point CTAs write buffer (c + 1) % 3, last read
-// by the matrix CTAs of launch c - 1, which has completed by then because every matrix
-// CTA of launch c signals only after its own wait.  One stream, one launch per chunk:
-// the same schedule inside a CUDA graph (whose replay of a two-stream pipeline
-// overlapped the stages less).  Every matrix CTA shape is at most 128 threads; threads
-// beyond it leave at once.
-template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, bool WANT_M, int EOS = kEosChemicals>
-__global__ void __launch_bounds__(128, point_min_ctas<FORM, EOS>())
-    interior_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ pt_out, long long pt_first, long long pt_n,
-                    int pt_ctas, const QP<DIM, NEN, NC, S>* __restrict__ mx_in, long long mx_first, long long mx_n) {
-  static_assert(MatShape<DIM, NEN, NC>::CTA <= 128, "matrix CTA fits the 128-thread launch");
-  if ((int)blockIdx.x < pt_ctas) {
-    griddep_launch_dependents();
-    point_block<DIM, NEN, NC, NQ, FORM, S, EOS>(k, pt_out, pt_first, pt_n, (int)blockIdx.x);
-    return;
+    matrix_kernel(const KParams k, const S* __restrict__ in, long long first, long long n) {
+  using RB = RecBlock<DIM, NEN, NC, NQ, S>;
+  using SM = MatSmem<DIM, NEN, NC, NQ, S>;
+  using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
+  constexpr int EPC = MatShape<DIM, NEN, NC>::EPC, ET = MatShape<DIM, NEN, NC>::ET;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  S* buf[2] = {reinterpret_cast<S*>(smem_raw), reinterpret_cast<S*>(smem_raw + RB::BYTES)};
+  ES& E = *reinterpret_cast<ES*>(smem_raw + SM::OFF_ES + (size_t)(threadIdx.x / ET) * SM::ES_BYTES);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + SM::OFF_BAR);
+  const long long ngroups = (n + EPC - 1) / EPC;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
   }
-  if ((int)threadIdx.x >= MatShape<DIM, NEN, NC>::CTA) return;
-  griddep_wait();
-  griddep_launch_dependents();
-  matrix_block<DIM, NEN, NC, NQ, S, WANT_M>(k, mx_in, mx_first, mx_n, (int)blockIdx.x - pt_ctas);
+  __syncthreads();
+  long long grp = blockIdx.x;
+  if (threadIdx.x == 0 && grp < ngroups) bulk_load(buf[0], in + grp * RB::WORDS, (uint32_t)RB::BYTES, &bar[0]);
+  for (int it = 0; grp < ngroups; ++it, grp += gridDim.x) {
+    const int cur = it & 1;
+    const long long nxt = grp + gridDim.x;
+    if (threadIdx.x == 0 && nxt < ngroups)
+      bulk_load(buf[cur ^ 1], in + nxt * RB::WORDS, (uint32_t)RB::BYTES, &bar[cur ^ 1]);
+    const bool ok = mbar_wait(&bar[cur], (uint32_t)((it >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        flag_error(k, GALES_ERR_TIMEOUT, first + grp * EPC);
+        if (nxt < ngroups) mbar_wait(&bar[cur ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+      }
+      return;
+    }
+    matrix_group<DIM, NEN, NC, NQ, S, WANT_M>(k, buf[cur], E, first, n, grp);
+    __syncthreads();  // the buffer and the element slots are free again
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -19,9 +19,12 @@ template <int DIM, int NEN, int NC, int NQ, int FORM, int EOS = kEosChemicals>
 struct InteriorInst {
   using S = typename std::conditional<FORM == GALES_FORM_FP64, double, float>::type;
   using Rec = QP<DIM, NEN, NC, S>;
-  using ES = ElemSmem<DIM, NEN, NC, NQ, S>;
+  using RB = RecBlock<DIM, NEN, NC, NQ, S>;
+  using SM = MatSmem<DIM, NEN, NC, NQ, S>;
   using M = MatShape<DIM, NEN, NC>;
-  static size_t rec_bytes() { return sizeof(Rec) * NQ; }
+  // record bytes per element, rounded up: (elements + 4) of them hold the blocks of a
+  // chunk of elements
+  static size_t rec_bytes() { return (RB::BYTES + M::EPC - 1) / M::EPC; }
   // resident point-kernel CTAs (128 threads) per SM
   static int point_occupancy() {
     int nb = 0;
@@ -37,55 +40,36 @@ struct InteriorInst {
         k, reinterpret_cast<Rec*>(buf), first, n);
     return {cudaGetLastError(), 1};
   }
+  // resident matrix CTAs per SM (set by prepare)
+  static int& matrix_occupancy() {
+    static int occ = 1;
+    return occ;
+  }
   // dynamic shared memory limits, set once per device before any launch (also before
-  // a stream capture)
+  // a stream capture), and the matrix kernel's occupancy
   static cudaError_t prepare() {
-    const int smem = (int)(sizeof(ES) * M::EPC);
+    const int smem = (int)SM::BYTES;
     cudaError_t e = cudaFuncSetAttribute(matrix_kernel<DIM, NEN, NC, NQ, S, true>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(matrix_kernel<DIM, NEN, NC, NQ, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(interior_kernel<DIM, NEN, NC, NQ, FORM, S, true, EOS>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, matrix_kernel<DIM, NEN, NC, NQ, S, true>, M::CTA, smem);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(interior_kernel<DIM, NEN, NC, NQ, FORM, S, false, EOS>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    matrix_occupancy() = nb > 0 ? nb : 1;
+    return cudaSuccess;
   }
-  // point stage of pt_n elements into pt_buf and matrix stage of mx_n elements from
-  // mx_buf in one launch (either count may be zero); pdl: programmatic dependence on
-  // the previous launch in the stream (see interior_kernel)
-  static LaunchResult interior(const KParams& k, bool want_m, void* pt_buf, long long pt_first, long long pt_n,
-                               const void* mx_buf, long long mx_first, long long mx_n, bool pdl, cudaStream_t st) {
-    const long long pt_ctas = (pt_n * NQ + 127) / 128, mx_ctas = (mx_n + M::EPC - 1) / M::EPC;
-    if (pt_ctas + mx_ctas == 0) return {cudaSuccess, 0};
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(pt_ctas + mx_ctas));
-    cfg.blockDim = dim3(128);
-    cfg.dynamicSmemBytes = sizeof(ES) * M::EPC;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = pdl ? 1 : 0;
-    Rec* po = reinterpret_cast<Rec*>(pt_buf);
-    const Rec* mi = reinterpret_cast<const Rec*>(mx_buf);
-    const int pc = (int)pt_ctas;
-    cudaError_t e = want_m
-        ? cudaLaunchKernelEx(&cfg, interior_kernel<DIM, NEN, NC, NQ, FORM, S, true, EOS>, k, po, pt_first, pt_n, pc,
-                             mi, mx_first, mx_n)
-        : cudaLaunchKernelEx(&cfg, interior_kernel<DIM, NEN, NC, NQ, FORM, S, false, EOS>, k, po, pt_first, pt_n, pc,
-                             mi, mx_first, mx_n);
-    return {e != cudaSuccess ? e : cudaGetLastError(), 1};
-  }
+  // persistent: at most (SMs x resident CTAs) CTAs, each looping over element groups
   static LaunchResult matrix(const KParams& k, bool want_m, const void* buf, long long first, long long n,
                              cudaStream_t st) {
     if (n <= 0) return {cudaSuccess, 0};
-    const size_t smem = sizeof(ES) * M::EPC;
-    const unsigned blocks = (unsigned)((n + M::EPC - 1) / M::EPC);
-    const Rec* in = reinterpret_cast<const Rec*>(buf);
+    const size_t smem = SM::BYTES;
+    const long long groups = (n + M::EPC - 1) / M::EPC;
+    const long long cap = (long long)(k.sms > 0 ? k.sms : 1) * matrix_occupancy();
+    const unsigned blocks = (unsigned)(groups < cap ? groups : cap);
+    const S* in = reinterpret_cast<const S*>(buf);
     if (want_m) matrix_kernel<DIM, NEN, NC, NQ, S, true><<<blocks, M::CTA, smem, st>>>(k, in, first, n);
     else matrix_kernel<DIM, NEN, NC, NQ, S, false><<<blocks, M::CTA, smem, st>>>(k, in, first, n);
     return {cudaGetLastError(), 1};
@@ -123,8 +107,6 @@ struct InteriorOps {
   LaunchResult (*point)(const KParams&, int nc, void* buf, long long first, long long n, cudaStream_t);
   LaunchResult (*matrix)(const KParams&, int nc, bool want_m, const void* buf, long long first, long long n,
                          cudaStream_t);
-  LaunchResult (*interior)(const KParams&, int nc, bool want_m, void* pt_buf, long long pt_first, long long pt_n,
-                           const void* mx_buf, long long mx_first, long long mx_n, bool pdl, cudaStream_t);
 };
 
 #define GALES_NC_SWITCH(expr_nc, CALL) \
@@ -169,17 +151,7 @@ struct InteriorDispatch {
 #undef GALES_C
     return {cudaErrorInvalidValue, 0};
   }
-  static LaunchResult interior(const KParams& k, int nc, bool want_m, void* pt_buf, long long pt_first,
-                               long long pt_n, const void* mx_buf, long long mx_first, long long mx_n, bool pdl,
-                               cudaStream_t st) {
-#define GALES_C(NC)                                                                                              \
-  return InteriorInst<DIM, NEN, NC, NQ, FORM, EOS>::interior(k, want_m, pt_buf, pt_first, pt_n, mx_buf, mx_first, mx_n, \
-                                                        pdl, st)
-    GALES_NC_SWITCH(nc, GALES_C)
-#undef GALES_C
-    return {cudaErrorInvalidValue, 0};
-  }
-  static InteriorOps ops() { return {&prepare, &point_occupancy, &rec_bytes, &point, &matrix, &interior}; }
+  static InteriorOps ops() { return {&prepare, &point_occupancy, &rec_bytes, &point, &matrix}; }
 };
 
 // Boundary pass of one element type; S is the matrix arithmetic type of the form.

@@ -58,6 +58,8 @@ extern "C" {
 #define GALES_ERR_MAGMA 128        /* a magma property outside its lookup tables or a zero
                                       viscosity denominator (mixtures.hpp:342-412,
                                       GiordanoEtAlViscosityModel.hpp; the reference stops) */
+#define GALES_ERR_TIMEOUT 256      /* a bounded device wait (a bulk copy of point records) ran
+                                      out; not expected on a working device */
 
 /* numerical forms */
 #define GALES_FORM_FP64 0    /* every operation in FP64 (the reference's arithmetic) */
