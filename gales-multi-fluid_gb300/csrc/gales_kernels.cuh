@@ -1816,6 +1816,36 @@ __device__ __forceinline__ T a_entry_bd(const Coef<DIM, NC, T>& c, const gales_s
   return T(0);
 }
 
+// BA and BK of one boundary point from its narrowed coefficients and area vector,
+// every entry at a compile-time (row, column), so that the entry functions fold to
+// their closed forms; one thread per point (the boundary point stage).  dst_* may be
+// global or shared memory.
+template <int DIM, int NC, typename S>
+__device__ __forceinline__ void bpoint_blocks(const Coef<DIM, NC, S>& c, const S* JNxW, const gales_side_bc& bc,
+                                              S (*BA)[Layout<DIM, NC>::ND], S (*BK)[Layout<DIM, NC>::ND][Layout<DIM, NC>::ND]) {
+  constexpr int ND = Layout<DIM, NC>::ND;
+#pragma unroll
+  for (int r = 0; r < ND; ++r)
+#pragma unroll
+    for (int col = 0; col < ND; ++col) {
+      S x = S(0);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) x = madd(a_entry_bd<DIM, NC, S>(c, bc, d, r, col), JNxW[d], x);
+      BA[r][col] = x;
+    }
+#pragma unroll
+  for (int l = 0; l < DIM; ++l)
+#pragma unroll
+    for (int r = 0; r < ND; ++r)
+#pragma unroll
+      for (int col = 0; col < ND; ++col) {
+        S x = S(0);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) x = madd(k_entry_bd<DIM, NC, S>(c, bc, d, l, r, col), JNxW[d], x);
+        BK[l][r][col] = x;
+      }
+}
+
 // Per boundary point data (one side quadrature point): the state coefficients, the
 // area vector, shape data and the boundary residual vector
 //   rb = sum_k (F_adv,k - F_dif,k) JNxW_k                       (fluid_2d.hpp:343-349)
@@ -1829,14 +1859,28 @@ struct alignas(16) BPoint {
   int flag;
 };
 
+// A boundary point's record: its data and its two matrices
+//   BA = sum_k A'_k JNxW_k,  BK_l = sum_k K'_kl JNxW_k
+// (A' and K' with the side's prescribed fluxes, fluid_2d.hpp:610-817), in S.
+template <int DIM, int NEN, int NC, typename S>
+struct alignas(16) BPointRec {
+  static constexpr int ND = Layout<DIM, NC>::ND;
+  BPoint<DIM, NEN, NC, S> pt;
+  S BA[ND][ND];
+  S BK[DIM][ND][ND];
+};
+
 template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
 struct BoundarySmem {
   static constexpr int ND = Layout<DIM, NC>::ND, N = NEN * ND;
-  BPoint<DIM, NEN, NC, S> pt[NS * NSQ];
-  S BA[ND][ND];          // sum_k A'_k JNxW_k
-  S BK[DIM][ND][ND];     // sum_k K'_kl JNxW_k
+  BPointRec<DIM, NEN, NC, S> pt[NS * NSQ];
   S m[N * N];            // element block accumulator
   double r[N];
+  double wsum;
+  int64_t rowbase[NEN];
+  int32_t rowlen[NEN];
+  uint32_t blocked[NEN];
+  uint16_t slot[NEN][NEN];
 };
 
 // Boundary point physics (fluid_2d.hpp:341-349, 610-817) at one side point with
@@ -2038,8 +2082,11 @@ __global__ void __launch_bounds__(128) bpoint_kernel(const KParams k) {
 #pragma unroll
   for (int d = 0; d < DIM; ++d) JN[d] = g.JNxW[d];
   BPoint<DIM, NEN, NC, S> P;
-  bpoint_phase<DIM, NEN, NC, S, EOS>(k, nodes, (int)k.bd_sides[li * NS + ip / NSQ], sh, ds, JN, P, e);
-  reinterpret_cast<BPoint<DIM, NEN, NC, S>*>(k.bpt_rec)[t] = P;
+  const int flag = (int)k.bd_sides[li * NS + ip / NSQ];
+  bpoint_phase<DIM, NEN, NC, S, EOS>(k, nodes, flag, sh, ds, JN, P, e);
+  BPointRec<DIM, NEN, NC, S>& O = reinterpret_cast<BPointRec<DIM, NEN, NC, S>*>(k.bpt_rec)[t];
+  O.pt = P;
+  bpoint_blocks<DIM, NC, S>(P.c, P.JNxW, k.side_bc[flag < GALES_MAX_FLAGS ? flag : 0], O.BA, O.BK);
 }
 
 // Boundary pass, one warp per listed boundary element.  Lanes first evaluate one
@@ -2055,6 +2102,7 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   constexpr int N = NEN * ND;
   constexpr int NT = N * N;
   using BS = BoundarySmem<DIM, NEN, NC, NS, NSQ, S>;
+  using BR = BPointRec<DIM, NEN, NC, S>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BS& B = *reinterpret_cast<BS*>(smem_raw);
   const int lane = threadIdx.x;
@@ -2066,24 +2114,32 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   for (int a = 0; a < NEN; ++a) nodes[a] = __ldg(k.conn + e * NEN + a);
   for (int t = lane; t < NT; t += 32) B.m[t] = S(0);
   for (int t = lane; t < N; t += 32) B.r[t] = 0.0;
-  // (1) point physics: from the boundary point records of this element when the
-  // boundary point stage ran (k.bpt_rec), otherwise one lane per (side, point)
+  // rows of the element's nodes and the element's slot table, for the scatter
+  if (lane < NEN) {
+    const int fl = k.node_flag ? __ldg(k.node_flag + nodes[lane]) : 0;
+    B.blocked[lane] = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
+    const int64_t r0 = __ldg(k.node_rp + nodes[lane]), r1 = __ldg(k.node_rp + nodes[lane] + 1);
+    B.rowbase[lane] = r0 * (int64_t)(ND * ND);
+    B.rowlen[lane] = (int32_t)((r1 - r0) * ND);
+  }
+  for (int t = lane; t < NEN * NEN; t += 32) B.slot[t / NEN][t % NEN] = __ldg(k.slot + e * NEN * NEN + t);
+  // (1) point physics and matrices: from the boundary point records of this element
+  // when the boundary point stage ran (k.bpt_rec), otherwise one lane per (side, point)
   if (k.bpt_rec) {
-    for (int t = lane; t < NS * NSQ; t += 32) B.pt[t].flag = 0;
+    for (int t = lane; t < NS * NSQ; t += 32) B.pt[t].pt.flag = 0;
     __syncwarp();
     const int p0 = k.bpt_off[li], p1 = k.bpt_off[li + 1];
-    using BP = BPoint<DIM, NEN, NC, S>;
-    static_assert(sizeof(BP) % 16 == 0, "point record must be int4-aligned");
-    constexpr int W4 = sizeof(BP) / 16;
+    static_assert(sizeof(BR) % 16 == 0, "point record must be int4-aligned");
+    constexpr int W4 = sizeof(BR) / 16;
     for (int t = lane; t < (p1 - p0) * W4; t += 32) {
       const int pt = p0 + t / W4, w = t % W4;
-      reinterpret_cast<int4*>(&B.pt[k.bpt_ip[pt]])[w] = reinterpret_cast<const int4*>(
-          reinterpret_cast<const BP*>(k.bpt_rec) + pt)[w];
+      reinterpret_cast<int4*>(&B.pt[k.bpt_ip[pt]])[w] =
+          reinterpret_cast<const int4*>(reinterpret_cast<const BR*>(k.bpt_rec) + pt)[w];
     }
   } else if (lane < NS * NSQ) {
     const int s = lane / NSQ, iq = lane % NSQ;
     const int flag = k.bd_sides[li * NS + s];
-    BPoint<DIM, NEN, NC, S>& P = B.pt[lane];
+    BPoint<DIM, NEN, NC, S>& P = B.pt[lane].pt;
     P.flag = flag;
     if (flag > 0) {
       double X[NEN][DIM];
@@ -2098,35 +2154,23 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
 #pragma unroll
       for (int d = 0; d < DIM; ++d) JNxW[d] = q.JN[d] * k.W_bd;
       bpoint_phase<DIM, NEN, NC, S, EOS>(k, nodes, flag, q.sh, q.ds, JNxW, P, e);
+      bpoint_blocks<DIM, NC, S>(P.c, P.JNxW, k.side_bc[flag < GALES_MAX_FLAGS ? flag : 0], B.pt[lane].BA,
+                                B.pt[lane].BK);
     }
   }
   __syncwarp();
-  // (2) per flagged point: BA, BK entry-parallel, then the block and residual
+  // (2) per flagged point, the block m_ba += N_b (N_a BA - sum_l dN_a/dx_l BK_l) and the
+  // residual
   for (int ip = 0; ip < NS * NSQ; ++ip) {
-    const BPoint<DIM, NEN, NC, S>& P = B.pt[ip];
+    const BR& R = B.pt[ip];
+    const BPoint<DIM, NEN, NC, S>& P = R.pt;
     if (P.flag <= 0) continue;
-    const gales_side_bc& bc = k.side_bc[P.flag < GALES_MAX_FLAGS ? P.flag : 0];
-    for (int t = lane; t < (1 + DIM) * ND * ND; t += 32) {
-      const int w = t / (ND * ND), r = (t / ND) % ND, col = t % ND;
-      S x = S(0);
-      if (w == 0) {
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) x = madd(a_entry_bd<DIM, NC, S>(P.c, bc, d, r, col), P.JNxW[d], x);
-        B.BA[r][col] = x;
-      } else {
-        const int l = w - 1;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) x = madd(k_entry_bd<DIM, NC, S>(P.c, bc, d, l, r, col), P.JNxW[d], x);
-        B.BK[l][r][col] = x;
-      }
-    }
-    __syncwarp();
     for (int t = lane; t < NT; t += 32) {
       const int row = t / N, colx = t % N;
       const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-      S x = P.sh[a] * B.BA[jb][ja];
+      S x = P.sh[a] * R.BA[jb][ja];
 #pragma unroll
-      for (int l = 0; l < DIM; ++l) x = madd(-P.ds[l][a], B.BK[l][jb][ja], x);
+      for (int l = 0; l < DIM; ++l) x = madd(-P.ds[l][a], R.BK[l][jb][ja], x);
       B.m[t] = madd(P.sh[b], x, B.m[t]);
     }
     for (int t = lane; t < N; t += 32) B.r[t] = madd(P.shr[t / ND], P.rb[t % ND], B.r[t]);
@@ -2138,20 +2182,18 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
       for (int t = lane; t < NT; t += 32) k.local_m[li * NT + t] = widen(B.m[t]);
     return;
   }
-  // second scatter pass with its own Dirichlet average (scatter.hpp:62-78)
-  double avg = 1.0;
-  for (int i = 0; i < N; ++i) avg += widen(B.m[i * N + i]);
-  avg /= N;
-  uint32_t blocked[NEN];
-  int64_t rowbase[NEN];
-  int32_t rowlen[NEN];
+  // second scatter pass with its own Dirichlet average avg = (1 + trace)/n
+  // (scatter.hpp:62-78), formed only where the element has a blocked row
+  uint32_t any_blocked = 0u;
 #pragma unroll
-  for (int a = 0; a < NEN; ++a) {
-    const int fl = k.node_flag ? __ldg(k.node_flag + nodes[a]) : 0;
-    blocked[a] = (fl >= 0 && fl < GALES_MAX_FLAGS) ? k.dirichlet_mask[fl] : 0u;
-    const int64_t r0 = __ldg(k.node_rp + nodes[a]), r1 = __ldg(k.node_rp + nodes[a] + 1);
-    rowbase[a] = r0 * (int64_t)(ND * ND);
-    rowlen[a] = (int32_t)((r1 - r0) * ND);
+  for (int a = 0; a < NEN; ++a) any_blocked |= B.blocked[a];
+  double avg = 0.0;
+  if (any_blocked != 0u || k.vjp_lam) {
+    double tr = 0.0;
+    for (int i = lane; i < N; i += 32) tr += widen(B.m[i * N + i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    avg = (1.0 + tr) * (1.0 / N);
   }
   if (k.vjp_lam) {
     // frozen-tangent VJP: g += K^T lambda for this element's boundary block
@@ -2159,7 +2201,7 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
       double sum = 0.0;
       for (int rw = 0; rw < N; ++rw) {
         const int b = rw / ND, jb = rw % ND;
-        const double val = ((blocked[b] >> jb) & 1u) ? (rw == cx ? avg : 0.0) : widen(B.m[rw * N + cx]);
+        const double val = ((B.blocked[b] >> jb) & 1u) ? (rw == cx ? avg : 0.0) : widen(B.m[rw * N + cx]);
         sum += __ldg(k.vjp_lam + (long long)nodes[b] * ND + jb) * val;
       }
       if (sum != 0.0) atomicAdd(k.vjp_g + (long long)nodes[cx / ND] * ND + cx % ND, sum);
@@ -2169,19 +2211,16 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   const int mode = k.scatter_mode;
   for (int t = lane; t < N; t += 32) {
     const int b = t / ND, jb = t % ND;
-    const bool blk = (blocked[b] >> jb) & 1u;
-    const double rv = blk ? avg * 0.0 : -B.r[t];
-    add_to(k.rhs + (long long)nodes[b] * ND + jb, rv, mode);
+    if (!((B.blocked[b] >> jb) & 1u)) add_to(k.rhs + (long long)nodes[b] * ND + jb, -B.r[t], mode);
   }
   if (k.vals) {
     for (int t = lane; t < NT; t += 32) {
       const int row = t / N, colx = t % N;
       const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
       double val = widen(B.m[t]);
-      if ((blocked[b] >> jb) & 1u) val = (row == colx) ? avg : 0.0;
+      if ((B.blocked[b] >> jb) & 1u) val = (row == colx) ? avg : 0.0;
       if (val != 0.0) {
-        const int64_t off = rowbase[b] + (int64_t)jb * rowlen[b] +
-                            (int64_t)__ldg(k.slot + (e * NEN + b) * NEN + a) * ND + ja;
+        const int64_t off = B.rowbase[b] + (int64_t)jb * B.rowlen[b] + (int64_t)B.slot[b][a] * ND + ja;
         add_to(k.vals + off, val, mode);
       }
     }

@@ -236,8 +236,8 @@ struct BoundaryInfoDispatch {
   static BoundaryInfo info(int nc) {
     BoundaryInfo b{sizeof(BGeo<DIM, NEN>), {0, 0}, &geometry};
 #define GALES_C(NC)                                                      \
-  b.rec_bytes[0] = sizeof(BPoint<DIM, NEN, NC, double>);               \
-  b.rec_bytes[1] = sizeof(BPoint<DIM, NEN, NC, float>);                \
+  b.rec_bytes[0] = sizeof(BPointRec<DIM, NEN, NC, double>);            \
+  b.rec_bytes[1] = sizeof(BPointRec<DIM, NEN, NC, float>);             \
   break
     GALES_NC_SWITCH(nc, GALES_C)
 #undef GALES_C
