@@ -1011,7 +1011,10 @@ KParams base_params(gales_asm* h, double dt) {
   memcpy(k.gp, h->ei.gp, sizeof(k.gp));
   memcpy(k.sgp, h->ei.sgp, sizeof(k.sgp));
   k.W_in = h->ei.W_in;
-  for (int q = 0; q < h->ei.nq; ++q) shape_values(h->dim, h->nen, h->ei.gp[q], k.sh_tab[q]);
+  for (int q = 0; q < h->ei.nq; ++q) {
+    shape_values(h->dim, h->nen, h->ei.gp[q], k.sh_tab[q]);
+    for (int i = 0; i < 8; ++i) k.sh_tab_f[q][i] = (float)k.sh_tab[q][i];  // round to nearest, as narrow_rn
+  }
   k.geo = h->d_geo.p;
   k.W_bd = h->ei.W_bd;
   k.tau = h->setup.tau;

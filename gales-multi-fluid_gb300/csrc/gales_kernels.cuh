@@ -67,6 +67,7 @@ struct KParams {
   int32_t sms;                 // multiprocessors of the device (persistent grids)
   const void* geo;             // ElemGeo records (per element, or per element and point)
   double sh_tab[8][8];         // shape functions at the interior points [q][node]
+  float sh_tab_f[8][8];        // the same rounded to binary32 (mixed form)
   double* local_m;             // element-level output [n_list][(nen*nd)^2] (no scatter) or null
   double* local_r;             // element-level output [n_list][nen*nd] (r = -r_) or null
   // vector-Jacobian products: lambda, g_state (+=) and g_params (+=); when vjp_lam is set
@@ -385,6 +386,7 @@ struct alignas(16) ElemGeo {
   double J;
   double G[DIM][DIM];
   double g[DIM];
+  float ds_f[DIM][NEN];  // ds rounded to binary32 (narrow_rn), for the mixed form
 };
 
 template <int DIM, int NEN>
@@ -412,7 +414,10 @@ __global__ void __launch_bounds__(128) geometry_kernel(const double* __restrict_
 #pragma unroll
   for (int d = 0; d < DIM; ++d)
 #pragma unroll
-    for (int i = 0; i < NEN; ++i) o.ds[d][i] = q.ds[d][i];
+    for (int i = 0; i < NEN; ++i) {
+      o.ds[d][i] = q.ds[d][i];
+      o.ds_f[d][i] = narrow_rn(q.ds[d][i]);
+    }
   o.J = q.J;
 #pragma unroll
   for (int i = 0; i < DIM; ++i) {
@@ -558,7 +563,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
         }
         const float dif = narrow_rn(a - b0);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) c[d] = fmaf(narrow_rn(q.ds[d][i]), dif, c[d]);
+        for (int d = 0; d < DIM; ++d) c[d] = fmaf(q.ds_f[d][i], dif, c[d]);
       }
 #pragma unroll
       for (int d = 0; d < DIM; ++d) colv[sl][d] = c[d];
@@ -578,7 +583,7 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
       for (int j = 0; j < ND; ++j) {
         const float dif = narrow_rn(Ie[i][j] - Ie[0][j]);
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) dI[d][j] = fmaf(narrow_rn(q.ds[d][i]), dif, dI[d][j]);
+        for (int d = 0; d < DIM; ++d) dI[d][j] = fmaf(q.ds_f[d][i], dif, dI[d][j]);
       }
   }
   // velocity gradient in FP64 (input of compute_h; fused in the mixed form, whose
@@ -692,6 +697,11 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
   }
   const double dt = k.dt;
   // source S (gravity; fluid_2d.hpp:597-599) and the mass-term coefficient (U - U_P)/dt - S
+  // the coefficients in the form's type R
+  using CR = Coef<DIM, NC, R>;
+  CR cr;
+  if constexpr (FORM == GALES_FORM_FP64) cr = c;
+  else cr = narrow<DIM, NC>(c);
   R SvR[ND];
 #pragma unroll
   for (int r = 0; r < ND; ++r) SvR[r] = R(0);
@@ -712,27 +722,22 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
       GALES_RECA(rv, j) = (U[j] - UP[j]) / dt - Sv[j];
     }
   } else {
-    const float rf = narrow_rn(pr.rho);
+    const float rf = cr.rho;
     float gv = 0.f;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       const float gd = k.gravity_f[d];
       SvR[1 + d] = rf * gd;
-      gv = fmaf(gd, narrow_rn(v[d]), gv);
+      gv = fmaf(gd, cr.v[d], gv);
     }
     SvR[L::iT] = rf * gv;
     const float idt = k.inv_dt_f;
 #pragma unroll
     for (int j = 0; j < ND; ++j) GALES_RECA(rv, j) = fmaf(narrow_rn(U[j] - UP[j]), idt, -SvR[j]);
   }
-  R Ur[ND];  // U in the form's type (discontinuity capturing)
+  R Ur[ND];  // U in the form's type (discontinuity capturing); U[0] = rho
 #pragma unroll
-  for (int j = 0; j < ND; ++j) Ur[j] = to_s<R>(U[j]);
-  // the coefficients in the form's type R
-  using CR = Coef<DIM, NC, R>;
-  CR cr;
-  if constexpr (FORM == GALES_FORM_FP64) cr = c;
-  else cr = narrow<DIM, NC>(c);
+  for (int j = 0; j < ND; ++j) Ur[j] = j == 0 ? cr.rho : to_s<R>(U[j]);
   // tau (fluid_2d.hpp:877-1022).  The branches give its diagonal parameters td; the FP64
   // form then forms DUDY^{-1} diag(td) by LU, the mixed form in closed form, narrowed to
   // FP32 entry by entry and only where it can be nonzero (tau_nz).
@@ -1012,27 +1017,37 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
 #pragma unroll
     for (int j = 0; j < ND; ++j) GALES_RECA(rf, (d) * ND + (j)) = S(fd[j] - fa[j] + nu * dU[d][j]);
   }
-  // write the record
+  // write the record (the mixed form takes the coefficients already rounded in cr and
+  // the shape data rounded once per mesh)
+  if constexpr (FORM == GALES_FORM_MIXED) {
 #pragma unroll
-  for (int i = 0; i < NEN; ++i) {
-    GALES_RECA(sh, i) = to_s<S>(sh[i]);
+    for (int i = 0; i < NEN; ++i) {
+      GALES_RECA(sh, i) = S(k.sh_tab_f[iq][i]);
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) GALES_RECA(ds, (d) * NEN + (i)) = to_s<S>(q.ds[d][i]);
+      for (int d = 0; d < DIM; ++d) GALES_RECA(ds, (d) * NEN + (i)) = S(q.ds_f[d][i]);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < NEN; ++i) {
+      GALES_RECA(sh, i) = to_s<S>(sh[i]);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) GALES_RECA(ds, (d) * NEN + (i)) = to_s<S>(q.ds[d][i]);
+    }
   }
   GALES_REC(JxW) = to_s<S>(JxW);
-  GALES_REC(p) = to_s<S>(p);
+  GALES_REC(p) = S(cr.p);
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) GALES_RECA(v, d) = to_s<S>(v[d]);
+  for (int d = 0; d < DIM; ++d) GALES_RECA(v, d) = S(cr.v[d]);
 #pragma unroll
-  for (int i = 0; i < NC; ++i) GALES_RECA(Y, i) = to_s<S>(Y[i]);
-  GALES_REC(rho) = to_s<S>(c.rho); GALES_REC(E) = to_s<S>(c.E);
-  GALES_REC(drho_dp) = to_s<S>(c.drho_dp); GALES_REC(drho_dT) = to_s<S>(c.drho_dT);
-  GALES_REC(de_dp) = to_s<S>(c.de_dp); GALES_REC(de_dT) = to_s<S>(c.de_dT);
-  GALES_REC(mu) = to_s<S>(c.mu); GALES_REC(lambda) = to_s<S>(c.lambda); GALES_REC(kappa) = to_s<S>(c.kappa);
+  for (int i = 0; i < NC; ++i) GALES_RECA(Y, i) = S(cr.Y[i]);
+  GALES_REC(rho) = S(cr.rho); GALES_REC(E) = S(cr.E);
+  GALES_REC(drho_dp) = S(cr.drho_dp); GALES_REC(drho_dT) = S(cr.drho_dT);
+  GALES_REC(de_dp) = S(cr.de_dp); GALES_REC(de_dT) = S(cr.de_dT);
+  GALES_REC(mu) = S(cr.mu); GALES_REC(lambda) = S(cr.lambda); GALES_REC(kappa) = S(cr.kappa);
 #pragma unroll
   for (int i = 0; i < L::NYA; ++i) {
-    GALES_RECA(drho_dY, i) = to_s<S>(c.drho_dY[i]); GALES_RECA(dE_dY, i) = to_s<S>(c.dE_dY[i]);
-    GALES_RECA(rhoD, i) = to_s<S>(c.rhoD[i]); GALES_RECA(rhoDH, i) = to_s<S>(c.rhoDH[i]);
+    GALES_RECA(drho_dY, i) = S(cr.drho_dY[i]); GALES_RECA(dE_dY, i) = S(cr.dE_dY[i]);
+    GALES_RECA(rhoD, i) = S(cr.rhoD[i]); GALES_RECA(rhoDH, i) = S(cr.rhoDH[i]);
   }
   GALES_REC(nu) = S(nu);
 #pragma unroll
