@@ -16,10 +16,12 @@
 //
 // Parallelism.  A node row of the factor and of the forward substitution depends on
 // the rows of its lower blocks, a row of the backward substitution on those of its
-// upper blocks: rows are grouped by level (longest dependency chain) on the host, and
-// each level is one launch with a warp per node row.  The two substitutions of one
-// preconditioner application are captured once into a CUDA graph whose kernels take
-// the Krylov vector's index from device memory.  The Arnoldi step (two classical
+// upper blocks: rows are grouped by level (longest dependency chain) on the host.  The
+// factorisation runs one launch per level with a warp per node row; each substitution
+// is one persistent launch in which warps take rows in level order and wait on per-row
+// ready flags (see ilu_lower_sweep_kernel).  The preconditioner application is
+// captured once into a CUDA graph whose kernels take the Krylov vector's index from
+// device memory.  The Arnoldi step (two classical
 // Gram-Schmidt passes) uses blocked dot products with fixed partial-sum order, so
 // repeated solves are bit-identical.
 #include <cuda_runtime.h>
@@ -375,7 +377,7 @@ __global__ void ilu_factor_level_smem_kernel(T* __restrict__ F, const int64_t* _
 // up to 8 blocks per lane are loaded first, so that every block's loads are in flight at
 // once (a row's substitution is one dependency level, bound by memory latency).  The
 // group partial sums are added in group order (deterministic).
-template <int ND, typename T>
+template <int ND, typename T, bool L2Z = false>
 __device__ __forceinline__ T block_row_sum(const T* __restrict__ F, const int32_t* __restrict__ f_col, int64_t pa,
                                            int64_t pb, const T* z, T* red) {
   constexpr int BB = ND * ND, G = 32 / ND;
@@ -396,7 +398,7 @@ __device__ __forceinline__ T block_row_sum(const T* __restrict__ F, const int32_
         const T* B = F + (base + (int64_t)k * G) * BB + r * ND;
         const T* zc = z + (int64_t)cidx[k] * ND;
 #pragma unroll
-        for (int c = 0; c < ND; ++c) s += B[c] * zc[c];
+        for (int c = 0; c < ND; ++c) s += B[c] * (L2Z ? __ldcg(zc + c) : zc[c]);
       }
     }
   }
@@ -471,6 +473,145 @@ __global__ void ilu_upper_level_kernel(const T* __restrict__ F, const int64_t* _
   if (lane < ND) {
     zw[(int64_t)I * ND + lane] = s;
     if (!zw_follows) zout[(int64_t)I * ND + lane] = (double)s;
+  }
+}
+
+// Sync-free substitutions: one persistent launch per triangle instead of one launch per
+// level.  A warp claims node rows from a ticket counter in level order (rows[] lists
+// them level by level), waits until the rows of its row's lower (upper) blocks are
+// marked ready, substitutes exactly as the level kernels do, and marks its row ready.
+// A warp only ever waits on rows of earlier levels, whose tickets were claimed before
+// its own by warps that are running, so the sweep always progresses; every wait is
+// still bounded (kSpinMax polls), after which GALES_ERR_TIMEOUT is set in the status
+// word and the row is left as it stands.  One lane writes a finished row and releases
+// its flag; waiting lanes acquire the flags and then read the rows from L2 (the
+// writer's L1 is not this SM's).  The row's factor blocks are prefetched into L1 before
+// it waits, so that only the dependent loads remain on the critical path.
+constexpr long long kSpinMax = 1ll << 22;
+
+__device__ __forceinline__ int ld_acquire(const int* f) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* f, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(f), "r"(v) : "memory");
+}
+__device__ __forceinline__ bool wait_flag(const int* f) {
+  for (long long i = 0; i < kSpinMax; ++i) {
+    if (ld_acquire(f) != 0) return true;
+    __nanosleep(32);
+  }
+  return false;
+}
+
+// Prefetch into L1 the factor blocks rows [pa, pb) that lane (g, r) of block_row_sum
+// will read (and their column indices), before the row waits on its dependencies.
+template <int ND, typename T>
+__device__ __forceinline__ void prefetch_row(const T* __restrict__ F, const int32_t* __restrict__ f_col, int64_t pa,
+                                             int64_t pb) {
+  constexpr int BB = ND * ND, G = 32 / ND;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / ND, r = lane - g * ND;
+  if (g < G)
+    for (int64_t p = pa + g; p < pb; p += G) {
+      const T* row = F + p * BB + r * ND;
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(row));
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(row + ND - 1));
+    }
+  for (int64_t p = pa + lane; p < pb; p += 32) asm volatile("prefetch.global.L1 [%0];" ::"l"(f_col + p));
+}
+
+template <int ND, typename T>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    ilu_lower_sweep_kernel(const T* __restrict__ F, const int64_t* __restrict__ f_rp, const int32_t* __restrict__ f_col,
+                           const int64_t* __restrict__ f_diag, const int32_t* __restrict__ rows, int64_t n,
+                           const double* vbase, T* zwbase, const int* __restrict__ jidx, int64_t ld, int zw_follows,
+                           unsigned int* ticket, int* ready, unsigned int* status) {
+  constexpr int BB = ND * ND;
+  __shared__ T red[kWarpsPerBlock][32];
+  const int lane = threadIdx.x & 31;
+  const int64_t off = jidx ? (int64_t)(*jidx) * ld : 0;
+  const double* v = vbase + off;
+  T* zw = zwbase + (zw_follows ? off : 0);
+  for (;;) {
+    unsigned int t = 0;
+    if (lane == 0) t = atomicAdd(ticket, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if ((int64_t)t >= n) break;
+    const int32_t I = rows[t];
+    const int64_t p0 = f_rp[I], pd = f_diag[I];
+    prefetch_row<ND, T>(F, f_col, p0, pd + 1);
+    bool ok = true;
+    for (int64_t p = p0 + lane; p < pd && ok; p += 32) ok = wait_flag(ready + f_col[p]);
+    if (!ok) atomicOr(status, (unsigned)GALES_ERR_TIMEOUT);
+    __syncwarp();
+    const int r = lane < ND ? lane : 0;
+    const T vi = (T)v[(int64_t)I * ND + r];
+    T s = vi - block_row_sum<ND, T, true>(F, f_col, p0, pd, zw, red[threadIdx.x >> 5]);
+    const T* D = F + pd * BB + r * ND;
+#pragma unroll
+    for (int c = 0; c < ND - 1; ++c) {
+      const T zc = __shfl_sync(0xffffffffu, s, c);
+      if (lane > c) s -= D[c] * zc;
+    }
+    // lane 0 writes the row, then releases its ready flag
+    T row[ND];
+#pragma unroll
+    for (int c = 0; c < ND; ++c) row[c] = __shfl_sync(0xffffffffu, s, c);
+    if (lane == 0) {
+#pragma unroll
+      for (int c = 0; c < ND; ++c) zw[(int64_t)I * ND + c] = row[c];
+      st_release(ready + I, 1);
+    }
+  }
+}
+
+template <int ND, typename T>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    ilu_upper_sweep_kernel(const T* __restrict__ F, const int64_t* __restrict__ f_rp, const int32_t* __restrict__ f_col,
+                           const int64_t* __restrict__ f_diag, const int32_t* __restrict__ rows, int64_t n, T* zwbase,
+                           double* zoutbase, const int* __restrict__ jidx, int64_t ld, int zw_follows,
+                           unsigned int* ticket, int* ready, unsigned int* status) {
+  constexpr int BB = ND * ND;
+  __shared__ T red[kWarpsPerBlock][32];
+  const int lane = threadIdx.x & 31;
+  const int64_t off = jidx ? (int64_t)(*jidx) * ld : 0;
+  T* zw = zwbase + (zw_follows ? off : 0);
+  double* zout = zoutbase + off;
+  for (;;) {
+    unsigned int t = 0;
+    if (lane == 0) t = atomicAdd(ticket, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if ((int64_t)t >= n) break;
+    const int32_t I = rows[t];
+    const int64_t p1 = f_rp[I + 1], pd = f_diag[I];
+    prefetch_row<ND, T>(F, f_col, pd, p1);
+    bool ok = true;
+    for (int64_t p = pd + 1 + lane; p < p1 && ok; p += 32) ok = wait_flag(ready + f_col[p]);
+    if (!ok) atomicOr(status, (unsigned)GALES_ERR_TIMEOUT);
+    __syncwarp();
+    const int r = lane < ND ? lane : 0;
+    const T yi = __ldcg(zw + (int64_t)I * ND + r);
+    T s = yi - block_row_sum<ND, T, true>(F, f_col, pd + 1, p1, zw, red[threadIdx.x >> 5]);
+    const T* D = F + pd * BB + r * ND;
+#pragma unroll
+    for (int c = ND - 1; c >= 0; --c) {
+      const T mine = s / D[c];  // meaningful on lane c only
+      const T xc = __shfl_sync(0xffffffffu, mine, c);
+      if (lane == c) s = xc;
+      else if (lane < c) s -= D[c] * xc;
+    }
+    if (!zw_follows && lane < ND) zout[(int64_t)I * ND + lane] = (double)s;
+    // lane 0 writes the row of the working vector, then releases its ready flag
+    T row[ND];
+#pragma unroll
+    for (int c = 0; c < ND; ++c) row[c] = __shfl_sync(0xffffffffu, s, c);
+    if (lane == 0) {
+#pragma unroll
+      for (int c = 0; c < ND; ++c) zw[(int64_t)I * ND + c] = row[c];
+      st_release(ready + I, 1);
+    }
   }
 }
 
@@ -611,6 +752,7 @@ struct gales_solver {
   Dev<double> d_F, d_V, d_Z, d_w, d_r, d_x, d_part, d_h, d_h2, d_y, d_vals, d_b;
   Dev<float> d_Ff, d_zf;     // FP32 factor and its substitution vector (GALES_PRECOND_ILU_FP32)
   Dev<int> d_j;
+  Dev<int> d_sync;           // sweep tickets [2] and ready flags [2][n_nodes] of the substitutions
   Dev<unsigned int> d_status;
   double* h_buf = nullptr;   // pinned: Hessenberg column and the least-squares solution
   int m = 0;                 // Krylov vectors per cycle
@@ -708,6 +850,22 @@ struct Kernels {
         kF64 ? 1 : 0);
     return cudaGetLastError();
   }
+  // both substitutions as sync-free sweeps (tickets and ready flags cleared by the caller)
+  static cudaError_t sweeps(gales_solver* s, const double* v, double* z, const int* j, int64_t ld, cudaStream_t st) {
+    T* zw = kF64 ? reinterpret_cast<T*>(z) : reinterpret_cast<T*>(s->d_zf.p);
+    const unsigned g = std::min<unsigned>(grid_for(s->n_nodes), (unsigned)s->sms);
+    unsigned int* tk = reinterpret_cast<unsigned int*>(s->d_sync.p);
+    int* ready = s->d_sync.p + 2;
+    ilu_lower_sweep_kernel<ND, T><<<g, 32 * kWarpsPerBlock, 0, st>>>(
+        factor_ptr<T>(s), s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_f.p, s->n_nodes, v, zw, j, ld,
+        kF64 ? 1 : 0, tk, ready, s->d_status.p);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    ilu_upper_sweep_kernel<ND, T><<<g, 32 * kWarpsPerBlock, 0, st>>>(
+        factor_ptr<T>(s), s->d_f_rp.p, s->d_f_col.p, s->d_f_diag.p, s->d_rows_b.p, s->n_nodes, zw, z, j, ld,
+        kF64 ? 1 : 0, tk + 1, ready + s->n_nodes, s->d_status.p);
+    return cudaGetLastError();
+  }
   static cudaError_t spmv(gales_solver* s, const double* vals, const double* x, const double* b, double* y,
                           cudaStream_t st) {
     spmv_kernel<ND><<<grid_for(s->n_rows), 32 * kWarpsPerBlock, 0, st>>>(vals, s->d_node_rp.p, s->d_node_col.p,
@@ -722,13 +880,14 @@ struct Ops {
   cudaError_t (*factor_level)(gales_solver*, int, cudaStream_t);
   cudaError_t (*lower_level)(gales_solver*, int, const double*, double*, const int*, int64_t, cudaStream_t);
   cudaError_t (*upper_level)(gales_solver*, int, double*, const int*, int64_t, cudaStream_t);
+  cudaError_t (*sweeps)(gales_solver*, const double*, double*, const int*, int64_t, cudaStream_t);
   cudaError_t (*spmv)(gales_solver*, const double*, const double*, const double*, double*, cudaStream_t);
 };
 
 template <int ND, typename T>
 Ops ops_for() {
   using K = Kernels<ND, T>;
-  return {K::prepare, K::to_factor, K::factor_level, K::lower_level, K::upper_level, K::spmv};
+  return {K::prepare, K::to_factor, K::factor_level, K::lower_level, K::upper_level, K::sweeps, K::spmv};
 }
 
 template <typename T>
@@ -755,12 +914,12 @@ inline bool has_ilu(const gales_solver* s) {
   return s->prm.precond == GALES_PRECOND_ILU || s->prm.precond == GALES_PRECOND_ILU_FP32;
 }
 
-// z = M^-1 v for columns addressed by *j (graph) or plain pointers (j null).
+// z = M^-1 v for columns addressed by *j (graph) or plain pointers (j null): the two
+// sync-free sweeps after clearing their tickets and ready flags.
 int apply_prec(gales_solver* s, const Ops& o, const double* v, double* z, const int* j, int64_t ld, cudaStream_t st) {
-  const int nf = (int)s->lev_off_f.size() - 1, nb = (int)s->lev_off_b.size() - 1;
-  for (int l = 0; l < nf; ++l) SCK(s, o.lower_level(s, l, v, z, j, ld, st), "lower substitution");
-  for (int l = 0; l < nb; ++l) SCK(s, o.upper_level(s, l, z, j, ld, st), "upper substitution");
-  s->launches += nf + nb;
+  SCK(s, cudaMemsetAsync(s->d_sync.p, 0, s->d_sync.n * sizeof(int), st), "clear sweep flags");
+  SCK(s, o.sweeps(s, v, z, j, ld, st), "substitutions");
+  s->launches += 2;
   return 0;
 }
 
@@ -914,7 +1073,7 @@ int gales_solver_create(gales_asm* h, const gales_solver_params* prm, gales_solv
       s->d_V.alloc((size_t)(s->m + 1) * n_rows) || s->d_Z.alloc((size_t)s->m * n_rows) || s->d_w.alloc(n_rows) ||
       s->d_r.alloc(n_rows) || s->d_x.alloc(n_rows) || s->d_part.alloc((size_t)s->dot_blocks * (s->m + 2)) ||
       s->d_h.alloc(s->m + 2) || s->d_h2.alloc(s->m + 2) || s->d_y.alloc(s->m + 2) || s->d_j.alloc(1) ||
-      s->d_status.alloc(1)) {
+      s->d_sync.alloc(2 + 2 * (size_t)n_nodes) || s->d_status.alloc(1)) {
     cudaGetLastError();
     return bail(GALES_ERR_NO_MEMORY);
   }
@@ -1062,7 +1221,7 @@ int gales_solver_solve(gales_solver* s, const double* vals, const double* rhs, d
         if (s->prec_graph) {
           set_index_kernel<<<1, 1, 0, st>>>(s->d_j.p, j);
           SCK(s, cudaGraphLaunch(s->prec_graph, st), "preconditioner graph");
-          s->launches += 1 + (int64_t)s->lev_off_f.size() - 1 + (int64_t)s->lev_off_b.size() - 1;
+          s->launches += 3;
         } else {
           rc = apply_prec(s, o, vj, zj, nullptr, 0, st);
           if (rc) return rc;
@@ -1132,6 +1291,12 @@ int gales_solver_solve(gales_solver* s, const double* vals, const double* rhs, d
   if (!x_dev) {
     SCK(s, cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, st), "copy x");
     SCK(s, cudaStreamSynchronize(st), "copy x");
+  }
+  if (prec) {  // a substitution wait that ran out (not expected on a working device)
+    unsigned int stat = 0;
+    SCK(s, cudaMemcpyAsync(&stat, s->d_status.p, sizeof(stat), cudaMemcpyDeviceToHost, st), "status");
+    SCK(s, cudaStreamSynchronize(st), "status");
+    if (stat & GALES_ERR_TIMEOUT) return sfail(s, GALES_ERR_TIMEOUT, "a substitution wait ran out");
   }
   if (res) {
     res->iterations = iters;
