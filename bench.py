@@ -62,6 +62,47 @@ def peaks():
         return {}
 
 
+# Per-element instruction counts of the mixed tet pass (3 components), from ncu on the
+# 163,618-tet mesh of the 30^3 lattice (profiles/point_matrix_kernels_mixed_tet4_lattice30.md):
+# FP64 thread instructions per quadrature point of the point kernel and warp
+# instructions per element of the matrix kernel.
+POINT_FP64_PER_POINT = {"dfma": 206.8, "dmul_dadd": 199.1}
+MATRIX_WARP_INST_PER_ELEM = 2854
+NQ_TET = 4
+
+
+def pipe_rates():
+    """The device's FP64/FP32 arithmetic rates (pipe_rates probe built with the library)."""
+    exe = ROOT / "gales-multi-fluid_gb300" / "pipe_rates"
+    try:
+        out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+        return json.loads(out.stdout.strip().splitlines()[-1])
+    except Exception as e:  # reported, never fatal
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def compute_roofline(n_el, point_ms, matrix_ms):
+    """Compute side of the interior pass: the point kernel against the FP64 rate (its FP64
+    instructions per point at the measured DFMA / DMUL rates), the matrix kernel against
+    the issue rate (4 warp instructions per SM per clock)."""
+    pr = pipe_rates()
+    out = {"pipe_rates": pr, "point_kernel_ms": point_ms, "matrix_kernel_ms": matrix_ms}
+    if "error" in pr or not (point_ms and matrix_ms and point_ms > 0 and matrix_ms > 0):
+        return out
+    sms, hz = pr["sm_count"], pr["clock_mhz"] * 1e6
+    fp64_cycles = n_el * NQ_TET * (POINT_FP64_PER_POINT["dfma"] / pr["dfma_per_clk_sm"] +
+                                   POINT_FP64_PER_POINT["dmul_dadd"] / pr["dmul_per_clk_sm"])
+    t_fp64 = fp64_cycles / sms / hz * 1e3
+    t_issue = n_el * MATRIX_WARP_INST_PER_ELEM / (4.0 * sms) / hz * 1e3
+    out["point_kernel"] = {"bound": "fp64 (the FMA pipe, shared with FP32 on this GPU)",
+                           "ms_at_peak": t_fp64, "frac": t_fp64 / point_ms,
+                           "fp64_per_point": POINT_FP64_PER_POINT}
+    out["matrix_kernel"] = {"bound": "instruction issue (4 warp instructions per SM per clock)",
+                            "ms_at_peak": t_issue, "frac": t_issue / matrix_ms,
+                            "warp_inst_per_element": MATRIX_WARP_INST_PER_ELEM}
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -314,7 +355,7 @@ def hex_block(args, torch, dev, with_clocks=False):
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm if hbm else None, "traffic": TRAFFIC_BYTES_PER_ELEM_HEX * ne,
                      "traffic_source": "ncu DRAM bytes per element of a 64,000-hex assembly x elements",
-                     "kernel": "interior_kernel (mixed form)",
+                     "kernel": "interior pass (point_kernel + matrix_kernel, mixed form)",
                      "kernel_ms": k_mx, "bytes_per_element": BYTES_PER_ELEM_HEX,
                      "peak_source": "measured (MEASURED_PEAKS.json)"},
         "objective_vjp": {"J": Jval, "ms": vjp_ms,
@@ -530,15 +571,27 @@ def vjp_block(gm, syn, torch, dev, n=32):
 
     r64 = t(lambda: fa.residual(Id, Pd, 1e-3, b, form=gm.FORM_FP64))
     rmx = t(lambda: fa.residual(Id, Pd, 1e-3, b, form=gm.FORM_MIXED))
+    # the exact VJP keeps its per-point reverse-mode tape in registers and, beyond them,
+    # in per-thread local memory, which the driver reserves for every thread the device
+    # can hold when the kernel first runs: that reservation is the recompute design's
+    # real footprint
+    torch.cuda.synchronize(dev)
+    free0 = torch.cuda.mem_get_info(dev)[0]
+    fa.vjp(Id, Pd, 1e-3, lam, gm.VJP_EXACT, g, th)
+    torch.cuda.synchronize(dev)
+    local_reserved = max(0, free0 - torch.cuda.mem_get_info(dev)[0])
     ex = t(lambda: fa.vjp(Id, Pd, 1e-3, lam, gm.VJP_EXACT, g, th))
     fr = t(lambda: fa.vjp(Id, Pd, 1e-3, lam, gm.VJP_FROZEN, g))
     nq = 4
     return {"workload": f"{mesh.n_elements} Delaunay tets ({n}^3 lattice), 3 components, lambda a seeded unit vector",
             "exact_ms": ex, "frozen_ms": fr, "residual_fp64_ms": r64, "residual_mixed_ms": rmx,
             "exact_over_residual_fp64": ex / r64, "exact_over_residual_mixed": ex / rmx,
-            "memory": {"recompute_extra_bytes": 0,
+            "memory": {"recompute_extra_bytes": int(local_reserved),
                        "store_points_bytes": int(mesh.n_elements * nq * 8 * 360),
-                       "note": "recompute: no per-point storage; store: ~360 doubles of forward tape per point"}}
+                       "note": "recompute: the device-wide local-memory reservation of the exact VJP kernel "
+                               "(its spilled per-thread tape, independent of the mesh size), measured as the "
+                               "drop in free device memory at its first launch; store: ~360 doubles of forward "
+                               "tape per point"}}
 
 
 def run_reference(args):
@@ -638,21 +691,24 @@ def main():
             dist.barrier()
         torch.cuda.synchronize(dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        kern = []
+        kern, stages = [], []
         launches0 = fa.launch_count()
         e0.record(stream)
         for _ in range(k):
             step(form)
             kern.append(fa.phase_ms(1))
+            stages.append((fa.phase_ms(3), fa.phase_ms(4)))
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ms = max_over_ranks(e0.elapsed_time(e1) / k, dist, dev)
+        timed.stages = (statistics.median(x[0] for x in stages), statistics.median(x[1] for x in stages))
         return ms, statistics.median(kern), fa.launch_count() - launches0
 
     ms64, k64, _ = timed(gm.FORM_FP64, args.fp64_steps, 1)
     with ClockSampler(local) as clk:
         ms_mx, k_mx, launches = timed(gm.FORM_MIXED, args.steps, args.warmup)
     clocks = clk.summary()
+    point_ms, matrix_ms = timed.stages
 
     # e2e: host pinned buffers through the C ABI, copies inside the timed region
     Ih = torch.from_numpy(I).pin_memory()
@@ -674,6 +730,16 @@ def main():
         e2e_steps.append((time.perf_counter() - ts) * 1e3)
     torch.cuda.synchronize(dev)
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dist, dev)
+    # the device-to-host copy of the CSR values alone (same pinned buffer and stream)
+    d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        lph.vals.copy_(lp.vals, non_blocking=True)
+        d0.record(stream)
+        for _ in range(3):
+            lph.vals.copy_(lp.vals, non_blocking=True)
+        d1.record(stream)
+    torch.cuda.synchronize(dev)
+    d2h_ms = d0.elapsed_time(d1) / 3
 
     ne = mesh.n_elements
     value = whole_job_rate(ne, ms_mx, world)
@@ -694,16 +760,21 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if hbm else None, "traffic": TRAFFIC_BYTES_PER_ELEM_TET * ne,
                      "traffic_source": "ncu DRAM bytes per element of a 163,618-tet assembly x elements",
-                     "kernel": "interior_kernel (mixed form)", "kernel_ms": k_mx,
+                     "kernel": "interior pass (point_kernel + matrix_kernel, mixed form)", "kernel_ms": k_mx,
                      "bytes_per_element": BYTES_PER_ELEM_TET, "peak_source": "measured (MEASURED_PEAKS.json)"},
         "e2e": {"value": whole_job_rate(ne, e2e_s * 1e3, world), "unit": "elements/s",
                 "h2d_bytes_per_step": 2 * fa.n_rows * 8, "d2h_bytes_per_step": (nnz + fa.n_rows) * 8,
                 "ms_per_step": e2e_s * 1e3,
                 "step_ms": {"median": statistics.median(e2e_steps), "min": min(e2e_steps),
                             "max": max(e2e_steps)},
-                "over_device_buffers": (e2e_s * 1e3) / ms_mx},
+                "over_device_buffers": (e2e_s * 1e3) / ms_mx,
+                "d2h_values_alone_ms": d2h_ms, "d2h_gbs": nnz * 8 / (d2h_ms * 1e-3) / 1e9,
+                "note": "a host-buffer call ends with the copy of the CSR values to the host; the rows are "
+                        "copied while the pass runs, chunk by chunk, so the step is bound by the larger of "
+                        "the assembly and the copy of all values (d2h_values_alone_ms)"},
         "gpu_launches": int(launches),
         "clocks": clocks,
+        "compute": compute_roofline(ne, point_ms, matrix_ms),
     }
     if rank == 0 and not args.no_vjp:
         syn = importlib.import_module("gales-multi-fluid_gb300.synthetic")

@@ -517,7 +517,8 @@ class FluidAssembly:
         return self._L.gales_asm_last_ms(self._h)
 
     def phase_ms(self, phase: int) -> float:
-        """0 = clear, 1 = interior kernel(s), 2 = boundary pass (CUDA events, last call)."""
+        """0 = clear, 1 = interior kernel(s), 2 = boundary pass, 3 / 4 = point / matrix stage
+        of the interior pass's first chunk (CUDA events, last call)."""
         return self._L.gales_asm_last_phase_ms(self._h, phase)
 
     def launch_count(self) -> int:

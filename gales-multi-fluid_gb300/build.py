@@ -17,6 +17,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = HERE / "libgales_asm.so"
+PIPE_RATES = HERE / "pipe_rates"   # arithmetic pipe-rate probe (compute roofline of bench.py)
 SOURCES = (["gales_host.cu", "gales_mesh_io.cu", "gales_solver.cu", "gales_magma.cu"] + [f"gales_{t}_{f}.cu" for t in ("hex8", "tet4", "tri3", "quad4") for f in ("fp64", "mixed")]
            + [f"gales_vjp_{t}.cu" for t in ("hex8", "tet4", "tri3", "quad4")]
            + [f"gales_{t}_magma_{f}.cu" for t in ("hex8", "tet4", "tri3", "quad4") for f in ("fp64", "mixed")])
@@ -55,6 +56,9 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             flags = [("-fmad=true" if (f == "-fmad=false" and "_mixed" in src.name) else f) for f in FLAGS]
             cmd = [nvcc, *ARCH, *flags, "-I", str(HERE.parent / "include"), "-c", str(src), "-o", str(obj)]
             jobs.append((s, cmd))
+    pr_src = CSRC / "pipe_rates.cu"
+    if force or not PIPE_RATES.exists() or PIPE_RATES.stat().st_mtime < pr_src.stat().st_mtime:
+        jobs.append(("pipe_rates.cu", [nvcc, *ARCH, "-std=c++17", "-O3", "-o", str(PIPE_RATES), str(pr_src)]))
     if jobs:
         workers = max(1, min(len(jobs), os.cpu_count() or 1))
         with cf.ThreadPoolExecutor(workers) as ex:

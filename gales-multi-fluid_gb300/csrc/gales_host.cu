@@ -251,6 +251,7 @@ struct gales_asm {
   double* h_aux = nullptr;                       // pinned scalar
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t evp[4] = {nullptr, nullptr, nullptr, nullptr};  // clear | interior | boundary | end
+  cudaEvent_t evs[2] = {nullptr, nullptr};  // end of the first chunk's point and matrix stages
   int32_t scatter_mode = GALES_SCATTER_ATOMIC;
   // interior pass: point-record chunk buffers (scratch) and, for the FP64 form, two
   // internal streams
@@ -789,6 +790,8 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
   if ((ce = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(ce, "event");
   for (int i = 0; i < 4; ++i)
     if ((ce = cudaEventCreate(&h->evp[i])) != cudaSuccess) return bail(ce, "event");
+  for (int i = 0; i < 2; ++i)
+    if ((ce = cudaEventCreate(&h->evs[i])) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreateWithFlags(&h->ev_bfork, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaEventCreateWithFlags(&h->ev_bjoin, cudaEventDisableTiming)) != cudaSuccess) return bail(ce, "event");
   if ((ce = cudaStreamCreateWithFlags(&h->bst, cudaStreamNonBlocking)) != cudaSuccess) return bail(ce, "stream");
@@ -903,6 +906,8 @@ void gales_asm_destroy(gales_asm* h) {
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (int i = 0; i < 4; ++i)
     if (h->evp[i]) cudaEventDestroy(h->evp[i]);
+  for (int i = 0; i < 2; ++i)
+    if (h->evs[i]) cudaEventDestroy(h->evs[i]);
   if (h->ev_bfork) cudaEventDestroy(h->ev_bfork);
   if (h->ev_bjoin) cudaEventDestroy(h->ev_bjoin);
   if (h->bst) cudaStreamDestroy(h->bst);
@@ -1074,7 +1079,7 @@ int copy_finished_rows(gales_asm* h, RowCopy& rc, int64_t elements_done, bool la
 // point kernel, then the matrix kernel, on the caller's stream, with the optional
 // device-to-host copy of finished rows (rc) after each chunk.
 int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long long n, cudaStream_t st,
-                 RowCopy* rc = nullptr) {
+                 RowCopy* rc = nullptr, bool stage_events = false) {
   const InteriorOps& ops = h->ops[form];
   const size_t rb = ops.rec_bytes(h->nc);
   if (rb == 0) return fail(h, GALES_ERR_UNSUPPORTED, "no interior kernel for this element/component count");
@@ -1087,9 +1092,11 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
     LaunchResult r = ops.point(k, h->nc, buf, first, cnt, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "point kernel");
     h->launches += r.launches;
+    if (stage_events && c == 0) CK(h, cudaEventRecord(h->evs[0], st), "event");
     r = ops.matrix(k, h->nc, want_m, buf, first, cnt, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "matrix kernel");
     h->launches += r.launches;
+    if (stage_events && c == 0) CK(h, cudaEventRecord(h->evs[1], st), "event");
     if (rc) {
       const int e = copy_finished_rows(h, *rc, first + cnt, c == nchunks - 1, st);
       if (e) return e;
@@ -1287,7 +1294,7 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
   } else {
     k.el_list = rc ? h->d_sweep_rows.p : h->d_sweep.p;
     k.n_list = h->n_el;
-    int e = run_interior(h, k, form, want_m, h->n_el, st, rc);
+    int e = run_interior(h, k, form, want_m, h->n_el, st, rc, timed);
     if (e) return e;
   }
   if (timed) CK(h, cudaEventRecord(h->evp[2], st), "event");
@@ -1854,9 +1861,11 @@ const char* gales_asm_last_error(gales_asm* h) { return h ? h->err.c_str() : "nu
 double gales_asm_last_ms(gales_asm* h) { return h ? h->last_ms : 0.0; }
 
 double gales_asm_last_phase_ms(gales_asm* h, int32_t phase) {
-  if (!h || phase < 0 || phase > 2) return -1.0;
+  if (!h || phase < 0 || phase > 4) return -1.0;
   float ms = -1.f;
-  if (cudaEventElapsedTime(&ms, h->evp[phase], h->evp[phase + 1]) != cudaSuccess) {
+  const cudaEvent_t a = phase == 3 ? h->evp[1] : (phase == 4 ? h->evs[0] : h->evp[phase]);
+  const cudaEvent_t b = phase == 3 ? h->evs[0] : (phase == 4 ? h->evs[1] : h->evp[phase + 1]);
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
     cudaGetLastError();
     return -1.0;
   }

@@ -443,9 +443,11 @@ const char* gales_asm_last_error(gales_asm* h);
 /* Device time in ms of the last assemble/residual/vjp call (CUDA events on its stream). */
 double gales_asm_last_ms(gales_asm* h);
 /* Device time in ms of one phase of the last assemble/residual call, CUDA events on
- * its stream: 0 = clearing A and b, 1 = interior element kernel(s), 2 = boundary pass.
- * With the atomic scatter the boundary pass runs beside the interior kernels, so
- * phase 2 is only the part of it that outlasts them. */
+ * its stream: 0 = clearing A and b, 1 = interior element kernel(s), 2 = boundary pass,
+ * 3 / 4 = the point / matrix stage of the interior pass's first chunk (the whole pass
+ * when it has one chunk; atomic scatter only).  With the atomic scatter the boundary
+ * pass runs beside the interior kernels, so phase 2 is only the part of it that
+ * outlasts them. */
 double gales_asm_last_phase_ms(gales_asm* h, int32_t phase);
 /* Number of kernel launches made by the library since the handle was created. */
 int64_t gales_asm_launch_count(gales_asm* h);
