@@ -47,11 +47,11 @@ for p in (ROOT, ROOT / "oracle"):
 
 METRIC = "residual+Jacobian elements/s, mixed vs FP64 on 1 GB300 at <=1e-6 rel err; HBM %"
 BYTES_PER_ELEM_TET = 4 * 4 + 8 * 3 * 4 + 2 * 8 * 4 * 7 + 16 * (4 * 7) ** 2 + 16 * 4 * 7  # 13,552
-# DRAM bytes per element of one mixed tet assembly: dram__bytes_read.sum +
-# dram__bytes_write.sum summed by ncu over every kernel of an assembly (interior
-# launches, zero fill, boundary) on the 163,618-tet mesh of the 30^3 lattice, whose CSR
-# bytes per element (1,002) match the 1.0M-tet mesh's (982); scaled by the element count.
-TRAFFIC_BYTES_PER_ELEM_TET = 6877
+# DRAM bytes per element of the mixed tet interior pass (point and matrix kernels):
+# dram__bytes_read.sum + dram__bytes_write.sum from ncu on the 163,618-tet mesh of the
+# 30^3 lattice, whose CSR bytes per element (1,002) match the 1.0M-tet mesh's (982);
+# scaled by the element count (profiles/dram_traffic_tet4_lattice30_assembly.md).
+TRAFFIC_BYTES_PER_ELEM_TET = 9318
 LATTICE_N = 54
 
 
@@ -66,7 +66,7 @@ def peaks():
 # 163,618-tet mesh of the 30^3 lattice (profiles/point_matrix_kernels_mixed_tet4_lattice30.md):
 # FP64 thread instructions per quadrature point of the point kernel and warp
 # instructions per element of the matrix kernel.
-POINT_FP64_PER_POINT = {"dfma": 206.8, "dmul_dadd": 199.1}
+POINT_FP64_PER_POINT = {"dfma": 206.8, "dmul_dadd": 202.1}
 MATRIX_WARP_INST_PER_ELEM = 2854
 NQ_TET = 4
 
@@ -212,10 +212,10 @@ def cpu_oracle_rate(mesh, mat, setup, I, P, dt, row_ptr, col, colour, n_colours,
 
 
 BYTES_PER_ELEM_HEX = 4 * 8 + 8 * 3 * 8 + 2 * 8 * 8 * 8 + 16 * (8 * 8) ** 2 + 16 * 8 * 8  # 67,808
-# DRAM bytes per element of one mixed hex assembly, summed by ncu over every kernel of
-# an assembly on the 64,000-hex mesh of a 40^3 grid (CSR bytes per element 14,172, 1.9%
-# above the 160x160x156 mesh's 13,911); scaled by the element count.
-TRAFFIC_BYTES_PER_ELEM_HEX = 64105
+# DRAM bytes per element of the mixed hex interior pass, from ncu on the 64,000-hex mesh
+# of a 40^3 grid (CSR bytes per element 14,172, 1.9% above the 160x160x156 mesh's
+# 13,911); scaled by the element count (profiles/dram_traffic_hex8_40cube_assembly.md).
+TRAFFIC_BYTES_PER_ELEM_HEX = 64059
 
 
 def top_gas_flux_lambda(mesh, mat, I, nd):
@@ -354,7 +354,7 @@ def hex_block(args, torch, dev, with_clocks=False):
         "mixed_rel_err_vs_fp64": err,
         "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm if hbm else None, "traffic": TRAFFIC_BYTES_PER_ELEM_HEX * ne,
-                     "traffic_source": "ncu DRAM bytes per element of a 64,000-hex assembly x elements",
+                     "traffic_source": "ncu DRAM bytes per element of the interior pass on 64,000 hexes x elements",
                      "kernel": "interior pass (point_kernel + matrix_kernel, mixed form)",
                      "kernel_ms": k_mx, "bytes_per_element": BYTES_PER_ELEM_HEX,
                      "peak_source": "measured (MEASURED_PEAKS.json)"},
@@ -759,7 +759,7 @@ def main():
                                                "against the oracle on this mesh (<= 1e-12)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if hbm else None, "traffic": TRAFFIC_BYTES_PER_ELEM_TET * ne,
-                     "traffic_source": "ncu DRAM bytes per element of a 163,618-tet assembly x elements",
+                     "traffic_source": "ncu DRAM bytes per element of the interior pass on 163,618 tets x elements",
                      "kernel": "interior pass (point_kernel + matrix_kernel, mixed form)", "kernel_ms": k_mx,
                      "bytes_per_element": BYTES_PER_ELEM_TET, "peak_source": "measured (MEASURED_PEAKS.json)"},
         "e2e": {"value": whole_job_rate(ne, e2e_s * 1e3, world), "unit": "elements/s",
