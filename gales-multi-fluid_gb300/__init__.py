@@ -407,6 +407,10 @@ class FluidAssembly:
     def set_scatter(self, mode: int):
         self._check(self._L.gales_asm_set_scatter(self._h, mode))
 
+    def set_chunk(self, elements: int = 0):
+        """Elements per interior chunk (0: the default, as many as 3 GiB of records hold)."""
+        self._check(self._L.gales_asm_set_chunk(self._h, int(elements)))
+
     # the hot path
     def execute(self, I, P, dt: float, lp: LinearSystem, form: int = FORM_FP64, stream: int = 0) -> float:
         """fluid_assembly::execute(): fill lp.vals and lp.rhs; returns wall seconds."""

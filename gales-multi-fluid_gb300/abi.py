@@ -143,6 +143,8 @@ def lib() -> C.CDLL:
     L.gales_asm_colouring.restype = C.c_int
     L.gales_asm_set_scatter.argtypes = [vp, i32]
     L.gales_asm_set_scatter.restype = C.c_int
+    L.gales_asm_set_chunk.argtypes = [vp, C.c_int64]
+    L.gales_asm_set_chunk.restype = C.c_int
     L.gales_asm_assemble.argtypes = [vp, vp, vp, C.c_double, i32, vp, vp, vp]
     L.gales_asm_assemble.restype = C.c_int
     L.gales_asm_assemble_noalloc.argtypes = [vp, vp, vp, C.c_double, i32, vp, vp, vp]
@@ -232,7 +234,7 @@ def lib() -> C.CDLL:
 EXPORTED = [
     "gales_chemical_custom", "gales_chemical_ideal_gas", "gales_setup_default",
     "gales_asm_create", "gales_asm_destroy", "gales_asm_pattern", "gales_asm_node_graph",
-    "gales_asm_colouring", "gales_asm_set_scatter", "gales_asm_assemble", "gales_asm_assemble_noalloc",
+    "gales_asm_colouring", "gales_asm_set_scatter", "gales_asm_set_chunk", "gales_asm_assemble", "gales_asm_assemble_noalloc",
     "gales_asm_residual", "gales_asm_enqueue", "gales_asm_sync",
     "gales_asm_vjp", "gales_asm_element_blocks", "gales_asm_norm2", "gales_asm_status", "gales_asm_last_error",
     "gales_asm_last_ms", "gales_asm_last_phase_ms", "gales_asm_launch_count",

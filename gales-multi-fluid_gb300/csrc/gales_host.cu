@@ -263,6 +263,7 @@ struct gales_asm {
   MagmaOps mops{};
   DevBuf<unsigned char> qpbuf;          // point records of one chunk
   long long chunk_elems[2] = {1, 1};   // elements per chunk, per form
+  long long chunk_default[2] = {1, 1};  // the chunk the record buffer was sized for
   int sms = 1;                          // multiprocessors of the device
   DevBuf<unsigned char> d_geo;   // element geometry at the interior points (mesh.hpp:468-495)
   cudaStream_t bst = nullptr;                  // boundary pass, concurrent with the interior
@@ -823,6 +824,7 @@ int gales_asm_create(const gales_mesh_desc* m, const gales_material_desc* mat,
       if (rb == 0) continue;
       const long long cap = std::max<long long>(4, (long long)(kRecordBytes / rb) / 4 * 4);
       h->chunk_elems[f] = std::max<long long>(1, std::min<long long>(cap, std::max<int64_t>(h->n_el, 1)));
+      h->chunk_default[f] = h->chunk_elems[f];
       // records are written in blocks of (elements per matrix CTA, at most 4) elements
       bytes = std::max(bytes, rb * (size_t)(h->chunk_elems[f] + 4));
     }
@@ -971,6 +973,20 @@ int gales_asm_set_scatter(gales_asm* h, int32_t mode) {
   if (mode != GALES_SCATTER_ATOMIC && mode != GALES_SCATTER_COLOURED)
     return fail(h, GALES_ERR_BAD_INPUT, "unknown scatter mode");
   h->scatter_mode = mode;
+  return 0;
+}
+
+int gales_asm_set_chunk(gales_asm* h, int64_t elements) {
+  if (!h) return GALES_ERR_BAD_INPUT;
+  if (elements < 0) return fail(h, GALES_ERR_BAD_INPUT, "negative chunk size");
+  for (int f = 0; f < 2; ++f) {
+    if (elements == 0) {
+      h->chunk_elems[f] = h->chunk_default[f];
+    } else {
+      const long long c = std::max<long long>(4, (long long)elements / 4 * 4);
+      h->chunk_elems[f] = std::min<long long>(c, h->chunk_default[f]);
+    }
+  }
   return 0;
 }
 

@@ -185,6 +185,12 @@ int gales_asm_node_graph(gales_asm* h, int64_t* n_nodes, int64_t* nnz_nodes,
 /* Greedy element colouring: no two elements of one colour share a node. */
 int gales_asm_colouring(gales_asm* h, int32_t* n_colours, const int32_t** colour);
 int gales_asm_set_scatter(gales_asm* h, int32_t mode); /* GALES_SCATTER_* */
+/* Elements per chunk of the interior pass (rounded down to a multiple of 4, at least 4,
+ * at most the chunk the handle's record buffer was sized for: as many elements as 3 GiB
+ * of point records hold); 0 restores that default.  Each chunk runs the point kernel,
+ * then the matrix kernel.  No counterpart in the reference (its assembly has no
+ * chunks); smaller chunks cost launch tails, the results are the same. */
+int gales_asm_set_chunk(gales_asm* h, int64_t elements);
 
 /* One assembly: vals[nnz] and rhs[n_rows] are overwritten (linear_system::clear
  * is part of the call, linear_system.hpp:90-94).  stream: cudaStream_t or NULL. */

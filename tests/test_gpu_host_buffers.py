@@ -13,7 +13,7 @@ from cases import gm, rel, syn
 def test_host_buffers_match_device_buffers(form, cuda_lib):
     torch = pytest.importorskip("torch")
     f = gm.FORM_MIXED if form == "mixed" else gm.FORM_FP64
-    mesh = syn.box_tet_delaunay(22, seed=3)          # ~60k tets: several interior chunks
+    mesh = syn.box_tet_delaunay(22, seed=3)          # ~60k tets; pinned buffers: 8 interior chunks
     mat, setup = syn.material_for(3, 0), syn.setup_for(3, 3)
     I, P = syn.state_for(mesh, 3, 0)
     dt = 1e-3

@@ -88,6 +88,8 @@ def test_magma_multichunk_and_scatter_modes(scatter, cuda_lib, orc):
     mm = magma.MagmaMaterial(comps)
     fa = gm.FluidAssembly(mesh, mat, setup)
     fa.set_magma(mm)
+    fa.set_chunk(4096)                      # several interior chunks
+    assert mesh.n_elements >= 3 * 4096
     if scatter == "coloured":
         fa.set_scatter(gm.SCATTER_COLOURED)
     vals, rhs = _oracle(orc, mesh, comps, mat, setup, I, P, 1e-3, fa.nd)

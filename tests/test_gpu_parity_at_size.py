@@ -3,11 +3,12 @@
 The small cases of test_gpu_parity.py fit in one interior chunk.  These run the
 production schedule: the 999,931-tet benchmark mesh (Delaunay of a jittered 54^3
 lattice, 3 components, 7 dofs) compared with the oracle's full FP64 assembly
-(fluid_assembly.hpp:39-68 with scatter.hpp:37-98), meshes of several interior
-chunks in both forms and both scatter modes with device, page-locked and pageable
-buffers (the programmatically chained chunk launches, the ring of record buffers,
-the Morton and lowest-node-bucket element orders and the row-prefix copies to the
-host), a multi-chunk hex mesh, and the adjoint on the 200k-tet workload.
+(fluid_assembly.hpp:39-68 with scatter.hpp:37-98), meshes cut into several interior
+chunks (gales_asm_set_chunk) in both forms and both scatter modes with device,
+page-locked and pageable buffers (the point kernel then the persistent matrix kernel per
+chunk reusing one record buffer, the Morton and lowest-node-bucket element orders and
+the row-prefix copies to the host), a multi-chunk hex mesh, and the adjoint on the
+200k-tet workload.
 
 Bars: CSR pattern and colouring bit-exact; FP64 form <= 1e-12 relative
 (Frobenius / L2); mixed form <= 1e-6 relative, against the oracle.
@@ -116,6 +117,7 @@ def test_multichunk_tets_match_oracle(form, scatter, buffers, chunked):
     f = gm.FORM_MIXED if form == "mixed" else gm.FORM_FP64
     tol = MIXED_TOL if form == "mixed" else FP64_TOL
     fa = gm.FluidAssembly(mesh, mat, setup)
+    fa.set_chunk(14_592)
     if scatter == "coloured":
         fa.set_scatter(gm.SCATTER_COLOURED)
     dev = torch.device("cuda:0")
@@ -130,15 +132,15 @@ def test_multichunk_tets_match_oracle(form, scatter, buffers, chunked):
         lp = fa.linear_system()
         Iin, Pin = I, P
     n0 = fa.launch_count()
-    for _ in range(2):      # a second call reuses the ring, the copy events and the orders
+    for _ in range(2):      # a second call reuses the record buffer, the copy events and the orders
         fa.execute(Iin, Pin, dt, lp, form=f)
         torch.cuda.synchronize(dev)
         v = lp.vals.cpu().numpy() if torch.is_tensor(lp.vals) else lp.vals
         b = lp.rhs.cpu().numpy() if torch.is_tensor(lp.rhs) else lp.rhs
         assert rel(v, ref["vals"]) <= tol
         assert rel(b, ref["rhs"]) <= tol
-    # the mesh spans at least five interior chunks: at least five interior launches per call
-    assert (fa.launch_count() - n0) // 2 >= 5
+    # the mesh spans at least five interior chunks: a point and a matrix launch each
+    assert (fa.launch_count() - n0) // 2 >= 2 * 5
     assert mesh.n_elements >= 5 * 14_592
 
 
@@ -158,8 +160,9 @@ def hexes(orc, cuda_lib):
 @pytest.mark.parametrize("form", ["fp64", "mixed"])
 def test_multichunk_hexes_match_oracle(form, hexes):
     mesh, mat, setup, I, P, dt, ref = hexes
-    assert mesh.n_elements >= 3 * 7_296           # 7,296 hexes per mixed chunk
+    assert mesh.n_elements >= 3 * 7_296
     fa = gm.FluidAssembly(mesh, mat, setup)
+    fa.set_chunk(7_296)                          # several chunks
     v, b = _device_assembly(fa, I, P, dt, gm.FORM_MIXED if form == "mixed" else gm.FORM_FP64)
     tol = MIXED_TOL if form == "mixed" else FP64_TOL
     assert rel(v, ref["vals"]) <= tol
