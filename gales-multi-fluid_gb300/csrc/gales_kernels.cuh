@@ -1194,12 +1194,13 @@ struct PointVecs {
 };
 
 // Shared memory of one element slot of a matrix CTA: the per-point vectors t_b, the
-// element block staged for the scatter (FP64), and the per-warp partial traces.
+// element block staged for the scatter (in the form's type; widened to FP64 as it is
+// scattered), and the per-warp partial traces.
 template <int DIM, int NEN, int NC, int NQ, typename S>
 struct ElemSmem {
   using M = MatShape<DIM, NEN, NC>;
   PointVecs<DIM, NEN, NC, NQ, S> pv;
-  double stage[M::N * M::NS];
+  S stage[M::N * M::NS];
   double wsum[M::WPE];
 };
 
@@ -1521,21 +1522,27 @@ __device__ __forceinline__ void matrix_group(const KParams& k, const S* __restri
       avg = (1.0 + tr) * (1.0 / N);
     }
     if (active) {
-      double* srow = E.stage + row * NS + a0 * ND;
+      S* srow = E.stage + row * NS + a0 * ND;
 #pragma unroll
       for (int ai = 0; ai < NA; ++ai)
 #pragma unroll
-        for (int j = 0; j < ND; ++j)
-          srow[ai * ND + j] = blk_row ? ((a0 + ai == b && j == r) ? avg : 0.0) : widen(acc[ai][j]);
+        for (int j = 0; j < ND; ++j) srow[ai * ND + j] = acc[ai][j];
     }
     elem_sync<WPE>(ec);
   }
+  // staged entry (row rw, column cx) as scattered: a blocked row (Dirichlet) is avg on
+  // the diagonal and zero elsewhere (scatter.hpp:62-78)
+  auto staged = [&](int rw, int cx) -> double {
+    const int bn = rw / ND, jr = rw - bn * ND;
+    if (!local && ((((uint32_t)d_int(bn, GALES_W(d_blocked))) >> jr) & 1u)) return rw == cx ? avg : 0.0;
+    return widen(E.stage[rw * NS + cx]);
+  };
   if (WANT_M && k.vjp_lam) {
     // frozen-tangent VJP: g += K^T lambda for this element's block (Dirichlet rows included)
     for (int cx = gl; cx < N; cx += ET) {
       double sum = 0.0;
       for (int rw = 0; rw < N; ++rw)
-        sum += __ldg(k.vjp_lam + (long long)d_int(rw / ND, GALES_W(d_node)) * ND + rw % ND) * E.stage[rw * NS + cx];
+        sum += __ldg(k.vjp_lam + (long long)d_int(rw / ND, GALES_W(d_node)) * ND + rw % ND) * staged(rw, cx);
       if (sum != 0.0) atomicAdd(k.vjp_g + (long long)d_int(cx / ND, GALES_W(d_node)) * ND + cx % ND, sum);
     }
     return;
@@ -1543,7 +1550,7 @@ __device__ __forceinline__ void matrix_group(const KParams& k, const S* __restri
   if (local) {  // element-level output of execute_i (fluid_2d.hpp:200-201): m = m_, r = -r_
     if (active && grp_a == 0) k.local_r[g * N + row] = widen(-racc);
     if (WANT_M && k.local_m)
-      for (int t = gl; t < NT; t += ET) k.local_m[g * NT + t] = E.stage[(t / N) * NS + t % N];
+      for (int t = gl; t < NT; t += ET) k.local_m[g * NT + t] = widen(E.stage[(t / N) * NS + t % N]);
     return;
   }
   const int mode = k.scatter_mode;
@@ -1562,10 +1569,15 @@ __device__ __forceinline__ void matrix_group(const KParams& k, const S* __restri
       const int a = cx / ND, ja = cx - a * ND;
       for (int sb_ = 0; sb_ < NEN; ++sb_) {
         const int64_t rl = d_int(sb_, GALES_W(d_rowlen));
+        const uint32_t bl = (uint32_t)d_int(sb_, GALES_W(d_blocked));
         double* rowp = k.vals + (int64_t)d_int(sb_, GALES_W(d_off) + a) * ND + (int64_t)warp * rl + ja;
         const int64_t step = (int64_t)WPE * rl;
         for (int jb = warp; jb < ND; jb += WPE, rowp += step) {
-          const double val = E.stage[(sb_ * ND + jb) * NS + cx];
+          if ((bl >> jb) & 1u) {  // blocked row: avg on its diagonal only
+            if (cx == sb_ * ND + jb) add_to(rowp, avg, mode);
+            continue;
+          }
+          const double val = widen(E.stage[(sb_ * ND + jb) * NS + cx]);
           if ((__double2hiint(val) & 0x7fffffff) | __double2loint(val)) add_to(rowp, val, mode);
         }
       }
