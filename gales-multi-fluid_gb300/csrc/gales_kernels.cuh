@@ -1900,8 +1900,9 @@ struct alignas(16) BPointRec {
 template <int DIM, int NEN, int NC, int NS, int NSQ, typename S>
 struct BoundarySmem {
   static constexpr int ND = Layout<DIM, NC>::ND, N = NEN * ND;
+  static constexpr int MS = N + 1;   // row stride of m: rows and columns bank-conflict free
   BPointRec<DIM, NEN, NC, S> pt[NS * NSQ];
-  S m[N * N];            // element block accumulator
+  S m[N * MS];           // element block accumulator
   double r[N];
   double wsum;
   int64_t rowbase[NEN];
@@ -2129,6 +2130,7 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   constexpr int N = NEN * ND;
   constexpr int NT = N * N;
   using BS = BoundarySmem<DIM, NEN, NC, NS, NSQ, S>;
+  constexpr int MS = BS::MS;
   using BR = BPointRec<DIM, NEN, NC, S>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BS& B = *reinterpret_cast<BS*>(smem_raw);
@@ -2139,7 +2141,7 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   int nodes[NEN];
 #pragma unroll
   for (int a = 0; a < NEN; ++a) nodes[a] = __ldg(k.conn + e * NEN + a);
-  for (int t = lane; t < NT; t += 32) B.m[t] = S(0);
+  for (int t = lane; t < N * MS; t += 32) B.m[t] = S(0);
   for (int t = lane; t < N; t += 32) B.r[t] = 0.0;
   // rows of the element's nodes and the element's slot table, for the scatter
   if (lane < NEN) {
@@ -2187,26 +2189,61 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   }
   __syncwarp();
   // (2) per flagged point, the block m_ba += N_b (N_a BA - sum_l dN_a/dx_l BK_l) and the
-  // residual
+  // residual.  Lane l owns block rows l, l + 32, ...: its row's BA and BK rows are read
+  // once per point, the columns run at compile time; a block of at most 32 rows is
+  // accumulated in registers, a larger one in shared memory.
+  constexpr int RPL = (N + 31) / 32;
+  constexpr bool kRegs = N <= 32;
+  S acc[kRegs ? N : 1];
+#pragma unroll
+  for (int c = 0; c < (kRegs ? N : 1); ++c) acc[c] = S(0);
   for (int ip = 0; ip < NS * NSQ; ++ip) {
     const BR& R = B.pt[ip];
     const BPoint<DIM, NEN, NC, S>& P = R.pt;
     if (P.flag <= 0) continue;
-    for (int t = lane; t < NT; t += 32) {
-      const int row = t / N, colx = t % N;
-      const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-      S x = P.sh[a] * R.BA[jb][ja];
 #pragma unroll
-      for (int l = 0; l < DIM; ++l) x = madd(-P.ds[l][a], R.BK[l][jb][ja], x);
-      B.m[t] = madd(P.sh[b], x, B.m[t]);
+    for (int rr = 0; rr < RPL; ++rr) {
+      const int row = lane + 32 * rr;
+      if (row < N) {
+        const int b = row / ND, jb = row - (row / ND) * ND;
+        const S shb = P.sh[b];
+        S ba[ND], bk[DIM][ND];
+#pragma unroll
+        for (int ja = 0; ja < ND; ++ja) {
+          ba[ja] = R.BA[jb][ja];
+#pragma unroll
+          for (int l = 0; l < DIM; ++l) bk[l][ja] = R.BK[l][jb][ja];
+        }
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+          const S sha = P.sh[a];
+          S dsa[DIM];
+#pragma unroll
+          for (int l = 0; l < DIM; ++l) dsa[l] = P.ds[l][a];
+#pragma unroll
+          for (int ja = 0; ja < ND; ++ja) {
+            S x = sha * ba[ja];
+#pragma unroll
+            for (int l = 0; l < DIM; ++l) x = madd(-dsa[l], bk[l][ja], x);
+            if constexpr (kRegs) acc[a * ND + ja] = madd(shb, x, acc[a * ND + ja]);
+            else B.m[row * MS + a * ND + ja] = madd(shb, x, B.m[row * MS + a * ND + ja]);
+          }
+        }
+      }
     }
     for (int t = lane; t < N; t += 32) B.r[t] = madd(P.shr[t / ND], P.rb[t % ND], B.r[t]);
+    __syncwarp();
+  }
+  if constexpr (kRegs) {
+    if (lane < N)
+#pragma unroll
+      for (int c = 0; c < N; ++c) B.m[lane * MS + c] = acc[c];
     __syncwarp();
   }
   if (k.local_r) {  // element-level output of execute_b: m = m_, r = -r_
     for (int t = lane; t < N; t += 32) k.local_r[li * N + t] = -B.r[t];
     if (k.local_m)
-      for (int t = lane; t < NT; t += 32) k.local_m[li * NT + t] = widen(B.m[t]);
+      for (int t = lane; t < NT; t += 32) k.local_m[li * NT + t] = widen(B.m[(t / N) * MS + t % N]);
     return;
   }
   // second scatter pass with its own Dirichlet average avg = (1 + trace)/n
@@ -2217,7 +2254,7 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
   double avg = 0.0;
   if (any_blocked != 0u || k.vjp_lam) {
     double tr = 0.0;
-    for (int i = lane; i < N; i += 32) tr += widen(B.m[i * N + i]);
+    for (int i = lane; i < N; i += 32) tr += widen(B.m[i * MS + i]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
     avg = (1.0 + tr) * (1.0 / N);
@@ -2228,7 +2265,7 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
       double sum = 0.0;
       for (int rw = 0; rw < N; ++rw) {
         const int b = rw / ND, jb = rw % ND;
-        const double val = ((B.blocked[b] >> jb) & 1u) ? (rw == cx ? avg : 0.0) : widen(B.m[rw * N + cx]);
+        const double val = ((B.blocked[b] >> jb) & 1u) ? (rw == cx ? avg : 0.0) : widen(B.m[rw * MS + cx]);
         sum += __ldg(k.vjp_lam + (long long)nodes[b] * ND + jb) * val;
       }
       if (sum != 0.0) atomicAdd(k.vjp_g + (long long)nodes[cx / ND] * ND + cx % ND, sum);
@@ -2241,14 +2278,31 @@ __global__ void __launch_bounds__(32) boundary_kernel(const KParams k) {
     if (!((B.blocked[b] >> jb) & 1u)) add_to(k.rhs + (long long)nodes[b] * ND + jb, -B.r[t], mode);
   }
   if (k.vals) {
-    for (int t = lane; t < NT; t += 32) {
-      const int row = t / N, colx = t % N;
-      const int b = row / ND, jb = row % ND, a = colx / ND, ja = colx % ND;
-      double val = widen(B.m[t]);
-      if ((B.blocked[b] >> jb) & 1u) val = (row == colx) ? avg : 0.0;
-      if (val != 0.0) {
-        const int64_t off = B.rowbase[b] + (int64_t)jb * B.rowlen[b] + (int64_t)B.slot[b][a] * ND + ja;
-        add_to(k.vals + off, val, mode);
+    // lane = column (a, ja): one block row per step, consecutive lanes on consecutive
+    // columns of node a's run in the row
+    constexpr int CH = (N + 31) / 32;
+#pragma unroll
+    for (int h = 0; h < CH; ++h) {
+      const int cx = lane + 32 * h;
+      if (cx >= N) break;
+      const int a = cx / ND, ja = cx - (cx / ND) * ND;
+#pragma unroll
+      for (int bq = 0; bq < NEN; ++bq) {
+        const uint32_t bl = B.blocked[bq];
+        const int64_t rl = B.rowlen[bq];
+        double* rowp = k.vals + B.rowbase[bq] + (int64_t)B.slot[bq][a] * ND + ja;
+#pragma unroll
+        for (int jb = 0; jb < ND; ++jb, rowp += rl) {
+          const int row = bq * ND + jb;
+          double val;
+          if ((bl >> jb) & 1u) {
+            if (row != cx) continue;
+            val = avg;
+          } else {
+            val = widen(B.m[row * MS + cx]);
+          }
+          if ((__double2hiint(val) & 0x7fffffff) | __double2loint(val)) add_to(rowp, val, mode);
+        }
       }
     }
   }
