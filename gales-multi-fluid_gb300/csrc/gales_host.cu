@@ -153,9 +153,10 @@ constexpr int kVjpAux = 3 * GALES_MAX_COMP + GALES_MAX_ND;
 // Chunks are as large as kRecordBytes of point records allow (the whole mesh for the
 // 1.0M-tet workload), so that few launch tails remain; the records go through DRAM,
 // which the compute-bound stages leave mostly idle.  A host-buffer call cuts the pass
-// into kCopyChunks chunks, after each of which the finished CSR rows are copied.
+// into chunks that shrink toward its end, after each of which the finished CSR rows
+// are copied.
 constexpr size_t kRecordBytes = size_t(3) << 30;
-constexpr int kCopyChunks = 8;
+constexpr int kCopyTail = 64;    // smallest host-buffer chunk: n / kCopyTail elements
 constexpr int kCopyEvents = 24;  // row copies per host-buffer assembly (at most)
 
 GeometryOps geometry_ops(int dim, int nen) {
@@ -1099,12 +1100,20 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
   const InteriorOps& ops = h->ops[form];
   const size_t rb = ops.rec_bytes(h->nc);
   if (rb == 0) return fail(h, GALES_ERR_UNSUPPORTED, "no interior kernel for this element/component count");
-  long long chunk = h->chunk_elems[form];
-  if (rc) chunk = std::min(chunk, std::max<long long>(4, (n + kCopyChunks - 1) / kCopyChunks));
-  const long long nchunks = (n + chunk - 1) / chunk;
+  const long long chunk = h->chunk_elems[form];
+  // host-buffer calls: chunks that shrink toward the end of the pass (a third of what
+  // remains, down to n / 64), so that the rows copied after the last chunk are few
+  const long long tail = std::max<long long>(4, (n + kCopyTail - 1) / kCopyTail / 4 * 4);
   void* buf = h->qpbuf.p;
-  for (long long c = 0; c < nchunks; ++c) {
-    const long long first = c * chunk, cnt = std::min(chunk, n - first);
+  long long first = 0;
+  for (long long c = 0; first < n; ++c) {
+    long long cnt = chunk;
+    if (rc) {
+      const long long rem = n - first;
+      cnt = rem <= 2 * tail ? rem : std::max(tail, (rem / 3 + 3) / 4 * 4);
+      cnt = std::min(cnt, chunk);
+    }
+    cnt = std::min(cnt, n - first);
     LaunchResult r = ops.point(k, h->nc, buf, first, cnt, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "point kernel");
     h->launches += r.launches;
@@ -1114,9 +1123,10 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
     h->launches += r.launches;
     if (stage_events && c == 0) CK(h, cudaEventRecord(h->evs[1], st), "event");
     if (rc) {
-      const int e = copy_finished_rows(h, *rc, first + cnt, c == nchunks - 1, st);
+      const int e = copy_finished_rows(h, *rc, first + cnt, first + cnt >= n, st);
       if (e) return e;
     }
+    first += cnt;
   }
   return 0;
 }
