@@ -28,6 +28,7 @@ collective); value = all ranks' elements / the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import gc
 import importlib
 import json
 import os
@@ -726,6 +727,8 @@ def main():
     # on the shared host link weighs less in the mean
     e2e_n = 3 * args.steps
     e2e_steps = []
+    gc.collect()
+    gc.disable()      # no collector pause of the Python host loop inside the timing
     t0 = time.perf_counter()
     for _ in range(e2e_n):
         ts = time.perf_counter()
@@ -733,6 +736,7 @@ def main():
         e2e_steps.append((time.perf_counter() - ts) * 1e3)
     torch.cuda.synchronize(dev)
     e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_n, dist, dev)
+    gc.enable()
     # the device-to-host copy of the CSR values alone (same pinned buffer and stream)
     d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
