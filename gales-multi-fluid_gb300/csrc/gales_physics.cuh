@@ -50,22 +50,26 @@ struct DevChem {
 // signed zero instead of a subnormal.
 __device__ __forceinline__ float narrow_rn(double d) {
   const unsigned int hi = (unsigned int)__double2hiint(d), lo = (unsigned int)__double2loint(d);
-  const unsigned int sign = hi & 0x80000000u;
-  const int e64 = (int)((hi >> 20) & 0x7ffu);
-  const int e = e64 - (1023 - 127);
-  const unsigned int m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-  unsigned int bits;
-  if (e >= 1 && e <= 254) {
-    const unsigned int rest = lo & 0x1fffffffu;
-    bits = sign | ((unsigned int)e << 23) | m;
-    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) bits += 1u;
-  } else if (e64 == 0x7ff) {
-    const bool nan = ((hi & 0xfffffu) | lo) != 0u;
-    bits = sign | 0x7f800000u | (nan ? (m | 0x400000u) : 0u);
-  } else {
-    bits = sign | (e >= 255 ? 0x7f800000u : 0u);
+  const unsigned int ah = hi & 0x7fffffffu, sign = hi & 0x80000000u;
+  if (ah - 0x38100000u < 0x0fe00000u) {
+    // binary64 exponent e64 in [897, 1150], a normal binary32 before rounding.  The
+    // funnel shift of (hi:lo) by 3 holds the low 9 bits of e64 above the top 23
+    // significand bits; subtracting 384 << 23 rebiases the exponent field modulo 2^9
+    // (e64 - 896 < 256, so bit 31 ends clear).  Round to nearest even on the 29 dropped
+    // bits: adding 2^28 - 1 + (bits & 1) to them carries into bit 29 exactly when they
+    // exceed half, or equal half with bits odd; a carry out of the significand steps the
+    // exponent (to infinity from the largest binade).
+    unsigned int bits = __funnelshift_l(lo, hi, 3) - 0xc0000000u;
+    bits += ((lo & 0x1fffffffu) + 0x0fffffffu + (bits & 1u)) >> 29;
+    return __uint_as_float(bits | sign);
   }
-  return __uint_as_float(bits);
+  if (ah < 0x38100000u) return __uint_as_float(sign);       // below the binary32 normals
+  if (ah >= 0x7ff00000u) {                                  // infinity or NaN (kept quiet)
+    const unsigned int m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const bool nan = ((hi & 0xfffffu) | lo) != 0u;
+    return __uint_as_float(sign | 0x7f800000u | (nan ? (m | 0x400000u) : 0u));
+  }
+  return __uint_as_float(sign | 0x7f800000u);               // finite beyond the range: overflow
 }
 
 // isfinite on the high word (integer pipe): the exponent field is not all ones

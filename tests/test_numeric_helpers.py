@@ -27,6 +27,9 @@ static inline double __longlong_as_double(long long x) { double d; std::memcpy(&
 static inline unsigned int __float_as_uint(float f) { unsigned int x; std::memcpy(&x, &f, 4); return x; }
 static inline float __uint_as_float(unsigned int x) { float f; std::memcpy(&f, &x, 4); return f; }
 static inline int __clz(int x) { return x == 0 ? 32 : __builtin_clz((unsigned int)x); }
+static inline unsigned int __funnelshift_l(unsigned int lo, unsigned int hi, unsigned int s) {
+  return (unsigned int)(((((unsigned long long)hi) << 32) | lo) << (s & 31u) >> 32);
+}
 static inline int __double2hiint(double d) { return (int)(__double_as_longlong(d) >> 32); }
 static inline int __double2loint(double d) { return (int)(unsigned int)__double_as_longlong(d); }
 static inline double __hiloint2double(int hi, int lo) {
