@@ -52,7 +52,7 @@ BYTES_PER_ELEM_TET = 4 * 4 + 8 * 3 * 4 + 2 * 8 * 4 * 7 + 16 * (4 * 7) ** 2 + 16 
 # dram__bytes_read.sum + dram__bytes_write.sum from ncu on the 163,618-tet mesh of the
 # 30^3 lattice, whose CSR bytes per element (1,002) match the 1.0M-tet mesh's (982);
 # scaled by the element count (profiles/dram_traffic_tet4_lattice30_assembly.md).
-TRAFFIC_BYTES_PER_ELEM_TET = 9318
+TRAFFIC_BYTES_PER_ELEM_TET = 9305
 LATTICE_N = 54
 
 
@@ -67,8 +67,8 @@ def peaks():
 # 163,618-tet mesh of the 30^3 lattice (profiles/point_matrix_kernels_mixed_tet4_lattice30.md):
 # FP64 thread instructions per quadrature point of the point kernel and warp
 # instructions per element of the matrix kernel.
-POINT_FP64_PER_POINT = {"dfma": 206.8, "dmul_dadd": 202.1}
-MATRIX_WARP_INST_PER_ELEM = 2854
+POINT_FP64_PER_POINT = {"dfma": 206.8, "dmul_dadd": 201.1}
+MATRIX_WARP_INST_PER_ELEM = 2758
 NQ_TET = 4
 
 
@@ -216,7 +216,7 @@ BYTES_PER_ELEM_HEX = 4 * 8 + 8 * 3 * 8 + 2 * 8 * 8 * 8 + 16 * (8 * 8) ** 2 + 16 
 # DRAM bytes per element of the mixed hex interior pass, from ncu on the 64,000-hex mesh
 # of a 40^3 grid (CSR bytes per element 14,172, 1.9% above the 160x160x156 mesh's
 # 13,911); scaled by the element count (profiles/dram_traffic_hex8_40cube_assembly.md).
-TRAFFIC_BYTES_PER_ELEM_HEX = 64059
+TRAFFIC_BYTES_PER_ELEM_HEX = 64817
 
 
 def top_gas_flux_lambda(mesh, mat, I, nd):
