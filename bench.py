@@ -48,11 +48,12 @@ for p in (ROOT, ROOT / "oracle"):
 
 METRIC = "residual+Jacobian elements/s, mixed vs FP64 on 1 GB300 at <=1e-6 rel err; HBM %"
 BYTES_PER_ELEM_TET = 4 * 4 + 8 * 3 * 4 + 2 * 8 * 4 * 7 + 16 * (4 * 7) ** 2 + 16 * 4 * 7  # 13,552
-# DRAM bytes per element of the mixed tet interior pass (point and matrix kernels):
+# DRAM bytes per element of the mixed tet interior pass (point and matrix kernels; the
+# point kernel's clear of A and b included):
 # dram__bytes_read.sum + dram__bytes_write.sum from ncu on the 163,618-tet mesh of the
 # 30^3 lattice, whose CSR bytes per element (1,002) match the 1.0M-tet mesh's (982);
 # scaled by the element count (profiles/dram_traffic_tet4_lattice30_assembly.md).
-TRAFFIC_BYTES_PER_ELEM_TET = 9305
+TRAFFIC_BYTES_PER_ELEM_TET = 10502
 LATTICE_N = 54
 
 
@@ -67,7 +68,7 @@ def peaks():
 # 163,618-tet mesh of the 30^3 lattice (profiles/point_matrix_kernels_mixed_tet4_lattice30.md):
 # FP64 thread instructions per quadrature point of the point kernel and warp
 # instructions per element of the matrix kernel.
-POINT_FP64_PER_POINT = {"dfma": 206.8, "dmul_dadd": 201.1}
+POINT_FP64_PER_POINT = {"dfma": 193.5, "dmul_dadd": 197.2}
 MATRIX_WARP_INST_PER_ELEM = 2758
 NQ_TET = 4
 
@@ -272,6 +273,8 @@ def hex_block(args, torch, dev, with_clocks=False):
     t0 = time.perf_counter()
     fa = gm.FluidAssembly(mesh, mat, setup, device=dev.index or 0)
     t_create = time.perf_counter() - t0
+    if args.hex_chunk:
+        fa.set_chunk(args.hex_chunk)
     lp = fa.device_system(dev)
     nnz = lp.vals.numel()
     Id, Pd = torch.tensor(I, device=dev), torch.tensor(P, device=dev)
@@ -633,6 +636,8 @@ def main():
     ap.add_argument("--workload", default="tet", choices=["tet", "hex"],
                     help="tet: 1.0M tets (default); hex: 4.0M hexahedra with a CUDA graph of 10 assemblies")
     ap.add_argument("--hex-dims", type=int, nargs=3, default=[160, 160, 156])
+    ap.add_argument("--hex-chunk", type=int, default=0,
+                    help="hex elements per interior chunk (0: as many as the record buffer holds)")
     ap.add_argument("--no-vjp", action="store_true", help="skip the adjoint block")
     ap.add_argument("--no-hex", action="store_true", help="skip the 4.0M-hex block")
     ap.add_argument("--no-newton", action="store_true", help="skip the Newton block")

@@ -1094,9 +1094,12 @@ int copy_finished_rows(gales_asm* h, RowCopy& rc, int64_t elements_done, bool la
 
 // Interior pass over n listed elements (k.el_list, or elements 0..n-1): per chunk the
 // point kernel, then the matrix kernel, on the caller's stream, with the optional
-// device-to-host copy of finished rows (rc) after each chunk.
+// device-to-host copy of finished rows (rc) after each chunk.  The arrays k.clear_*
+// names are zeroed by the first chunk's point kernel only; after_first_point runs on
+// the host once that launch is enqueued (before the first matrix launch).
 int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long long n, cudaStream_t st,
-                 RowCopy* rc = nullptr, bool stage_events = false) {
+                 RowCopy* rc = nullptr, bool stage_events = false,
+                 const std::function<int()>* after_first_point = nullptr) {
   const InteriorOps& ops = h->ops[form];
   const size_t rb = ops.rec_bytes(h->nc);
   if (rb == 0) return fail(h, GALES_ERR_UNSUPPORTED, "no interior kernel for this element/component count");
@@ -1105,6 +1108,8 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
   // remains, down to n / 64), so that the rows copied after the last chunk are few
   const long long tail = std::max<long long>(4, (n + kCopyTail - 1) / kCopyTail / 4 * 4);
   void* buf = h->qpbuf.p;
+  KParams kl;  // the later chunks' parameters: nothing left to clear
+  const KParams* kp = &k;
   long long first = 0;
   for (long long c = 0; first < n; ++c) {
     long long cnt = chunk;
@@ -1114,11 +1119,22 @@ int run_interior(gales_asm* h, const KParams& k, int form, bool want_m, long lon
       cnt = std::min(cnt, chunk);
     }
     cnt = std::min(cnt, n - first);
-    LaunchResult r = ops.point(k, h->nc, buf, first, cnt, st);
+    LaunchResult r = ops.point(*kp, h->nc, buf, first, cnt, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "point kernel");
     h->launches += r.launches;
-    if (stage_events && c == 0) CK(h, cudaEventRecord(h->evs[0], st), "event");
-    r = ops.matrix(k, h->nc, want_m, buf, first, cnt, st);
+    if (c == 0) {
+      if (stage_events) CK(h, cudaEventRecord(h->evs[0], st), "event");
+      if (after_first_point) {
+        const int e = (*after_first_point)();
+        if (e) return e;
+      }
+      if (k.clear_n[0] > 0 || k.clear_n[1] > 0) {
+        kl = k;
+        kl.clear_n[0] = kl.clear_n[1] = 0;
+        kp = &kl;
+      }
+    }
+    r = ops.matrix(*kp, h->nc, want_m, buf, first, cnt, st);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "matrix kernel");
     h->launches += r.launches;
     if (stage_events && c == 0) CK(h, cudaEventRecord(h->evs[1], st), "event");
@@ -1279,36 +1295,60 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
     CK(h, cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st), "memset status");
     CK(h, cudaMemsetAsync(h->d_first_bad.p, 0xff, sizeof(unsigned long long), st), "memset first_bad");
   }
-  if (dvals) {
-    CK(h, launch_zero(dvals, h->nnz, h->sms, st), "zero vals");
+  // A and b start at zero.  A device-buffer call with the atomic scatter whose interior
+  // pass is one chunk has its point kernel clear them beside its own work (it neither
+  // reads nor writes them; the matrix and boundary stages, their first writers, come
+  // after it); otherwise a clear kernel runs first.  Over several chunks the first
+  // chunk's point kernel is too short to hide the clear.  A host-buffer call keeps the
+  // clear kernel so that its boundary pass can start at once: the rows finished by the
+  // first chunk are copied only once the boundary pass is done, and copying is what
+  // bounds that call.
+  const bool atomic = h->scatter_mode != GALES_SCATTER_COLOURED;
+  const bool fold_clear = atomic && h->n_el > 0 && h->n_el <= h->chunk_elems[form] && rc == nullptr;
+  if (fold_clear) {
+    k.clear_p[0] = dvals;
+    k.clear_n[0] = dvals ? h->nnz : 0;
+    k.clear_p[1] = drhs;
+    k.clear_n[1] = h->n_rows;
+  } else {
+    if (dvals) {
+      CK(h, launch_zero(dvals, h->nnz, h->sms, st), "zero vals");
+      ++h->launches;
+    }
+    CK(h, launch_zero(drhs, h->n_rows, h->sms, st), "zero rhs");
     ++h->launches;
   }
-  CK(h, launch_zero(drhs, h->n_rows, h->sms, st), "zero rhs");
-  ++h->launches;
   if (timed) CK(h, cudaEventRecord(h->evp[1], st), "event");
-  h->launches += 0;
   // boundary pass (fluid_assembly.hpp:57-63): always atomics, since boundary elements
   // of one colour may still share nodes.  With the atomic interior scatter the two
   // passes only add into A and b, so the boundary pass runs on its own stream beside
-  // the interior chunks; with the coloured (plain read-modify-write) scatter it waits.
+  // the interior chunks, from the end of the first point launch when that launch
+  // clears A and b, else from the start; with the coloured (plain read-modify-write)
+  // scatter it waits for the interior.
   const bool has_bd = !h->bd_list.empty();
-  const bool bd_concurrent = has_bd && h->scatter_mode != GALES_SCATTER_COLOURED;
+  const bool bd_concurrent = has_bd && atomic;
   KParams kb = k;
   kb.scatter_mode = 0;
   kb.el_list = h->d_bd_list.p;
   kb.n_list = (int64_t)h->bd_list.size();
   kb.bd_sides = h->d_bd_sides.p;
+  kb.clear_n[0] = kb.clear_n[1] = 0;
   set_boundary_points(h, kb);
-  if (bd_concurrent) {
+  const std::function<int()> fork_boundary = [&]() -> int {
     CK(h, cudaEventRecord(h->ev_bfork, st), "event");
     CK(h, cudaStreamWaitEvent(h->bst, h->ev_bfork, 0), "stream wait");
     LaunchResult r = dispatch_boundary(h, kb, form, kb.n_list, h->bst);
     if (r.err != cudaSuccess) return cuda_fail(h, r.err, "boundary kernel");
     h->launches += r.launches;
     CK(h, cudaEventRecord(h->ev_bjoin, h->bst), "event");
+    // finished rows may be copied only once the boundary pass has added into them
+    if (rc) CK(h, cudaStreamWaitEvent(h->cst, h->ev_bjoin, 0), "stream wait");
+    return 0;
+  };
+  if (bd_concurrent && !fold_clear) {
+    const int e = fork_boundary();
+    if (e) return e;
   }
-  // finished rows may be copied only once the boundary pass has added into them
-  if (rc && bd_concurrent) CK(h, cudaStreamWaitEvent(h->cst, h->ev_bjoin, 0), "stream wait");
   if (h->scatter_mode == GALES_SCATTER_COLOURED) {
     for (int c = 0; c < h->n_colours; ++c) {
       KParams kc = k;
@@ -1320,7 +1360,8 @@ int run_assembly(gales_asm* h, const double* dI, const double* dP, double dt, in
   } else {
     k.el_list = rc ? h->d_sweep_rows.p : h->d_sweep.p;
     k.n_list = h->n_el;
-    int e = run_interior(h, k, form, want_m, h->n_el, st, rc, timed);
+    int e = run_interior(h, k, form, want_m, h->n_el, st, rc, timed,
+                         (bd_concurrent && fold_clear) ? &fork_boundary : nullptr);
     if (e) return e;
   }
   if (timed) CK(h, cudaEventRecord(h->evp[2], st), "event");

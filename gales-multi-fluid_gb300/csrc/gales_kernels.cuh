@@ -84,6 +84,10 @@ struct KParams {
   const void* bgeo;
   void* bpt_rec;
   int64_t n_bpt;
+  // arrays the point stage zeroes beside its own work (the first chunk's launch clears
+  // A and b, whose first writers are the matrix and boundary stages after it)
+  double* clear_p[2];
+  int64_t clear_n[2];
 };
 
 __device__ __forceinline__ void flag_error(const KParams& k, unsigned int bits, long long e) {
@@ -749,16 +753,16 @@ __device__ void point_phase(const KParams& k, long long e, int iq, const RecOut<
   if (v_nrm >= kEps && k.tau != GALES_TAU_NONE) {
     double h, idet = 0.0;
     bool have_idet = false;
+    double trG = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) trG += q.G[d][d];
     if constexpr (FORM == GALES_FORM_FP64) {
       h = compute_h<DIM>(q.G, v, dv);
     } else {
       bool decided;
-      h = compute_h_fast<DIM>(q.G, v, iv, dv, decided);
+      h = compute_h_fast<DIM>(q.G, trG, v, iv, dv, decided);
       if (!decided) h = compute_h_reference<DIM, NEN, ND>(k.I, nodes, sh, q);
     }
-    double trG = 0.0;
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) trG += q.G[d][d];
     const double cs = pr.c, rho = pr.rho, mu = pr.mu, cv = pr.cv, kappa = pr.kappa;
     double td[ND];
 #pragma unroll
@@ -1153,10 +1157,33 @@ constexpr int point_min_ctas() {
   return FORM == GALES_FORM_MIXED ? (EOS == kEosMagma ? 2 : 4) : 1;
 }
 
+// Zeroes k.clear_p[a][0 .. k.clear_n[a]) with every thread of the launch (grid-stride;
+// 16-byte stores on the 16-byte-aligned body, scalar stores for an unaligned head and
+// an odd tail).  A thread issues its stores after its point, so that they drain while
+// the CTAs of later waves compute.
+__device__ __forceinline__ void clear_arrays(const KParams& k) {
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+#pragma unroll 1
+  for (int a = 0; a < 2; ++a) {
+    double* p = k.clear_p[a];
+    const long long n = k.clear_n[a];
+    if (n <= 0) continue;
+    const long long head = (reinterpret_cast<uintptr_t>(p) & 15u) != 0 ? 1 : 0;
+    const long long body = n - head;
+    if (tid == 0 && head) p[0] = 0.0;
+    if (tid == 0 && (body & 1)) p[n - 1] = 0.0;
+    double2* q = reinterpret_cast<double2*>(p + head);
+#pragma unroll 1
+    for (long long i = tid; i < body / 2; i += stride) q[i] = make_double2(0.0, 0.0);
+  }
+}
+
 template <int DIM, int NEN, int NC, int NQ, int FORM, typename S, int EOS = kEosChemicals>
 __global__ void __launch_bounds__(128, point_min_ctas<FORM, EOS>()) point_kernel(const KParams k, QP<DIM, NEN, NC, S>* __restrict__ out,
                                                      long long first, long long n) {
   point_block<DIM, NEN, NC, NQ, FORM, S, EOS>(k, out, first, n, (int)blockIdx.x);
+  if (k.clear_n[0] > 0 || k.clear_n[1] > 0) clear_arrays(k);
 }
 
 // Interior pass, stage 2: element matrices.  Lane (b, r, g) owns row (b, r) of the

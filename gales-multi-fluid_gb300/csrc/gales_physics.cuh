@@ -840,10 +840,14 @@ __device__ __forceinline__ double qform_fma(const double (&G)[DIM][DIM], const d
 // caller runs compute_h on the velocity and gradient formed with the reference's
 // operations.  With w1 = s1 unnormalised and w2 = s0 x w1, alpha_1 = w1^T G w1/|w1|^2
 // and alpha_2 = w2^T G w2/|w2|^2, so h = 1/alpha_0 + |w1|^2/A1 + |w2|^2/A2 takes one
-// reciprocal square root at the end.
+// reciprocal square root at the end.  In 3D, where |w1| > 1e-3 |dv v| the basis
+// {s0, w1/|w1|, w2/|w2|} is orthonormal to ~1e-13, and alpha_2 = tr G - alpha_0 -
+// alpha_1 (the trace does not change under an orthonormal change of basis): then
+// B2 = n1 alpha_2 = n1 (tr G - A0) - A1 replaces w2 and its quadratic form wherever
+// alpha_2 > 1e-6 tr G, which keeps its rounding below ~1e-10 relative.
 template <int DIM>
-__device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], const double* v, double iv,
-                                                 const double (&dv)[DIM][DIM], bool& decided) {
+__device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], double trG, const double* v,
+                                                 double iv, const double (&dv)[DIM][DIM], bool& decided) {
   decided = false;
   double s0[DIM], acc[DIM], w1[DIM];
 #pragma unroll
@@ -869,6 +873,15 @@ __device__ __forceinline__ double compute_h_fast(const double (&G)[DIM][DIM], co
   const double A0 = qform_fma<DIM>(G, s0), A1 = qform_fma<DIM>(G, w1);
   double A2 = 0.0, n2 = 0.0;
   if constexpr (DIM == 3) {
+    if (n1 > 1.0e-6 * aa) {
+      const double B2 = fma(n1, trG - A0, -A1);
+      if (B2 > 1.0e-6 * (n1 * trG) && A0 != 0.0 && A1 != 0.0) {
+        decided = true;
+        // 1/A0 + n1/A1 + n1/B2 = (A1 B2 + n1 A0 (B2 + A1)) / (A0 A1 B2), all terms > 0
+        const double num = fma(A1, B2, (n1 * A0) * (B2 + A1)), den = A0 * A1 * B2;
+        return 2.0 * num * rsqrt(num * den);
+      }
+    }
     double w2[3];
     w2[0] = fma(s0[1], w1[2], -s0[2] * w1[1]);
     w2[1] = fma(w1[0], s0[2], -w1[2] * s0[0]);

@@ -255,7 +255,10 @@ def read_lookup_tables(directory, mix: MagmaMix) -> MagmaMix:
     n = n_p
     if (d / "temperature.txt").exists():
         tv = _read_table(d / "temperature.txt")
-        T = tv[1:1 + int(tv[0])]
+        n_T = int(tv[0])
+        if len(tv) < 1 + n_T:
+            raise ValueError(f"{d / 'temperature.txt'}: {len(tv) - 1} temperatures, the header declares {n_T}")
+        T = tv[1:1 + n_T]
         n = len(T) * n_p
     h2o = _read_table(d / f"wf_l_h2o_onliq_{mix.name}.txt", n)
     co2 = _read_table(d / f"wf_l_co2_onliq_{mix.name}.txt", n)

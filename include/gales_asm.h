@@ -451,9 +451,12 @@ double gales_asm_last_ms(gales_asm* h);
 /* Device time in ms of one phase of the last assemble/residual call, CUDA events on
  * its stream: 0 = clearing A and b, 1 = interior element kernel(s), 2 = boundary pass,
  * 3 / 4 = the point / matrix stage of the interior pass's first chunk (the whole pass
- * when it has one chunk; atomic scatter only).  With the atomic scatter the boundary
- * pass runs beside the interior kernels, so phase 2 is only the part of it that
- * outlasts them. */
+ * when it has one chunk; atomic scatter only).  With the atomic scatter, device
+ * buffers and a one-chunk interior pass, the point stage clears A and b beside its own
+ * work (phase 0 is then only the reset of the status word; phases 1 and 3 include the
+ * clear) and the boundary pass runs beside the interior kernels from the end of that
+ * point stage; otherwise it runs beside them from the start.  Phase 2 is only the part of
+ * the boundary pass that outlasts the interior kernels. */
 double gales_asm_last_phase_ms(gales_asm* h, int32_t phase);
 /* Number of kernel launches made by the library since the handle was created. */
 int64_t gales_asm_launch_count(gales_asm* h);

@@ -171,3 +171,41 @@ def test_p_equals_i_newton_iteration0(cuda_lib, gm, orc):
     fa, lp, vals, rhs = _run(gm, orc, mesh, mat, setup, I, I.copy(), dt, gm.FORM_FP64)
     assert rel(lp.vals, vals) <= FP64_TOL
     assert rel(lp.rhs, rhs) <= FP64_TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+@pytest.mark.parametrize("offset", [0, 1])
+@pytest.mark.parametrize("chunks", ["one", "several"])
+@pytest.mark.parametrize("kind,nc", [("tet", 3), ("hex", 4)])
+def test_outputs_cleared_by_the_call(kind, nc, chunks, offset, form, cuda_lib, gm, orc):
+    """The call clears A and b itself (with the atomic scatter and one interior chunk,
+    inside the point launch; over several chunks with a clear kernel): outputs
+    prefilled with NaN, at a 16-byte-aligned and at an odd-word offset, give the
+    oracle's values, twice in a row, and the words beside them stay untouched."""
+    import torch
+    mesh, mat, setup, I, P, dt = cases.make(kind, nc)
+    fa = gm.FluidAssembly(mesh, mat, setup)
+    if chunks == "several":
+        chunk = max(4, mesh.n_elements // 5 // 4 * 4)
+        fa.set_chunk(chunk)
+        assert mesh.n_elements > 3 * chunk
+    row_ptr, col = fa.pattern()
+    nnz, nr = int(row_ptr[-1]), len(row_ptr) - 1
+    dev = torch.device("cuda:0")
+    vbuf = torch.full((nnz + 2,), float("nan"), dtype=torch.float64, device=dev)
+    rbuf = torch.full((nr + 2,), float("nan"), dtype=torch.float64, device=dev)
+    lp = gm.LinearSystem(row_ptr, col, vbuf[offset:offset + nnz], rbuf[offset:offset + nr])
+    f = gm.FORM_MIXED if form == "mixed" else gm.FORM_FP64
+    tol = MIXED_TOL if form == "mixed" else FP64_TOL
+    Id, Pd = torch.tensor(I, device=dev), torch.tensor(P, device=dev)
+    ref_vals, ref_rhs, s, fb = orc.assemble(mesh, mat, setup, I, P, dt, row_ptr, col)
+    assert s == 0
+    for _ in range(2):
+        fa.execute(Id, Pd, dt, lp, form=f)
+        torch.cuda.synchronize(dev)
+        assert rel(lp.vals.cpu().numpy(), ref_vals) <= tol
+        assert rel(lp.rhs.cpu().numpy(), ref_rhs) <= tol
+    outside_v = [i for i in range(nnz + 2) if not offset <= i < offset + nnz]
+    outside_r = [i for i in range(nr + 2) if not offset <= i < offset + nr]
+    assert bool(torch.isnan(vbuf[outside_v]).all()) and bool(torch.isnan(rbuf[outside_r]).all())
