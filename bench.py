@@ -215,8 +215,10 @@ def cpu_oracle_rate(mesh, mat, setup, I, P, dt, row_ptr, col, colour, n_colours,
 
 BYTES_PER_ELEM_HEX = 4 * 8 + 8 * 3 * 8 + 2 * 8 * 8 * 8 + 16 * (8 * 8) ** 2 + 16 * 8 * 8  # 67,808
 # DRAM bytes per element of the mixed hex interior pass, from ncu on the 64,000-hex mesh
-# of a 40^3 grid (CSR bytes per element 14,172, 1.9% above the 160x160x156 mesh's
-# 13,911); scaled by the element count (profiles/dram_traffic_hex8_40cube_assembly.md).
+# of a 40^3 grid in one chunk with a separate clear kernel, like the chunks of the
+# 160x160x156 assembly (point records far larger than L2); CSR bytes per element 14,172,
+# 1.9% above that mesh's 13,911; scaled by the element count
+# (profiles/dram_traffic_hex8_40cube_assembly.md, capture B).
 TRAFFIC_BYTES_PER_ELEM_HEX = 64817
 
 
