@@ -730,9 +730,10 @@ def main():
     torch.cuda.synchronize(dev)
     # a host-buffer call returns when A and b are in host memory, so each step is timed
     # on its own as well as the whole run
-    # three times the device-buffer step count (each step ~9 ms), so that one slow step
-    # on the shared host link weighs less in the mean
-    e2e_n = 3 * args.steps
+    # six times the device-buffer step count (each step ~9 ms), so that one slow step
+    # on the shared host link (single steps of 20-60 ms have been seen) weighs less in
+    # the mean; every step is counted
+    e2e_n = 6 * args.steps
     e2e_steps = []
     gc.collect()
     gc.disable()      # no collector pause of the Python host loop inside the timing
