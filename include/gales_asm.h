@@ -268,8 +268,8 @@ double gales_dt_update(double dt_elem_min, double dt, double dt_min, double dt_m
 /* Secondary variables at the nodes (secondary_dofs::execute, secondary_dofs.hpp:56-101,
  * the mixture of every node's state at shear rate 0): out[f * n_nodes + node] for
  * f = 0..7 = rho, mu, cp, cv, alpha, beta, kappa, sound speed (host or device, 8 n_nodes
- * doubles).  The magma volume and mass fractions (pp_vf_g) need the magma mixtures and
- * are not provided.  The call synchronises its stream. */
+ * doubles).  The magma volume and mass fractions of the same routine (pp_vf_g) come
+ * from gales_asm_magma_fractions.  The call synchronises its stream. */
 int gales_asm_secondary_dofs(gales_asm* h, const double* I, double* out, void* stream);
 
 /* Hydrostatic pressure column of the multicomponent solver (pressure_profile_mc,
