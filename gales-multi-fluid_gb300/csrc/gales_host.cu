@@ -1427,8 +1427,9 @@ int assemble_impl(gales_asm* h, const double* I, const double* P, double dt, int
     CK(h, h->s_rhs.alloc(h->n_rows), "staging rhs");
     drhs = h->s_rhs.p;
   }
-  // host CSR values: copied row prefix by row prefix while the single-launch interior
-  // pass runs (mixed form, atomic scatter), else after the assembly
+  // host CSR values: copied row prefix by row prefix while the interior pass runs chunk
+  // by chunk (mixed form, atomic scatter, page-locked destination), else after the
+  // assembly
   const bool pipelined =
       hV && form == GALES_FORM_MIXED && h->scatter_mode == GALES_SCATTER_ATOMIC && is_pinned_host_ptr(vals);
   RowCopy copy{vals, dvals};
