@@ -459,17 +459,55 @@ def newton_block(gm, syn, mesh, mat, torch, dev):
     return out
 
 
-def linear_solve_block(gm, fa, lp, torch, dev, tstream):
+def linear_solve_block(gm, fa, lp, torch, dev, tstream, with_cpu=True):
     """The linear solve after the assembly (belos_linear_solver::execute with the shipped
     setup.txt settings: flexible GMRES(200), 5 restarts, ILU(1), 1e-9) on the mixed-form
     system the timed steps left in device memory, with the factor in FP64 (the
     reference's arithmetic) and in FP32: wall time of the call (factorisation included),
-    its factorisation alone and one preconditioner application."""
+    its factorisation alone and one preconditioner application; and the CPU oracle's
+    solve beside the library's on a bounded sample."""
     out = {"what": "FGMRES(200) + ILU(1), rel. residual 1e-9, x0 = 0, device CSR of the mixed assembly",
            "rows": fa.n_rows}
     out["ilu_fp64"] = _solve_once(gm, fa, lp, torch, dev, tstream, gm.PRECOND_ILU)
     out["ilu_fp32"] = _solve_once(gm, fa, lp, torch, dev, tstream, gm.PRECOND_ILU_FP32)
+    if with_cpu:
+        out["cpu_oracle_sample"] = solve_cpu_sample(gm, torch, dev, tstream)
     return out
+
+
+def solve_cpu_sample(gm, torch, dev, tstream, lattice=30):
+    """The solve on a bounded sample beside the oracle's restatement on one host core:
+    the FP64-form system of the 163,618-tet mesh of the 30^3 lattice (189,000 unknowns;
+    same material, setup and kind of state as the benchmark), solved by the library
+    (FP64 factor) and by the oracle's ILU(1) + flexible GMRES on the host (factorisation
+    included in both)."""
+    try:
+        import oracle
+        syn = importlib.import_module("gales-multi-fluid_gb300.synthetic")
+        mesh = syn.box_tet_delaunay(lattice, seed=1)
+        mat, setup = syn.material_for(3, 0), syn.setup_for(3, 3)
+        I, P = syn.state_for(mesh, 3, 0)
+        fa = gm.FluidAssembly(mesh, mat, setup, device=dev.index or 0)
+        try:
+            rows = fa.n_rows
+            lp = fa.linear_system(device=dev)
+            fa.execute(torch.tensor(I, device=dev), torch.tensor(P, device=dev), 1e-3, lp, form=gm.FORM_FP64,
+                       stream=tstream.cuda_stream)
+            torch.cuda.synchronize(dev)
+            gpu = _solve_once(gm, fa, lp, torch, dev, tstream, gm.PRECOND_ILU)
+            vals, rhs = lp.vals.cpu().numpy(), lp.rhs.cpu().numpy()
+        finally:
+            fa.close()
+        t0 = time.perf_counter()
+        _, info = oracle.fgmres(lp.row_ptr, lp.col, vals, rhs, tol=1e-9, maxsubspace=200, maxrestarts=5, fill=1)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        gpu_ms = gpu.get("ms")
+        return {"workload": f"{mesh.n_elements} tets ({lattice}^3 lattice), {rows} unknowns, FP64-form system",
+                "cpu_cores": 1, "cpu_ms": cpu_ms, "cpu_iterations": info["iterations"],
+                "cpu_rel_res": info["rel_res"], "gpu_ms": gpu_ms, "gpu_iterations": gpu.get("iterations"),
+                "gpu_rel_res": gpu.get("rel_res"), "cpu_over_gpu": (cpu_ms / gpu_ms) if gpu_ms else None}
+    except Exception as e:  # reported, never fatal to the assembly line
+        return {"error": f"{type(e).__name__}: {e}"}
 
 
 def _solve_once(gm, fa, lp, torch, dev, tstream, precond):
@@ -798,7 +836,7 @@ def main():
     if rank == 0:
         line["adaptive_dt"] = adaptive_dt_block(gm, fa, mesh, mat, setup, I, dt, torch, dev, not args.no_cpu)
     if rank == 0 and not args.no_solve:
-        line["linear_solve"] = linear_solve_block(gm, fa, lp, torch, dev, stream)
+        line["linear_solve"] = linear_solve_block(gm, fa, lp, torch, dev, stream, not args.no_cpu)
     if rank == 0:
         line["magma_properties"] = magma_block(torch, dev, not args.no_cpu)
     if rank == 0 and not args.no_newton:
