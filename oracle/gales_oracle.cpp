@@ -5,9 +5,12 @@
  * used only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
  * as the checker.  It is never linked into, or called by, the CUDA library.
  *
- * PARITY UNPINNED: the reference cannot be compiled here (it needs Boost uBLAS,
- * OpenMPI and Trilinos, which are absent) and ships no tests, golden vectors or
- * fixtures.  This file restates the reference's arithmetic line by line,
+ * PARITY UNPINNED for the assembly itself: the reference's element integral and
+ * mixtures cannot be compiled here (they need Boost uBLAS, OpenMPI and Trilinos, which
+ * are absent) and it ships no tests, golden vectors or fixtures.  The chemicals' EOS
+ * this file mixes (custom_chemical, ideal_gas) is pinned against the reference's own
+ * chemicals.hpp, compiled from its checkout (ref_chemicals.cpp,
+ * tests/test_reference_pins.py).  This file restates the reference's arithmetic line by line,
  * keeping the reference's expression forms and summation orders so that, built
  * with -ffp-contract=off, it reproduces the reference's FP64 results up to
  * libm's pow and Boost uBLAS's internal loop orders.  Each function cites the

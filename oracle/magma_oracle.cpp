@@ -12,8 +12,12 @@
  *     dissolved_volatiles (chemicals.hpp:149-194) and named ideal gases (198-271);
  *   - GiordanoEtAlViscosityModel (GiordanoEtAlViscosityModel.hpp:36-116);
  *   - fluid_properties' mixture of sub-mixtures (fluid_properties.hpp:171-200).
- * The constants and operation orders are the reference's.  PARITY UNPINNED: the
- * reference cannot be built here and ships no expected values for these functions.
+ * The constants and operation orders are the reference's.  The chemicals (melt,
+ * dissolved_volatiles, ideal_gas) and the Giordano model are pinned bit for bit against
+ * the reference's own chemicals.hpp and GiordanoEtAlViscosityModel.hpp, compiled from its
+ * checkout (ref_chemicals.cpp, tests/test_reference_pins.py).  The rest (the magma
+ * mixture of mixtures.hpp, which needs Boost uBLAS) is UNPINNED: it cannot be built here
+ * and the reference ships no expected values for it.
  * Pal 2003's Newton iteration (mixtures.hpp:266-289) loops while F < 1e-9; the
  * restatement stops after 200 steps and reports that.
  */
@@ -467,6 +471,56 @@ int gor_magma_properties(const gales_magma_desc* comps, int32_t nc, const double
 }
 
 }  // extern "C"
+
+// The restated chemicals and viscosity model one at a time, for the pins against the
+// reference's own classes (tests/test_reference_pins.py): out[0..8] = rho, mu, cp, cv,
+// kappa, sound speed, alpha, beta, chemical diffusivity, set up as build() sets them up.
+namespace {
+void chem_out(const Chem& c, double* o) {
+  const double v[9] = {c.rho, c.mu, c.cp, c.cv, c.kappa, c.c, c.alpha, c.beta, c.D};
+  for (int k = 0; k < 9; ++k) o[k] = v[k];
+}
+}  // namespace
+
+extern "C" int gor_melt_props(const double* oxide_wf, double kappa, double p, double T, double* out) {
+  Melt m;
+  m.init(oxide_wf, kappa);
+  Chem c;
+  m.props(p, T, c);
+  chem_out(c, out);
+  return 0;
+}
+
+// molar_mass 0.01802 (H2O) or 0.04401 (CO2), as build() sets them
+extern "C" int gor_volatile_props(double molar_mass, double cp, double kappa, double p, double T, double* out) {
+  Volatile v;
+  v.M = molar_mass;
+  v.cp = cp;
+  v.kappa = kappa;
+  Chem c;
+  v.props(p, T, c);
+  chem_out(c, out);
+  return 0;
+}
+
+extern "C" int gor_gas_props(double molar_mass, double p, double T, double* out) {
+  Gas g;
+  g.init(molar_mass);
+  Chem c;
+  g.props(p, T, c);
+  chem_out(c, out);
+  return 0;
+}
+
+// Giordano viscosity of the melt of the given oxide weight fractions; -1 on the
+// reference's error exits
+extern "C" int gor_giordano_mu(const double* oxide_wf, double T, double wf_h2o_l, double wf_co2_l, double* mu) {
+  Melt m;
+  m.init(oxide_wf, 1.0);
+  Giordano g;
+  g.set(m.wf, m.mm);
+  return g.mu(T, wf_h2o_l, wf_co2_l, *mu) ? 0 : -1;
+}
 
 // secondary_dofs::execute's gas fractions (pp_vf_g, secondary_dofs.hpp:56-131) at one
 // node's (p, T, Y) with the set magmas, shear rate 0: out[2c] = vf_g_comp_c,

@@ -1,9 +1,10 @@
 """TEST INFRASTRUCTURE — ctypes binding of the CPU oracle (gales_oracle.cpp).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this,
-as the checker.  PARITY UNPINNED: the reference itself cannot be built here
-(Boost, MPI and Trilinos are absent) and ships no golden data; see the header
-of gales_oracle.cpp.
+as the checker.  PARITY UNPINNED for the assembly: the reference's element integral
+cannot be built here (Boost, MPI and Trilinos are absent) and it ships no golden data;
+its chemicals and magma viscosity model compile, and the oracle is pinned against them
+(tests/test_reference_pins.py); see the header of gales_oracle.cpp.
 """
 from __future__ import annotations
 
@@ -273,6 +274,35 @@ def shear_rate(dim, dI):
     (3, GALES_MAX_ND)."""
     dI = np.ascontiguousarray(dI, dtype=np.float64)
     return float(lib().gor_shear_rate(int(dim), _d(dI)))
+
+
+def chemical_props(kind, *args):
+    """One restated chemical or the viscosity model (magma_oracle.cpp), for the pins
+    against the reference's classes: kind "melt" (oxide_wf[10], kappa, p, T), "volatile"
+    (molar_mass, cp, kappa, p, T), "gas" (molar_mass, p, T) -> dict of rho, mu, cp, cv,
+    kappa, c, alpha, beta, D; "giordano" (oxide_wf[10], T, wf_h2o_l, wf_co2_l) -> mu or
+    None on the reference's error exits."""
+    out = np.zeros(9)
+    L = lib()
+    if kind == "melt":
+        wf, kappa, p, T = args
+        L.gor_melt_props(_d(np.ascontiguousarray(wf, dtype=np.float64)), C.c_double(kappa), C.c_double(p),
+                         C.c_double(T), _d(out))
+    elif kind == "volatile":
+        M, cp, kappa, p, T = args
+        L.gor_volatile_props(*(C.c_double(x) for x in (M, cp, kappa, p, T)), _d(out))
+    elif kind == "gas":
+        M, p, T = args
+        L.gor_gas_props(*(C.c_double(x) for x in (M, p, T)), _d(out))
+    elif kind == "giordano":
+        wf, T, h2o, co2 = args
+        mu = C.c_double()
+        r = L.gor_giordano_mu(_d(np.ascontiguousarray(wf, dtype=np.float64)), *(C.c_double(x) for x in (T, h2o, co2)),
+                              C.byref(mu))
+        return None if r else mu.value
+    else:
+        raise ValueError(kind)
+    return dict(zip(["rho", "mu", "cp", "cv", "kappa", "c", "alpha", "beta", "D"], out))
 
 
 def magma_fractions(p, T, Y):
