@@ -9,7 +9,7 @@
  * mixtures cannot be compiled here (they need Boost uBLAS, OpenMPI and Trilinos, which
  * are absent) and it ships no tests, golden vectors or fixtures.  The chemicals' EOS
  * this file mixes (custom_chemical, ideal_gas) is pinned against the reference's own
- * chemicals.hpp, compiled from its checkout (ref_chemicals.cpp,
+ * chemicals.hpp, compiled from its checkout (ref_classes.cpp,
  * tests/test_reference_pins.py).  This file restates the reference's arithmetic line by line,
  * keeping the reference's expression forms and summation orders so that, built
  * with -ffp-contract=off, it reproduces the reference's FP64 results up to

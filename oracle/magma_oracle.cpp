@@ -15,7 +15,7 @@
  * The constants and operation orders are the reference's.  The chemicals (melt,
  * dissolved_volatiles, ideal_gas) and the Giordano model are pinned bit for bit against
  * the reference's own chemicals.hpp and GiordanoEtAlViscosityModel.hpp, compiled from its
- * checkout (ref_chemicals.cpp, tests/test_reference_pins.py).  The rest (the magma
+ * checkout (ref_classes.cpp, tests/test_reference_pins.py).  The rest (the magma
  * mixture of mixtures.hpp, which needs Boost uBLAS) is UNPINNED: it cannot be built here
  * and the reference ships no expected values for it.
  * Pal 2003's Newton iteration (mixtures.hpp:266-289) loops while F < 1e-9; the

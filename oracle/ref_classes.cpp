@@ -1,15 +1,18 @@
 /*
  * TEST INFRASTRUCTURE — NOT PART OF THE PRODUCT.
  *
- * The reference's own property classes, compiled from its checkout by oracle/build.py
- * (build_ref) into oracle/_ref/libref_chemicals.so, so that the tests can pin the
- * oracle's restatement against the reference itself where the reference compiles:
+ * The reference's own classes that compile here, built from its checkout by
+ * oracle/build.py (build_ref) into oracle/_ref/libref_classes.so, so that the tests can
+ * pin the oracle's restatement against the reference itself where the reference
+ * compiles:
  *   - src/fem/physical_props/fluid/chemicals.hpp: custom_chemical (19-49), melt
  *     (56-145, Lange-Carmichael), dissolved_volatiles (149-194), ideal_gas (198-271),
  *     over base_chemical.hpp;
  *   - src/fem/physical_props/fluid/GiordanoEtAlViscosityModel.hpp (the magma viscosity),
- *     driven as magma_mixture drives it (mixtures.hpp:161, 180).
- * Those headers need only the standard library, except two helpers that the reference
+ *     driven as magma_mixture drives it (mixtures.hpp:161, 180);
+ *   - src/fem/mesh/element.hpp (over node.hpp and point.hpp): the element types' interior
+ *     Gauss points, side node tables and side Gauss points (gauss_data).
+ * The property headers need only the standard library, except two helpers that the reference
  * takes from base headers which include mpi.h and Boost: the Error macro
  * (src/fem/base/algorithm.hpp:42) and print_in_file (src/fem/base/print_tools.hpp).
  * Neither takes part in the arithmetic; stand-ins follow (Error throws, so the wrappers
@@ -17,8 +20,11 @@
  * The mixtures (mixtures.hpp) and the element integral need Boost uBLAS and Trilinos
  * and are not built.
  */
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <stdexcept>
 #include <string>
@@ -33,6 +39,7 @@ inline void ref_error(const std::string& m) { throw std::runtime_error(m); }
 
 #include "chemicals.hpp"
 #include "GiordanoEtAlViscosityModel.hpp"
+#include "element.hpp"
 
 namespace {
 
@@ -102,6 +109,40 @@ int ref_giordano(const double* oxides_wf, double T, double wf_h2o_l, double wf_c
   } catch (const std::exception&) {
     return -1;
   }
+}
+
+// The element type's tables as gauss_data sets them: gp[i * 3 + d] interior points,
+// sides[s * nsn + j] side node tables, sgp[(s * nqs + j) * 3 + d] side points (unused
+// coordinates 0), counts = {nq, nsides, nsn, nqs}.  Returns nq, or -1 for an element
+// the reference does not define.
+int ref_element_tables(int dim, int nen, double* gp, int32_t* sides, double* sgp, int32_t* counts) {
+  auto fill = [&](const auto& el, auto coords) {
+    const int nq = el.nb_gp(), ns = el.nb_sides(), nsn = el.nb_side_nds();
+    const int nqs = ns > 0 ? el.nb_side_gp(0) : 0;
+    for (int i = 0; i < nq; ++i) coords(el.gp(i), gp + i * 3);
+    for (int s = 0; s < ns; ++s)
+      for (int j = 0; j < nsn; ++j) sides[s * nsn + j] = el.side(s, j);
+    for (int s = 0; s < ns; ++s)
+      for (int j = 0; j < nqs; ++j) coords(el.side_gp(s, j), sgp + (s * nqs + j) * 3);
+    counts[0] = nq;
+    counts[1] = ns;
+    counts[2] = nsn;
+    counts[3] = nqs;
+    return nq;
+  };
+  if (dim == 2 && (nen == 3 || nen == 4)) {
+    GALES::element<2> el(nen);
+    return fill(el, [](const GALES::point<2>& p, double* o) { o[0] = p.get_x(); o[1] = p.get_y(); o[2] = 0.0; });
+  }
+  if (dim == 3 && (nen == 4 || nen == 8)) {
+    GALES::element<3> el(nen);
+    return fill(el, [](const GALES::point<3>& p, double* o) {
+      o[0] = p.get_x();
+      o[1] = p.get_y();
+      o[2] = p.get_z();
+    });
+  }
+  return -1;
 }
 
 }  // extern "C"

@@ -1,15 +1,17 @@
 """The oracle pinned against the reference's own code where the reference compiles.
 
-oracle/_ref/libref_chemicals.so is the reference's chemicals.hpp (custom_chemical, melt,
-dissolved_volatiles, ideal_gas over base_chemical.hpp) and its
-GiordanoEtAlViscosityModel.hpp, compiled from a checkout of the reference by
-oracle/build.py (build_ref; see oracle/ref_chemicals.cpp).  These tests compare the
-oracle's restatement of the same quantities with it on seeded random states:
+oracle/_ref/libref_classes.so is the reference's chemicals.hpp (custom_chemical, melt,
+dissolved_volatiles, ideal_gas over base_chemical.hpp), its
+GiordanoEtAlViscosityModel.hpp and its element.hpp (over node.hpp and point.hpp),
+compiled from a checkout of the reference by oracle/build.py (build_ref; see
+oracle/ref_classes.cpp).  These tests compare the oracle's restatement of the same
+quantities with it, on seeded random states where the quantity depends on one:
   - the chemicals' EOS as the assembly's mixture sees them (one-component materials
     built with the package's descriptor constructors, evaluated by the oracle's
     mixture): rho, mu, cp, cv, kappa, sound speed, alpha, beta and the diffusivity;
   - the magma chemicals (Lange-Carmichael melt, dissolved H2O and CO2, the H2O and CO2
-    gases) and the Giordano et al. (2008) viscosity, one at a time.
+    gases) and the Giordano et al. (2008) viscosity, one at a time;
+  - the element types' interior Gauss points, side node tables and side Gauss points.
 The GPU kernels are compared with the oracle elsewhere (test_gpu_parity.py,
 test_magma.py, test_gpu_magma_assembly.py), so these pins close the chain for these
 functions.  Skipped where no reference checkout was present at build time.
@@ -23,7 +25,7 @@ import pytest
 import oracle
 from cases import gm
 
-LIB = pathlib.Path(__file__).resolve().parents[1] / "oracle" / "_ref" / "libref_chemicals.so"
+LIB = pathlib.Path(__file__).resolve().parents[1] / "oracle" / "_ref" / "libref_classes.so"
 KEYS = ["rho", "mu", "cp", "cv", "kappa", "c", "alpha", "beta", "D"]
 
 pytestmark = pytest.mark.skipif(not LIB.exists(), reason="no reference checkout at build time (oracle/_ref)")
@@ -40,6 +42,8 @@ def ref():
     lib.ref_melt.argtypes = [dp, d, d, d, dp]
     lib.ref_dissolved_volatile.argtypes = [C.c_char_p, d, d, d, d, dp]
     lib.ref_giordano.argtypes = [dp, d, d, d, dp]
+    ip = C.POINTER(C.c_int32)
+    lib.ref_element_tables.argtypes = [C.c_int, C.c_int, dp, ip, dp, ip]
     return lib
 
 
@@ -173,3 +177,22 @@ def test_giordano_viscosity_matches_reference(ref):
     wf = _oxides(rng)
     assert ref.ref_giordano(wf.ctypes.data_as(C.POINTER(C.c_double)), 1200.0, 0.01, 1.0, C.byref(mu)) == -1
     assert oracle.chemical_props("giordano", wf, 1200.0, 0.01, 1.0) is None
+
+
+@pytest.mark.parametrize("dim,nen", [(2, 3), (2, 4), (3, 4), (3, 8)])
+def test_element_tables_match_reference(ref, dim, nen):
+    """element.hpp's gauss_data: the oracle's (and, through the GPU parity tests, the
+    kernels') interior points, side node tables and side points, bit for bit."""
+    gp, sgp = np.zeros(8 * 3), np.zeros(6 * 4 * 3)
+    sides, cnt = np.zeros(6 * 4, dtype=np.int32), np.zeros(4, dtype=np.int32)
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int32)
+    nq = ref.ref_element_tables(dim, nen, gp.ctypes.data_as(dp), sides.ctypes.data_as(ip), sgp.ctypes.data_as(dp),
+                                cnt.ctypes.data_as(ip))
+    assert nq > 0
+    nq, ns, nsn, nqs = (int(x) for x in cnt)
+    o = oracle.gauss(dim, nen)
+    assert o["gp"].shape == (nq, 3) and o["sides"].shape == (ns, nsn) and o["sgp"].shape == (ns, nqs, 3)
+    assert np.array_equal(o["gp"], gp[:nq * 3].reshape(nq, 3))
+    assert np.array_equal(o["sides"], sides[:ns * nsn].reshape(ns, nsn))
+    assert np.array_equal(o["sgp"], sgp[:ns * nqs * 3].reshape(ns, nqs, 3))
